@@ -1,0 +1,362 @@
+"""Benchmark of the Laplace/diffusion assembly hot path (one step = one whole-mesh assembly).
+
+Workload: 128^3 trilinear hexahedra on the unit cube (E = 2,097,152, N = 2,146,689 nodes,
+nnz = 57,066,625), 2x2x2 Gauss, interior nodes jittered uniformly by +-0.1h and per-element
+conductivity log-uniform in [0.1, 10] (seeded synthetic inputs).  The headline `value` is
+assembled elements/s with inputs resident in HBM; `e2e` is the same metric through the C ABI with
+host buffers (coordinates and conductivities copied in, the assembled CSR values copied out,
+inside the timed region).  The solve (Jacobi-CG to relative residual 1e-12, FP64 and mixed
+refinement) is reported beside it.
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl gfe|reference] [--n 128]
+
+--impl reference times the CPU restatement of Iron's element loop (the oracle, Iron's own
+algorithm: per-element gather, Gauss loop, bisection insert into CSR) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+L2_BYTES = 129 * 1024 * 1024
+WORKLOAD = "laplace_diffusion_trilinear_hex"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gfe", choices=["gfe", "reference"])
+    ap.add_argument("--n", type=int, default=128, help="elements per side")
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--cpu-sample-n", type=int, default=96, help="side of the CPU-baseline sample mesh")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_problem(n: int, seed: int = 0):
+    from iron_gb300 import mesh as M
+
+    m = M.RegularMesh((n, n, n))
+    m.jitter_interior(seed)
+    kappa = np.exp(np.random.default_rng(seed + 1).uniform(np.log(0.1), np.log(10.0), m.n_elements))
+    return m, kappa
+
+
+def algorithmic_bytes(E: int, N: int, nnz: int) -> int:
+    # E*(8*4 connectivity + 8 conductivity) + N*(3*8 coordinates + 8 rhs) + nnz*8 (values written once)
+    return E * (8 * 4 + 8) + N * (3 * 8 + 8) + nnz * 8
+
+
+def algorithmic_flops(E: int) -> int:
+    # per element: ng*(18 nen + 45 + 18 nen + 6 nen^2) with nen = 8, ng = 8
+    return E * 8 * (18 * 8 + 45 + 18 * 8 + 6 * 64)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason sampling during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic_per_unit():
+    """DRAM bytes per element of the colour kernel from the committed ncu summary, if present."""
+    p = ROOT / "profiles" / "laplace_assemble_color_traffic.txt"
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.startswith("dram_bytes_per_element:"):
+            return float(ln.split(":", 1)[1])
+    return None
+
+
+def cpu_baseline(n_sample: int, threads: int):
+    """The oracle (Iron's algorithm restated in C++) timed on a bounded sample on the host cores."""
+    import oracle
+
+    m, kappa = make_problem(n_sample, seed=0)
+    rp, ci = oracle.csr_structure(m.elem_nodes, m.n_nodes)
+    oracle.laplace_assemble(3, [1, 1, 1], [2, 2, 2], m.elem_nodes[:64], m.coords, kappa[:64], rp, ci, 1)
+    t0 = time.perf_counter()
+    oracle.laplace_assemble(3, [1, 1, 1], [2, 2, 2], m.elem_nodes, m.coords, kappa, rp, ci, threads)
+    dt = time.perf_counter() - t0
+    return m.n_elements / dt, dt, m.n_elements
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    n = args.cpu_sample_n
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, dt, E = cpu_baseline(n, threads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": "assembled_elements_per_s", "value": value, "unit": "elements/s",
+        "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "elements_per_side": args.n, "sample_elements_per_side": n,
+                   "gauss": "2x2x2", "conductivity": "log-uniform [0.1,10]", "jitter": "+-0.1h"},
+        "cpu_baseline": {"value": value, "unit": "elements/s", "cores": threads, "kind": "port",
+                         "sample": f"{n}^3 = {n**3} elements per step (same element density as the {args.n}^3 "
+                                   f"workload); Iron's algorithm restated in C++ (oracle/), Iron itself cannot be "
+                                   f"built here (Fortran+MPI+PETSc)"},
+        "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gfe(args):
+    import torch
+
+    from iron_gb300 import _lib
+    from iron_gb300.laplace import LaplaceAssembly
+
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local if ws > 1 else 0)
+    torch.cuda.set_device(dev)
+    _lib.load()
+
+    m, kappa = make_problem(args.n, seed=rank)
+    A = LaplaceAssembly.from_regular_mesh(m, kappa=kappa, device=dev)
+    E, N, nnz = A.n_elements, A.n_nodes, A.nnz
+    ncol = len(A.colour_ptr) - 1
+    stream = torch.cuda.current_stream(dev)
+
+    # accuracy of both precisions against the FP64 assembly, and the solve
+    v64 = A.assemble("fp64").clone()
+    vmx = A.assemble("mixed").clone()
+    asm_err = float((vmx - v64).abs().max() / v64.abs().max())
+    precisions = ["fp64", "mixed"]
+    timings = {}
+    for prec in precisions:
+        for _ in range(args.warmup):
+            A.assemble(prec, check=False)
+        torch.cuda.synchronize()
+        _lib.profile_enable(True)
+        _lib.profile_read(_lib.STAGE_LAPLACE_ELEMENTS, reset=True)
+        if ws > 1:
+            torch.distributed.barrier()
+        with ClockSampler(dev.index) as clk:
+            torch.cuda.synchronize()
+            t0 = torch.cuda.Event(enable_timing=True)
+            t1 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            for _ in range(args.steps):
+                A.assemble(prec, check=False)
+            t1.record(stream)
+            torch.cuda.synchronize()
+        _lib.profile_enable(False)
+        kern_ms, launches = _lib.profile_read(_lib.STAGE_LAPLACE_ELEMENTS, reset=True)
+        _lib.raise_device_errors("bench assembly")
+        ms = t0.elapsed_time(t1) / args.steps
+        if ws > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        timings[prec] = {"ms_per_step": ms, "kernel_ms_total": kern_ms, "launches": launches,
+                         "clocks": clk.summary()}
+
+    # end to end through the C ABI with host buffers: H2D geometry + conductivity, D2H values
+    coords_h = torch.from_numpy(m.coords).pin_memory()
+    kappa_h = torch.from_numpy(kappa).pin_memory()
+    vals_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    e2e = {}
+    for prec in precisions:
+        for i in range(args.warmup + args.steps):
+            if i == args.warmup:
+                torch.cuda.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            A.coords.copy_(coords_h, non_blocking=True)
+            A.kappa.copy_(kappa_h, non_blocking=True)
+            A.assemble(prec, check=False)
+            vals_h.copy_(A.values, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e[prec] = e0.elapsed_time(e1) / args.steps
+    _lib.raise_device_errors("bench e2e")
+    h2d = int(coords_h.numel() * 8 + kappa_h.numel() * 8)
+    d2h = int(nnz * 8)
+
+    solve = None
+    if not args.no_solve:
+        fixed = torch.zeros(N, dtype=torch.uint8, device=dev)
+        x0 = torch.zeros(N, dtype=torch.float64, device=dev)
+        left, right = torch.from_numpy(m.face_nodes(0, 0)).to(dev), torch.from_numpy(m.face_nodes(0, 1)).to(dev)
+        fixed[left] = 1
+        fixed[right] = 1
+        x0[right] = 1.0
+        solve = {}
+        xs = {}
+        for prec in precisions:
+            A.assemble(prec)
+            x = x0.clone()
+            torch.cuda.synchronize()
+            s0 = time.perf_counter()
+            info = A.solve(fixed, x, rtol=1e-12, precision=prec)
+            torch.cuda.synchronize()
+            solve[prec] = {"ms": (time.perf_counter() - s0) * 1e3, "iterations": info.iterations,
+                           "rel_residual": info.relative_residual}
+            xs[prec] = x
+        solve["mixed"]["rel_err_vs_fp64"] = float((xs["mixed"] - xs["fp64"]).abs().max() / xs["fp64"].abs().max())
+        solve["note"] = "Jacobi-CG, u=0 at x=0 and u=1 at x=1, rtol 1e-12; mixed = FP32 inner CG + FP64 refinement"
+
+    # headline: mixed only when its solution meets the 1e-10 accuracy bar, else FP64 plain
+    head = "fp64"
+    if args.precision != "auto":
+        head = args.precision
+    elif solve is not None and solve["mixed"].get("rel_err_vs_fp64", 1.0) <= 1e-10:
+        if timings["mixed"]["ms_per_step"] < timings["fp64"]["ms_per_step"]:
+            head = "mixed"
+    T = timings[head]
+    value = ws * E / (T["ms_per_step"] * 1e-3)
+    per_launch_ms = T["kernel_ms_total"] / max(T["launches"], 1)
+    units_per_launch = E / ncol
+    bytes_per_elem = algorithmic_bytes(E, N, nnz) / E
+    achieved = bytes_per_elem * units_per_launch / (per_launch_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    tpu = profile_traffic_per_unit()
+    line = {
+        "metric": "assembled_elements_per_s", "value": value, "unit": "elements/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": T["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f32+f64acc",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "elements_per_side": args.n, "elements": E, "nodes": N, "nnz": nnz,
+                   "gauss": "2x2x2", "conductivity": "log-uniform [0.1,10] seeded", "jitter": "+-0.1h seeded",
+                   "precision": head, "l2": "inputs larger than L2 (CSR values %.0f MB > 129 MB)" % (nnz * 8 / 1e6),
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "clocks": T["clocks"],
+        "e2e": {"value": ws * E / (e2e[head] * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(args.steps * (ncol + (1 if head == "mixed" else 0))),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind,
+                     "traffic": None if tpu is None else tpu * units_per_launch,
+                     "kernel": f"laplace_assemble_color<{'double' if head == 'fp64' else 'float'}>",
+                     "per_launch_ms": per_launch_ms, "units_per_launch": units_per_launch,
+                     "algorithmic_bytes_per_element": bytes_per_elem},
+        "precisions": {p: {"ms_per_step": timings[p]["ms_per_step"],
+                           "elements_per_s": ws * E / (timings[p]["ms_per_step"] * 1e-3),
+                           "e2e_ms": e2e[p], "kernel_ms_per_launch": timings[p]["kernel_ms_total"] /
+                           max(timings[p]["launches"], 1)} for p in precisions},
+        "assembly_rel_err_mixed_vs_fp64": asm_err,
+    }
+    try:
+        line["fp64_pipe_gflops"] = _lib.probe_fma_rate(_lib.GFE_FP64)
+        line["fp32_pipe_gflops"] = _lib.probe_fma_rate(_lib.GFE_MIXED)
+        fl = algorithmic_flops(E) / (T["ms_per_step"] * 1e-3) / 1e9
+        line["flops"] = {"algorithmic_gflops_per_s": fl, "formula": "E*8*(18*8+45+18*8+6*64)"}
+    except Exception as exc:  # diagnostic only
+        line["probe_error"] = str(exc)
+    if solve is not None:
+        line["solve"] = solve
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        v, dt, Es = cpu_baseline(args.cpu_sample_n, threads)
+        line["cpu_baseline"] = {"value": v, "unit": "elements/s", "cores": threads, "kind": "port",
+                                "sample": f"{args.cpu_sample_n}^3 = {Es} elements, one assembly ({dt:.2f} s)"}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gfe(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

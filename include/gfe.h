@@ -1,0 +1,153 @@
+/* gfe.h -- C ABI of the GB300 finite-element assembly engine (libgfe.so).
+ *
+ * The engine replaces OpenCMISS-Iron's element-loop hot path: the Gauss-point stiffness /
+ * residual / Jacobian evaluation and its scatter into compressed-row storage.  Each entry point
+ * below is a batched, whole-mesh equivalent of an Iron routine that loops over elements one at a
+ * time; the citation beside each names the Iron routine (file:line, relative to the Iron source
+ * tree) it stands in for.
+ *
+ * Conventions
+ *  - Every function returns an int status: GFE_OK (0) or a negative GFE_ERR_* code.  The message
+ *    of the last failure on the calling host thread is copied out by gfe_last_error().  This
+ *    mirrors Iron's (err, error) pair and cmfe_ExtractErrorMessage (src/opencmiss_iron.F90:13159).
+ *  - Array arguments are DEVICE pointers unless their name ends in _host.
+ *  - Node, element and DOF numbers are 0-based in element/connectivity arrays; the CSR structure
+ *    row_ptr / col_idx is 1-based, exactly as Iron stores it (src/types.F90:909-929).
+ *  - Nodal field parameters are in Iron's separated-component order: all DOFs of component 1,
+ *    then component 2, ... (src/field_routines.F90:10050-10060).
+ *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy default stream.  All work is
+ *    stream-ordered; functions that must report a count to the host synchronise that stream.
+ *  - Element connectivity uses Iron's local node order (xi1 fastest,
+ *    src/basis_routines.F90:3243-3370).
+ */
+#ifndef GFE_H
+#define GFE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GFE_OK 0
+#define GFE_ERR_ARG (-1)       /* invalid argument (sizes, null pointers, unsupported option) */
+#define GFE_ERR_CUDA (-2)      /* a CUDA runtime call failed */
+#define GFE_ERR_STRUCTURE (-3) /* an element entry has no slot in the CSR structure */
+#define GFE_ERR_NUMERIC (-4)   /* non-finite value, non-positive Jacobian, or breakdown */
+#define GFE_ERR_NOCONV (-5)    /* iterative solve did not reach its tolerance */
+#define GFE_ERR_TIMEOUT (-6)   /* a bounded device-side wait ran out */
+#define GFE_ERR_NOMEM (-7)     /* device allocation failed or an admission budget was exceeded */
+
+/* precision selectors */
+#define GFE_FP64 0  /* plain: element arithmetic and storage in FP64 */
+#define GFE_MIXED 1 /* FP32 element arithmetic, FP64 accumulation */
+
+/* ---- library -------------------------------------------------------------------------- */
+
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+int gfe_version(void);
+
+/* Copy the last error message of this host thread into buf (NUL-terminated, truncated to len).
+ * Returns the message length.  Replaces cmfe_ExtractErrorMessage (src/opencmiss_iron.F90:13159). */
+int gfe_last_error(char* buf, int len);
+
+/* Read and clear the device error word (bit set of GFE_DEVERR_* raised by kernels). */
+int gfe_device_errors(uint32_t* bits_host, void* stream);
+
+#define GFE_DEVERR_SLOT 1u     /* CSR slot not found during a scatter */
+#define GFE_DEVERR_JACOBIAN 2u /* non-positive Jacobian / det(F) at a Gauss point */
+#define GFE_DEVERR_NONFINITE 4u
+#define GFE_DEVERR_TIMEOUT 8u
+
+/* ---- stage timing ------------------------------------------------------------------------ */
+
+/* When enabled, entry points record CUDA events on their stream around the kernels of each
+ * stage below; gfe_profile_read() waits for the recorded events and returns the summed device
+ * time (ms) and the number of kernel launches of a stage since the last reset.  Off by default.
+ * Plays the role of Iron's per-assembly timing output (src/equations_set_routines.F90:1239-1353). */
+#define GFE_STAGE_LAPLACE_ELEMENTS 0 /* element + scatter kernels of gfe_laplace_assemble */
+#define GFE_STAGE_SPMV 1             /* SpMV kernels of the CG solver */
+#define GFE_STAGE_MR_RESIDUAL 2
+#define GFE_STAGE_MR_JACOBIAN 3
+#define GFE_STAGE_COUNT 8
+int gfe_profile_enable(int on);
+int gfe_profile_read(int stage, double* ms_host, int64_t* launches_host, int reset);
+
+/* Diagnostic: runs a dependent fused-multiply-add chain on every SM and reports the device's
+ * sustained arithmetic rate in GFLOP/s (2 flops per FMA) for precision GFE_FP64 or GFE_MIXED
+ * (FP32).  Used as the FP64 / FP32 pipe roof of the element kernels. */
+int gfe_probe_fma_rate(int32_t precision, double* gflops_host, void* stream);
+
+/* ---- CSR structure (K3) ------------------------------------------------------------------ */
+
+/* Compressed-row sparsity of an FEM matrix whose rows and columns are the DOFs of one field
+ * variable.  Replaces EquationsMatrix_StructureCalculate / JacobianMatrix_StructureCalculate
+ * (src/equations_matrices_routines.F90:4316-4602, :4609-4948): for every row DOF, the union of all
+ * DOFs of all elements that contain it, sorted ascending, unique, 1-based.
+ *  elem_dofs  [n_elem][dofs_per_elem] 0-based DOF numbers of each element (all components)
+ *  row_ptr    [n_dofs+1] out, 1-based
+ *  col_idx    [col_capacity] out, 1-based; may be NULL to query nnz only
+ *  nnz_host   out: number of structural non-zeros
+ * Synchronises `stream`.  Allocates and frees its scratch on `stream`. */
+int gfe_csr_structure(int32_t n_elem, int32_t dofs_per_elem, const int32_t* elem_dofs, int32_t n_dofs,
+                      int32_t* row_ptr, int32_t* col_idx, int64_t col_capacity, int64_t* nnz_host, void* stream);
+
+/* ---- Laplace / diffusion assembly (K1 + K2) -------------------------------------------- */
+
+/* Assemble the global stiffness matrix of the Laplace equation on trilinear-Lagrange hexahedra
+ * with 2x2x2 Gauss quadrature into a fixed CSR structure, and zero the RHS.
+ * Replaces the element loop of EquationsSet_AssembleStaticLinearFEM
+ * (src/equations_set_routines.F90:1203-1364) around LaplaceEquation_FiniteElementCalculate
+ * (src/Laplace_equations_routines.F90:433-747, standard and generalised-isotropic subtypes) and
+ * EquationsMatrices_ElementAdd -> MATRIX_VALUES_ADD_DP2 (src/equations_matrices_routines.F90:1140-1265,
+ * src/matrix_vector.F90:3202-3240).
+ *  elem_nodes   [n_elem][8] 0-based node numbers (Iron local node order)
+ *  coords       [3][n_nodes] geometric field, separated components
+ *  kappa        [n_elem] element conductivity (generalised subtype, isotropic) or NULL (standard)
+ *  color_elems  [n_elem] element numbers grouped by colour: no two elements of one colour share a node
+ *  color_ptr_host [n_colors+1] host offsets into color_elems
+ *  row_ptr/col_idx  CSR structure from gfe_csr_structure (1-based), nnz entries
+ *  values       [nnz] out: assembled matrix (FP64)
+ *  values32     [nnz] optional out (may be NULL): FP32 copy of the matrix for mixed-precision solves
+ *  rhs          [n_nodes] optional out (may be NULL): zeroed RHS vector
+ *  precision    GFE_FP64 or GFE_MIXED
+ * The scatter is deterministic: colours are processed in order and each CSR entry receives at
+ * most one addition per colour.  Asynchronous: device-side failures (missing CSR slot, degenerate
+ * element) are reported through gfe_device_errors(). */
+int gfe_laplace_assemble(int32_t n_elem, int32_t n_nodes, const int32_t* elem_nodes, const double* coords,
+                         const double* kappa, const int32_t* color_elems, const int32_t* color_ptr_host,
+                         int32_t n_colors, const int32_t* row_ptr, const int32_t* col_idx, int64_t nnz,
+                         double* values, float* values32, double* rhs, int32_t precision, void* stream);
+
+/* Element matrices only (no scatter): K_out[n_elem][8][8] row-major, for parity checks of the
+ * element routine itself (LaplaceEquation_FiniteElementCalculate). */
+int gfe_laplace_element_matrices(int32_t n_elem, int32_t n_nodes, const int32_t* elem_nodes, const double* coords,
+                                 const double* kappa, double* K_out, int32_t precision, void* stream);
+
+/* ---- linear solve (K7) ------------------------------------------------------------------ */
+
+/* y = A x on the rows with fixed[i] == 0; y[i] = 0 on fixed rows.  fixed may be NULL. */
+int gfe_csr_spmv(int32_t n_rows, const int32_t* row_ptr, const int32_t* col_idx, const double* values,
+                 const double* x, double* y, const uint8_t* fixed, void* stream);
+
+/* Solve K x = f with Dirichlet conditions x[i] = x_in[i] where fixed[i] != 0, by
+ * Jacobi-preconditioned conjugate gradients on the Dirichlet-eliminated system (the solver
+ * matrix of SOLVER_MATRICES_STATIC_ASSEMBLE, src/solver_routines.F90:14025-15050, solved by
+ * PETSc KSP in Iron, src/solver_routines.F90:11775-11991).
+ *  f          [n] right-hand side (may be NULL = zero)
+ *  x          [n] in: Dirichlet values on fixed DOFs; out: solution
+ *  values32   optional FP32 copy of values: when given and precision == GFE_MIXED, runs
+ *             FP64-residual iterative refinement around FP32 inner CG solves
+ *  rtol       relative residual target ||f - K x|| / ||f - K x0||
+ *  iters_host out: total (inner) iterations;  rel_host out: final relative FP64 residual
+ * Synchronises `stream`.  Allocates and frees its scratch on `stream`. */
+int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const double* values,
+                 const float* values32, const double* f, const uint8_t* fixed, double* x, double rtol,
+                 int32_t max_iters, int32_t precision, int32_t* iters_host, double* rel_host, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GFE_H */

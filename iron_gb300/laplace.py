@@ -1,0 +1,140 @@
+"""Laplace / diffusion assembly and solve on the GPU (the classical-field half of the hot path).
+
+`LaplaceAssembly` owns, for one mesh, the device-resident connectivity, geometry, colouring and
+the Iron-identical CSR structure, and assembles the global stiffness matrix with libgfe's fused
+element + scatter kernels.  It stands in for EquationsSet_AssembleStaticLinearFEM
+(src/equations_set_routines.F90:1203-1364) for the Laplace equations set; `solve` stands in for
+the static linear solve (src/problem_routines.F90:2533 -> PETSc KSP).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import GFE_FP64, GFE_MIXED, GfeError
+
+PRECISIONS = {"fp64": GFE_FP64, "mixed": GFE_MIXED}
+
+
+def csr_structure(elem_dofs: torch.Tensor, n_dofs: int, stream=None):
+    """Iron-identical CSR structure (1-based) of an FEM matrix on the GPU.  K3."""
+    elem_dofs = elem_dofs.to(torch.int32).contiguous()
+    E, ndpe = elem_dofs.shape
+    dev = elem_dofs.device
+    rp = torch.empty(n_dofs + 1, dtype=torch.int32, device=dev)
+    nnz = C.c_int64(0)
+    st = _lib.stream_handle(stream)
+    _lib.call("gfe_csr_structure", E, ndpe, _lib.ptr(elem_dofs), n_dofs, _lib.ptr(rp), None, 0, C.byref(nnz), st)
+    ci = torch.empty(max(int(nnz.value), 1), dtype=torch.int32, device=dev)
+    _lib.call("gfe_csr_structure", E, ndpe, _lib.ptr(elem_dofs), n_dofs, _lib.ptr(rp), _lib.ptr(ci),
+              int(ci.numel()), C.byref(nnz), st)
+    return rp, ci[: int(nnz.value)]
+
+
+@dataclass
+class SolveInfo:
+    iterations: int
+    relative_residual: float
+    precision: str
+
+
+class LaplaceAssembly:
+    """Device-resident Laplace problem on a trilinear hexahedral mesh.
+
+    elem_nodes: [E][8] int (0-based, Iron local node order); coords: [3][N] float64;
+    kappa: [E] element conductivity or None (standard Laplace subtype);
+    colour_elems / colour_ptr: an element colouring (elements of one colour share no node).
+    """
+
+    def __init__(self, elem_nodes, coords, kappa=None, colour_elems=None, colour_ptr=None, device=None,
+                 structure=None):
+        dev = device if device is not None else _lib.require_cuda()
+        _lib.load()
+        self.device = torch.device(dev)
+        en = np.ascontiguousarray(elem_nodes, dtype=np.int32)
+        if en.ndim != 2 or en.shape[1] != 8:
+            raise GfeError(-1, "trilinear hexahedra need [E][8] connectivity")
+        xyz = np.ascontiguousarray(coords, dtype=np.float64)
+        if xyz.ndim != 2 or xyz.shape[0] != 3:
+            raise GfeError(-1, "coords must be [3][N] (separated components)")
+        self.n_elements = en.shape[0]
+        self.n_nodes = xyz.shape[1]
+        if en.size and (en.min() < 0 or en.max() >= self.n_nodes):
+            raise GfeError(-1, "connectivity refers to a node outside coords")
+        if colour_elems is None:
+            from .mesh import greedy_colouring
+            colour_elems, colour_ptr = greedy_colouring(en, self.n_nodes)
+        self.colour_ptr = np.ascontiguousarray(colour_ptr, dtype=np.int32)
+        self.elem_nodes = torch.from_numpy(en).to(self.device)
+        self.coords = torch.from_numpy(xyz).to(self.device)
+        self.kappa = None if kappa is None else torch.as_tensor(np.asarray(kappa, np.float64)).to(self.device)
+        self.colour_elems = torch.from_numpy(np.ascontiguousarray(colour_elems, dtype=np.int32)).to(self.device)
+        if structure is None:
+            self.row_ptr, self.col_idx = csr_structure(self.elem_nodes, self.n_nodes)
+        else:
+            self.row_ptr, self.col_idx = structure
+        self.nnz = int(self.col_idx.numel())
+        self.values = torch.empty(self.nnz, dtype=torch.float64, device=self.device)
+        self.values32 = None
+        self.rhs = torch.empty(self.n_nodes, dtype=torch.float64, device=self.device)
+
+    @classmethod
+    def from_regular_mesh(cls, mesh, kappa=None, device=None):
+        order, ptr = mesh.colouring()
+        return cls(mesh.elem_nodes, mesh.coords, kappa=kappa, colour_elems=order, colour_ptr=ptr, device=device)
+
+    def assemble(self, precision: str = "fp64", stream=None, check: bool = True) -> torch.Tensor:
+        """Assemble K (FP64 values in self.values); mixed precision also fills self.values32."""
+        prec = PRECISIONS[precision]
+        if prec == GFE_MIXED and self.values32 is None:
+            self.values32 = torch.empty(self.nnz, dtype=torch.float32, device=self.device)
+        v32 = self.values32 if prec == GFE_MIXED else None
+        cp = self.colour_ptr
+        _lib.call("gfe_laplace_assemble", self.n_elements, self.n_nodes, _lib.ptr(self.elem_nodes),
+                  _lib.ptr(self.coords), _lib.ptr(self.kappa), _lib.ptr(self.colour_elems),
+                  cp.ctypes.data_as(C.c_void_p), len(cp) - 1, _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx),
+                  self.nnz, _lib.ptr(self.values), _lib.ptr(v32), _lib.ptr(self.rhs), prec,
+                  _lib.stream_handle(stream))
+        if check:
+            _lib.raise_device_errors("gfe_laplace_assemble", stream)
+        return self.values
+
+    def element_matrices(self, precision: str = "fp64", stream=None) -> torch.Tensor:
+        K = torch.empty((self.n_elements, 8, 8), dtype=torch.float64, device=self.device)
+        _lib.call("gfe_laplace_element_matrices", self.n_elements, self.n_nodes, _lib.ptr(self.elem_nodes),
+                  _lib.ptr(self.coords), _lib.ptr(self.kappa), _lib.ptr(K), PRECISIONS[precision],
+                  _lib.stream_handle(stream))
+        return K
+
+    def spmv(self, x: torch.Tensor, fixed: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        y = torch.empty_like(x)
+        _lib.call("gfe_csr_spmv", self.n_nodes, _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx),
+                  _lib.ptr(self.values), _lib.ptr(x.contiguous()), _lib.ptr(y), _lib.ptr(fixed),
+                  _lib.stream_handle(stream))
+        return y
+
+    def solve(self, fixed: torch.Tensor, x: torch.Tensor, f: torch.Tensor | None = None, rtol: float = 1e-12,
+              max_iters: int = 200000, precision: str = "fp64", stream=None) -> SolveInfo:
+        """Solve K x = f with x fixed (Dirichlet) where fixed != 0; x holds the fixed values on
+        entry and the solution on exit."""
+        prec = PRECISIONS[precision]
+        if prec == GFE_MIXED and self.values32 is None:
+            raise GfeError(-1, "mixed-precision solve needs assemble(precision='mixed') first")
+        fixed = fixed.to(device=self.device, dtype=torch.uint8).contiguous()
+        it = C.c_int32(0)
+        rel = C.c_double(0.0)
+        _lib.call("gfe_cg_solve", self.n_nodes, _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx),
+                  _lib.ptr(self.values), _lib.ptr(self.values32 if prec == GFE_MIXED else None), _lib.ptr(f),
+                  _lib.ptr(fixed), _lib.ptr(x), float(rtol), int(max_iters), prec, C.byref(it), C.byref(rel),
+                  _lib.stream_handle(stream))
+        return SolveInfo(int(it.value), float(rel.value), precision)
+
+    def to_iron_csr(self):
+        """Host copy of the CSR matrix exactly as Iron stores it: (row_ptr 1-based, col_idx 1-based,
+        values).  Analogue of cmfe_DistributedMatrix_StorageLocationsGet / DataGet
+        (src/opencmiss_iron.F90:45823, :45903)."""
+        return (self.row_ptr.cpu().numpy(), self.col_idx.cpu().numpy(), self.values.cpu().numpy())

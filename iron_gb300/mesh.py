@@ -1,0 +1,161 @@
+"""Regular generated hexahedral meshes with Iron's numbering, plus the element colouring the
+deterministic scatter needs.
+
+Numbering follows Iron's generated regular mesh (src/generated_mesh_routines.F90:1568-1640):
+nodes are numbered xi1 fastest over the grid of the first basis; elements are numbered xi1
+fastest; the element's local nodes are xi1 fastest.  A second, linear mesh component of a
+quadratic mesh takes the corner nodes of each quadratic element
+(src/generated_mesh_routines.F90:4941-5100) and numbers its own nodes by ascending global node
+number (src/mesh_routines.F90:9159-9272).  Geometry: origin + index * extent / (nodes_xi - 1)
+(src/generated_mesh_routines.F90:3217-3383).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+def _grid_nodes(nelem, order):
+    return [order * n + 1 for n in nelem]
+
+
+def regular_elements(nelem, order: int) -> np.ndarray:
+    """elem_nodes[E][(order+1)^3] (0-based) of a 3D regular mesh of Lagrange order 1 or 2."""
+    nx, ny, nz = nelem
+    tx, ty, _ = _grid_nodes(nelem, order)
+    e1, e2, e3 = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    # element numbering xi1 fastest -> flatten with e1 fastest
+    e1 = e1.transpose(2, 1, 0).reshape(-1)
+    e2 = e2.transpose(2, 1, 0).reshape(-1)
+    e3 = e3.transpose(2, 1, 0).reshape(-1)
+    first = e1 * order + e2 * order * tx + e3 * order * tx * ty
+    a = np.arange(order + 1)
+    a1, a2, a3 = np.meshgrid(a, a, a, indexing="ij")
+    off = (a1 + a2 * tx + a3 * tx * ty).transpose(2, 1, 0).reshape(-1)  # local nodes xi1 fastest
+    return (first[:, None] + off[None, :]).astype(np.int32)
+
+
+def regular_coords(nelem, order: int, origin=(0.0, 0.0, 0.0), extent=(1.0, 1.0, 1.0)) -> np.ndarray:
+    """coords[3][N] in separated component order."""
+    tx, ty, tz = _grid_nodes(nelem, order)
+    i = np.arange(tx, dtype=np.float64)
+    j = np.arange(ty, dtype=np.float64)
+    k = np.arange(tz, dtype=np.float64)
+    out = np.empty((3, tx * ty * tz))
+    K, J, I = np.meshgrid(k, j, i, indexing="ij")
+    out[0] = (origin[0] + I * (extent[0] / (tx - 1))).reshape(-1)
+    out[1] = (origin[1] + J * (extent[1] / (ty - 1))).reshape(-1)
+    out[2] = (origin[2] + K * (extent[2] / (tz - 1))).reshape(-1)
+    return out
+
+
+def linear_component(elem_first: np.ndarray, order_first: int):
+    """Corner (trilinear) component of a higher-order mesh.
+
+    Returns (elem_lin[E][8] in component-local numbers, lin_to_global[n_lin])."""
+    n = order_first
+    corners = [a1 + (n + 1) * (a2 + (n + 1) * a3) for a3 in (0, n) for a2 in (0, n) for a1 in (0, n)]
+    c = elem_first[:, corners]
+    glob, inv = np.unique(c.reshape(-1), return_inverse=True)
+    return inv.reshape(c.shape).astype(np.int32), glob.astype(np.int32)
+
+
+def boundary_node_mask(nelem, order: int) -> np.ndarray:
+    tx, ty, tz = _grid_nodes(nelem, order)
+    K, J, I = np.meshgrid(np.arange(tz), np.arange(ty), np.arange(tx), indexing="ij")
+    b = (I == 0) | (I == tx - 1) | (J == 0) | (J == ty - 1) | (K == 0) | (K == tz - 1)
+    return b.reshape(-1)
+
+
+def parity_colouring(nelem):
+    """8-colour element colouring of a regular hex mesh: colour = parity of (e1, e2, e3).
+
+    Elements of one colour share no node.  Returns (colour_elems[E], colour_ptr[9])."""
+    nx, ny, nz = nelem
+    e = np.arange(nx * ny * nz)
+    e1, e2, e3 = e % nx, (e // nx) % ny, e // (nx * ny)
+    col = (e1 & 1) + 2 * (e2 & 1) + 4 * (e3 & 1)
+    order = np.argsort(col, kind="stable").astype(np.int32)
+    ptr = np.zeros(9, np.int32)
+    np.cumsum(np.bincount(col, minlength=8), out=ptr[1:])
+    return order, ptr
+
+
+def greedy_colouring(elem_nodes: np.ndarray, n_nodes: int, max_colours: int = 64):
+    """Greedy element colouring for an arbitrary mesh (elements in order, lowest free colour).
+
+    Elements of one colour share no node.  Returns (colour_elems, colour_ptr)."""
+    used = np.zeros(n_nodes, np.uint64)
+    E = elem_nodes.shape[0]
+    col = np.empty(E, np.int64)
+    for e in range(E):
+        nodes = elem_nodes[e]
+        mask = np.bitwise_or.reduce(used[nodes])
+        c = 0
+        while (int(mask) >> c) & 1:
+            c += 1
+        if c >= max_colours:
+            raise ValueError("mesh needs more than 64 colours")
+        col[e] = c
+        used[nodes] |= np.uint64(1 << c)
+    nc = int(col.max()) + 1 if E else 1
+    order = np.argsort(col, kind="stable").astype(np.int32)
+    ptr = np.zeros(nc + 1, np.int32)
+    np.cumsum(np.bincount(col, minlength=nc), out=ptr[1:])
+    return order, ptr
+
+
+@dataclass
+class RegularMesh:
+    """A generated regular hex mesh on a box (Iron's GENERATED_MESH_REGULAR_TYPE)."""
+
+    nelem: tuple
+    order: int = 1
+    origin: tuple = (0.0, 0.0, 0.0)
+    extent: tuple = (1.0, 1.0, 1.0)
+    elem_nodes: np.ndarray = field(init=False)
+    coords: np.ndarray = field(init=False)
+
+    def __post_init__(self):
+        self.nelem = tuple(int(n) for n in self.nelem)
+        self.elem_nodes = regular_elements(self.nelem, self.order)
+        self.coords = regular_coords(self.nelem, self.order, self.origin, self.extent)
+
+    @property
+    def n_elements(self) -> int:
+        return int(np.prod(self.nelem))
+
+    @property
+    def n_nodes(self) -> int:
+        return self.coords.shape[1]
+
+    @property
+    def nodes_xi(self):
+        return _grid_nodes(self.nelem, self.order)
+
+    def h(self):
+        return np.array(self.extent, dtype=np.float64) / np.array(self.nelem)
+
+    def jitter_interior(self, seed: int, fraction: float = 0.1) -> None:
+        """Move every interior node uniformly within +-fraction*h per coordinate (seeded)."""
+        rng = np.random.default_rng(seed)
+        hh = self.h() / self.order if self.order > 1 else self.h()
+        d = rng.uniform(-1.0, 1.0, size=self.coords.shape) * (fraction * hh)[:, None]
+        d[:, boundary_node_mask(self.nelem, self.order)] = 0.0
+        self.coords = self.coords + d
+
+    def colouring(self):
+        return parity_colouring(self.nelem)
+
+    def node_index(self, i, j, k):
+        tx, ty, _ = self.nodes_xi
+        return i + tx * (j + ty * k)
+
+    def face_nodes(self, axis: int, side: int) -> np.ndarray:
+        """Nodes on the face axis = 0 (side 0) or axis = max (side 1)."""
+        tx, ty, tz = self.nodes_xi
+        K, J, I = np.meshgrid(np.arange(tz), np.arange(ty), np.arange(tx), indexing="ij")
+        idx = (I, J, K)[axis]
+        lim = (tx, ty, tz)[axis] - 1
+        return np.nonzero((idx == (0 if side == 0 else lim)).reshape(-1))[0].astype(np.int64)

@@ -1,0 +1,178 @@
+"""Parity oracle: ctypes bindings of the C++ restatement of Iron's FE assembly hot path.
+
+TEST INFRASTRUCTURE ONLY.  Imported by tests/, __graft_entry__.smoke() and the CPU-baseline
+leg of bench.py as the checker; the product package iron_gb300 never imports it.
+
+Parity pins: see tests/test_oracle_golden.py (Iron's analytic-Laplace fixture, known-answer
+tests).  The linear solve (PETSc KSP in Iron) is not restated and is parity-unpinned.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+_HERE = Path(__file__).resolve().parent
+_lib = None
+
+i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(str(path))
+        L.orc_gauss_legendre.argtypes = [C.c_int, f64p, f64p]
+        L.orc_tp_basis.argtypes = [C.c_int, i32p, i32p, C.c_void_p, C.c_void_p]
+        L.orc_regular_mesh.argtypes = [C.c_int, i32p, C.c_int, i32p]
+        L.orc_regular_coords.argtypes = [C.c_int, i32p, C.c_int, f64p, f64p, f64p]
+        L.orc_linear_component.argtypes = [C.c_int, C.c_int, C.c_int, i32p, i32p, i32p, i32p]
+        L.orc_csr_structure.argtypes = [C.c_int, C.c_int, i32p, C.c_int, C.c_void_p, C.c_void_p]
+        L.orc_csr_structure.restype = C.c_int64
+        L.orc_csr_location.argtypes = [i32p, i32p, C.c_int, C.c_int]
+        L.orc_csr_location.restype = C.c_int64
+        L.orc_laplace_element.argtypes = [C.c_int, i32p, i32p, C.c_int, f64p, C.c_double, f64p]
+        L.orc_laplace_assemble.argtypes = [C.c_int, i32p, i32p, C.c_int, C.c_int, i32p, f64p, C.c_void_p,
+                                           i32p, i32p, f64p, C.c_void_p, C.c_int]
+        L.orc_csr_spmv.argtypes = [C.c_int, i32p, i32p, f64p, f64p, f64p]
+        L.orc_cg_dirichlet.argtypes = [C.c_int, i32p, i32p, f64p, C.c_void_p, u8p, f64p, C.c_double, C.c_int,
+                                       C.POINTER(C.c_double)]
+        _register_mr(L)
+        _lib = L
+    return _lib
+
+
+def _register_mr(L):
+    """Bindings of the finite-elasticity part (present once the oracle provides it)."""
+    if hasattr(L, "orc_mr_element_residual"):
+        L.orc_mr_element_residual.argtypes = [f64p, f64p, f64p, C.c_double, C.c_double, f64p]
+        L.orc_mr_element_residual.restype = C.c_int
+    if hasattr(L, "orc_mr_element_jacobian"):
+        L.orc_mr_element_jacobian.argtypes = [f64p, f64p, f64p, C.c_double, C.c_double, f64p]
+        L.orc_mr_element_jacobian.restype = C.c_int
+    if hasattr(L, "orc_mr_element_jacobian_fd"):
+        L.orc_mr_element_jacobian_fd.argtypes = [f64p, f64p, f64p, C.c_double, C.c_double, C.c_double, f64p]
+        L.orc_mr_element_jacobian_fd.restype = C.c_int
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def gauss_legendre(n: int):
+    x = np.zeros(n)
+    w = np.zeros(n)
+    if lib().orc_gauss_legendre(n, x, w) != 0:
+        raise ValueError(n)
+    return x, w
+
+
+def tp_basis(nxi: int, order, ngauss):
+    order = _i32(order)
+    ngauss = _i32(ngauss)
+    code = lib().orc_tp_basis(nxi, order, ngauss, None, None)
+    if code < 0:
+        raise ValueError("bad basis")
+    nns, ng = divmod(code, 1000)
+    tab = np.zeros((ng, nxi + 1, nns))
+    wts = np.zeros(ng)
+    lib().orc_tp_basis(nxi, order, ngauss, tab.ctypes.data, wts.ctypes.data)
+    return tab, wts
+
+
+def regular_mesh(nelem, order: int):
+    nelem = _i32(nelem)
+    nxi = len(nelem)
+    E = int(np.prod(nelem))
+    out = np.zeros((E, (order + 1) ** nxi), np.int32)
+    lib().orc_regular_mesh(nxi, nelem, order, out)
+    return out
+
+
+def regular_coords(nelem, order: int, origin, extent):
+    nelem = _i32(nelem)
+    nxi = len(nelem)
+    N = int(np.prod(order * nelem + 1))
+    out = np.zeros((nxi, N))
+    lib().orc_regular_coords(nxi, nelem, order, _f64(origin), _f64(extent), out)
+    return out
+
+
+def linear_component(elem_first, nnx_first):
+    elem_first = _i32(elem_first)
+    nnx = _i32(list(nnx_first) + [1] * (3 - len(nnx_first)))
+    nxi = len(nnx_first)
+    E, nns = elem_first.shape
+    elem_lin = np.zeros((E, 2 ** nxi), np.int32)
+    l2g = np.zeros(E * 2 ** nxi, np.int32)
+    n_lin = lib().orc_linear_component(nxi, E, nns, nnx, elem_first, elem_lin, l2g)
+    return elem_lin, l2g[:n_lin].copy()
+
+
+def csr_structure(elem_dofs, n_dofs: int):
+    elem_dofs = _i32(elem_dofs)
+    E, ndpe = elem_dofs.shape
+    nnz = lib().orc_csr_structure(E, ndpe, elem_dofs, n_dofs, None, None)
+    rp = np.zeros(n_dofs + 1, np.int32)
+    ci = np.zeros(nnz, np.int32)
+    lib().orc_csr_structure(E, ndpe, elem_dofs, n_dofs, rp.ctypes.data, ci.ctypes.data)
+    return rp, ci
+
+
+def csr_location(rp, ci, row: int, col: int) -> int:
+    return int(lib().orc_csr_location(_i32(rp), _i32(ci), row, col))
+
+
+def laplace_element(nxi, order, ngauss, xe, kappa=1.0):
+    xe = _f64(xe)
+    nns = xe.shape[1]
+    K = np.zeros((nns, nns))
+    rc = lib().orc_laplace_element(nxi, _i32(order), _i32(ngauss), xe.shape[0], xe, float(kappa), K)
+    if rc != 0:
+        raise ValueError("bad element")
+    return K
+
+
+def laplace_assemble(nxi, order, ngauss, elem_nodes, coords, kappa, rp, ci, n_threads=1):
+    elem_nodes = _i32(elem_nodes)
+    coords = _f64(coords)
+    E = elem_nodes.shape[0]
+    N = coords.shape[1]
+    vals = np.zeros(int(rp[-1]) - 1)
+    rhs = np.zeros(N)
+    kap = None if kappa is None else _f64(kappa)
+    rc = lib().orc_laplace_assemble(nxi, _i32(order), _i32(ngauss), E, N, elem_nodes, coords,
+                                    None if kap is None else kap.ctypes.data, _i32(rp), _i32(ci), vals,
+                                    rhs.ctypes.data, n_threads)
+    if rc != 0:
+        raise RuntimeError(f"oracle assembly failed ({rc})")
+    return vals, rhs
+
+
+def spmv(rp, ci, vals, x):
+    n = len(rp) - 1
+    y = np.zeros(n)
+    lib().orc_csr_spmv(n, _i32(rp), _i32(ci), _f64(vals), _f64(x), y)
+    return y
+
+
+def cg_dirichlet(rp, ci, vals, f, fixed, x_fixed, rtol=1e-12, max_it=100000):
+    n = len(rp) - 1
+    x = _f64(x_fixed).copy()
+    rel = C.c_double(0.0)
+    fv = None if f is None else _f64(f)
+    it = lib().orc_cg_dirichlet(n, _i32(rp), _i32(ci), _f64(vals), None if fv is None else fv.ctypes.data,
+                                np.ascontiguousarray(fixed, dtype=np.uint8), x, rtol, max_it, C.byref(rel))
+    if it < 0:
+        raise RuntimeError("oracle CG did not converge")
+    return x, it, rel.value

@@ -1,0 +1,518 @@
+// gfe_oracle.cpp -- CPU restatement of OpenCMISS-Iron's finite-element assembly hot path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the parity oracle for the GB300 engine in
+// iron_gb300/: only tests, the smoke check and the CPU-baseline leg of bench.py load it.
+// The product path never links or calls it.
+//
+// Iron itself (Fortran 2003 + MPI + PETSc) cannot be built in this environment, so the
+// oracle restates Iron's algorithms routine by routine, citing the reference file:line
+// (paths relative to the reference project root) it follows.  It is pinned against the
+// reference's own fixtures and known-answer tests (tests/test_oracle_golden.py).
+//
+// Conventions: all node / element / DOF indices exchanged through this C ABI are 0-based;
+// the CSR structure is emitted 1-based exactly as Iron stores it
+// (src/types.F90:909-929, ROW_INDICES(M+1), COLUMN_INDICES(nnz)).
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <thread>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------------------------------
+// Quadrature.  src/basis_routines.F90:6804-6890 (Gauss_Legendre): tabulated closed forms of
+// the 1..4 point rules on [0,1].
+// ---------------------------------------------------------------------------------------
+bool gauss_legendre(int n, double* x, double* w) {
+  if (n < 1 || n > 4) return false;
+  const double s3 = std::sqrt(3.0), s06 = std::sqrt(0.6), s65 = std::sqrt(6.0 / 5.0), s30 = std::sqrt(30.0);
+  const double loc[10] = {0.5,
+                          (-1.0 / s3 + 1.0) / 2.0, (+1.0 / s3 + 1.0) / 2.0,
+                          (-s06 + 1.0) / 2.0, 0.5, (+s06 + 1.0) / 2.0,
+                          (-std::sqrt((3.0 + 2.0 * s65) / 7.0) + 1.0) / 2.0,
+                          (-std::sqrt((3.0 - 2.0 * s65) / 7.0) + 1.0) / 2.0,
+                          (+std::sqrt((3.0 - 2.0 * s65) / 7.0) + 1.0) / 2.0,
+                          (+std::sqrt((3.0 + 2.0 * s65) / 7.0) + 1.0) / 2.0};
+  const double wt[10] = {1.0, 0.5, 0.5, 2.5 / 9.0, 4.0 / 9.0, 2.5 / 9.0,
+                         (18.0 - s30) / 72.0, (18.0 + s30) / 72.0, (18.0 + s30) / 72.0, (18.0 - s30) / 72.0};
+  const int start[4] = {0, 1, 3, 6};
+  for (int i = 0; i < n; ++i) {
+    x[i] = loc[start[n - 1] + i];
+    w[i] = wt[start[n - 1] + i];
+  }
+  return true;
+}
+
+// 1D Lagrange basis on [0,1]; node index a is 0-based.  deriv 0 = value, 1 = first derivative.
+// src/basis_routines.F90:7969-8020 (LAGRANGE_LINEAR_EVALUATE), :8027-8090 (QUADRATIC).
+double lagrange1d(int order, int a, int deriv, double xi) {
+  if (order == 1) {
+    if (deriv == 0) return a == 0 ? 1.0 - xi : xi;
+    return a == 0 ? -1.0 : 1.0;
+  }
+  if (order == 2) {
+    if (deriv == 0) {
+      if (a == 0) return 1.0 - 3.0 * xi + 2.0 * xi * xi;
+      if (a == 1) return 4.0 * xi * (1.0 - xi);
+      return xi * (xi + xi - 1.0);
+    }
+    if (a == 0) return 4.0 * xi - 3.0;
+    if (a == 1) return 4.0 - 8.0 * xi;
+    return 4.0 * xi - 1.0;
+  }
+  return 0.0;
+}
+
+// Tensor-product table in Iron's order: element parameter ns with xi1 fastest
+// (src/basis_routines.F90:3243-3370), Gauss point ng = i + (j-1 + (k-1) n2) n1 (:3820).
+// Layout of the returned table: tab[(ng * (nxi+1) + nu) * nns + ns], nu 0 = value,
+// nu = 1..nxi = d/dxi_nu (Iron's partial-derivative indices 2, 4, 7: src/constants.F90:180-185).
+struct TPBasis {
+  int nxi = 0, nns = 0, ng = 0;
+  int nnx[3] = {1, 1, 1}, ngx[3] = {1, 1, 1}, order[3] = {1, 1, 1};
+  std::vector<double> tab, wts;
+};
+
+bool make_tp_basis(int nxi, const int* order, const int* ngauss, TPBasis& b) {
+  if (nxi < 1 || nxi > 3) return false;
+  b.nxi = nxi;
+  b.nns = 1;
+  b.ng = 1;
+  double gx[3][4], gw[3][4];
+  for (int d = 0; d < 3; ++d) {
+    b.nnx[d] = 1; b.ngx[d] = 1; b.order[d] = 1;
+    gx[d][0] = 0.5; gw[d][0] = 1.0;
+  }
+  for (int d = 0; d < nxi; ++d) {
+    if (order[d] < 1 || order[d] > 2) return false;
+    b.order[d] = order[d];
+    b.nnx[d] = order[d] + 1;
+    b.ngx[d] = ngauss[d];
+    if (!gauss_legendre(ngauss[d], gx[d], gw[d])) return false;
+    b.nns *= b.nnx[d];
+    b.ng *= b.ngx[d];
+  }
+  b.tab.assign((size_t)b.ng * (nxi + 1) * b.nns, 0.0);
+  b.wts.assign(b.ng, 0.0);
+  for (int g3 = 0; g3 < b.ngx[2]; ++g3)
+    for (int g2 = 0; g2 < b.ngx[1]; ++g2)
+      for (int g1 = 0; g1 < b.ngx[0]; ++g1) {
+        int g = g1 + b.ngx[0] * (g2 + b.ngx[1] * g3);
+        const int gi[3] = {g1, g2, g3};
+        double w = 1.0;
+        for (int d = 0; d < nxi; ++d) w *= gw[d][gi[d]];
+        b.wts[g] = w;
+        for (int a3 = 0; a3 < b.nnx[2]; ++a3)
+          for (int a2 = 0; a2 < b.nnx[1]; ++a2)
+            for (int a1 = 0; a1 < b.nnx[0]; ++a1) {
+              int ns = a1 + b.nnx[0] * (a2 + b.nnx[1] * a3);
+              const int ai[3] = {a1, a2, a3};
+              for (int nu = 0; nu <= nxi; ++nu) {
+                double v = 1.0;
+                for (int d = 0; d < nxi; ++d) v *= lagrange1d(b.order[d], ai[d], (nu == d + 1) ? 1 : 0, gx[d][gi[d]]);
+                b.tab[((size_t)g * (nxi + 1) + nu) * b.nns + ns] = v;
+              }
+            }
+      }
+  return true;
+}
+
+// 3x3 / 2x2 inverse and determinant, src/maths.F90:2807-2868 (InvertFullDP).
+double invert(int n, const double A[3][3], double B[3][3]) {
+  double det;
+  if (n == 1) {
+    det = A[0][0];
+    B[0][0] = 1.0 / A[0][0];
+  } else if (n == 2) {
+    det = A[0][0] * A[1][1] - A[1][0] * A[0][1];
+    B[0][0] = A[1][1] / det; B[0][1] = -A[0][1] / det;
+    B[1][0] = -A[1][0] / det; B[1][1] = A[0][0] / det;
+  } else {
+    det = A[0][0] * A[1][1] * A[2][2] + A[0][1] * A[1][2] * A[2][0] + A[0][2] * A[1][0] * A[2][1] -
+          A[0][0] * A[2][1] * A[1][2] - A[1][0] * A[0][1] * A[2][2] - A[2][0] * A[1][1] * A[0][2];
+    B[0][0] = (A[1][1] * A[2][2] - A[2][1] * A[1][2]) / det;
+    B[1][0] = (A[1][2] * A[2][0] - A[2][2] * A[1][0]) / det;
+    B[2][0] = (A[1][0] * A[2][1] - A[2][0] * A[1][1]) / det;
+    B[0][1] = (A[2][1] * A[0][2] - A[0][1] * A[2][2]) / det;
+    B[1][1] = (A[2][2] * A[0][0] - A[0][2] * A[2][0]) / det;
+    B[2][1] = (A[2][0] * A[0][1] - A[0][0] * A[2][1]) / det;
+    B[0][2] = (A[0][1] * A[1][2] - A[1][1] * A[0][2]) / det;
+    B[1][2] = (A[0][2] * A[1][0] - A[1][2] * A[0][0]) / det;
+    B[2][2] = (A[0][0] * A[1][1] - A[1][0] * A[0][1]) / det;
+  }
+  return det;
+}
+
+// Metrics at one Gauss point for a rectangular-cartesian geometric field whose element
+// parameters are x[comp][ns] (separated component order).  src/coordinate_routines.F90:639-1026
+// (COORDINATE_METRICS_CALCULATE): DX_DXI from the interpolated first derivatives
+// (src/field_routines.F90:5771-5982 / src/basis_routines.F90:2075-2130), GL = DX_DXI^T DX_DXI,
+// GU = inv(GL), volume Jacobian = sqrt(|det GL|) (:818-822), DXI_DX = inv(DX_DXI) (:832).
+struct Metrics {
+  double dx_dxi[3][3], dxi_dx[3][3], gl[3][3], gu[3][3], jac;
+};
+
+void metrics_at(const TPBasis& b, int g, const double* const* x, int ncomp, Metrics& m) {
+  const int nxi = b.nxi;
+  std::memset(&m, 0, sizeof(m));
+  for (int i = 0; i < ncomp; ++i)
+    for (int xi = 0; xi < nxi; ++xi) {
+      double s = 0.0;
+      const double* t = &b.tab[((size_t)g * (nxi + 1) + xi + 1) * b.nns];
+      for (int ns = 0; ns < b.nns; ++ns) s += t[ns] * x[i][ns];
+      m.dx_dxi[i][xi] = s;
+    }
+  for (int mi = 0; mi < nxi; ++mi)
+    for (int ni = 0; ni < nxi; ++ni) {
+      double s = 0.0;
+      for (int i = 0; i < ncomp; ++i) s += m.dx_dxi[i][mi] * m.dx_dxi[i][ni];
+      m.gl[mi][ni] = s;
+    }
+  double detgl = invert(nxi, m.gl, m.gu);
+  m.jac = std::sqrt(std::fabs(detgl));
+  if (nxi == ncomp) invert(nxi, m.dx_dxi, m.dxi_dx);
+}
+
+// ---------------------------------------------------------------------------------------
+// CSR value add.  src/matrix_vector.F90:3202-3240 (MATRIX_VALUES_ADD_DP2, compressed-row
+// branch): bisection over the row's sorted columns until the window is <= 10 wide
+// (bisectionToLinearSearchThreshold, :184), then a linear scan; error when absent.
+// row/col indices here are 1-based like Iron's.
+// ---------------------------------------------------------------------------------------
+const int kBisectionToLinear = 10;
+
+int csr_values_add(const int32_t* rp, const int32_t* ci, double* data, int nr, const int32_t* rows, int nc,
+                   const int32_t* cols, const double* vals /* [nr][nc] row-major */) {
+  int prev = -1;
+  for (int i = 0; i < nr; ++i) {
+    int row = rows[i];
+    int lo = rp[row - 1], up = rp[row];
+    for (int j = 0; j < nc; ++j) {
+      int loc = 0, col = cols[j];
+      if (col <= prev) lo = rp[row - 1]; else up = rp[row];
+      prev = col;
+      while (up - lo > kBisectionToLinear) {
+        int mid = (up + lo) / 2;
+        if (ci[mid - 1] > col) up = mid; else lo = mid;
+      }
+      for (int k = lo; k <= up && k < rp[row]; ++k) {
+        if (ci[k - 1] == col) { loc = k; lo = k + 1; break; }
+      }
+      if (loc == 0) return -1;
+      data[loc - 1] += vals[(size_t)i * nc + j];
+    }
+  }
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---------------------------------------------------------------------------------------
+// Tables
+// ---------------------------------------------------------------------------------------
+int orc_gauss_legendre(int n, double* x, double* w) { return gauss_legendre(n, x, w) ? 0 : -1; }
+
+// tab: [ng][nxi+1][nns], wts: [ng].  Returns nns*1000+ng on success so callers can size arrays
+// (call with tab == nullptr first).
+int orc_tp_basis(int nxi, const int* order, const int* ngauss, double* tab, double* wts) {
+  TPBasis b;
+  if (!make_tp_basis(nxi, order, ngauss, b)) return -1;
+  if (tab) std::memcpy(tab, b.tab.data(), b.tab.size() * sizeof(double));
+  if (wts) std::memcpy(wts, b.wts.data(), b.wts.size() * sizeof(double));
+  return b.nns * 1000 + b.ng;
+}
+
+// ---------------------------------------------------------------------------------------
+// Regular generated mesh.  src/generated_mesh_routines.F90:1568-1640: elements stepped
+// xi1 fastest; first element node np = 1+(ne1-1)(nn1-1)+(ne2-1)NX(nn2-1)+(ne3-1)NX NY(nn3-1);
+// element nodes xi1 fastest.  Output 0-based node numbers, elem_nodes[E][nns].
+// ---------------------------------------------------------------------------------------
+int orc_regular_mesh(int nxi, const int* nelem, int order, int32_t* elem_nodes) {
+  int ne[3] = {1, 1, 1}, nnx[3] = {1, 1, 1}, tot[3] = {1, 1, 1};
+  for (int d = 0; d < nxi; ++d) {
+    ne[d] = nelem[d];
+    nnx[d] = order + 1;
+    tot[d] = (nnx[d] - 1) * ne[d] + 1;
+  }
+  const int nns = nnx[0] * nnx[1] * nnx[2];
+  for (int e3 = 0; e3 < ne[2]; ++e3)
+    for (int e2 = 0; e2 < ne[1]; ++e2)
+      for (int e1 = 0; e1 < ne[0]; ++e1) {
+        int e = e1 + ne[0] * (e2 + ne[1] * e3);
+        int np = e1 * (nnx[0] - 1) + e2 * tot[0] * (nnx[1] - 1) + e3 * tot[0] * tot[1] * (nnx[2] - 1);
+        int nn = 0;
+        for (int a3 = 0; a3 < nnx[2]; ++a3)
+          for (int a2 = 0; a2 < nnx[1]; ++a2)
+            for (int a1 = 0; a1 < nnx[0]; ++a1)
+              elem_nodes[(size_t)e * nns + nn++] = np + a1 + a2 * tot[0] + a3 * tot[0] * tot[1];
+      }
+  return 0;
+}
+
+// Node coordinates of a regular mesh, separated layout coords[comp][N].
+// src/generated_mesh_routines.F90:3217-3383: value = origin + (position-1) * extent/(nodes_xi-1).
+int orc_regular_coords(int nxi, const int* nelem, int order, const double* origin, const double* extent,
+                       double* coords) {
+  int tot[3] = {1, 1, 1};
+  for (int d = 0; d < nxi; ++d) tot[d] = order * nelem[d] + 1;
+  const size_t N = (size_t)tot[0] * tot[1] * tot[2];
+  for (int k = 0; k < tot[2]; ++k)
+    for (int j = 0; j < tot[1]; ++j)
+      for (int i = 0; i < tot[0]; ++i) {
+        size_t n = i + (size_t)tot[0] * (j + (size_t)tot[1] * k);
+        const int p[3] = {i, j, k};
+        for (int c = 0; c < nxi; ++c) coords[c * N + n] = origin[c] + (double)p[c] * (extent[c] / (double)(tot[c] - 1));
+      }
+  return 0;
+}
+
+// Second (linear) mesh component of a mesh whose first basis is quadratic:
+// src/generated_mesh_routines.F90:4941-5100 takes the corner nodes' user numbers from the first
+// basis (GLOBAL_ELEMENT_NODES of the corner local nodes); the linear component's own node
+// numbers are the rank of those global numbers in ascending order
+// (src/mesh_routines.F90:9159-9272, tree of global nodes detached in order).
+// Outputs: elem_lin[E][2^nxi] (component-local 0-based numbers), lin_to_global[n_lin]
+// (0-based first-basis node), returns n_lin.
+int orc_linear_component(int nxi, int n_elem, int nns_first, const int* nnx_first, const int32_t* elem_first,
+                         int32_t* elem_lin, int32_t* lin_to_global) {
+  const int ncorner = 1 << nxi;
+  std::vector<int32_t> corners((size_t)n_elem * ncorner);
+  for (int e = 0; e < n_elem; ++e) {
+    int c = 0;
+    for (int b3 = 0; b3 < (nxi > 2 ? 2 : 1); ++b3)
+      for (int b2 = 0; b2 < (nxi > 1 ? 2 : 1); ++b2)
+        for (int b1 = 0; b1 < 2; ++b1) {
+          int a1 = b1 ? nnx_first[0] - 1 : 0;
+          int a2 = b2 ? nnx_first[1] - 1 : 0;
+          int a3 = b3 ? nnx_first[2] - 1 : 0;
+          int ns = a1 + nnx_first[0] * (a2 + nnx_first[1] * a3);
+          corners[(size_t)e * ncorner + c++] = elem_first[(size_t)e * nns_first + ns];
+        }
+  }
+  std::vector<int32_t> sorted(corners);
+  std::sort(sorted.begin(), sorted.end());
+  sorted.erase(std::unique(sorted.begin(), sorted.end()), sorted.end());
+  for (size_t i = 0; i < corners.size(); ++i)
+    elem_lin[i] = (int32_t)(std::lower_bound(sorted.begin(), sorted.end(), corners[i]) - sorted.begin());
+  if (lin_to_global) std::copy(sorted.begin(), sorted.end(), lin_to_global);
+  return (int)sorted.size();
+}
+
+// ---------------------------------------------------------------------------------------
+// CSR structure.  src/equations_matrices_routines.F90:4399-4457 (EquationsMatrix_StructureCalculate,
+// FEM + compressed-row): for each row DOF, loop the surrounding elements of its node and add
+// every DOF of every component of those elements; List_RemoveDuplicates sorts ascending and
+// removes duplicates (src/lists.F90:2652-2700); rowIndices(i+1) = nnz+1 (1-based).
+// Input: per-element DOF lists elem_dofs[E][ndpe] (0-based global DOF numbers; an element
+// "surrounds" a DOF's node exactly when the DOF is in its list).
+// Call with col_idx == nullptr to get nnz only.
+// ---------------------------------------------------------------------------------------
+int64_t orc_csr_structure(int n_elem, int ndpe, const int32_t* elem_dofs, int n_dofs, int32_t* row_ptr,
+                          int32_t* col_idx) {
+  std::vector<int64_t> cnt(n_dofs + 1, 0);
+  for (size_t i = 0; i < (size_t)n_elem * ndpe; ++i) cnt[elem_dofs[i] + 1]++;
+  for (int i = 0; i < n_dofs; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int32_t> dof_elems(cnt[n_dofs]);
+  std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+  for (int e = 0; e < n_elem; ++e)
+    for (int k = 0; k < ndpe; ++k) dof_elems[fill[elem_dofs[(size_t)e * ndpe + k]]++] = e;
+  int64_t nnz = 0;
+  std::vector<int32_t> list;
+  if (row_ptr) row_ptr[0] = 1;
+  for (int r = 0; r < n_dofs; ++r) {
+    list.clear();
+    for (int64_t s = cnt[r]; s < cnt[r + 1]; ++s) {
+      int e = dof_elems[s];
+      for (int k = 0; k < ndpe; ++k) list.push_back(elem_dofs[(size_t)e * ndpe + k] + 1);
+    }
+    std::sort(list.begin(), list.end());
+    list.erase(std::unique(list.begin(), list.end()), list.end());
+    if (col_idx) std::copy(list.begin(), list.end(), col_idx + nnz);
+    nnz += (int64_t)list.size();
+    if (row_ptr) row_ptr[r + 1] = (int32_t)(nnz + 1);
+  }
+  return nnz;
+}
+
+// Single CSR location lookup (src/matrix_vector.F90:1724-1860 MATRIX_STORAGE_LOCATION_FIND);
+// returns the 1-based location or 0 when absent.  row, col 1-based.
+int64_t orc_csr_location(const int32_t* rp, const int32_t* ci, int row, int col) {
+  int lo = rp[row - 1], up = rp[row];
+  if (up <= lo) return 0;
+  if (col < ci[lo - 1] || col > ci[up - 2]) return 0;
+  while (up - lo > kBisectionToLinear) {
+    int mid = (up + lo) / 2;
+    if (ci[mid - 1] > col) up = mid; else lo = mid;
+  }
+  for (int k = lo; k < up; ++k)
+    if (ci[k - 1] == col) return k;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// Laplace element matrix.  src/Laplace_equations_routines.F90:482-552 (standard subtype):
+// per Gauss point interpolate geometry with first derivatives, metrics, RWG = Jacobian*w,
+// K(ms,ns) += sum_{mi,ni} dphi_ms/dxi_mi * dphi_ns/dxi_ni * GU(mi,ni) * RWG.  RHS = 0 (:546).
+// Generalised subtype (:585-707) with an isotropic, element-constant conductivity kappa*I
+// rotates kappa*I into xi space (unchanged, the rotation of a multiple of the identity is the
+// identity) and reduces to kappa times the standard integrand; the oracle applies kappa per
+// Gauss-point term.
+// x: element geometric parameters x[comp][ns] (ns < nns), out: K[nns][nns] row-major.
+// ---------------------------------------------------------------------------------------
+void laplace_element(const TPBasis& b, const double* const* x, int ncomp, double kappa, double* K) {
+  const int n = b.nns, nxi = b.nxi;
+  std::fill(K, K + (size_t)n * n, 0.0);
+  Metrics m;
+  for (int g = 0; g < b.ng; ++g) {
+    metrics_at(b, g, x, ncomp, m);
+    const double rwg = m.jac * b.wts[g];
+    for (int ms = 0; ms < n; ++ms) {
+      double pgm[3];
+      for (int i = 0; i < nxi; ++i) pgm[i] = b.tab[((size_t)g * (nxi + 1) + i + 1) * n + ms];
+      for (int ns = 0; ns < n; ++ns) {
+        double pgn[3];
+        for (int i = 0; i < nxi; ++i) pgn[i] = b.tab[((size_t)g * (nxi + 1) + i + 1) * n + ns];
+        double sum = 0.0;
+        for (int mi = 0; mi < nxi; ++mi)
+          for (int ni = 0; ni < nxi; ++ni) sum += pgm[mi] * pgn[ni] * m.gu[mi][ni];
+        K[(size_t)ms * n + ns] += kappa * sum * rwg;
+      }
+    }
+  }
+}
+
+// Element matrix of one element of a (possibly 2D) Lagrange mesh.
+int orc_laplace_element(int nxi, const int* order, const int* ngauss, int ncomp, const double* xe /*[ncomp][nns]*/,
+                        double kappa, double* K) {
+  TPBasis b;
+  if (!make_tp_basis(nxi, order, ngauss, b)) return -1;
+  const double* x[3] = {xe, xe + b.nns, xe + 2 * b.nns};
+  laplace_element(b, x, ncomp, kappa, K);
+  return 0;
+}
+
+// Whole-mesh assembly, following src/equations_set_routines.F90:1203-1364
+// (EquationsSet_AssembleStaticLinearFEM): zero the matrix (EquationsMatrices_VectorValuesInitialise
+// :4206 of equations_matrices_routines.F90), then per element: gather element geometric parameters
+// (FIELD_INTERPOLATION_PARAMETERS_ELEMENT_GET, src/field_routines.F90:8042-8260), element matrix,
+// EquationsMatrices_ElementAdd (src/equations_matrices_routines.F90:1140-1265) with row DOFs =
+// column DOFs = element node DOFs (one component, one domain).
+// n_threads > 1: element-partitioned threads with private value copies summed at the end
+// (used for the multi-core CPU baseline only).
+int orc_laplace_assemble(int nxi, const int* order, const int* ngauss, int n_elem, int n_nodes,
+                         const int32_t* elem_nodes, const double* coords /*[nxi][N]*/, const double* kappa,
+                         const int32_t* row_ptr, const int32_t* col_idx, double* values, double* rhs,
+                         int n_threads) {
+  TPBasis b;
+  if (!make_tp_basis(nxi, order, ngauss, b)) return -1;
+  const int n = b.nns;
+  const int64_t nnz = (int64_t)row_ptr[n_nodes] - 1;
+  std::fill(values, values + nnz, 0.0);
+  if (rhs) std::fill(rhs, rhs + n_nodes, 0.0);
+  if (n_threads < 1) n_threads = 1;
+  std::vector<std::vector<double>> priv(n_threads > 1 ? n_threads : 0);
+  std::vector<int> status(n_threads, 0);
+  auto work = [&](int t, int e0, int e1, double* out) {
+    std::vector<double> xe((size_t)nxi * n), K((size_t)n * n);
+    std::vector<int32_t> dofs(n);
+    const double* x[3] = {xe.data(), xe.data() + n, xe.data() + 2 * n};
+    for (int e = e0; e < e1; ++e) {
+      for (int s = 0; s < n; ++s) {
+        int node = elem_nodes[(size_t)e * n + s];
+        dofs[s] = node + 1;
+        for (int c = 0; c < nxi; ++c) xe[(size_t)c * n + s] = coords[(size_t)c * n_nodes + node];
+      }
+      laplace_element(b, x, nxi, kappa ? kappa[e] : 1.0, K.data());
+      if (csr_values_add(row_ptr, col_idx, out, n, dofs.data(), n, dofs.data(), K.data()) != 0) {
+        status[t] = -2;
+        return;
+      }
+    }
+  };
+  if (n_threads == 1) {
+    work(0, 0, n_elem, values);
+  } else {
+    std::vector<std::thread> th;
+    for (int t = 0; t < n_threads; ++t) {
+      priv[t].assign(nnz, 0.0);
+      int e0 = (int)((int64_t)n_elem * t / n_threads), e1 = (int)((int64_t)n_elem * (t + 1) / n_threads);
+      th.emplace_back(work, t, e0, e1, priv[t].data());
+    }
+    for (auto& x : th) x.join();
+    for (int t = 0; t < n_threads; ++t)
+      for (int64_t k = 0; k < nnz; ++k) values[k] += priv[t][k];
+  }
+  for (int s : status)
+    if (s) return s;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// Sparse kernels used by the oracle's solve.  CSR 1-based.
+// ---------------------------------------------------------------------------------------
+void orc_csr_spmv(int n, const int32_t* rp, const int32_t* ci, const double* v, const double* x, double* y) {
+  for (int r = 0; r < n; ++r) {
+    double s = 0.0;
+    for (int k = rp[r] - 1; k < rp[r + 1] - 1; ++k) s += v[k] * x[ci[k] - 1];
+    y[r] = s;
+  }
+}
+
+// Dirichlet-eliminated Jacobi-preconditioned conjugate gradients in FP64.
+// The solver matrix of src/solver_routines.F90:14025-15050 (SOLVER_MATRICES_STATIC_ASSEMBLE)
+// removes the rows and columns of fixed DOFs and moves K_FD u_D to the right-hand side; the
+// same system is solved here in the full index space with fixed DOFs masked.  Iron hands the
+// system to PETSc KSP (src/solver_routines.F90:11775-11991); PETSc's CG is not restated, so the
+// solve is parity-unpinned and compared by solution tolerance only.
+// x: in = Dirichlet values at fixed DOFs (others ignored), out = solution.  Returns iterations
+// or -1 on failure to converge.
+int orc_cg_dirichlet(int n, const int32_t* rp, const int32_t* ci, const double* v, const double* f,
+                     const uint8_t* fixed, double* x, double rtol, int max_it, double* final_rel) {
+  std::vector<double> r(n), z(n), p(n), q(n), dinv(n), xd(n, 0.0);
+  for (int i = 0; i < n; ++i) {
+    if (fixed[i]) xd[i] = x[i];
+    double d = 0.0;
+    for (int k = rp[i] - 1; k < rp[i + 1] - 1; ++k)
+      if (ci[k] - 1 == i) d = v[k];
+    dinv[i] = fixed[i] ? 0.0 : 1.0 / d;
+  }
+  orc_csr_spmv(n, rp, ci, v, xd.data(), q.data());
+  double bnorm = 0.0;
+  for (int i = 0; i < n; ++i) {
+    r[i] = fixed[i] ? 0.0 : (f ? f[i] : 0.0) - q[i];
+    x[i] = fixed[i] ? xd[i] : 0.0;
+    bnorm += r[i] * r[i];
+  }
+  bnorm = std::sqrt(bnorm);
+  if (bnorm == 0.0) { if (final_rel) *final_rel = 0.0; return 0; }
+  double rz = 0.0;
+  for (int i = 0; i < n; ++i) { z[i] = dinv[i] * r[i]; p[i] = z[i]; rz += r[i] * z[i]; }
+  for (int it = 1; it <= max_it; ++it) {
+    for (int i = 0; i < n; ++i) xd[i] = fixed[i] ? 0.0 : p[i];
+    orc_csr_spmv(n, rp, ci, v, xd.data(), q.data());
+    double pq = 0.0;
+    for (int i = 0; i < n; ++i) { if (fixed[i]) q[i] = 0.0; pq += p[i] * q[i]; }
+    double alpha = rz / pq, rn = 0.0;
+    for (int i = 0; i < n; ++i) {
+      if (fixed[i]) continue;
+      x[i] += alpha * p[i];
+      r[i] -= alpha * q[i];
+      rn += r[i] * r[i];
+    }
+    rn = std::sqrt(rn);
+    if (rn <= rtol * bnorm) { if (final_rel) *final_rel = rn / bnorm; return it; }
+    double rz2 = 0.0;
+    for (int i = 0; i < n; ++i) { z[i] = dinv[i] * r[i]; rz2 += r[i] * z[i]; }
+    double beta = rz2 / rz;
+    rz = rz2;
+    for (int i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+  }
+  return -1;
+}
+
+}  // extern "C"

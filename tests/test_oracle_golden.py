@@ -1,0 +1,163 @@
+"""Pins of the C++ oracle against Iron's own fixtures and known-answer tests (CPU only)."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def e12_5_half_ulp(v: float) -> float:
+    """Half a unit in the 5th significant digit of a value printed with Fortran E12.5."""
+    if v == 0.0:
+        return 1e-300
+    return 0.5 * 10.0 ** (np.floor(np.log10(abs(v))) - 4) * (1 + 1e-9)
+
+
+def test_gauss_legendre_matches_closed_forms():
+    # src/basis_routines.F90:6804-6890: points/weights on [0,1]; exact for degree 2n-1
+    for n in range(1, 5):
+        x, w = oracle.gauss_legendre(n)
+        assert abs(w.sum() - 1.0) < 1e-15
+        for deg in range(2 * n):
+            assert abs((w * x**deg).sum() - 1.0 / (deg + 1)) < 1e-14
+    x, w = oracle.gauss_legendre(2)
+    assert np.allclose(x, [(1 - 1 / np.sqrt(3)) / 2, (1 + 1 / np.sqrt(3)) / 2], rtol=0, atol=1e-16)
+
+
+def test_basis_table_partition_of_unity_and_order():
+    tab, w = oracle.tp_basis(3, [2, 2, 2], [3, 3, 3])
+    assert tab.shape == (27, 4, 27)
+    assert np.allclose(tab[:, 0, :].sum(axis=1), 1.0, atol=1e-14)
+    assert np.allclose(tab[:, 1:, :].sum(axis=2), 0.0, atol=1e-13)
+    assert abs(w.sum() - 1.0) < 1e-14
+    # Gauss point order ng = i + (j-1 + (k-1) n2) n1: point 1 has xi1 varying fastest
+    x, _ = oracle.gauss_legendre(3)
+    # value of basis node 0 (xi=0,0,0) at gauss point 1 (x[1], x[0], x[0])
+    L0 = lambda t: 1 - 3 * t + 2 * t * t
+    assert abs(tab[1, 0, 0] - L0(x[1]) * L0(x[0]) ** 2) < 1e-15
+
+
+def test_analytic_laplace_fixture():
+    """Iron's tests/ClassicalField/output_analytic_laplace/AnalyticLaplaceLinearLagrange.opanal:
+    bilinear 2x2 mesh, u = cos(x)cosh(y) on the boundary; the interior node's numerical value and
+    the integrals are Iron's own output, printed to 5 significant digits."""
+    g = json.loads((GOLDEN / "analytic_laplace_linear_lagrange.json").read_text())
+    s = g["setup"]
+    en = oracle.regular_mesh(s["nelem"], 1)
+    xy = oracle.regular_coords(s["nelem"], 1, s["origin"], s["extent"])
+    rp, ci = oracle.csr_structure(en, xy.shape[1])
+    vals, rhs = oracle.laplace_assemble(2, [1, 1], s["gauss"], en, xy, None, rp, ci)
+    assert np.all(rhs == 0.0)
+    u = np.cos(xy[0]) * np.cosh(xy[1])
+    interior = np.zeros(9, bool)
+    interior[4] = True
+    x, _, _ = oracle.cg_dirichlet(rp, ci, vals, None, (~interior).astype(np.uint8), np.where(interior, 0.0, u))
+    for nd in g["nodes"]:
+        i = nd["node"] - 1
+        # E12.5: 5 significant digits
+        assert abs(u[i] - nd["analytic"]) <= e12_5_half_ulp(nd["analytic"])
+        assert abs(x[i] - nd["numerical"]) <= e12_5_half_ulp(nd["numerical"])
+    # integrals of the numerical and of the interpolated analytic solution
+    tab, wts = oracle.tp_basis(2, [1, 1], s["gauss"])
+    def integral(vals_nodal, power):
+        tot = 0.0
+        for e in range(en.shape[0]):
+            xe = xy[:, en[e]]
+            for gp in range(len(wts)):
+                J = np.array([[tab[gp, 1 + a, :] @ xe[c] for a in range(2)] for c in range(2)])
+                uh = tab[gp, 0, :] @ vals_nodal[en[e]]
+                tot += wts[gp] * np.sqrt(abs(np.linalg.det(J.T @ J))) * uh**power
+        return tot
+    for key, power in (("integral", 1), ("integral_sq", 2)):
+        num = integral(x, power)
+        ana = integral(u, power)
+        assert abs(num - g[key]["numerical"]) <= e12_5_half_ulp(g[key]["numerical"])
+        assert abs(ana - g[key]["analytic"]) <= e12_5_half_ulp(g[key]["analytic"])
+
+
+def test_unit_cube_element_matrix_known_answer():
+    """Trilinear unit cube: K = (1/12) [4 on the diagonal, 0 for edge neighbours, -1 for face- and
+    body-diagonal neighbours] (derived by hand, exact under 2x2x2 Gauss)."""
+    en = oracle.regular_mesh([1, 1, 1], 1)
+    xyz = oracle.regular_coords([1, 1, 1], 1, [0, 0, 0], [1, 1, 1])
+    K = oracle.laplace_element(3, [1, 1, 1], [2, 2, 2], xyz[:, en[0]])
+    exp = np.zeros((8, 8))
+    for m in range(8):
+        for n in range(8):
+            d = bin(m ^ n).count("1")
+            exp[m, n] = {0: 4, 1: 0, 2: -1, 3: -1}[d] / 12.0
+    assert np.abs(K - exp).max() < 1e-15
+    # scaled element: K scales with h for the 3D Laplacian
+    K2 = oracle.laplace_element(3, [1, 1, 1], [2, 2, 2], 0.5 * xyz[:, en[0]])
+    assert np.abs(K2 - 0.5 * exp).max() < 1e-15
+
+
+def _jittered_mesh(ne, seed):
+    en = oracle.regular_mesh(ne, 1)
+    xyz = oracle.regular_coords(ne, 1, [0, 0, 0], [1, 1, 1])
+    rng = np.random.default_rng(seed)
+    h = 1.0 / np.array(ne, float)
+    d = rng.uniform(-1.0, 1.0, size=xyz.shape) * (0.1 * h)[:, None]
+    tx, ty, tz = (n + 1 for n in ne)
+    K, J, I = np.meshgrid(np.arange(tz), np.arange(ty), np.arange(tx), indexing="ij")
+    bnd = ((I == 0) | (I == tx - 1) | (J == 0) | (J == ty - 1) | (K == 0) | (K == tz - 1)).reshape(-1)
+    d[:, bnd] = 0.0
+    return en, xyz + d, I.reshape(-1), tx
+
+
+def test_patch_test_u_equals_x():
+    """Known answer: u = 0 at x = 0, u = 1 at x = 1 on a jittered unit cube; isoparametric
+    trilinear elements reproduce u = x at every node."""
+    en, xyz, I, tx = _jittered_mesh((4, 4, 4), seed=0)
+    rp, ci = oracle.csr_structure(en, xyz.shape[1])
+    vals, _ = oracle.laplace_assemble(3, [1, 1, 1], [2, 2, 2], en, xyz, None, rp, ci)
+    fixed = ((I == 0) | (I == tx - 1)).astype(np.uint8)
+    x0 = np.where(I == tx - 1, 1.0, 0.0)
+    u, it, rel = oracle.cg_dirichlet(rp, ci, vals, None, fixed, x0, rtol=1e-13)
+    assert np.abs(u - xyz[0]).max() < 1e-11
+
+
+def test_structure_counts_and_pattern():
+    # config 1: 8^3 trilinear, 729 nodes, nnz = 15,625 (27-point pattern with boundary truncation)
+    en = oracle.regular_mesh([8, 8, 8], 1)
+    rp, ci = oracle.csr_structure(en, 729)
+    assert rp[0] == 1 and rp[-1] - 1 == 15625 == len(ci)
+    n = 1 + 9 + 81  # interior node (1,1,1)
+    cols = ci[rp[n] - 1: rp[n + 1] - 1] - 1
+    exp = sorted(n + di + 9 * dj + 81 * dk for dk in (-1, 0, 1) for dj in (-1, 0, 1) for di in (-1, 0, 1))
+    assert list(cols) == exp
+    for r in range(729):
+        row = ci[rp[r] - 1: rp[r + 1] - 1]
+        assert np.all(np.diff(row) > 0)
+
+
+def test_csr_location_matches_search():
+    en = oracle.regular_mesh([3, 2, 4], 1)
+    N = 4 * 3 * 5
+    rp, ci = oracle.csr_structure(en, N)
+    rng = np.random.default_rng(1)
+    for _ in range(300):
+        r = int(rng.integers(1, N + 1))
+        c = int(rng.integers(1, N + 1))
+        row = ci[rp[r - 1] - 1: rp[r] - 1]
+        k = np.searchsorted(row, c)
+        exp = (rp[r - 1] + k) if (k < len(row) and row[k] == c) else 0
+        assert oracle.csr_location(rp, ci, r, c) == exp
+
+
+def test_q2p1_structure_count():
+    """Mixed u-p structure: rows of all 4 components, columns over all element DOFs."""
+    ne = (2, 1, 1)
+    e2 = oracle.regular_mesh(ne, 2)
+    el, l2g = oracle.linear_component(e2, (3, 3, 3))
+    nq = (2 * 2 + 1) * 3 * 3
+    nl = len(l2g)
+    dofs = np.concatenate([e2, e2 + nq, e2 + 2 * nq, el + 3 * nq], axis=1)
+    rp, ci = oracle.csr_structure(dofs, 3 * nq + nl)
+    # a row of an interior-face node shared by both elements sees all DOFs of both elements
+    assert rp[-1] - 1 == len(ci)
+    assert len(l2g) == 12
