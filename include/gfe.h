@@ -125,6 +125,57 @@ int gfe_laplace_assemble(int32_t n_elem, int32_t n_nodes, const int32_t* elem_no
 int gfe_laplace_element_matrices(int32_t n_elem, int32_t n_nodes, const int32_t* elem_nodes, const double* coords,
                                  const double* kappa, double* K_out, int32_t precision, void* stream);
 
+/* ---- finite elasticity: Mooney-Rivlin, mixed u-p (K4, K5) -------------------------------- */
+
+/* Mesh of the mixed formulation: eq2 [n_elem][27] triquadratic element nodes (0-based, numbers of
+ * the n_q2 quadratic-grid nodes), elin [n_elem][8] trilinear pressure nodes (0-based numbers of the
+ * n_lin pressure-component nodes), xg [3][n_q2] geometric field.  The dependent vector `dep` of one
+ * problem holds, in Iron's separated order, the deformed positions z1, z2, z3 over the quadratic
+ * nodes followed by the pressure over the linear nodes (ndof = 3 n_q2 + n_lin).  Material
+ * parameters cpar = (c10, c01) per problem.  3x3x3 Gauss quadrature. */
+
+/* Global residual of `batch` independent problems on one mesh (dep and R are [batch][ndof], cpar
+ * is [batch][2]).  Replaces the element loop of EquationsSet_ResidualEvaluateStaticFEM
+ * (src/equations_set_routines.F90:5164-5286) around the MOONEY_RIVLIN_SUBTYPE branch of
+ * FiniteElasticity_FiniteElementResidualEvaluate (src/finite_elasticity_routines.F90:1669-1756).
+ * Colouring as in gfe_laplace_assemble.  R is zeroed first. */
+int gfe_mr_residual(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, int32_t n_lin,
+                    const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
+                    int32_t batch, const double* dep, const double* cpar, double* R, void* stream);
+
+/* Per-element CSR positions (0-based) of all 89x89 element entries, elements in colour order:
+ * slots[n_elem][89][89] (-1 where absent).  Built once per mesh and structure. */
+int gfe_mr_slot_map(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, const int32_t* color_elems,
+                    const int32_t* row_ptr, const int32_t* col_idx, int32_t* slots, void* stream);
+
+/* Iron's analytic Jacobian of one problem assembled into CSR values (zeroed first; needs `slots`)
+ * and/or written as dense element matrices K_out[n_elem][89][89] (may be NULL).  Replaces the
+ * element loop of EquationsSet_JacobianEvaluateStaticFEM (src/equations_set_routines.F90:4677-4798)
+ * around FiniteElasticity_FiniteElementJacobianEvaluate (src/finite_elasticity_routines.F90:879-1296)
+ * and EquationsMatrices_JacobianElementAdd (src/equations_matrices_routines.F90:2866-2909). */
+int gfe_mr_jacobian(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, int32_t n_lin,
+                    const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
+                    const double* dep, const double* cpar, const int32_t* slots, double* values, int64_t nnz,
+                    double* K_out, void* stream);
+
+/* Consistent tangent: the exact derivative of the residual of gfe_mr_residual with respect to
+ * the dependent vector (what Iron's finite-difference Jacobian, EquationsSet_FiniteElementJacobianEvaluateFD
+ * src/equations_set_routines.F90:2839-2962, approximates column by column).  Same outputs as
+ * gfe_mr_jacobian.  Used by the Newton solver and checked against finite differences. */
+int gfe_mr_tangent(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, int32_t n_lin,
+                   const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
+                   const double* dep, const double* cpar, const int32_t* slots, double* values, int64_t nnz,
+                   double* K_out, void* stream);
+
+/* Adjoint of the residual (K6): for `batch` problems, du[b] = v[b]^T dR/d(dep) ([batch][ndof]) and
+ * dc[b] = v[b]^T dR/d(c10, c01) ([batch][2]).  No counterpart routine in Iron (its gradients come
+ * from finite differences); checked against central differences and Iron-style one-sided FD.
+ * Allocates and frees per-element partial sums on `stream`; the dc sum is in fixed element order. */
+int gfe_mr_residual_vjp(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, int32_t n_lin,
+                        const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
+                        int32_t batch, const double* dep, const double* cpar, const double* v, double* du, double* dc,
+                        void* stream);
+
 /* ---- linear solve (K7) ------------------------------------------------------------------ */
 
 /* y = A x on the rows with fixed[i] == 0; y[i] = 0 on fixed rows.  fixed may be NULL. */

@@ -1,0 +1,1089 @@
+// mr.cu -- K4 / K5: Mooney-Rivlin (mixed u-p, triquadratic u + trilinear p) residual and Iron's
+// analytic Jacobian, batched over elements (and over parameter sets for the residual).
+//
+// Reference: FiniteElasticity_FiniteElementResidualEvaluate, MOONEY_RIVLIN_SUBTYPE branch
+// (src/finite_elasticity_routines.F90:1669-1756), FINITE_ELASTICITY_GAUSS_STRESS_TENSOR (:6985-7061),
+// FiniteElasticity_GaussDeformationGradientTensor (:5148-5215) with the material frame of
+// Coordinates_MaterialSystemCalculate (src/coordinate_routines.F90:3841-3947),
+// FiniteElasticity_FiniteElementJacobianEvaluate (:1016-1274) and
+// FINITE_ELASTICITY_GAUSS_ELASTICITY_TENSOR (:649-795).
+//
+// Field layout (Iron's separated component order): the dependent vector holds the deformed
+// positions z1, z2, z3 over the n_q2 quadratic nodes followed by the pressure over the n_lin
+// linear (corner) nodes; the geometric field x is [3][n_q2].  Element DOF order: 27 z1, 27 z2,
+// 27 z3, 8 p (Iron's element parameter order, local nodes xi1 fastest).
+//
+// Residual: one warp per (element, parameter set).  Lane g < 27 evaluates Gauss point g (metrics,
+// deformation gradient, stress) and leaves P_g = J_z w_g Z^-1 sigma (3x3) and
+// J_x w_g (J_z/J_x - 1) in shared memory; the lanes then form the 89 entries as sums over Gauss
+// points in a fixed order (deterministic) and scatter them into the global residual.  Elements
+// are processed colour by colour, so no two elements of a launch share a DOF.
+//
+// Jacobian: one CTA per element.  Threads 0..26 build, per Gauss point, the spatial basis
+// gradients dphi/dz and the 3x3 blocks J_z w (c + sigma) of Iron's analytic tangent; all threads
+// then form the lower u-u triangle and the u-p / p-u blocks and add them into the CSR values
+// through a precomputed per-element slot map (u-u upper triangle mirrored, p-p structurally zero).
+#include <mutex>
+
+#include "gfe_internal.cuh"
+
+namespace {
+
+constexpr int NQ = 27;   // quadratic element nodes
+constexpr int NL = 8;    // linear (pressure) element nodes
+constexpr int NG = 27;   // Gauss points (3x3x3)
+constexpr int ND = 89;   // element DOFs
+
+struct Tables {
+  double dphi[NG][3][NQ];  // d phi_ns / d xi_k at Gauss point g (quadratic basis)
+  double w[NG];
+  double psi[NG][NL];      // linear basis values at the Gauss points
+};
+
+// Host construction of the tables (Gauss-Legendre 3-point rule on [0,1], Lagrange bases),
+// src/basis_routines.F90:3720-4090, 6804-6890, 7969-8090.
+void build_tables(Tables& t) {
+  const double s = std::sqrt(0.6);
+  const double gx[3] = {(-s + 1.0) / 2.0, 0.5, (s + 1.0) / 2.0};
+  const double gw[3] = {2.5 / 9.0, 4.0 / 9.0, 2.5 / 9.0};
+  auto q = [](int a, int d, double x) {
+    if (d == 0) return a == 0 ? 1.0 - 3.0 * x + 2.0 * x * x : (a == 1 ? 4.0 * x * (1.0 - x) : x * (x + x - 1.0));
+    return a == 0 ? 4.0 * x - 3.0 : (a == 1 ? 4.0 - 8.0 * x : 4.0 * x - 1.0);
+  };
+  auto l = [](int a, double x) { return a == 0 ? 1.0 - x : x; };
+  for (int g3 = 0; g3 < 3; ++g3)
+    for (int g2 = 0; g2 < 3; ++g2)
+      for (int g1 = 0; g1 < 3; ++g1) {
+        const int g = g1 + 3 * (g2 + 3 * g3);
+        const double xg[3] = {gx[g1], gx[g2], gx[g3]};
+        t.w[g] = gw[g1] * gw[g2] * gw[g3];
+        for (int a3 = 0; a3 < 3; ++a3)
+          for (int a2 = 0; a2 < 3; ++a2)
+            for (int a1 = 0; a1 < 3; ++a1) {
+              const int ns = a1 + 3 * (a2 + 3 * a3);
+              const int ai[3] = {a1, a2, a3};
+              for (int k = 0; k < 3; ++k) {
+                double v = 1.0;
+                for (int d = 0; d < 3; ++d) v *= q(ai[d], d == k ? 1 : 0, xg[d]);
+                t.dphi[g][k][ns] = v;
+              }
+            }
+        for (int b3 = 0; b3 < 2; ++b3)
+          for (int b2 = 0; b2 < 2; ++b2)
+            for (int b1 = 0; b1 < 2; ++b1) t.psi[g][b1 + 2 * (b2 + 2 * b3)] = l(b1, xg[0]) * l(b2, xg[1]) * l(b3, xg[2]);
+      }
+}
+
+std::mutex g_tab_mu;
+Tables* g_tables[64] = {nullptr};
+
+int device_tables(const Tables** out) {
+  int dev = 0;
+  GFE_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_tab_mu);
+  if (!g_tables[dev]) {
+    Tables h;
+    build_tables(h);
+    void* p = nullptr;
+    GFE_CUDA_TRY(cudaMalloc(&p, sizeof(Tables)));
+    GFE_CUDA_TRY(cudaMemcpy(p, &h, sizeof(Tables), cudaMemcpyHostToDevice));
+    g_tables[dev] = static_cast<Tables*>(p);
+  }
+  *out = g_tables[dev];
+  return GFE_OK;
+}
+
+__device__ __constant__ int kT2V[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+__device__ __constant__ int kV2T[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+
+// Inverse and determinant with Iron's cofactor formulas (src/maths.F90:2807-2868).
+__device__ __forceinline__ double inv3(const double A[3][3], double B[3][3]) {
+  const double det = A[0][0] * A[1][1] * A[2][2] + A[0][1] * A[1][2] * A[2][0] + A[0][2] * A[1][0] * A[2][1] -
+                     A[0][0] * A[2][1] * A[1][2] - A[1][0] * A[0][1] * A[2][2] - A[2][0] * A[1][1] * A[0][2];
+  const double r = 1.0 / det;
+  B[0][0] = (A[1][1] * A[2][2] - A[2][1] * A[1][2]) * r;
+  B[1][0] = (A[1][2] * A[2][0] - A[2][2] * A[1][0]) * r;
+  B[2][0] = (A[1][0] * A[2][1] - A[2][0] * A[1][1]) * r;
+  B[0][1] = (A[2][1] * A[0][2] - A[0][1] * A[2][2]) * r;
+  B[1][1] = (A[2][2] * A[0][0] - A[0][2] * A[2][0]) * r;
+  B[2][1] = (A[2][0] * A[0][1] - A[0][0] * A[2][1]) * r;
+  B[0][2] = (A[0][1] * A[1][2] - A[1][1] * A[0][2]) * r;
+  B[1][2] = (A[0][2] * A[1][0] - A[1][2] * A[0][0]) * r;
+  B[2][2] = (A[0][0] * A[1][1] - A[1][0] * A[0][1]) * r;
+  return det;
+}
+
+__device__ __forceinline__ double det3(const double A[3][3]) {
+  return A[0][0] * A[1][1] * A[2][2] + A[0][1] * A[1][2] * A[2][0] + A[0][2] * A[1][0] * A[2][1] -
+         A[0][0] * A[2][1] * A[1][2] - A[1][0] * A[0][1] * A[2][2] - A[2][0] * A[1][1] * A[0][2];
+}
+
+// Volume Jacobian sqrt|det(M^T M)| (src/coordinate_routines.F90:818-822).
+__device__ __forceinline__ double vol_jacobian(const double M[3][3]) {
+  double G[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) G[i][j] = M[0][i] * M[0][j] + M[1][i] * M[1][j] + M[2][i] * M[2][j];
+  return sqrt(fabs(det3(G)));
+}
+
+// Per-Gauss-point kinematics shared by residual and Jacobian.
+struct GP {
+  double Zi[3][3];  // dxi/dz
+  double F[3][3];   // dz/dnu
+  double Jz, Jx, p, w;
+};
+
+__device__ __forceinline__ bool gauss_point(const Tables& T, int g, const double* sz, const double* sx,
+                                            const double* sp, GP& o) {
+  double Z[3][3], X[3][3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double a = 0.0, b = 0.0;
+#pragma unroll 9
+      for (int ns = 0; ns < NQ; ++ns) {
+        const double d = T.dphi[g][k][ns];
+        a += d * sz[c * NQ + ns];
+        b += d * sx[c * NQ + ns];
+      }
+      Z[c][k] = a;
+      X[c][k] = b;
+    }
+  o.Jz = vol_jacobian(Z);
+  o.Jx = vol_jacobian(X);
+  const double dz = inv3(Z, o.Zi);
+  // material frame without fibres: dX/dNu columns = normalised DX_DXI columns
+  double N[3][3], NX[3][3], A[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double n = sqrt(X[0][k] * X[0][k] + X[1][k] * X[1][k] + X[2][k] * X[2][k]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) N[c][k] = X[c][k] / n;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) NX[i][j] = N[0][i] * X[0][j] + N[1][i] * X[1][j] + N[2][i] * X[2][j];
+  inv3(NX, A);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) o.F[i][j] = Z[i][0] * A[0][j] + Z[i][1] * A[1][j] + Z[i][2] * A[2][j];
+  double p = 0.0;
+#pragma unroll
+  for (int m = 0; m < NL; ++m) p += T.psi[g][m] * sp[m];
+  o.p = p;
+  o.w = T.w[g];
+  return dz > 0.0 && o.Jx > 0.0 && isfinite(dz);
+}
+
+// push-forward matrix t (src/finite_elasticity_routines.F90:1343-1375)
+__device__ __forceinline__ void push_t(const double F[3][3], double t[6][6]) {
+#pragma unroll
+  for (int j = 0; j < 6; ++j)
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      const int ai = kV2T[i][0], bi = kV2T[i][1], aj = kV2T[j][0], bj = kV2T[j][1];
+      double v = F[ai][aj] * F[bi][bj];
+      if (j >= 3) v += F[ai][bj] * F[bi][aj];
+      t[i][j] = v;
+    }
+}
+
+__device__ __forceinline__ void push_vec(const double t[6][6], double S[6], double J) {
+  double o[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) s += t[i][j] * S[j];
+    o[i] = s / J;
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) S[i] = o[i];
+}
+
+// Cauchy stress of the residual (deviatoric MR + p), src/finite_elasticity_routines.F90:6985-7061.
+__device__ __forceinline__ void residual_stress(const GP& q, double c1, double c2, double sig[6]) {
+  const double J = q.Jz / q.Jx;
+  const double s = pow(J, -1.0 / 3.0);
+  double Fb[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Fb[i][j] = q.F[i][j] * s;
+  double C[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[i][j] = Fb[0][i] * Fb[0][j] + Fb[1][i] * Fb[1][j] + Fb[2][i] * Fb[2][j];
+  const double I1 = C[0][0] + C[1][1] + C[2][2];
+  const double t1 = -2.0 * c2, t2 = 2.0 * (c1 + I1 * c2);
+  sig[0] = t1 * C[0][0] + t2; sig[1] = t1 * C[1][1] + t2; sig[2] = t1 * C[2][2] + t2;
+  sig[3] = t1 * C[1][0]; sig[4] = t1 * C[2][0]; sig[5] = t1 * C[2][1];
+  double t[6][6];
+  push_t(Fb, t);
+  push_vec(t, sig, J);
+  const double tr3 = (sig[0] + sig[1] + sig[2]) / 3.0;
+  sig[0] = sig[0] - tr3 + q.p; sig[1] = sig[1] - tr3 + q.p; sig[2] = sig[2] - tr3 + q.p;
+}
+
+// ----------------------------------------------------------------------------------------------
+// residual
+// ----------------------------------------------------------------------------------------------
+constexpr int kResWarps = 4;
+
+__global__ void __launch_bounds__(kResWarps * 32)
+mr_residual_kernel(const int32_t* __restrict__ elems, int32_t count, int32_t batch, const int32_t* __restrict__ eq2,
+                   const int32_t* __restrict__ elin, int32_t nq2, int32_t nlin, const double* __restrict__ xg,
+                   const double* __restrict__ dep, const double* __restrict__ cpar, const Tables* __restrict__ Tg,
+                   double* __restrict__ R, int64_t dep_stride, unsigned* err) {
+  extern __shared__ double smem[];
+  Tables& T = *reinterpret_cast<Tables*>(smem);
+  double* wbase = smem + sizeof(Tables) / sizeof(double);
+  // stage the tables
+  {
+    const double* src = reinterpret_cast<const double*>(Tg);
+    double* dst = smem;
+    for (int i = threadIdx.x; i < (int)(sizeof(Tables) / sizeof(double)); i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  // per-warp scratch: x[81], z[81], p[8], P[27][9], tp[27], dofs (int) [89]
+  double* sx = wbase + w * (81 + 81 + 8 + NG * 9 + NG + 48);
+  double* sz = sx + 81;
+  double* sp = sz + 81;
+  double* sP = sp + 8;
+  double* stp = sP + NG * 9;
+  int* sd = reinterpret_cast<int*>(stp + NG);
+  const long long total = (long long)count * batch;
+  const int64_t ndof = 3ll * nq2 + nlin;
+  for (long long item = (long long)blockIdx.x * kResWarps + w; item < total; item += (long long)gridDim.x * kResWarps) {
+    const int b = (int)(item / count);
+    const int e = __ldg(elems + (item % count));
+    const double* d = dep + b * dep_stride;
+    for (int i = lane; i < NQ; i += 32) {
+      const int n = __ldg(eq2 + (size_t)e * NQ + i);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        sx[c * NQ + i] = __ldg(xg + (size_t)c * nq2 + n);
+        sz[c * NQ + i] = d[(size_t)c * nq2 + n];
+        sd[c * NQ + i] = c * nq2 + n;
+      }
+    }
+    if (lane < NL) {
+      const int n = __ldg(elin + (size_t)e * NL + lane);
+      sp[lane] = d[(size_t)3 * nq2 + n];
+      sd[81 + lane] = 3 * nq2 + n;
+    }
+    const double c1 = cpar[2 * b], c2 = cpar[2 * b + 1];
+    __syncwarp();
+    if (lane < NG) {
+      GP q;
+      if (!gauss_point(T, lane, sz, sx, sp, q)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+      double sig[6];
+      residual_stress(q, c1, c2, sig);
+      const double jgw = q.Jz * q.w;
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int mh = 0; mh < 3; ++mh)
+          sP[lane * 9 + k * 3 + mh] = jgw * (q.Zi[k][0] * sig[kT2V[0][mh]] + q.Zi[k][1] * sig[kT2V[1][mh]] +
+                                             q.Zi[k][2] * sig[kT2V[2][mh]]);
+      stp[lane] = q.Jx * q.w * (q.Jz / q.Jx - 1.0);
+    }
+    __syncwarp();
+    double* Rb = R + b * dep_stride;
+    for (int i = lane; i < ND; i += 32) {
+      double s = 0.0;
+      if (i < 81) {
+        const int ms = i % NQ, mh = i / NQ;
+        for (int g = 0; g < NG; ++g)
+          s += T.dphi[g][0][ms] * sP[g * 9 + 0 + mh] + T.dphi[g][1][ms] * sP[g * 9 + 3 + mh] +
+               T.dphi[g][2][ms] * sP[g * 9 + 6 + mh];
+      } else {
+        const int ms = i - 81;
+        for (int g = 0; g < NG; ++g) s += stp[g] * T.psi[g][ms];
+      }
+      if (!isfinite(s)) gfe_raise(err, GFE_DEVERR_NONFINITE);
+      Rb[sd[i]] += s;
+    }
+    __syncwarp();
+  }
+  (void)ndof;
+}
+
+// ----------------------------------------------------------------------------------------------
+// Iron's analytic Jacobian
+// ----------------------------------------------------------------------------------------------
+constexpr int kJacThreads = 128;
+
+struct JacShared {
+  double x[81], z[81], p[8];
+  double dphidz[NG][NQ][3];  // spatial basis gradients
+  double sub[NG][6][9];      // J_z w (D + sigma) diagonal blocks 0..2; J_z w D off-diagonal (1,0),(2,0),(2,1)
+  double hyd[NG][9];         // J_z w push(C^-1)
+  double jgw[NG];
+  int dofs[ND];
+};
+
+__device__ void jacobian_point(const Tables& T, int g, JacShared& S, double c1, double c2, unsigned* err) {
+  GP q;
+  if (!gauss_point(T, g, S.z, S.x, S.p, q)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+  const double J = q.Jz / q.Jx;
+  // unmodified right Cauchy-Green tensor and its inverse
+  double C[3][3], Ci[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[i][j] = q.F[0][i] * q.F[0][j] + q.F[1][i] * q.F[1][j] + q.F[2][i] * q.F[2][j];
+  const double I3 = inv3(C, Ci);
+  const double L[6] = {C[0][0], C[1][1], C[2][2], C[0][1], C[0][2], C[1][2]};
+  const double U[6] = {Ci[0][0], Ci[1][1], Ci[2][2], Ci[0][1], Ci[0][2], Ci[1][2]};
+  // I3EE as filled by Fortran RESHAPE (column j listed): I3EE[i][j] = col[j][i]
+  const double col[6][6] = {{0.0, 4 * L[2], 4 * L[1], 0.0, 0.0, -4 * L[5]},
+                            {4 * L[2], 0.0, 4 * L[0], 0.0, -4 * L[4], 0.0},
+                            {4 * L[1], 4 * L[0], 0.0, -2 * L[3], 0.0, 0.0},
+                            {0.0, 0.0, -4 * L[3], -2 * L[2], 2 * L[5], 2 * L[4]},
+                            {0.0, -4 * L[4], 0.0, 2 * L[5], -2 * L[1], 2 * L[3]},
+                            {-4 * L[5], 0.0, 0.0, 2 * L[4], 2 * L[3], -2 * L[0]}};
+  double D[6][6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      double v = 0.0;
+      if (i < 3 && j < 3 && i != j) v = 4.0 * c2;
+      if (i >= 3 && i == j) v = -2.0 * c2;
+      D[i][j] = v + q.p * (-2.0 * U[i] * U[j] + 0.5 * col[j][i] / I3);
+    }
+  const double I1 = C[0][0] + C[1][1] + C[2][2];
+  const double t2 = 2.0 * (c1 + I1 * c2);
+  double Sv[6] = {-2 * c2 * C[0][0] + t2, -2 * c2 * C[1][1] + t2, -2 * c2 * C[2][2] + t2,
+                  -2 * c2 * C[1][0], -2 * c2 * C[2][0], -2 * c2 * C[2][1]};
+  double H[6] = {U[0], U[1], U[2], U[3], U[4], U[5]};
+  double t[6][6];
+  push_t(q.F, t);
+  push_vec(t, Sv, J);
+  push_vec(t, H, J);
+  double tD[6][6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += t[i][k] * D[k][j];
+      tD[i][j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += tD[i][k] * t[j][k];
+      D[i][j] = s / J;
+    }
+  Sv[0] += q.p; Sv[1] += q.p; Sv[2] += q.p;
+  const double jgw = q.Jz * q.w;
+  S.jgw[g] = jgw;
+#pragma unroll
+  for (int nh = 0; nh < 3; ++nh)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) S.sub[g][nh][i * 3 + j] = jgw * (D[kT2V[i][nh]][kT2V[j][nh]] + Sv[kT2V[i][j]]);
+  // off-diagonal blocks rows mh, columns nh: (mh,nh) = (1,0), (2,0), (2,1)
+  const int om[3] = {1, 2, 2}, on[3] = {0, 0, 1};
+#pragma unroll
+  for (int o = 0; o < 3; ++o)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) S.sub[g][3 + o][i * 3 + j] = jgw * D[kT2V[i][om[o]]][kT2V[j][on[o]]];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) S.hyd[g][i * 3 + j] = jgw * H[kT2V[i][j]];
+  for (int ms = 0; ms < NQ; ++ms)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      S.dphidz[g][ms][k] =
+          q.Zi[0][k] * T.dphi[g][0][ms] + q.Zi[1][k] * T.dphi[g][1][ms] + q.Zi[2][k] * T.dphi[g][2][ms];
+}
+
+// Element Jacobian entry (row r, column c) of Iron's analytic tangent, 0 <= r, c < 89.
+__device__ __forceinline__ double jacobian_entry(const Tables& T, const JacShared& S, int r, int c) {
+  double s = 0.0;
+  if (r < 81 && c < 81) {
+    // use the lower triangle (Iron mirrors the lower u-u triangle to the upper)
+    int rr = r, cc = c;
+    if (rr < cc) { rr = c; cc = r; }
+    const int mh = rr / NQ, ms = rr % NQ, nh = cc / NQ, ns = cc % NQ;
+    int blk;
+    if (mh == nh) blk = mh;
+    else blk = 3 + (mh == 1 ? 0 : (nh == 0 ? 1 : 2));
+    for (int g = 0; g < NG; ++g) {
+      const double* B = S.sub[g][blk];
+      const double a0 = S.dphidz[g][ns][0], a1 = S.dphidz[g][ns][1], a2 = S.dphidz[g][ns][2];
+      const double t0 = B[0] * a0 + B[1] * a1 + B[2] * a2;
+      const double t1 = B[3] * a0 + B[4] * a1 + B[5] * a2;
+      const double t2 = B[6] * a0 + B[7] * a1 + B[8] * a2;
+      s += S.dphidz[g][ms][0] * t0 + S.dphidz[g][ms][1] * t1 + S.dphidz[g][ms][2] * t2;
+    }
+  } else if (r >= 81 && c < 81) {
+    const int ms = r - 81, nh = c / NQ, ns = c % NQ;
+    for (int g = 0; g < NG; ++g) s += S.jgw[g] * S.dphidz[g][ns][nh] * T.psi[g][ms];
+  } else if (r < 81 && c >= 81) {
+    const int mh = r / NQ, ms = r % NQ, ns = c - 81;
+    for (int g = 0; g < NG; ++g) {
+      const double* Hh = S.hyd[g];
+      const double tv = Hh[mh * 3 + 0] * S.dphidz[g][ms][0] + Hh[mh * 3 + 1] * S.dphidz[g][ms][1] +
+                        Hh[mh * 3 + 2] * S.dphidz[g][ms][2];
+      s += tv * T.psi[g][ns];
+    }
+  }
+  return s;
+}
+
+__global__ void __launch_bounds__(kJacThreads)
+mr_jacobian_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
+                   const int32_t* __restrict__ elin, int32_t nq2, int32_t nlin, const double* __restrict__ xg,
+                   const double* __restrict__ dep, const double* __restrict__ cpar, const Tables* __restrict__ Tg,
+                   const int32_t* __restrict__ slots, double* __restrict__ values, double* __restrict__ Kout,
+                   unsigned* err) {
+  extern __shared__ double smem[];
+  Tables& T = *reinterpret_cast<Tables*>(smem);
+  JacShared& S = *reinterpret_cast<JacShared*>(smem + sizeof(Tables) / sizeof(double));
+  {
+    const double* src = reinterpret_cast<const double*>(Tg);
+    for (int i = threadIdx.x; i < (int)(sizeof(Tables) / sizeof(double)); i += blockDim.x) smem[i] = src[i];
+  }
+  const double c1 = cpar[0], c2 = cpar[1];
+  for (int item = blockIdx.x; item < count; item += gridDim.x) {
+    const int e = __ldg(elems + item);
+    __syncthreads();
+    for (int i = threadIdx.x; i < NQ; i += blockDim.x) {
+      const int n = __ldg(eq2 + (size_t)e * NQ + i);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        S.x[c * NQ + i] = __ldg(xg + (size_t)c * nq2 + n);
+        S.z[c * NQ + i] = dep[(size_t)c * nq2 + n];
+      }
+    }
+    if (threadIdx.x < NL) S.p[threadIdx.x] = dep[(size_t)3 * nq2 + __ldg(elin + (size_t)e * NL + threadIdx.x)];
+    __syncthreads();
+    if (threadIdx.x < NG) jacobian_point(T, threadIdx.x, S, c1, c2, err);
+    __syncthreads();
+    const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
+    for (int k = threadIdx.x; k < ND * ND; k += blockDim.x) {
+      const int r = k / ND, c = k % ND;
+      if (r >= 81 && c >= 81) {
+        if (Kout) Kout[(size_t)e * ND * ND + k] = 0.0;
+        continue;
+      }
+      const double v = jacobian_entry(T, S, r, c);
+      if (Kout) Kout[(size_t)e * ND * ND + k] = v;
+      if (sl) {
+        const int pos = __ldg(sl + k);
+        if (pos < 0) gfe_raise(err, GFE_DEVERR_SLOT);
+        else values[pos] += v;
+      }
+    }
+  }
+}
+
+// slot map: for each element (in colour order) and each (r, c), the 0-based CSR position of
+// (dof_r, dof_c); -1 when absent.  One warp per (element, row).
+__global__ void mr_slot_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
+                               const int32_t* __restrict__ elin, int32_t nq2, const int32_t* __restrict__ rp,
+                               const int32_t* __restrict__ ci, int32_t* __restrict__ slots) {
+  const int lane = threadIdx.x & 31;
+  const long long nw = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; wid < (long long)count * ND;
+       wid += nw) {
+    const int item = (int)(wid / ND), r = (int)(wid % ND);
+    const int e = elems[item];
+    auto dof = [&](int i) {
+      return i < 81 ? (i / NQ) * nq2 + eq2[(size_t)e * NQ + i % NQ] : 3 * nq2 + elin[(size_t)e * NL + i - 81];
+    };
+    const int row = dof(r);
+    const int lo0 = rp[row] - 1, hi0 = rp[row + 1] - 1;
+    for (int c = lane; c < ND; c += 32) {
+      const int col = dof(c) + 1;
+      int lo = lo0, hi = hi0;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (ci[mid] < col) lo = mid + 1; else hi = mid;
+      }
+      slots[((size_t)item * ND + r) * ND + c] = (lo < hi0 && ci[lo] == col) ? lo : -1;
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------------------------
+// Consistent tangent and adjoint of Iron's residual (forward-mode dual numbers per Gauss point)
+// ----------------------------------------------------------------------------------------------
+// Per Gauss point the u-rows of the residual are R(ms,mh) += sum_xi g_ms[xi] P[xi][mh] with
+// P = w J_z Z^-1 sigma(Z, p) (Z = dz/dxi, g = reference basis gradients) and the p-rows
+// R(ms) += w (J_z - J_x) psi_ms.  The exact derivatives dP/dZ (81 numbers) and dP/dp (9) are
+// obtained by 10 forward-mode passes through the same formulas with dual numbers; dJ_z/dZ =
+// J_z Z^-T.  The element tangent / vector-Jacobian products are then contractions with the
+// constant basis tables.  This is the derivative that Iron's finite-difference Jacobian
+// (src/equations_set_routines.F90:2839-2962) approximates.
+struct Dual {
+  double v, d;
+};
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ Dual operator-(Dual a) { return {-a.v, -a.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.v * b.d + a.d * b.v}; }
+__device__ __forceinline__ Dual operator*(double a, Dual b) { return {a * b.v, a * b.d}; }
+__device__ __forceinline__ Dual operator*(Dual a, double b) { return {a.v * b, a.d * b}; }
+__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
+  const double r = 1.0 / b.v;
+  return {a.v * r, (a.d - a.v * r * b.d) * r};
+}
+__device__ __forceinline__ Dual operator/(Dual a, double b) { return {a.v / b, a.d / b}; }
+__device__ __forceinline__ Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
+__device__ __forceinline__ double val(double a) { return a; }
+__device__ __forceinline__ double val(Dual a) { return a.v; }
+__device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ Dual dsqrt(Dual a) {
+  const double s = sqrt(a.v);
+  return {s, a.d / (2.0 * s)};
+}
+__device__ __forceinline__ double dabs(double a) { return fabs(a); }
+__device__ __forceinline__ Dual dabs(Dual a) { return a.v < 0.0 ? -a : a; }
+// x^(-1/3)
+__device__ __forceinline__ double dpowm13(double a) { return pow(a, -1.0 / 3.0); }
+__device__ __forceinline__ Dual dpowm13(Dual a) {
+  const double v = pow(a.v, -1.0 / 3.0);
+  return {v, -v / (3.0 * a.v) * a.d};
+}
+__device__ __forceinline__ double cst(double a) { return a; }
+
+template <typename T>
+__device__ __forceinline__ T tdet3(const T A[3][3]) {
+  return A[0][0] * A[1][1] * A[2][2] + A[0][1] * A[1][2] * A[2][0] + A[0][2] * A[1][0] * A[2][1] -
+         A[0][0] * A[2][1] * A[1][2] - A[1][0] * A[0][1] * A[2][2] - A[2][0] * A[1][1] * A[0][2];
+}
+
+template <typename T>
+__device__ __forceinline__ void tinv3(const T A[3][3], T B[3][3]) {
+  const T det = tdet3(A);
+  B[0][0] = (A[1][1] * A[2][2] - A[2][1] * A[1][2]) / det;
+  B[1][0] = (A[1][2] * A[2][0] - A[2][2] * A[1][0]) / det;
+  B[2][0] = (A[1][0] * A[2][1] - A[2][0] * A[1][1]) / det;
+  B[0][1] = (A[2][1] * A[0][2] - A[0][1] * A[2][2]) / det;
+  B[1][1] = (A[2][2] * A[0][0] - A[0][2] * A[2][0]) / det;
+  B[2][1] = (A[2][0] * A[0][1] - A[0][0] * A[2][1]) / det;
+  B[0][2] = (A[0][1] * A[1][2] - A[1][1] * A[0][2]) / det;
+  B[1][2] = (A[0][2] * A[1][0] - A[1][2] * A[0][0]) / det;
+  B[2][2] = (A[0][0] * A[1][1] - A[1][0] * A[0][1]) / det;
+}
+
+// P = w Jz Z^-1 sigma(Z, p) of the residual; also returns Jz.
+template <typename T>
+__device__ __forceinline__ void point_P(const T Z[3][3], const double A[3][3], double Jx, double w, T p, double c1,
+                                        double c2, T P[3][3], T& Jz) {
+  T G[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) G[i][j] = Z[0][i] * Z[0][j] + Z[1][i] * Z[1][j] + Z[2][i] * Z[2][j];
+  Jz = dsqrt(dabs(tdet3(G)));
+  T Zi[3][3];
+  tinv3(Z, Zi);
+  const T J = Jz / Jx;
+  const T s = dpowm13(J);
+  T Fb[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Fb[i][j] = (Z[i][0] * A[0][j] + Z[i][1] * A[1][j] + Z[i][2] * A[2][j]) * s;
+  T C[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[i][j] = Fb[0][i] * Fb[0][j] + Fb[1][i] * Fb[1][j] + Fb[2][i] * Fb[2][j];
+  const T I1 = C[0][0] + C[1][1] + C[2][2];
+  const double t1 = -2.0 * c2;
+  const T t2 = 2.0 * (I1 * c2 + c1);
+  T Sv[6] = {t1 * C[0][0] + t2, t1 * C[1][1] + t2, t1 * C[2][2] + t2, t1 * C[1][0], t1 * C[2][0], t1 * C[2][1]};
+  // sigma_bar = Fb S Fb^T / J (full tensor form of the Voigt push-forward)
+  T Sm[3][3] = {{Sv[0], Sv[3], Sv[4]}, {Sv[3], Sv[1], Sv[5]}, {Sv[4], Sv[5], Sv[2]}};
+  T FS[3][3], sg[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) FS[i][j] = Fb[i][0] * Sm[0][j] + Fb[i][1] * Sm[1][j] + Fb[i][2] * Sm[2][j];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) sg[i][j] = (FS[i][0] * Fb[j][0] + FS[i][1] * Fb[j][1] + FS[i][2] * Fb[j][2]) / J;
+  const T tr3 = (sg[0][0] + sg[1][1] + sg[2][2]) / 3.0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) sg[i][i] = sg[i][i] - tr3 + p;
+  const T wj = Jz * w;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int mh = 0; mh < 3; ++mh) P[k][mh] = wj * (Zi[k][0] * sg[0][mh] + Zi[k][1] * sg[1][mh] + Zi[k][2] * sg[2][mh]);
+}
+
+// Gauss-point inputs of the tangent: Z (3x3), the material-frame matrix A, J_x, w, p
+struct GPIn {
+  double Z[3][3], A[3][3], Jx, w, p;
+};
+
+__device__ __forceinline__ void gauss_inputs(const Tables& T, int g, const double* sz, const double* sx,
+                                             const double* sp, GPIn& o) {
+  double X[3][3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double a = 0.0, b = 0.0;
+      for (int ns = 0; ns < NQ; ++ns) {
+        const double d = T.dphi[g][k][ns];
+        a += d * sz[c * NQ + ns];
+        b += d * sx[c * NQ + ns];
+      }
+      o.Z[c][k] = a;
+      X[c][k] = b;
+    }
+  o.Jx = vol_jacobian(X);
+  double N[3][3], NX[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double n = sqrt(X[0][k] * X[0][k] + X[1][k] * X[1][k] + X[2][k] * X[2][k]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) N[c][k] = X[c][k] / n;
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) NX[i][j] = N[0][i] * X[0][j] + N[1][i] * X[1][j] + N[2][i] * X[2][j];
+  inv3(NX, o.A);
+  double p = 0.0;
+  for (int m = 0; m < NL; ++m) p += T.psi[g][m] * sp[m];
+  o.p = p;
+  o.w = T.w[g];
+}
+
+// dP/d(seed) for seed 0..8 = Z[seed/3][seed%3], seed 9 = p.  out[9] = dP[xi][mh] row-major.
+__device__ __forceinline__ void point_dP(const GPIn& in, int seed, double c1, double c2, double out[9], double* Jz_v) {
+  Dual Z[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Z[i][j] = {in.Z[i][j], (i * 3 + j == seed) ? 1.0 : 0.0};
+  const Dual p = {in.p, seed == 9 ? 1.0 : 0.0};
+  Dual P[3][3], Jz;
+  point_P<Dual>(Z, in.A, in.Jx, in.w, p, c1, c2, P, Jz);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) out[i * 3 + j] = P[i][j].d;
+  if (Jz_v) *Jz_v = Jz.v;
+}
+
+constexpr int kTanThreads = 128;
+
+struct TanShared {
+  double x[81], z[81], p[8];
+  GPIn in[NG];
+  double dPdZ[NG][10][9];  // [g][seed][xi*3+mh]
+  double wJZi[NG][9];      // w J_z Z^-1[zeta][nh] (p-row coefficients)
+  int dofs[ND];
+};
+
+__device__ void tangent_points(const Tables& T, TanShared& S, double c1, double c2) {
+  if (threadIdx.x < NG) gauss_inputs(T, threadIdx.x, S.z, S.x, S.p, S.in[threadIdx.x]);
+  __syncthreads();
+  for (int task = threadIdx.x; task < NG * 10; task += blockDim.x) {
+    const int g = task / 10, seed = task % 10;
+    double o[9];
+    point_dP(S.in[g], seed, c1, c2, o, nullptr);
+#pragma unroll
+    for (int k = 0; k < 9; ++k) S.dPdZ[g][seed][k] = o[k];
+  }
+  if (threadIdx.x < NG) {
+    const GPIn& in = S.in[threadIdx.x];
+    double Zi[3][3];
+    const double dz = inv3(in.Z, Zi);
+    double G[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) G[i][j] = in.Z[0][i] * in.Z[0][j] + in.Z[1][i] * in.Z[1][j] + in.Z[2][i] * in.Z[2][j];
+    const double Jz = sqrt(fabs(det3(G)));
+    (void)dz;
+    for (int z = 0; z < 3; ++z)
+      for (int nh = 0; nh < 3; ++nh) S.wJZi[threadIdx.x][z * 3 + nh] = in.w * Jz * Zi[z][nh];
+  }
+  __syncthreads();
+}
+
+// exact element tangent entry (r, c)
+__device__ __forceinline__ double tangent_entry(const Tables& T, const TanShared& S, int r, int c) {
+  double s = 0.0;
+  if (r < 81 && c < 81) {
+    const int mh = r / NQ, ms = r % NQ, nh = c / NQ, ns = c % NQ;
+    for (int g = 0; g < NG; ++g) {
+      // sum_xi g_ms[xi] sum_zeta dP[xi][mh]/dZ[nh][zeta] g_ns[zeta]
+      double t = 0.0;
+#pragma unroll
+      for (int zeta = 0; zeta < 3; ++zeta) {
+        const double* d = S.dPdZ[g][nh * 3 + zeta];
+        t += (T.dphi[g][0][ms] * d[0 * 3 + mh] + T.dphi[g][1][ms] * d[1 * 3 + mh] + T.dphi[g][2][ms] * d[2 * 3 + mh]) *
+             T.dphi[g][zeta][ns];
+      }
+      s += t;
+    }
+  } else if (r < 81 && c >= 81) {
+    const int mh = r / NQ, ms = r % NQ, ns = c - 81;
+    for (int g = 0; g < NG; ++g) {
+      const double* d = S.dPdZ[g][9];
+      s += (T.dphi[g][0][ms] * d[mh] + T.dphi[g][1][ms] * d[3 + mh] + T.dphi[g][2][ms] * d[6 + mh]) * T.psi[g][ns];
+    }
+  } else if (r >= 81 && c < 81) {
+    const int ms = r - 81, nh = c / NQ, ns = c % NQ;
+    for (int g = 0; g < NG; ++g) {
+      const double* a = S.wJZi[g];
+      s += T.psi[g][ms] * (a[0 * 3 + nh] * T.dphi[g][0][ns] + a[1 * 3 + nh] * T.dphi[g][1][ns] +
+                           a[2 * 3 + nh] * T.dphi[g][2][ns]);
+    }
+  }
+  return s;
+}
+
+__device__ __forceinline__ void load_element_state(int e, const int32_t* eq2, const int32_t* elin, int nq2,
+                                                   const double* xg, const double* dep, double* sx, double* sz,
+                                                   double* sp, int* dofs) {
+  for (int i = threadIdx.x; i < NQ; i += blockDim.x) {
+    const int n = __ldg(eq2 + (size_t)e * NQ + i);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      sx[c * NQ + i] = __ldg(xg + (size_t)c * nq2 + n);
+      sz[c * NQ + i] = dep[(size_t)c * nq2 + n];
+      if (dofs) dofs[c * NQ + i] = c * nq2 + n;
+    }
+  }
+  if (threadIdx.x < NL) {
+    const int n = __ldg(elin + (size_t)e * NL + threadIdx.x);
+    sp[threadIdx.x] = dep[(size_t)3 * nq2 + n];
+    if (dofs) dofs[81 + threadIdx.x] = 3 * nq2 + n;
+  }
+}
+
+__global__ void __launch_bounds__(kTanThreads)
+mr_tangent_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
+                  const int32_t* __restrict__ elin, int32_t nq2, const double* __restrict__ xg,
+                  const double* __restrict__ dep, const double* __restrict__ cpar, const Tables* __restrict__ Tg,
+                  const int32_t* __restrict__ slots, double* __restrict__ values, double* __restrict__ Kout) {
+  extern __shared__ double smem[];
+  Tables& T = *reinterpret_cast<Tables*>(smem);
+  TanShared& S = *reinterpret_cast<TanShared*>(smem + sizeof(Tables) / sizeof(double));
+  for (int i = threadIdx.x; i < (int)(sizeof(Tables) / sizeof(double)); i += blockDim.x)
+    smem[i] = reinterpret_cast<const double*>(Tg)[i];
+  const double c1 = cpar[0], c2 = cpar[1];
+  for (int item = blockIdx.x; item < count; item += gridDim.x) {
+    const int e = __ldg(elems + item);
+    __syncthreads();
+    load_element_state(e, eq2, elin, nq2, xg, dep, S.x, S.z, S.p, nullptr);
+    __syncthreads();
+    tangent_points(T, S, c1, c2);
+    const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
+    for (int k = threadIdx.x; k < ND * ND; k += blockDim.x) {
+      const int r = k / ND, c = k % ND;
+      const double v = (r >= 81 && c >= 81) ? 0.0 : tangent_entry(T, S, r, c);
+      if (Kout) Kout[(size_t)e * ND * ND + k] = v;
+      if (sl && !(r >= 81 && c >= 81)) {
+        const int pos = __ldg(sl + k);
+        if (pos >= 0) values[pos] += v;
+      }
+    }
+  }
+}
+
+// Vector-Jacobian products of `batch` problems: du[b] = v[b]^T dR/d(dep), dc[b] = v[b]^T dR/d(c10, c01).
+// Elements colour by colour (du scatter without conflicts); dc accumulated per element into
+// dc_elem[b][E][2] and summed afterwards in fixed order.
+__global__ void __launch_bounds__(kTanThreads)
+mr_vjp_kernel(const int32_t* __restrict__ elems, int32_t count, int32_t batch, const int32_t* __restrict__ eq2,
+              const int32_t* __restrict__ elin, int32_t nq2, int32_t nlin, const double* __restrict__ xg,
+              const double* __restrict__ dep, const double* __restrict__ cpar, const double* __restrict__ v,
+              const Tables* __restrict__ Tg, double* __restrict__ du, double* __restrict__ dc_elem, int32_t n_elem) {
+  extern __shared__ double smem[];
+  Tables& T = *reinterpret_cast<Tables*>(smem);
+  TanShared& S = *reinterpret_cast<TanShared*>(smem + sizeof(Tables) / sizeof(double));
+  double* vv = reinterpret_cast<double*>(&S + 1);  // [89] element adjoint
+  double* Vg = vv + ND;                            // [27][9] V_g[xi][mh] ; [27] Vp_g
+  double* Vp = Vg + NG * 9;
+  double* dcs = Vp + NG;                           // [27][2]
+  for (int i = threadIdx.x; i < (int)(sizeof(Tables) / sizeof(double)); i += blockDim.x)
+    smem[i] = reinterpret_cast<const double*>(Tg)[i];
+  const int64_t ndof = 3ll * nq2 + nlin;
+  for (long long item = blockIdx.x; item < (long long)count * batch; item += gridDim.x) {
+    const int b = (int)(item / count);
+    const int li = (int)(item % count);
+    const int e = __ldg(elems + li);
+    const double* d = dep + b * ndof;
+    const double c1 = cpar[2 * b], c2 = cpar[2 * b + 1];
+    __syncthreads();
+    load_element_state(e, eq2, elin, nq2, xg, d, S.x, S.z, S.p, S.dofs);
+    __syncthreads();
+    for (int i = threadIdx.x; i < ND; i += blockDim.x) vv[i] = v[b * ndof + S.dofs[i]];
+    tangent_points(T, S, c1, c2);  // contains __syncthreads
+    // V_g[xi][mh] = sum_ms v(mh,ms) g_ms[xi];  Vp_g = sum_ms v_p(ms) psi_ms
+    for (int t = threadIdx.x; t < NG * 10; t += blockDim.x) {
+      const int g = t / 10, k = t % 10;
+      if (k < 9) {
+        const int xi = k / 3, mh = k % 3;
+        double s = 0.0;
+        for (int ms = 0; ms < NQ; ++ms) s += vv[mh * NQ + ms] * T.dphi[g][xi][ms];
+        Vg[g * 9 + k] = s;
+      } else {
+        double s = 0.0;
+        for (int ms = 0; ms < NL; ++ms) s += vv[81 + ms] * T.psi[g][ms];
+        Vp[g] = s;
+      }
+    }
+    __syncthreads();
+    // dc: P is affine in (c1, c2) with the pressure term independent of c: dP/dc1 = P(1,0,p=0)
+    if (threadIdx.x < NG) {
+      const int g = threadIdx.x;
+      const GPIn& in = S.in[g];
+      double acc[2];
+      for (int q = 0; q < 2; ++q) {
+        double Pm[3][3], Jz;
+        point_P<double>(in.Z, in.A, in.Jx, in.w, 0.0, q == 0 ? 1.0 : 0.0, q == 0 ? 0.0 : 1.0, Pm, Jz);
+        double s = 0.0;
+        for (int xi = 0; xi < 3; ++xi)
+          for (int mh = 0; mh < 3; ++mh) s += Vg[g * 9 + xi * 3 + mh] * Pm[xi][mh];
+        acc[q] = s;
+      }
+      dcs[g * 2] = acc[0];
+      dcs[g * 2 + 1] = acc[1];
+    }
+    __syncthreads();
+    if (threadIdx.x < 2) {
+      double s = 0.0;
+      for (int g = 0; g < NG; ++g) s += dcs[g * 2 + threadIdx.x];
+      dc_elem[((size_t)b * n_elem + e) * 2 + threadIdx.x] = s;
+    }
+    // du entries: u columns (nh, ns) and p columns
+    double* dub = du + b * ndof;
+    for (int cidx = threadIdx.x; cidx < ND; cidx += blockDim.x) {
+      double s = 0.0;
+      if (cidx < 81) {
+        const int nh = cidx / NQ, ns = cidx % NQ;
+        for (int g = 0; g < NG; ++g) {
+          double t = 0.0;
+#pragma unroll
+          for (int zeta = 0; zeta < 3; ++zeta) {
+            const double* dp = S.dPdZ[g][nh * 3 + zeta];
+            double vz = 0.0;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) vz += Vg[g * 9 + k] * dp[k];
+            vz += Vp[g] * S.wJZi[g][zeta * 3 + nh];
+            t += vz * T.dphi[g][zeta][ns];
+          }
+          s += t;
+        }
+      } else {
+        const int ns = cidx - 81;
+        for (int g = 0; g < NG; ++g) {
+          double vz = 0.0;
+#pragma unroll
+          for (int k = 0; k < 9; ++k) vz += Vg[g * 9 + k] * S.dPdZ[g][9][k];
+          s += vz * T.psi[g][ns];
+        }
+      }
+      dub[S.dofs[cidx]] += s;
+    }
+  }
+}
+
+__global__ void sum_dc(const double* __restrict__ dc_elem, int32_t n_elem, int32_t batch, double* __restrict__ dc) {
+  const int b = blockIdx.x, q = threadIdx.x & 1;
+  if (threadIdx.x >= 2) return;
+  double s = 0.0;
+  for (int e = 0; e < n_elem; ++e) s += dc_elem[((size_t)b * n_elem + e) * 2 + q];
+  dc[b * 2 + q] = s;
+}
+
+size_t tangent_smem() { return sizeof(Tables) + sizeof(TanShared); }
+size_t vjp_smem() { return sizeof(Tables) + sizeof(TanShared) + sizeof(double) * (ND + NG * 9 + NG + NG * 2); }
+
+size_t residual_smem() { return sizeof(Tables) + kResWarps * sizeof(double) * (81 + 81 + 8 + NG * 9 + NG + 48); }
+size_t jacobian_smem() { return sizeof(Tables) + sizeof(JacShared); }
+
+int check_mesh(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin, const double* xg,
+               const char* fn) {
+  if (n_elem < 0 || nq2 <= 0 || nlin <= 0 || (n_elem > 0 && (!eq2 || !elin || !xg)))
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid mesh arguments", fn);
+  return GFE_OK;
+}
+
+int set_smem(const void* kernel, size_t bytes) {
+  GFE_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return GFE_OK;
+}
+
+}  // namespace
+
+extern "C" int gfe_mr_residual(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
+                               const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host,
+                               int32_t n_colors, int32_t batch, const double* dep, const double* cpar, double* R,
+                               void* stream) {
+  const char* fn = "gfe_mr_residual";
+  int rc = check_mesh(n_elem, eq2, elin, nq2, nlin, xg, fn);
+  if (rc) return rc;
+  if (batch <= 0 || !dep || !cpar || !R || (n_elem > 0 && (!color_elems || !color_ptr_host || n_colors <= 0)))
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (color_ptr_host[0] != 0 || color_ptr_host[n_colors] != n_elem)
+    return gfe::set_error(GFE_ERR_ARG, "%s: colour offsets must run from 0 to n_elem", fn);
+  const Tables* T = nullptr;
+  if ((rc = device_tables(&T))) return rc;
+  cudaStream_t s = gfe::as_stream(stream);
+  const int64_t ndof = 3ll * nq2 + nlin;
+  GFE_CUDA_TRY(cudaMemsetAsync(R, 0, sizeof(double) * ndof * batch, s));
+  const size_t sm = residual_smem();
+  if ((rc = set_smem((const void*)mr_residual_kernel, sm))) return rc;
+  unsigned* err = gfe::device_error_word();
+  void* prof = gfe::stage_begin(GFE_STAGE_MR_RESIDUAL, s);
+  int launches = 0;
+  for (int c = 0; c < n_colors; ++c) {
+    const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
+    if (cnt <= 0) continue;
+    const long long items = (long long)cnt * batch;
+    const int grid = (int)std::min<long long>((items + kResWarps - 1) / kResWarps, 16ll * gfe::sm_count());
+    mr_residual_kernel<<<grid, kResWarps * 32, sm, s>>>(color_elems + c0, cnt, batch, eq2, elin, nq2, nlin, xg, dep,
+                                                       cpar, T, R, ndof, err);
+    ++launches;
+  }
+  gfe::stage_end(GFE_STAGE_MR_RESIDUAL, prof, s, launches);
+  GFE_LAUNCH_CHECK(fn);
+  return GFE_OK;
+}
+
+extern "C" int gfe_mr_slot_map(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2,
+                               const int32_t* color_elems, const int32_t* row_ptr, const int32_t* col_idx,
+                               int32_t* slots, void* stream) {
+  const char* fn = "gfe_mr_slot_map";
+  if (n_elem < 0 || !eq2 || !elin || !color_elems || !row_ptr || !col_idx || !slots)
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (n_elem == 0) return GFE_OK;
+  cudaStream_t s = gfe::as_stream(stream);
+  mr_slot_kernel<<<16 * gfe::sm_count(), 256, 0, s>>>(color_elems, n_elem, eq2, elin, nq2, row_ptr, col_idx, slots);
+  GFE_LAUNCH_CHECK(fn);
+  return GFE_OK;
+}
+
+extern "C" int gfe_mr_jacobian(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
+                               const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host,
+                               int32_t n_colors, const double* dep, const double* cpar, const int32_t* slots,
+                               double* values, int64_t nnz, double* K_out, void* stream) {
+  const char* fn = "gfe_mr_jacobian";
+  int rc = check_mesh(n_elem, eq2, elin, nq2, nlin, xg, fn);
+  if (rc) return rc;
+  if (!dep || !cpar || (n_elem > 0 && (!color_elems || !color_ptr_host || n_colors <= 0)))
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (!K_out && (!slots || !values)) return gfe::set_error(GFE_ERR_ARG, "%s: need CSR values + slots or K_out", fn);
+  if (color_ptr_host[0] != 0 || color_ptr_host[n_colors] != n_elem)
+    return gfe::set_error(GFE_ERR_ARG, "%s: colour offsets must run from 0 to n_elem", fn);
+  const Tables* T = nullptr;
+  if ((rc = device_tables(&T))) return rc;
+  cudaStream_t s = gfe::as_stream(stream);
+  if (values) GFE_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)nnz, s));
+  const size_t sm = jacobian_smem();
+  if ((rc = set_smem((const void*)mr_jacobian_kernel, sm))) return rc;
+  unsigned* err = gfe::device_error_word();
+  void* prof = gfe::stage_begin(GFE_STAGE_MR_JACOBIAN, s);
+  int launches = 0;
+  for (int c = 0; c < n_colors; ++c) {
+    const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
+    if (cnt <= 0) continue;
+    const int grid = std::min(cnt, 8 * gfe::sm_count());
+    mr_jacobian_kernel<<<grid, kJacThreads, sm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, nlin, xg, dep, cpar, T,
+                                                      slots ? slots + (size_t)c0 * ND * ND : nullptr, values, K_out,
+                                                      err);
+    ++launches;
+  }
+  gfe::stage_end(GFE_STAGE_MR_JACOBIAN, prof, s, launches);
+  GFE_LAUNCH_CHECK(fn);
+  return GFE_OK;
+}
+
+extern "C" int gfe_mr_tangent(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
+                              const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host,
+                              int32_t n_colors, const double* dep, const double* cpar, const int32_t* slots,
+                              double* values, int64_t nnz, double* K_out, void* stream) {
+  const char* fn = "gfe_mr_tangent";
+  int rc = check_mesh(n_elem, eq2, elin, nq2, nlin, xg, fn);
+  if (rc) return rc;
+  if (!dep || !cpar || (n_elem > 0 && (!color_elems || !color_ptr_host || n_colors <= 0)))
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (!K_out && (!slots || !values)) return gfe::set_error(GFE_ERR_ARG, "%s: need CSR values + slots or K_out", fn);
+  if (color_ptr_host[0] != 0 || color_ptr_host[n_colors] != n_elem)
+    return gfe::set_error(GFE_ERR_ARG, "%s: colour offsets must run from 0 to n_elem", fn);
+  const Tables* T = nullptr;
+  if ((rc = device_tables(&T))) return rc;
+  cudaStream_t s = gfe::as_stream(stream);
+  if (values) GFE_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)nnz, s));
+  const size_t sm = tangent_smem();
+  if ((rc = set_smem((const void*)mr_tangent_kernel, sm))) return rc;
+  void* prof = gfe::stage_begin(GFE_STAGE_MR_JACOBIAN, s);
+  int launches = 0;
+  for (int c = 0; c < n_colors; ++c) {
+    const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
+    if (cnt <= 0) continue;
+    const int grid = std::min(cnt, 8 * gfe::sm_count());
+    mr_tangent_kernel<<<grid, kTanThreads, sm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar, T,
+                                                     slots ? slots + (size_t)c0 * ND * ND : nullptr, values, K_out);
+    ++launches;
+  }
+  gfe::stage_end(GFE_STAGE_MR_JACOBIAN, prof, s, launches);
+  GFE_LAUNCH_CHECK(fn);
+  return GFE_OK;
+}
+
+extern "C" int gfe_mr_residual_vjp(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2,
+                                   int32_t nlin, const double* xg, const int32_t* color_elems,
+                                   const int32_t* color_ptr_host, int32_t n_colors, int32_t batch, const double* dep,
+                                   const double* cpar, const double* v, double* du, double* dc, void* stream) {
+  const char* fn = "gfe_mr_residual_vjp";
+  int rc = check_mesh(n_elem, eq2, elin, nq2, nlin, xg, fn);
+  if (rc) return rc;
+  if (batch <= 0 || !dep || !cpar || !v || !du || !dc || (n_elem > 0 && (!color_elems || !color_ptr_host)))
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (color_ptr_host[0] != 0 || color_ptr_host[n_colors] != n_elem)
+    return gfe::set_error(GFE_ERR_ARG, "%s: colour offsets must run from 0 to n_elem", fn);
+  const Tables* T = nullptr;
+  if ((rc = device_tables(&T))) return rc;
+  cudaStream_t s = gfe::as_stream(stream);
+  const int64_t ndof = 3ll * nq2 + nlin;
+  GFE_CUDA_TRY(cudaMemsetAsync(du, 0, sizeof(double) * ndof * batch, s));
+  double* dc_elem = nullptr;
+  if ((rc = gfe::scratch_alloc((void**)&dc_elem, sizeof(double) * 2 * (size_t)n_elem * batch, s, "vjp partials")))
+    return rc;
+  const size_t sm = vjp_smem();
+  if ((rc = set_smem((const void*)mr_vjp_kernel, sm))) { gfe::scratch_free(dc_elem, s); return rc; }
+  for (int c = 0; c < n_colors; ++c) {
+    const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
+    if (cnt <= 0) continue;
+    const long long items = (long long)cnt * batch;
+    const int grid = (int)std::min<long long>(items, 8ll * gfe::sm_count());
+    mr_vjp_kernel<<<grid, kTanThreads, sm, s>>>(color_elems + c0, cnt, batch, eq2, elin, nq2, nlin, xg, dep, cpar, v,
+                                                T, du, dc_elem, n_elem);
+  }
+  sum_dc<<<batch, 32, 0, s>>>(dc_elem, n_elem, batch, dc);
+  gfe::scratch_free(dc_elem, s);
+  GFE_LAUNCH_CHECK(fn);
+  return GFE_OK;
+}

@@ -59,6 +59,10 @@ def _register_mr(L):
     if hasattr(L, "orc_mr_element_jacobian_fd"):
         L.orc_mr_element_jacobian_fd.argtypes = [f64p, f64p, f64p, C.c_double, C.c_double, C.c_double, f64p]
         L.orc_mr_element_jacobian_fd.restype = C.c_int
+    if hasattr(L, "orc_mr_assemble_residual"):
+        L.orc_mr_assemble_residual.argtypes = [C.c_int, i32p, i32p, C.c_int, C.c_int, f64p, f64p, f64p, f64p]
+        L.orc_mr_assemble_jacobian.argtypes = [C.c_int, i32p, i32p, C.c_int, C.c_int, f64p, f64p, f64p, i32p, i32p,
+                                               f64p, C.c_int, C.c_double]
 
 
 def _i32(a):
@@ -164,6 +168,44 @@ def spmv(rp, ci, vals, x):
     y = np.zeros(n)
     lib().orc_csr_spmv(n, _i32(rp), _i32(ci), _f64(vals), _f64(x), y)
     return y
+
+
+def mr_element_residual(xe, ze, pe, c1, c2):
+    R = np.zeros(89)
+    lib().orc_mr_element_residual(_f64(xe), _f64(ze), _f64(pe), float(c1), float(c2), R)
+    return R
+
+
+def mr_element_jacobian(xe, ze, pe, c1, c2):
+    K = np.zeros((89, 89))
+    lib().orc_mr_element_jacobian(_f64(xe), _f64(ze), _f64(pe), float(c1), float(c2), K)
+    return K
+
+
+def mr_element_jacobian_fd(xe, ze, pe, c1, c2, delta):
+    K = np.zeros((89, 89))
+    lib().orc_mr_element_jacobian_fd(_f64(xe), _f64(ze), _f64(pe), float(c1), float(c2), float(delta), K)
+    return K
+
+
+def mr_assemble_residual(eq2, elin, nq2, nlin, xg, dep, c):
+    E = eq2.shape[0]
+    cc = np.broadcast_to(np.asarray(c, np.float64), (E, 2)) if np.ndim(c) == 1 else np.asarray(c, np.float64)
+    R = np.zeros(3 * nq2 + nlin)
+    lib().orc_mr_assemble_residual(E, _i32(eq2), _i32(elin), nq2, nlin, _f64(xg), _f64(dep), _f64(cc), R)
+    return R
+
+
+def mr_assemble_jacobian(eq2, elin, nq2, nlin, xg, dep, c, rp, ci, fd_delta=None):
+    E = eq2.shape[0]
+    cc = np.broadcast_to(np.asarray(c, np.float64), (E, 2)) if np.ndim(c) == 1 else np.asarray(c, np.float64)
+    vals = np.zeros(int(rp[-1]) - 1)
+    rc = lib().orc_mr_assemble_jacobian(E, _i32(eq2), _i32(elin), nq2, nlin, _f64(xg), _f64(dep), _f64(cc), _i32(rp),
+                                        _i32(ci), vals, 0 if fd_delta is None else 1,
+                                        0.0 if fd_delta is None else float(fd_delta))
+    if rc != 0:
+        raise RuntimeError(f"oracle Jacobian assembly failed ({rc})")
+    return vals
 
 
 def cg_dirichlet(rp, ci, vals, f, fixed, x_fixed, rtol=1e-12, max_it=100000):

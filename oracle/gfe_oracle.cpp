@@ -516,3 +516,359 @@ int orc_cg_dirichlet(int n, const int32_t* rp, const int32_t* ci, const double* 
 }
 
 }  // extern "C"
+
+// =========================================================================================
+// Finite elasticity, Mooney-Rivlin subtype, mixed u-p (triquadratic u + trilinear p), 3D.
+// =========================================================================================
+namespace {
+
+// Voigt maps, src/constants.F90:305-306: 1=(1,1) 2=(2,2) 3=(3,3) 4=(1,2) 5=(1,3) 6=(2,3).
+const int kT2V[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
+const int kV2T[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+
+struct MRBases {
+  TPBasis q2;  // dependent / geometric basis
+  TPBasis q1;  // pressure basis (same Gauss scheme)
+};
+
+const MRBases& mr_bases(int ngauss) {
+  static MRBases b2, b3, b4;
+  MRBases* b = ngauss == 2 ? &b2 : (ngauss == 3 ? &b3 : &b4);
+  if (b->q2.nns == 0) {
+    int o2[3] = {2, 2, 2}, o1[3] = {1, 1, 1}, g[3] = {ngauss, ngauss, ngauss};
+    make_tp_basis(3, o2, g, b->q2);
+    make_tp_basis(3, o1, g, b->q1);
+  }
+  return *b;
+}
+
+void matmul3(const double A[3][3], const double B[3][3], double C[3][3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += A[i][k] * B[k][j];
+      C[i][j] = s;
+    }
+}
+
+// Deformation gradient dZ/dNu, src/finite_elasticity_routines.F90:5148-5215, with the material
+// frame of src/coordinate_routines.F90:3841-3947 when there is no fibre field: dX/dNu columns are
+// the normalised columns of DX_DXI (geometry); dNu/dXi = (dX/dNu)^T DX_DXI; dXi/dNu = inv(dNu/dXi).
+void deformation_gradient(const Metrics& mz, const Metrics& mx, double F[3][3]) {
+  double dXdNu[3][3], dNudX[3][3], dNudXi[3][3], dXidNu[3][3];
+  for (int xi = 0; xi < 3; ++xi) {
+    double n = std::sqrt(mx.dx_dxi[0][xi] * mx.dx_dxi[0][xi] + mx.dx_dxi[1][xi] * mx.dx_dxi[1][xi] +
+                         mx.dx_dxi[2][xi] * mx.dx_dxi[2][xi]);
+    for (int c = 0; c < 3; ++c) dXdNu[c][xi] = mx.dx_dxi[c][xi] / n;
+  }
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) dNudX[i][j] = dXdNu[j][i];
+  matmul3(dNudX, mx.dx_dxi, dNudXi);
+  invert(3, dNudXi, dXidNu);
+  matmul3(mz.dx_dxi, dXidNu, F);
+}
+
+// Push-forward of a Voigt 2nd-order tensor, src/finite_elasticity_routines.F90:1343-1375:
+// t(i,j) = F(a_i,a_j)F(b_i,b_j) (+ F(a_i,b_j)F(b_i,a_j) for shear columns), S <- t S / J.
+void push_tensor_t(const double F[3][3], double t[6][6]) {
+  for (int j = 0; j < 6; ++j)
+    for (int i = 0; i < 6; ++i) {
+      const int ai = kV2T[i][0], bi = kV2T[i][1], aj = kV2T[j][0], bj = kV2T[j][1];
+      double v = F[ai][aj] * F[bi][bj];
+      if (j >= 3) v += F[ai][bj] * F[bi][aj];
+      t[i][j] = v;
+    }
+}
+
+void push_stress(double S[6], const double F[3][3], double J) {
+  double t[6][6], out[6];
+  push_tensor_t(F, t);
+  for (int i = 0; i < 6; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < 6; ++j) s += t[i][j] * S[j];
+    out[i] = s / J;
+  }
+  for (int i = 0; i < 6; ++i) S[i] = out[i];
+}
+
+// src/finite_elasticity_routines.F90:1303-1336: D <- t D t^T / J
+void push_elasticity(double D[6][6], const double F[3][3], double J) {
+  double t[6][6], tmp[6][6];
+  push_tensor_t(F, t);
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 6; ++k) s += t[i][k] * D[k][j];
+      tmp[i][j] = s;
+    }
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 6; ++k) s += tmp[i][k] * t[j][k];
+      D[i][j] = s / J;
+    }
+}
+
+// Cauchy stress of the MR subtype in the residual, src/finite_elasticity_routines.F90:6985-7061:
+// Fbar = J^(-1/3) F, Cbar = Fbar^T Fbar, Sbar = -2 c2 Cbar + 2 (c1 + I1 c2) I (Voigt),
+// sigma_bar = push(Sbar, Fbar, J), sigma = dev(sigma_bar) + p I.
+void mr_cauchy_stress(const double F[3][3], double J, double p, double c1, double c2, double sig[6]) {
+  double Fb[3][3], C[3][3];
+  const double s = std::pow(J, -1.0 / 3.0);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) Fb[i][j] = F[i][j] * s;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double v = 0.0;
+      for (int k = 0; k < 3; ++k) v += Fb[k][i] * Fb[k][j];
+      C[i][j] = v;
+    }
+  const double I1 = C[0][0] + C[1][1] + C[2][2];
+  const double t1 = -2.0 * c2, t2 = 2.0 * (c1 + I1 * c2);
+  sig[0] = t1 * C[0][0] + t2; sig[1] = t1 * C[1][1] + t2; sig[2] = t1 * C[2][2] + t2;
+  sig[3] = t1 * C[1][0]; sig[4] = t1 * C[2][0]; sig[5] = t1 * C[2][1];
+  push_stress(sig, Fb, J);
+  const double tr3 = (sig[0] + sig[1] + sig[2]) / 3.0;
+  for (int i = 0; i < 3; ++i) sig[i] = sig[i] - tr3 + p;
+}
+
+struct MRPoint {
+  Metrics mx, mz;
+  double F[3][3], Jznu, p, dphidz[27][3], psi[8], w;
+};
+
+void mr_point(const MRBases& B, int g, const double* const* x, const double* const* z, const double* pe,
+              MRPoint& P) {
+  metrics_at(B.q2, g, z, 3, P.mz);
+  metrics_at(B.q2, g, x, 3, P.mx);
+  const int nns = B.q2.nns;
+  for (int ns = 0; ns < nns; ++ns)
+    for (int mh = 0; mh < 3; ++mh) {
+      double s = 0.0;
+      for (int mi = 0; mi < 3; ++mi) s += P.mz.dxi_dx[mi][mh] * B.q2.tab[((size_t)g * 4 + mi + 1) * nns + ns];
+      P.dphidz[ns][mh] = s;
+    }
+  deformation_gradient(P.mz, P.mx, P.F);
+  P.Jznu = P.mz.jac / P.mx.jac;
+  P.w = B.q2.wts[g];
+  double pv = 0.0;
+  for (int ms = 0; ms < 8; ++ms) {
+    P.psi[ms] = B.q1.tab[((size_t)g * 4 + 0) * 8 + ms];
+    pv += P.psi[ms] * pe[ms];
+  }
+  P.p = pv;
+}
+
+// Element residual (89), src/finite_elasticity_routines.F90:1669-1756.
+void mr_residual_element(const double* xg /*[3][27]*/, const double* zg /*[3][27]*/, const double* pe /*[8]*/,
+                         double c1, double c2, double* R /*[89]*/, int ngauss = 3) {
+  const MRBases& B = mr_bases(ngauss);
+  const double* x[3] = {xg, xg + 27, xg + 54};
+  const double* z[3] = {zg, zg + 27, zg + 54};
+  std::fill(R, R + 89, 0.0);
+  MRPoint P;
+  for (int g = 0; g < B.q2.ng; ++g) {
+    mr_point(B, g, x, z, pe, P);
+    double sig[6];
+    mr_cauchy_stress(P.F, P.Jznu, P.p, c1, c2, sig);
+    const double jgw = P.mz.jac * P.w;
+    double jgwc[3][3];
+    for (int mh = 0; mh < 3; ++mh)
+      for (int nh = 0; nh < 3; ++nh) jgwc[mh][nh] = jgw * sig[kT2V[mh][nh]];
+    for (int mh = 0; mh < 3; ++mh)
+      for (int ms = 0; ms < 27; ++ms) {
+        double d = 0.0;
+        for (int k = 0; k < 3; ++k) d += P.dphidz[ms][k] * jgwc[k][mh];
+        R[mh * 27 + ms] += d;
+      }
+    const double tt = P.mx.jac * P.w * (P.Jznu - 1.0);
+    for (int ms = 0; ms < 8; ++ms) R[81 + ms] += tt * P.psi[ms];
+  }
+}
+
+// Iron's analytic element Jacobian (89x89, row-major K[mhs][nhs]),
+// src/finite_elasticity_routines.F90:1016-1274 with FINITE_ELASTICITY_GAUSS_ELASTICITY_TENSOR :649-795.
+void mr_jacobian_element(const double* xg, const double* zg, const double* pe, double c1, double c2,
+                         double* K /*[89][89]*/, int ngauss = 3) {
+  const MRBases& B = mr_bases(ngauss);
+  const double* x[3] = {xg, xg + 27, xg + 54};
+  const double* z[3] = {zg, zg + 27, zg + 54};
+  std::fill(K, K + 89 * 89, 0.0);
+  MRPoint P;
+  for (int g = 0; g < B.q2.ng; ++g) {
+    mr_point(B, g, x, z, pe, P);
+    // elasticity tensor with the unmodified F (AZL = F^T F)
+    double C[3][3], Ci[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        double v = 0.0;
+        for (int k = 0; k < 3; ++k) v += P.F[k][i] * P.F[k][j];
+        C[i][j] = v;
+      }
+    const double I3 = invert(3, C, Ci);
+    const double L[6] = {C[0][0], C[1][1], C[2][2], C[0][1], C[0][2], C[1][2]};
+    const double U[6] = {Ci[0][0], Ci[1][1], Ci[2][2], Ci[0][1], Ci[0][2], Ci[1][2]};
+    // I3EE filled column by column (Fortran RESHAPE), I3EE[row][col]
+    const double cols[6][6] = {{0.0, 4 * L[2], 4 * L[1], 0.0, 0.0, -4 * L[5]},
+                               {4 * L[2], 0.0, 4 * L[0], 0.0, -4 * L[4], 0.0},
+                               {4 * L[1], 4 * L[0], 0.0, -2 * L[3], 0.0, 0.0},
+                               {0.0, 0.0, -4 * L[3], -2 * L[2], 2 * L[5], 2 * L[4]},
+                               {0.0, -4 * L[4], 0.0, 2 * L[5], -2 * L[1], 2 * L[3]},
+                               {-4 * L[5], 0.0, 0.0, 2 * L[4], 2 * L[3], -2 * L[0]}};
+    double D[6][6];
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j) D[i][j] = 0.0;
+    const double I1 = C[0][0] + C[1][1] + C[2][2];
+    double S[6] = {-2 * c2 * C[0][0] + 2 * (c1 + I1 * c2), -2 * c2 * C[1][1] + 2 * (c1 + I1 * c2),
+                   -2 * c2 * C[2][2] + 2 * (c1 + I1 * c2), -2 * c2 * C[1][0], -2 * c2 * C[2][0], -2 * c2 * C[2][1]};
+    D[1][0] = D[2][0] = D[0][1] = D[2][1] = D[0][2] = D[1][2] = 4 * c2;
+    D[3][3] = D[4][4] = D[5][5] = -2 * c2;
+    for (int i = 0; i < 6; ++i)
+      for (int j = 0; j < 6; ++j) D[i][j] += P.p * (-2.0 * U[i] * U[j] + 0.5 * cols[j][i] / I3);
+    double H[6] = {U[0], U[1], U[2], U[3], U[4], U[5]};
+    push_stress(S, P.F, P.Jznu);
+    push_stress(H, P.F, P.Jznu);
+    push_elasticity(D, P.F, P.Jznu);
+    for (int i = 0; i < 3; ++i) S[i] += P.p;
+    double sig[3][3], hyd[3][3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) { sig[i][j] = S[kT2V[i][j]]; hyd[i][j] = H[kT2V[i][j]]; }
+    const double jgw = P.mz.jac * P.w;
+    // diagonal component blocks, lower triangle ms >= ns
+    for (int nh = 0; nh < 3; ++nh) {
+      double sub[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) sub[i][j] = jgw * (D[kT2V[i][nh]][kT2V[j][nh]] + sig[i][j]);
+      for (int ns = 0; ns < 27; ++ns) {
+        double tv[3];
+        for (int i = 0; i < 3; ++i) tv[i] = sub[i][0] * P.dphidz[ns][0] + sub[i][1] * P.dphidz[ns][1] + sub[i][2] * P.dphidz[ns][2];
+        for (int ms = ns; ms < 27; ++ms)
+          K[(size_t)(nh * 27 + ms) * 89 + nh * 27 + ns] +=
+              P.dphidz[ms][0] * tv[0] + P.dphidz[ms][1] * tv[1] + P.dphidz[ms][2] * tv[2];
+      }
+    }
+    // off-diagonal component blocks (nh, mh) = (1,2), (1,3), (2,3): rows mh, columns nh
+    const int offn[3] = {0, 0, 1}, offm[3] = {1, 2, 2};
+    for (int oh = 0; oh < 3; ++oh) {
+      const int nh = offn[oh], mh = offm[oh];
+      double sub[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) sub[i][j] = jgw * D[kT2V[i][mh]][kT2V[j][nh]];
+      for (int ns = 0; ns < 27; ++ns) {
+        double tv[3];
+        for (int i = 0; i < 3; ++i) tv[i] = sub[i][0] * P.dphidz[ns][0] + sub[i][1] * P.dphidz[ns][1] + sub[i][2] * P.dphidz[ns][2];
+        for (int ms = 0; ms < 27; ++ms)
+          K[(size_t)(mh * 27 + ms) * 89 + nh * 27 + ns] +=
+              P.dphidz[ms][0] * tv[0] + P.dphidz[ms][1] * tv[1] + P.dphidz[ms][2] * tv[2];
+      }
+    }
+    // pressure rows, displacement columns
+    for (int nh = 0; nh < 3; ++nh)
+      for (int ns = 0; ns < 27; ++ns) {
+        const double a = jgw * P.dphidz[ns][nh];
+        for (int ms = 0; ms < 8; ++ms) K[(size_t)(81 + ms) * 89 + nh * 27 + ns] += a * P.psi[ms];
+      }
+    // displacement rows, pressure columns
+    for (int mh = 0; mh < 3; ++mh)
+      for (int ms = 0; ms < 27; ++ms) {
+        const double tvm = hyd[mh][0] * P.dphidz[ms][0] + hyd[mh][1] * P.dphidz[ms][1] + hyd[mh][2] * P.dphidz[ms][2];
+        const double a = jgw * tvm;
+        for (int ns = 0; ns < 8; ++ns) K[(size_t)(mh * 27 + ms) * 89 + 81 + ns] += a * P.psi[ns];
+      }
+  }
+  // mirror the displacement block's lower triangle to the upper (:1269-1274)
+  for (int nhs = 1; nhs < 81; ++nhs)
+    for (int mhs = 0; mhs < nhs; ++mhs) K[(size_t)mhs * 89 + nhs] = K[(size_t)nhs * 89 + mhs];
+}
+
+void mr_gather(int e, const int32_t* eq2, const int32_t* elin, int nq2, const double* xg_nodes, const double* dep,
+               double* xe, double* ze, double* pe) {
+  for (int s = 0; s < 27; ++s) {
+    int n = eq2[(size_t)e * 27 + s];
+    for (int c = 0; c < 3; ++c) {
+      xe[c * 27 + s] = xg_nodes[(size_t)c * nq2 + n];
+      ze[c * 27 + s] = dep[(size_t)c * nq2 + n];
+    }
+  }
+  for (int s = 0; s < 8; ++s) pe[s] = dep[(size_t)3 * nq2 + elin[(size_t)e * 8 + s]];
+}
+
+void mr_element_dofs(int e, const int32_t* eq2, const int32_t* elin, int nq2, int32_t* dofs /*1-based*/) {
+  for (int c = 0; c < 3; ++c)
+    for (int s = 0; s < 27; ++s) dofs[c * 27 + s] = c * nq2 + eq2[(size_t)e * 27 + s] + 1;
+  for (int s = 0; s < 8; ++s) dofs[81 + s] = 3 * nq2 + elin[(size_t)e * 8 + s] + 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_mr_element_residual(const double* xe, const double* ze, const double* pe, double c1, double c2, double* R) {
+  mr_residual_element(xe, ze, pe, c1, c2, R);
+  return 0;
+}
+
+int orc_mr_element_jacobian(const double* xe, const double* ze, const double* pe, double c1, double c2, double* K) {
+  mr_jacobian_element(xe, ze, pe, c1, c2, K);
+  return 0;
+}
+
+// Iron's one-sided finite-difference element Jacobian, src/equations_set_routines.F90:2839-2962:
+// column j = (R(u + delta e_j) - R(u)) / delta over the element's parameters in component order.
+// `delta` is (1 + ||all dependent parameters||_2) * step, computed by the caller.
+int orc_mr_element_jacobian_fd(const double* xe, const double* ze, const double* pe, double c1, double c2,
+                               double delta, double* K) {
+  double R0[89], R1[89], z[81], p[8];
+  std::copy(ze, ze + 81, z);
+  std::copy(pe, pe + 8, p);
+  mr_residual_element(xe, z, p, c1, c2, R0);
+  for (int j = 0; j < 89; ++j) {
+    double* v = j < 81 ? &z[j] : &p[j - 81];
+    const double orig = *v;
+    *v = orig + delta;
+    mr_residual_element(xe, z, p, c1, c2, R1);
+    *v = orig;
+    for (int i = 0; i < 89; ++i) K[(size_t)i * 89 + j] = (R1[i] - R0[i]) / delta;
+  }
+  return 0;
+}
+
+// Global residual (separated DOF order: z1, z2, z3 over the quadratic nodes, then p over the linear
+// nodes), assembled in element order like EquationsSet_ResidualEvaluateStaticFEM
+// (src/equations_set_routines.F90:5164-5286).  c: [E][2] (c10, c01) per element.
+int orc_mr_assemble_residual(int n_elem, const int32_t* eq2, const int32_t* elin, int nq2, int nlin,
+                             const double* xg_nodes, const double* dep, const double* c, double* R) {
+  const int ndof = 3 * nq2 + nlin;
+  std::fill(R, R + ndof, 0.0);
+  double xe[81], ze[81], pe[8], Re[89];
+  int32_t dofs[89];
+  for (int e = 0; e < n_elem; ++e) {
+    mr_gather(e, eq2, elin, nq2, xg_nodes, dep, xe, ze, pe);
+    mr_residual_element(xe, ze, pe, c[2 * e], c[2 * e + 1], Re);
+    mr_element_dofs(e, eq2, elin, nq2, dofs);
+    for (int i = 0; i < 89; ++i) R[dofs[i] - 1] += Re[i];
+  }
+  return 0;
+}
+
+// Global analytic Jacobian into a fixed CSR structure (JacobianElementAdd,
+// src/equations_matrices_routines.F90:2866-2909 -> MATRIX_VALUES_ADD_DP2).
+int orc_mr_assemble_jacobian(int n_elem, const int32_t* eq2, const int32_t* elin, int nq2, int nlin,
+                             const double* xg_nodes, const double* dep, const double* c, const int32_t* rp,
+                             const int32_t* ci, double* values, int fd, double fd_delta) {
+  const int ndof = 3 * nq2 + nlin;
+  std::fill(values, values + (rp[ndof] - 1), 0.0);
+  double xe[81], ze[81], pe[8];
+  std::vector<double> Ke(89 * 89);
+  int32_t dofs[89];
+  for (int e = 0; e < n_elem; ++e) {
+    mr_gather(e, eq2, elin, nq2, xg_nodes, dep, xe, ze, pe);
+    if (fd) orc_mr_element_jacobian_fd(xe, ze, pe, c[2 * e], c[2 * e + 1], fd_delta, Ke.data());
+    else mr_jacobian_element(xe, ze, pe, c[2 * e], c[2 * e + 1], Ke.data());
+    mr_element_dofs(e, eq2, elin, nq2, dofs);
+    if (csr_values_add(rp, ci, values, 89, dofs, 89, dofs, Ke.data()) != 0) return -2;
+  }
+  return 0;
+}
+
+}  // extern "C"

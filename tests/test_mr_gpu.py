@@ -1,0 +1,84 @@
+"""Parity of the GPU Mooney-Rivlin residual (K4) and Iron-analytic Jacobian (K5) with the oracle.
+
+Tolerances (FP64 on both sides, different summation order): residual within 1e-12 x max|R_ref|
+(undeformed-scale forces), Jacobian within 1e-12 x max|K|; CSR structure bit-exact.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from iron_gb300.elasticity import MooneyRivlinAssembly
+
+pytestmark = pytest.mark.gpu
+
+C1, C2 = 2.0, 6.0
+
+
+def _state(A, seed, amp=0.02, p=-1.0):
+    rng = np.random.default_rng(seed)
+    x = A.xg.cpu().numpy()
+    lam = 1.05
+    z = x * np.array([lam, lam ** -0.5, lam ** -0.5])[:, None]
+    z = z + rng.normal(0, amp / A.mesh.nelem[0], z.shape)
+    pr = p + rng.normal(0, 0.2, A.n_lin)
+    return np.r_[z.ravel(), pr]
+
+
+@pytest.mark.parametrize("ne", [(1, 1, 1), (2, 3, 2), (4, 4, 4)])
+def test_residual_matches_oracle(gfe_cuda, ne):
+    A = MooneyRivlinAssembly.from_regular_mesh(ne, build_jacobian=False)
+    dep = _state(A, 0)
+    R = A.residual(torch.from_numpy(dep).cuda(), [C1, C2]).cpu().numpy()
+    Ro = oracle.mr_assemble_residual(A.mesh.elem_nodes, A.elin.cpu().numpy(), A.n_q2, A.n_lin,
+                                     A.xg.cpu().numpy(), dep, [C1, C2])
+    assert np.abs(R - Ro).max() <= 1e-12 * np.abs(Ro).max()
+
+
+def test_residual_batched_parameter_sets(gfe_cuda):
+    A = MooneyRivlinAssembly.from_regular_mesh((3, 2, 2), build_jacobian=False)
+    B = 5
+    rng = np.random.default_rng(3)
+    deps = np.stack([_state(A, s) for s in range(B)])
+    cs = np.exp(rng.uniform(np.log(0.5), np.log(10.0), (B, 2)))
+    R = A.residual(torch.from_numpy(deps).cuda(), torch.from_numpy(cs)).cpu().numpy()
+    for b in range(B):
+        Ro = oracle.mr_assemble_residual(A.mesh.elem_nodes, A.elin.cpu().numpy(), A.n_q2, A.n_lin,
+                                         A.xg.cpu().numpy(), deps[b], cs[b])
+        assert np.abs(R[b] - Ro).max() <= 1e-12 * np.abs(Ro).max()
+    # each result is the same alone and in the batch
+    R1 = A.residual(torch.from_numpy(deps[2]).cuda(), torch.from_numpy(cs[2])).cpu().numpy()
+    assert np.array_equal(R1, R[2])
+
+
+def test_undeformed_residual_zero(gfe_cuda):
+    A = MooneyRivlinAssembly.from_regular_mesh((3, 3, 3), build_jacobian=False)
+    R = A.residual(A.initial_state(0.0), [C1, C2]).cpu().numpy()
+    assert np.abs(R).max() < 1e-13
+
+
+def test_element_jacobians_match_oracle(gfe_cuda):
+    A = MooneyRivlinAssembly.from_regular_mesh((2, 2, 1), build_jacobian=False)
+    dep = _state(A, 1)
+    K = A.element_jacobians(torch.from_numpy(dep).cuda(), [C1, C2]).cpu().numpy()
+    x = A.xg.cpu().numpy()
+    nq = A.n_q2
+    el = A.elin.cpu().numpy()
+    for e in range(A.n_elements):
+        en = A.mesh.elem_nodes[e]
+        Ko = oracle.mr_element_jacobian(x[:, en], dep[: 3 * nq].reshape(3, nq)[:, en], dep[3 * nq:][el[e]], C1, C2)
+        assert np.abs(K[e] - Ko).max() <= 1e-12 * np.abs(Ko).max(), e
+
+
+@pytest.mark.parametrize("ne", [(1, 1, 1), (3, 2, 2)])
+def test_assembled_jacobian_matches_oracle(gfe_cuda, ne):
+    A = MooneyRivlinAssembly.from_regular_mesh(ne)
+    dep = _state(A, 2)
+    v = A.jacobian(torch.from_numpy(dep).cuda(), [C1, C2]).cpu().numpy()
+    rp, ci, _ = A.to_iron_csr()
+    elem_dofs = A.elem_dofs.cpu().numpy()
+    orp, oci = oracle.csr_structure(elem_dofs, A.ndof)
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    vo = oracle.mr_assemble_jacobian(A.mesh.elem_nodes, A.elin.cpu().numpy(), A.n_q2, A.n_lin, A.xg.cpu().numpy(),
+                                     dep, [C1, C2], orp, oci)
+    assert np.abs(v - vo).max() <= 1e-12 * np.abs(vo).max()
