@@ -84,13 +84,17 @@ cg_spmv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, c
   constexpr int RPB = kThreads / LPR;  // rows per block-iteration
   const int sub = threadIdx.x % LPR, grp = threadIdx.x / LPR;
   double dot = 0.0;
-  for (int row = blockIdx.x * RPB + grp; row < n; row += gridDim.x * RPB) {
-    const int k0 = __ldg(rp + row) - 1, k1 = __ldg(rp + row + 1) - 1;
+  // The loop bound is block-uniform so every lane of a warp executes the same shuffles; lanes
+  // whose row is past the end contribute zero.
+  for (int base = blockIdx.x * RPB; base < n; base += gridDim.x * RPB) {
+    const int row = base + grp;
+    const bool valid = row < n;
+    const int k0 = valid ? __ldg(rp + row) - 1 : 0, k1 = valid ? __ldg(rp + row + 1) - 1 : 0;
     double s = 0.0;
     for (int k = k0 + sub; k < k1; k += LPR) s += (double)__ldg(val + k) * (double)p[__ldg(ci + k) - 1];
 #pragma unroll
     for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, LPR);
-    if (sub == 0) {
+    if (valid && sub == 0) {
       if (fixed && fixed[row]) s = 0.0;
       q[row] = (TV)s;
       dot += (double)p[row] * (double)(TV)s;
