@@ -205,7 +205,9 @@ def run_gfe(args):
     torch.cuda.set_device(dev)
     _lib.load()
 
+    log(f"mesh {args.n}^3")
     m, kappa = make_problem(args.n, seed=rank)
+    log("structure + device upload")
     A = LaplaceAssembly.from_regular_mesh(m, kappa=kappa, device=dev)
     E, N, nnz = A.n_elements, A.n_nodes, A.nnz
     ncol = len(A.colour_ptr) - 1
@@ -217,6 +219,7 @@ def run_gfe(args):
     asm_err = float((vmx - v64).abs().max() / v64.abs().max())
     precisions = ["fp64", "mixed"]
     timings = {}
+    log("timed assembly")
     for prec in precisions:
         for _ in range(args.warmup):
             A.assemble(prec, check=False)
@@ -245,6 +248,7 @@ def run_gfe(args):
         timings[prec] = {"ms_per_step": ms, "kernel_ms_total": kern_ms, "launches": launches,
                          "clocks": clk.summary()}
 
+    log("end-to-end timing")
     # end to end through the C ABI with host buffers: H2D geometry + conductivity, D2H values
     coords_h = torch.from_numpy(m.coords).pin_memory()
     kappa_h = torch.from_numpy(kappa).pin_memory()
@@ -279,6 +283,7 @@ def run_gfe(args):
         solve = {}
         xs = {}
         for prec in precisions:
+            log(f"solve {prec}")
             A.assemble(prec)
             x = x0.clone()
             torch.cuda.synchronize()
@@ -331,6 +336,7 @@ def run_gfe(args):
                            max(timings[p]["launches"], 1)} for p in precisions},
         "assembly_rel_err_mixed_vs_fp64": asm_err,
     }
+    log("fma probes")
     try:
         line["fp64_pipe_gflops"] = _lib.probe_fma_rate(_lib.GFE_FP64)
         line["fp32_pipe_gflops"] = _lib.probe_fma_rate(_lib.GFE_MIXED)
@@ -342,6 +348,7 @@ def run_gfe(args):
         line["solve"] = solve
     if rank == 0:
         threads = os.cpu_count() or 1
+        log("cpu baseline")
         v, dt, Es = cpu_baseline(args.cpu_sample_n, threads)
         line["cpu_baseline"] = {"value": v, "unit": "elements/s", "cores": threads, "kind": "port",
                                 "sample": f"{args.cpu_sample_n}^3 = {Es} elements, one assembly ({dt:.2f} s)"}
@@ -351,7 +358,15 @@ def run_gfe(args):
     return 0
 
 
+def log(msg: str) -> None:
+    """Progress on stderr (the JSON result line is the only stdout output)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def main():
+    import faulthandler
+
+    faulthandler.enable()
     args = parse()
     if args.impl == "reference":
         return run_reference(args)

@@ -318,7 +318,9 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
   const size_t vbytes = precision == GFE_FP64 ? sizeof(double) : sizeof(float);
   char* buf = nullptr;
   const size_t nb = (size_t)n;
-  const size_t bytes = nb * sizeof(double) * 2 + nb * vbytes * 5 + sizeof(double) * grid * 2 + sizeof(Scalars) + 1024;
+  // ten carved pieces, each rounded up to 256 bytes
+  const size_t bytes = nb * sizeof(double) * 2 + nb * vbytes * 5 + sizeof(double) * grid * 2 + sizeof(Scalars) +
+                       11 * 256;
   int rc = scratch_alloc((void**)&buf, bytes, s, "CG vectors");
   if (rc) return rc;
   auto carve = [&](size_t b) {
