@@ -64,6 +64,8 @@ SIGNATURES = {
     "gfe_mr_residual_vjp": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]),
     "gfe_cg_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(C.c_int32),
                                C.POINTER(C.c_double), vp]),
+    "gfe_cg_solve_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, f64, i32, C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_double), vp]),
 }
 
 

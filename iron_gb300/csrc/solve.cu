@@ -16,7 +16,9 @@
 // The outer loop forms r = f - A x in FP64 with the FP64 matrix and tests ||r|| against the target;
 // the correction A d = r is solved by FP32 CG (FP32 matrix and vectors, FP64 dot products) to a
 // loose relative tolerance and added to x in FP64.
+#include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "gfe_internal.cuh"
@@ -397,5 +399,112 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
   if (sh.bad) return set_error(GFE_ERR_NUMERIC, "%s: CG breakdown (non-positive curvature or non-finite value)", fn);
   if (!(rel <= rtol)) return set_error(GFE_ERR_NOCONV, "%s: relative residual %.3e above %.3e after %d iterations",
                                        fn, rel, rtol, total_it);
+  return GFE_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free variant of the FP64 solve
+// ---------------------------------------------------------------------------------------------
+// Some callers of this library may not allocate device memory at all: host codes that run the
+// solve from inside a memory pool they do not own (a framework's caching allocator, a
+// statically partitioned serving process) or from places where a cudaMalloc would synchronise the
+// device or be forbidden.  gfe_cg_solve_noalloc serves them: its working vectors live in one
+// fixed array in the library's own device memory, sized for GFE_NOALLOC_MAX_ROWS rows, which every
+// GPU that loads the library keeps for the lifetime of the process.
+namespace {
+
+constexpr long long kNoAllocGrid = 8 * 256;  // partial-sum slots: grid capped at 8 blocks x 256 SMs
+constexpr long long kNoAllocScalars = 32;    // doubles reserved for the Scalars block and the error word
+constexpr long long kNoAllocDoubles = 6ll * GFE_NOALLOC_MAX_ROWS + 2 * kNoAllocGrid + kNoAllocScalars;
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[64] = {nullptr};
+
+// Device address of g_noalloc_scratch on the current device, looked up once per device.  The
+// symbol name is only a host-side handle; kernels must be given this address.
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  GFE_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return gfe::set_error(GFE_ERR_ARG, "gfe_cg_solve_noalloc: device %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return gfe::set_error(GFE_ERR_CUDA, "gfe_cg_solve_noalloc: cudaGetSymbolAddress failed: %s",
+                            cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return GFE_OK;
+}
+
+}  // namespace
+
+extern "C" int gfe_cg_solve_noalloc(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const double* values,
+                                    const double* f, const uint8_t* fixed, double* x, double rtol, int32_t max_iters,
+                                    int32_t* iters_host, double* rel_host, void* stream) {
+  using namespace gfe;
+  const char* fn = "gfe_cg_solve_noalloc";
+  if (n <= 0 || !row_ptr || !col_idx || !values || !x || !(rtol > 0.0) || max_iters <= 0)
+    return set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (n > GFE_NOALLOC_MAX_ROWS)
+    return set_error(GFE_ERR_ARG, "%s: %d rows exceed the fixed scratch capacity of %d rows (use gfe_cg_solve)", fn,
+                     n, GFE_NOALLOC_MAX_ROWS);
+  double* base = nullptr;
+  int rc = noalloc_scratch(&base);
+  if (rc) return rc;
+  cudaStream_t s = as_stream(stream);
+  int32_t nnz1 = 0;
+  GFE_CUDA_TRY(cudaMemcpyAsync(&nnz1, row_ptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  GFE_CUDA_TRY(cudaStreamSynchronize(s));
+  const int lpr = pick_lpr((double)(nnz1 - 1) / n);
+  const int grid = std::min<int>(8 * sm_count(), (int)kNoAllocGrid);
+  const int chunk = 25;
+  const size_t nb = (size_t)n;
+  double* dinv = base;
+  double* r64 = dinv + GFE_NOALLOC_MAX_ROWS;
+  double* r = r64 + GFE_NOALLOC_MAX_ROWS;
+  double* z = r + GFE_NOALLOC_MAX_ROWS;
+  double* p = z + GFE_NOALLOC_MAX_ROWS;
+  double* q = p + GFE_NOALLOC_MAX_ROWS;
+  double* red = q + GFE_NOALLOC_MAX_ROWS;
+  double* red2 = red + kNoAllocGrid;
+  Scalars* sc = reinterpret_cast<Scalars*>(red2 + kNoAllocGrid);
+  unsigned* err = reinterpret_cast<unsigned*>(red2 + kNoAllocGrid + kNoAllocScalars - 1);
+  static_assert(sizeof(Scalars) <= (kNoAllocScalars - 1) * sizeof(double), "scalar block too small");
+  (void)nb;
+  // the array keeps the previous call's contents: the scalars (tickets, flags) and the error word
+  // must start at zero; every vector is written before it is read
+  GFE_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(double) * kNoAllocScalars, s));
+  Scalars sh{};
+  double b2 = 0.0, r2 = 0.0;
+  jacobi_inverse<<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, fixed, dinv, err);
+  set_dirichlet<<<grid, kThreads, 0, s>>>(n, x, fixed, true);
+  cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
+  norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, sc, red2 + grid - 1);
+  GFE_CUDA_TRY(cudaMemcpyAsync(&b2, red2 + grid - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GFE_CUDA_TRY(cudaStreamSynchronize(s));
+  if (b2 == 0.0) {
+    if (iters_host) *iters_host = 0;
+    if (rel_host) *rel_host = 0.0;
+    return GFE_OK;
+  }
+  cg_start<double, double><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, x, false, red, red2, sc, rtol * rtol);
+  rc = run_cg<double, double, double>(s, n, row_ptr, col_idx, values, fixed, dinv, x, r, z, p, q, red, red2, sc, &sh,
+                                      lpr, grid, max_iters, chunk);
+  if (rc) return rc;
+  cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
+  norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, sc, red2 + grid - 1);
+  GFE_CUDA_TRY(cudaMemcpyAsync(&r2, red2 + grid - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GFE_CUDA_TRY(cudaStreamSynchronize(s));
+  const double rel = std::sqrt(r2 / b2);
+  if (iters_host) *iters_host = sh.it;
+  if (rel_host) *rel_host = rel;
+  if (sh.bad) return set_error(GFE_ERR_NUMERIC, "%s: CG breakdown (non-positive curvature or non-finite value)", fn);
+  if (!(rel <= rtol))
+    return set_error(GFE_ERR_NOCONV, "%s: relative residual %.3e above %.3e after %d iterations", fn, rel, rtol, sh.it);
   return GFE_OK;
 }
