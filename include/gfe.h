@@ -42,6 +42,7 @@ extern "C" {
 /* precision selectors */
 #define GFE_FP64 0  /* plain: element arithmetic and storage in FP64 */
 #define GFE_MIXED 1 /* FP32 element arithmetic, FP64 accumulation */
+#define GFE_MIXED_DF 2 /* float-float element arithmetic on the FP32 pipes (~48-bit), FP64 accumulation */
 
 /* ---- library -------------------------------------------------------------------------- */
 
@@ -119,6 +120,21 @@ int gfe_laplace_assemble(int32_t n_elem, int32_t n_nodes, const int32_t* elem_no
                          const double* kappa, const int32_t* color_elems, const int32_t* color_ptr_host,
                          int32_t n_colors, const int32_t* row_ptr, const int32_t* col_idx, int64_t nnz,
                          double* values, float* values32, double* rhs, int32_t precision, void* stream);
+
+/* Same assembly for Iron's regular generated mesh of nx x ny x nz trilinear elements
+ * (GENERATED_MESH_REGULAR_TYPE, src/generated_mesh_routines.F90:1568-1640: nodes and elements
+ * numbered xi1 fastest), whose topology is implicit: no connectivity, colouring or column indices
+ * are read.  row_ptr must be the structure of that mesh (gfe_csr_structure of its connectivity,
+ * verified once with gfe_laplace_regular_check).  Every CSR entry is written exactly once (no
+ * zeroing pass); values32 (optional) receives the FP32 copy in the same pass; rhs is zeroed. */
+int gfe_laplace_assemble_regular(int32_t nx, int32_t ny, int32_t nz, const double* coords, const double* kappa,
+                                 const int32_t* row_ptr, double* values, float* values32, double* rhs,
+                                 int32_t precision, void* stream);
+
+/* Number of CSR rows/entries that differ from the clipped 27-point stencil of the regular mesh
+ * (0 = the structure is the one gfe_laplace_assemble_regular writes).  Synchronises `stream`. */
+int gfe_laplace_regular_check(int32_t nx, int32_t ny, int32_t nz, const int32_t* row_ptr, const int32_t* col_idx,
+                              int64_t* mismatches_host, void* stream);
 
 /* Element matrices only (no scatter): K_out[n_elem][8][8] row-major, for parity checks of the
  * element routine itself (LaplaceEquation_FiniteElementCalculate). */

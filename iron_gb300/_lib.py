@@ -56,6 +56,8 @@ SIGNATURES = {
     "gfe_csr_structure": (C.c_int, [i32, i32, vp, i32, vp, vp, i64, C.POINTER(C.c_int64), vp]),
     "gfe_laplace_assemble": (C.c_int, [i32, i32, vp, vp, vp, vp, vp, i32, vp, vp, i64, vp, vp, vp, i32, vp]),
     "gfe_laplace_element_matrices": (C.c_int, [i32, i32, vp, vp, vp, vp, i32, vp]),
+    "gfe_laplace_assemble_regular": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp]),
+    "gfe_laplace_regular_check": (C.c_int, [i32, i32, i32, vp, vp, C.POINTER(C.c_int64), vp]),
     "gfe_csr_spmv": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "gfe_mr_residual": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp]),
     "gfe_mr_slot_map": (C.c_int, [i32, vp, vp, i32, vp, vp, vp, vp, vp]),

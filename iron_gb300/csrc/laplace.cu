@@ -13,14 +13,24 @@
 //    basis at the 1D Gauss points takes only the values p = (1+1/sqrt3)/2 and q = (1-1/sqrt3)/2,
 //    and is symmetrised over (a,b) because GU is symmetric.
 // The result equals Iron's element matrix up to floating-point rounding (checked against the
-// oracle's literal restatement of Iron's loops).
+// oracle's literal restatement of Iron's loops).  The element arithmetic is templated on
+// double (GFE_FP64), float (GFE_MIXED) or float-float (GFE_MIXED_DF, df.cuh).
 //
-// Scatter: EquationsMatrices_ElementAdd -> MATRIX_VALUES_ADD_DP2 (src/matrix_vector.F90:3202-3240)
-// adds each element matrix into fixed CSR storage.  Elements are processed colour by colour (no
-// two elements of a colour share a node), so every CSR entry receives at most one read-modify-write
-// per colour launch: no atomics, and a summation order fixed by the colouring.
+// Two scatter strategies, both deterministic (fixed summation order, no atomics), both replacing
+// EquationsMatrices_ElementAdd -> MATRIX_VALUES_ADD_DP2 (src/matrix_vector.F90:3202-3240):
+//  * general meshes: elements colour by colour (no two elements of a colour share a node), one
+//    thread per element searches each of its 64 entries in the CSR row and adds it;
+//  * Iron's regular generated mesh (GENERATED_MESH_REGULAR_TYPE, implicit topology): a CTA owns a
+//    tile of nodes in the x-y plane and marches up the z layers; it computes the element matrices
+//    of the two element layers touching the current node layer into shared memory once, then each
+//    thread sums its node's 27-entry row from the 8 surrounding elements in a fixed order and
+//    writes the row exactly once.  CSR slot positions follow from the 27-point stencil
+//    (verified once against the structure by gfe_laplace_regular_check), so the kernel reads no
+//    column indices.
 #include <cmath>
+#include <type_traits>
 
+#include "df.cuh"
 #include "gfe_internal.cuh"
 
 namespace {
@@ -30,11 +40,6 @@ constexpr int kBlock = 128;
 __host__ __device__ constexpr int tri(int m, int n) {  // packed upper-triangular index, m <= n < 8
   return m * 8 - (m * (m - 1)) / 2 + (n - m);
 }
-
-template <typename T>
-struct Lin1D {
-  T p, q;  // 1D linear basis values at the two Gauss points: L_m(t_g) = (m == g) ? p : q
-};
 
 template <typename T>
 __device__ __forceinline__ T wv(int m, int g, T p, T q) {
@@ -52,6 +57,7 @@ __device__ __forceinline__ T wwv(int k, int g, T p, T q) {
 // symmetric 8x8 matrix (packed upper triangle, tri(m,n)).  Returns false if det(GL) <= 0.
 template <typename T>
 __device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T q, T (&K)[36]) {
+  const T zero = from_double<T>(0.0);
   // Jacobian columns: Jt[c][a][gd1][gd2]
   T Jt[3][3][2][2];
 #pragma unroll
@@ -79,6 +85,7 @@ __device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T
   // M_g[ab] for the 8 Gauss points, symmetric: 00 11 22 01 02 12
   T M[8][6];
   bool ok = true;
+  const T eighth = kappa * from_double<T>(0.125);
 #pragma unroll
   for (int g = 0; g < 8; ++g) {
     const int gb[3] = {g & 1, (g >> 1) & 1, (g >> 2) & 1};
@@ -103,14 +110,14 @@ __device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T
     T A02 = G01 * G12 - G02 * G11;
     T A12 = G01 * G02 - G00 * G12;
     T det = G00 * A00 + G01 * A01 + G02 * A02;
-    ok = ok && (det > T(0));
+    ok = ok && (det > zero);
     // GU * sqrt(det) * w = adj / det * sqrt(det) * w = adj * w * rsqrt(det); w = 1/8
-    T sc = kappa * T(0.125) * rsqrt(det);
+    T sc = eighth * rsqrt(det);
     M[g][0] = A00 * sc; M[g][1] = A11 * sc; M[g][2] = A22 * sc;
     M[g][3] = A01 * sc; M[g][4] = A02 * sc; M[g][5] = A12 * sc;
   }
 #pragma unroll
-  for (int k = 0; k < 36; ++k) K[k] = T(0);
+  for (int k = 0; k < 36; ++k) K[k] = zero;
 
   // diagonal pairs (a,a)
 #pragma unroll
@@ -140,8 +147,8 @@ __device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T
       for (int n = m; n < 8; ++n) {
         const int ma = (m >> a) & 1, na = (n >> a) & 1;
         const int k1 = ((m >> d1) & 1) + ((n >> d1) & 1), k2 = ((m >> d2) & 1) + ((n >> d2) & 1);
-        if (ma == na) K[tri(m, n)] += V[k1][k2];
-        else K[tri(m, n)] -= V[k1][k2];
+        if (ma == na) accum(K[tri(m, n)], V[k1][k2]);
+        else accum_sub(K[tri(m, n)], V[k1][k2]);
       }
   }
   // off-diagonal pairs (a,b), a < b, c the third direction; M index 3:(0,1) 4:(0,2) 5:(1,2)
@@ -179,14 +186,26 @@ __device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T
       for (int n = m; n < 8; ++n) {
         const int k = ((m >> c) & 1) + ((n >> c) & 1);
         // C_ab(m,n) = s(m_a) s(n_b) W[n_a][m_b][k];  C_ab(n,m) = s(n_a) s(m_b) W[m_a][n_b][k]
-        const int sa = ((m >> a) & 1) == ((n >> b) & 1) ? 1 : -1;
-        const int sb = ((n >> a) & 1) == ((m >> b) & 1) ? 1 : -1;
+        const bool sa = ((m >> a) & 1) == ((n >> b) & 1);
+        const bool sb = ((n >> a) & 1) == ((m >> b) & 1);
         const T t1 = W[(n >> a) & 1][(m >> b) & 1][k];
         const T t2 = W[(m >> a) & 1][(n >> b) & 1][k];
-        K[tri(m, n)] += (sa > 0 ? t1 : -t1) + (sb > 0 ? t2 : -t2);
+        if (sa) accum(K[tri(m, n)], t1); else accum_sub(K[tri(m, n)], t1);
+        if (sb) accum(K[tri(m, n)], t2); else accum_sub(K[tri(m, n)], t2);
       }
   }
+#pragma unroll
+  for (int k = 0; k < 36; ++k) finish(K[k]);
   return ok;
+}
+
+// Gauss-point constants of the 2-point rule on [0,1] (src/basis_routines.F90:6804-6890):
+// p = L_0(t_0) = 1 - (1 - 1/sqrt3)/2, q = L_1(t_0).
+template <typename T>
+__device__ __forceinline__ void gauss_pq(T& p, T& q) {
+  const double s3 = 1.0 / sqrt(3.0);
+  p = from_double<T>((s3 + 1.0) / 2.0);
+  q = from_double<T>((-s3 + 1.0) / 2.0);
 }
 
 template <typename T>
@@ -200,9 +219,12 @@ __device__ __forceinline__ void load_element(int e, const int32_t* __restrict__ 
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
-    for (int m = 0; m < 8; ++m) x[c][m] = (T)__ldg(coords + (size_t)c * n_nodes + nd[m]);
+    for (int m = 0; m < 8; ++m) x[c][m] = from_double<T>(__ldg(coords + (size_t)c * n_nodes + nd[m]));
 }
 
+// ---------------------------------------------------------------------------------------------
+// general meshes: colour by colour
+// ---------------------------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(kBlock)
 laplace_assemble_color(const int32_t* __restrict__ elems, int32_t count, int32_t n_nodes,
@@ -215,9 +237,9 @@ laplace_assemble_color(const int32_t* __restrict__ elems, int32_t count, int32_t
   int nd[8];
   T x[3][8];
   load_element<T>(e, elem_nodes, coords, n_nodes, nd, x);
-  const T kap = kappa ? (T)__ldg(kappa + e) : T(1);
-  const T s3 = T(1) / sqrt(T(3));
-  const T p = (s3 + T(1)) / T(2), q = (-s3 + T(1)) / T(2);
+  const T kap = from_double<T>(kappa ? __ldg(kappa + e) : 1.0);
+  T p, q;
+  gauss_pq(p, q);
   T K[36];
   if (!laplace_hex8<T>(x, kap, p, q, K)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
   bool missing = false;
@@ -234,7 +256,7 @@ laplace_assemble_color(const int32_t* __restrict__ elems, int32_t count, int32_t
         if (__ldg(ci + mid) < col) lo = mid + 1; else hi = mid;
       }
       if (lo < hi0 && __ldg(ci + lo) == col) {
-        values[lo] += (double)K[i <= j ? tri(i, j) : tri(j, i)];
+        values[lo] += to_double(K[i <= j ? tri(i, j) : tri(j, i)]);
       } else {
         missing = true;
       }
@@ -253,15 +275,15 @@ laplace_element_kernel(int32_t n_elem, int32_t n_nodes, const int32_t* __restric
   int nd[8];
   T x[3][8];
   load_element<T>(e, elem_nodes, coords, n_nodes, nd, x);
-  const T kap = kappa ? (T)kappa[e] : T(1);
-  const T s3 = T(1) / sqrt(T(3));
-  const T p = (s3 + T(1)) / T(2), q = (-s3 + T(1)) / T(2);
+  const T kap = from_double<T>(kappa ? kappa[e] : 1.0);
+  T p, q;
+  gauss_pq(p, q);
   T K[36];
   if (!laplace_hex8<T>(x, kap, p, q, K)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) Kout[(size_t)e * 64 + i * 8 + j] = (double)K[i <= j ? tri(i, j) : tri(j, i)];
+    for (int j = 0; j < 8; ++j) Kout[(size_t)e * 64 + i * 8 + j] = to_double(K[i <= j ? tri(i, j) : tri(j, i)]);
 }
 
 __global__ void to_fp32(const double* __restrict__ v, float* __restrict__ v32, long long n) {
@@ -269,12 +291,207 @@ __global__ void to_fp32(const double* __restrict__ v, float* __restrict__ v32, l
     v32[i] = (float)v[i];
 }
 
+// ---------------------------------------------------------------------------------------------
+// Iron's regular generated mesh: tiled, row-owning assembly
+// ---------------------------------------------------------------------------------------------
+// Node tile TX x TY in x-y; the element tile is (TX+1) x (TY+1) = 16 x 8 = 128 elements, one per
+// thread.  Element matrices are kept in shared memory in the element arithmetic type; the row sums
+// are accumulated in FP64 (GFE_FP64) or float-float (the FP32-pipe precisions), so the FP32 paths
+// issue FP64 instructions only for the final conversion of each written entry.
+constexpr int kRTX = 15, kRTY = 7;
+constexpr int kREX = kRTX + 1, kREY = kRTY + 1;  // 16 x 8 elements
+constexpr int kRThreads = kREX * kREY;           // 128
+constexpr int kRZ = 8;                           // node layers per CTA
+
+template <typename T>
+struct StoreOf {
+  using type = T;
+};
+template <typename T>
+struct AccOf {
+  using type = f2;
+};
+template <>
+struct AccOf<double> {
+  using type = double;
+};
+
+// Output of one assembled entry.  FP64: as accumulated.  Float-float: hi + lo in FP64 (one add,
+// the conversions done with integer operations) and hi + lo rounded to FP32 for the copy.  FP32
+// element arithmetic: the sum rounded to FP32, widened exactly to FP64.
+__device__ __forceinline__ void entry_out(double a, bool, double& v, float& v32) {
+  v = a;
+  v32 = (float)a;
+}
+__device__ __forceinline__ void entry_out(f2 a, bool full, double& v, float& v32) {
+  v32 = __fadd_rn(a.hi, a.lo);
+  v = full ? f32_to_f64_exact(a.hi) + f32_to_f64_exact(a.lo) : f32_to_f64_exact(v32);
+}
+
+// row-sum accumulation (the final FP64 conversion hi + lo needs no normalised form)
+__device__ __forceinline__ double acc_add(double a, double b) { return a + b; }
+__device__ __forceinline__ f2 acc_add(f2 a, float b) {
+  const f2 s = two_sum(a.hi, b);
+  return {s.hi, __fadd_rn(a.lo, s.lo)};
+}
+__device__ __forceinline__ f2 acc_add(f2 a, f2 b) {
+  accum(a, b);
+  return a;
+}
+
+// Coordinates are read in the element arithmetic type: the FP32-pipe precisions take them from a
+// copy split once per node (float or float-float), so no element converts FP64 values itself.
+template <typename T>
+__global__ void split_coords(long long n, const double* __restrict__ in, T* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = from_double<T>(in[i]);
+}
+
+__device__ __forceinline__ double load_coord(const double* p) { return __ldg(p); }
+__device__ __forceinline__ float load_coord(const float* p) { return __ldg(p); }
+__device__ __forceinline__ f2 load_coord(const f2* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return {v.x, v.y};
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kRThreads)
+laplace_regular_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ coords,
+                       const double* __restrict__ kappa, const int32_t* __restrict__ rp, double* __restrict__ values,
+                       float* __restrict__ values32, double* __restrict__ rhs, unsigned* err) {
+  using S = typename StoreOf<T>::type;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  S(*sK)[36][kRThreads] = reinterpret_cast<S(*)[36][kRThreads]>(smem_raw);  // [layer buffer][entry][element]
+  const int tid = threadIdx.x;
+  const int x0 = blockIdx.x * kRTX, y0 = blockIdx.y * kRTY, k0 = blockIdx.z * kRZ;
+  const int NX = nx + 1, NY = ny + 1, NZ = nz + 1;
+  const long long NXY = (long long)NX * NY;
+  const int k1 = min(k0 + kRZ, NZ);
+  // element owned by this thread in each element layer
+  const int ex = x0 - 1 + (tid % kREX), ey = y0 - 1 + (tid / kREX);
+  const bool e_in_xy = ex >= 0 && ex < nx && ey >= 0 && ey < ny;
+  // node owned by this thread (threads 0 .. TX*TY-1)
+  const int ni = x0 + tid % kRTX, nj = y0 + tid / kRTX;
+  const bool owns_node = tid < kRTX * kRTY && ni < NX && nj < NY;
+  T p, q;
+  gauss_pq(p, q);
+  bool bad = false;
+
+  auto compute_layer = [&](int ez, int buf) {
+    if (e_in_xy && ez >= 0 && ez < nz) {
+      T x[3][8];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const long long n = (long long)(ex + (m & 1)) + (long long)(ey + ((m >> 1) & 1)) * NX + (ez + (m >> 2)) * NXY;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) x[c][m] = load_coord(coords + c * NXY * NZ + n);
+      }
+      const long long e = (long long)ex + (long long)ey * nx + (long long)ez * nx * ny;
+      const T kap = from_double<T>(kappa ? __ldg(kappa + e) : 1.0);
+      T K[36];
+      if (!laplace_hex8<T>(x, kap, p, q, K)) bad = true;
+#pragma unroll
+      for (int k = 0; k < 36; ++k) sK[buf][k][tid] = K[k];
+    }
+  };
+  using A = typename AccOf<T>::type;
+
+  compute_layer(k0 - 1, (k0 - 1) & 1);
+  for (int k = k0; k < k1; ++k) {
+    compute_layer(k, k & 1);
+    __syncthreads();
+    if (owns_node) {
+      A acc[27];
+#pragma unroll
+      for (int s = 0; s < 27; ++s) acc[s] = from_double<A>(0.0);
+      // surrounding elements (i-1+a, j-1+b, k-1+c) in the fixed order c, b, a
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int ez = k - 1 + c;
+        if (ez < 0 || ez >= nz) continue;
+        const int buf = ez & 1;
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+          const int ey2 = nj - 1 + b;
+          if (ey2 < 0 || ey2 >= ny) continue;
+#pragma unroll
+          for (int a = 0; a < 2; ++a) {
+            const int ex2 = ni - 1 + a;
+            if (ex2 < 0 || ex2 >= nx) continue;
+            const int slot = (ex2 - (x0 - 1)) + (ey2 - (y0 - 1)) * kREX;
+            const int li = (1 - a) + 2 * (1 - b) + 4 * (1 - c);
+#pragma unroll
+            for (int lj = 0; lj < 8; ++lj) {
+              const int di = a - 1 + (lj & 1), dj = b - 1 + ((lj >> 1) & 1), dk = c - 1 + (lj >> 2);
+              const int m = li < lj ? li : lj, n = li < lj ? lj : li;
+              const int q = (dk + 1) * 9 + (dj + 1) * 3 + (di + 1);
+              acc[q] = acc_add(acc[q], sK[buf][tri(m, n)][slot]);
+            }
+          }
+        }
+      }
+      // write the row: the 27-point stencil clipped to the mesh, in ascending column order
+      const long long r = (long long)ni + (long long)nj * NX + (long long)k * NXY;
+      long long pos = (long long)__ldg(rp + r) - 1;
+#pragma unroll
+      for (int dk = -1; dk <= 1; ++dk) {
+        if (k + dk < 0 || k + dk >= NZ) continue;
+#pragma unroll
+        for (int dj = -1; dj <= 1; ++dj) {
+          if (nj + dj < 0 || nj + dj >= NY) continue;
+#pragma unroll
+          for (int di = -1; di <= 1; ++di) {
+            if (ni + di < 0 || ni + di >= NX) continue;
+            double v;
+            float v32;
+            entry_out(acc[(dk + 1) * 9 + (dj + 1) * 3 + (di + 1)], !std::is_same<T, float>::value, v, v32);
+            values[pos] = v;
+            if (values32) values32[pos] = v32;
+            ++pos;
+          }
+        }
+      }
+      if (rhs) rhs[r] = 0.0;
+    }
+    __syncthreads();
+  }
+  if (bad) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+}
+
+// Structure check: every row of the CSR is the clipped 27-point stencil of a regular mesh.
+__global__ void laplace_regular_check_kernel(int32_t nx, int32_t ny, int32_t nz, const int32_t* __restrict__ rp,
+                                             const int32_t* __restrict__ ci, unsigned long long* bad) {
+  const int NX = nx + 1, NY = ny + 1, NZ = nz + 1;
+  const long long N = (long long)NX * NY * NZ;
+  unsigned long long mism = 0;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < N; r += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(r % NX), j = (int)((r / NX) % NY), k = (int)(r / ((long long)NX * NY));
+    long long pos = rp[r] - 1;
+    const long long end = rp[r + 1] - 1;
+    for (int dk = -1; dk <= 1; ++dk)
+      for (int dj = -1; dj <= 1; ++dj)
+        for (int di = -1; di <= 1; ++di) {
+          if (i + di < 0 || i + di >= NX || j + dj < 0 || j + dj >= NY || k + dk < 0 || k + dk >= NZ) continue;
+          const long long col = r + di + (long long)dj * NX + (long long)dk * NX * NY;
+          if (pos >= end || ci[pos] != col + 1) ++mism;
+          ++pos;
+        }
+    if (pos != end) ++mism;
+  }
+  if (mism) atomicAdd(bad, mism);
+}
+
+int check_precision(int precision, const char* fn) {
+  if (precision != GFE_FP64 && precision != GFE_MIXED && precision != GFE_MIXED_DF)
+    return gfe::set_error(GFE_ERR_ARG, "%s: unknown precision %d", fn, precision);
+  return GFE_OK;
+}
+
 int check_common(int32_t n_elem, int32_t n_nodes, const int32_t* elem_nodes, const double* coords, int precision,
                  const char* fn) {
   if (n_elem < 0 || n_nodes <= 0 || (n_elem > 0 && (!elem_nodes || !coords)))
     return gfe::set_error(GFE_ERR_ARG, "%s: invalid mesh arguments (n_elem=%d n_nodes=%d)", fn, n_elem, n_nodes);
-  if (precision != GFE_FP64 && precision != GFE_MIXED)
-    return gfe::set_error(GFE_ERR_ARG, "%s: unknown precision %d", fn, precision);
+  if (int rc = check_precision(precision, fn)) return rc;
   if (reinterpret_cast<uintptr_t>(elem_nodes) % 16 != 0)
     return gfe::set_error(GFE_ERR_ARG, "%s: elem_nodes must be 16-byte aligned", fn);
   return GFE_OK;
@@ -295,6 +512,41 @@ int check_device_errors(cudaStream_t s, const char* fn, bool sync) {
     return gfe::set_error(GFE_ERR_NUMERIC, "%s: device error bits 0x%x", fn, bits);
   }
   return GFE_OK;
+}
+
+template <typename T>
+int launch_regular(dim3 grid, cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const double* coords,
+                   const double* kappa, const int32_t* rp, double* values, float* values32, double* rhs,
+                   unsigned* err) {
+  const size_t smem = 2 * 36 * kRThreads * sizeof(typename StoreOf<T>::type);
+  GFE_CUDA_TRY(cudaFuncSetAttribute((const void*)laplace_regular_kernel<T>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long long n3 = 3ll * (nx + 1) * (ny + 1) * (nz + 1);
+  T* ct = nullptr;
+  if (int rc = gfe::scratch_alloc((void**)&ct, sizeof(T) * n3, s, "split coordinates")) return rc;
+  split_coords<T><<<4 * gfe::sm_count(), 256, 0, s>>>(n3, coords, ct);
+  laplace_regular_kernel<T><<<grid, kRThreads, smem, s>>>(nx, ny, nz, ct, kappa, rp, values, values32, rhs, err);
+  gfe::scratch_free(ct, s);
+  return GFE_OK;
+}
+
+template <>
+int launch_regular<double>(dim3 grid, cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const double* coords,
+                           const double* kappa, const int32_t* rp, double* values, float* values32, double* rhs,
+                           unsigned* err) {
+  const size_t smem = 2 * 36 * kRThreads * sizeof(double);
+  GFE_CUDA_TRY(cudaFuncSetAttribute((const void*)laplace_regular_kernel<double>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  laplace_regular_kernel<double><<<grid, kRThreads, smem, s>>>(nx, ny, nz, coords, kappa, rp, values, values32, rhs,
+                                                               err);
+  return GFE_OK;
+}
+
+template <typename T>
+void launch_color(int grid, cudaStream_t s, const int32_t* ce, int cnt, int32_t n_nodes, const int32_t* en,
+                  const double* xyz, const double* kappa, const int32_t* rp, const int32_t* ci, double* values,
+                  unsigned* err) {
+  laplace_assemble_color<T><<<grid, kBlock, 0, s>>>(ce, cnt, n_nodes, en, xyz, kappa, rp, ci, values, err);
 }
 
 }  // namespace
@@ -324,16 +576,63 @@ extern "C" int gfe_laplace_assemble(int32_t n_elem, int32_t n_nodes, const int32
     if (cnt <= 0) continue;
     const int grid = (cnt + kBlock - 1) / kBlock;
     if (precision == GFE_FP64)
-      laplace_assemble_color<double><<<grid, kBlock, 0, s>>>(color_elems + c0, cnt, n_nodes, elem_nodes, coords,
-                                                             kappa, row_ptr, col_idx, values, err);
+      launch_color<double>(grid, s, color_elems + c0, cnt, n_nodes, elem_nodes, coords, kappa, row_ptr, col_idx,
+                           values, err);
+    else if (precision == GFE_MIXED)
+      launch_color<float>(grid, s, color_elems + c0, cnt, n_nodes, elem_nodes, coords, kappa, row_ptr, col_idx,
+                          values, err);
     else
-      laplace_assemble_color<float><<<grid, kBlock, 0, s>>>(color_elems + c0, cnt, n_nodes, elem_nodes, coords,
-                                                            kappa, row_ptr, col_idx, values, err);
+      launch_color<f2>(grid, s, color_elems + c0, cnt, n_nodes, elem_nodes, coords, kappa, row_ptr, col_idx, values,
+                       err);
     ++launches;
   }
   gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, launches);
   if (values32) to_fp32<<<4 * gfe::sm_count(), 256, 0, s>>>(values, values32, nnz);
   GFE_LAUNCH_CHECK(fn);
+  return GFE_OK;
+}
+
+extern "C" int gfe_laplace_assemble_regular(int32_t nx, int32_t ny, int32_t nz, const double* coords,
+                                            const double* kappa, const int32_t* row_ptr, double* values,
+                                            float* values32, double* rhs, int32_t precision, void* stream) {
+  const char* fn = "gfe_laplace_assemble_regular";
+  if (nx <= 0 || ny <= 0 || nz <= 0 || !coords || !row_ptr || !values)
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (int rc = check_precision(precision, fn)) return rc;
+  cudaStream_t s = gfe::as_stream(stream);
+  unsigned* err = gfe::device_error_word();
+  const dim3 grid((nx + 1 + kRTX - 1) / kRTX, (ny + 1 + kRTY - 1) / kRTY, (nz + 1 + kRZ - 1) / kRZ);
+  void* prof = gfe::stage_begin(GFE_STAGE_LAPLACE_ELEMENTS, s);
+  int rc;
+  if (precision == GFE_FP64)
+    rc = launch_regular<double>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err);
+  else if (precision == GFE_MIXED)
+    rc = launch_regular<float>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err);
+  else
+    rc = launch_regular<f2>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err);
+  gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, 1);
+  if (rc) return rc;
+  GFE_LAUNCH_CHECK(fn);
+  return GFE_OK;
+}
+
+extern "C" int gfe_laplace_regular_check(int32_t nx, int32_t ny, int32_t nz, const int32_t* row_ptr,
+                                         const int32_t* col_idx, int64_t* mismatches_host, void* stream) {
+  const char* fn = "gfe_laplace_regular_check";
+  if (nx <= 0 || ny <= 0 || nz <= 0 || !row_ptr || !col_idx || !mismatches_host)
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  cudaStream_t s = gfe::as_stream(stream);
+  unsigned long long* bad = nullptr;
+  int rc = gfe::scratch_alloc((void**)&bad, sizeof(unsigned long long), s, "check counter");
+  if (rc) return rc;
+  cudaMemsetAsync(bad, 0, sizeof(unsigned long long), s);
+  laplace_regular_check_kernel<<<8 * gfe::sm_count(), 256, 0, s>>>(nx, ny, nz, row_ptr, col_idx, bad);
+  unsigned long long h = 0;
+  cudaMemcpyAsync(&h, bad, sizeof(h), cudaMemcpyDeviceToHost, s);
+  gfe::scratch_free(bad, s);
+  GFE_CUDA_TRY(cudaStreamSynchronize(s));
+  GFE_LAUNCH_CHECK(fn);
+  *mismatches_host = (int64_t)h;
   return GFE_OK;
 }
 
@@ -350,8 +649,10 @@ extern "C" int gfe_laplace_element_matrices(int32_t n_elem, int32_t n_nodes, con
   const int grid = (n_elem + kBlock - 1) / kBlock;
   if (precision == GFE_FP64)
     laplace_element_kernel<double><<<grid, kBlock, 0, s>>>(n_elem, n_nodes, elem_nodes, coords, kappa, K_out, err);
-  else
+  else if (precision == GFE_MIXED)
     laplace_element_kernel<float><<<grid, kBlock, 0, s>>>(n_elem, n_nodes, elem_nodes, coords, kappa, K_out, err);
+  else
+    laplace_element_kernel<f2><<<grid, kBlock, 0, s>>>(n_elem, n_nodes, elem_nodes, coords, kappa, K_out, err);
   GFE_LAUNCH_CHECK(fn);
   return check_device_errors(s, fn, true);
 }

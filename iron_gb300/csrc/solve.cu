@@ -76,7 +76,10 @@ __device__ __forceinline__ double ordered_sum(const double* red, int n) {
   return t;
 }
 
-// q = A p on free rows (0 on fixed rows), partial <p, q>.  LPR lanes per row.
+// q = A p on free rows (0 on fixed rows), partial <p, q>.  LPR lanes per row.  The arithmetic is
+// done in the vector type TV: GB300's FP64 pipe issues a warp instruction in 64 cycles, so the FP64
+// solve uses one thread per row (no shuffle reduction, no idle lanes in the FMA chain) and the FP32
+// inner solve of the mixed scheme stays entirely on the FP32 pipe.
 template <typename TM, typename TV, int LPR>
 __global__ void __launch_bounds__(kThreads)
 cg_spmv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, const TM* __restrict__ val,
@@ -85,24 +88,25 @@ cg_spmv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, c
   if (sc->done) return;
   constexpr int RPB = kThreads / LPR;  // rows per block-iteration
   const int sub = threadIdx.x % LPR, grp = threadIdx.x / LPR;
-  double dot = 0.0;
+  TV dot = TV(0);
   // The loop bound is block-uniform so every lane of a warp executes the same shuffles; lanes
   // whose row is past the end contribute zero.
   for (int base = blockIdx.x * RPB; base < n; base += gridDim.x * RPB) {
     const int row = base + grp;
     const bool valid = row < n;
     const int k0 = valid ? __ldg(rp + row) - 1 : 0, k1 = valid ? __ldg(rp + row + 1) - 1 : 0;
-    double s = 0.0;
-    for (int k = k0 + sub; k < k1; k += LPR) s += (double)__ldg(val + k) * (double)p[__ldg(ci + k) - 1];
+    TV s = TV(0);
+#pragma unroll 4
+    for (int k = k0 + sub; k < k1; k += LPR) s += (TV)__ldg(val + k) * p[__ldg(ci + k) - 1];
 #pragma unroll
     for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, LPR);
     if (valid && sub == 0) {
-      if (fixed && fixed[row]) s = 0.0;
-      q[row] = (TV)s;
-      dot += (double)p[row] * (double)(TV)s;
+      if (fixed && fixed[row]) s = TV(0);
+      q[row] = s;
+      dot += p[row] * s;
     }
   }
-  double b = block_sum(dot);
+  double b = block_sum((double)dot);
   if (threadIdx.x == 0) red[blockIdx.x] = b;
   if (last_block(&sc->ticket1)) {
     double pq = ordered_sum(red, gridDim.x);
@@ -119,22 +123,21 @@ cg_spmv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, c
 template <typename TX, typename TV>
 __global__ void __launch_bounds__(kThreads)
 cg_update(int n, TX* __restrict__ x, TV* __restrict__ r, TV* __restrict__ z, const TV* __restrict__ p,
-          const TV* __restrict__ q, const double* __restrict__ dinv, double* red, double* red2, Scalars* sc) {
+          const TV* __restrict__ q, const TV* __restrict__ dinv, double* red, double* red2, Scalars* sc) {
   if (sc->done) return;
-  const double alpha = sc->alpha;
-  double rz = 0.0, rr = 0.0;
+  const TV alpha = (TV)sc->alpha;
+  TV rz = TV(0), rr = TV(0);
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
-    x[i] = (TX)((double)x[i] + alpha * (double)p[i]);
-    double ri = (double)r[i] - alpha * (double)q[i];
-    TV rv = (TV)ri;
+    x[i] = x[i] + alpha * p[i];
+    const TV rv = r[i] - alpha * q[i];
     r[i] = rv;
-    TV zv = (TV)(dinv[i] * (double)rv);
+    const TV zv = dinv[i] * rv;
     z[i] = zv;
-    rz += (double)rv * (double)zv;
-    rr += (double)rv * (double)rv;
+    rz += rv * zv;
+    rr += rv * rv;
   }
-  double b1 = block_sum(rz);
-  double b2 = block_sum(rr);
+  double b1 = block_sum((double)rz);
+  double b2 = block_sum((double)rr);
   if (threadIdx.x == 0) { red[blockIdx.x] = b1; red2[blockIdx.x] = b2; }
   if (last_block(&sc->ticket2)) {
     double rzn = ordered_sum(red, gridDim.x);
@@ -154,9 +157,12 @@ cg_update(int n, TX* __restrict__ x, TV* __restrict__ r, TV* __restrict__ z, con
 template <typename TV>
 __global__ void cg_direction(int n, TV* __restrict__ p, const TV* __restrict__ z, const Scalars* sc) {
   if (sc->done) return;
-  const double beta = sc->beta;
-  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
-    p[i] = (TV)((double)z[i] + beta * (double)p[i]);
+  const TV beta = (TV)sc->beta;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) p[i] = z[i] + beta * p[i];
+}
+
+__global__ void to_float(int n, const double* __restrict__ a, float* __restrict__ b) {
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) b[i] = (float)a[i];
 }
 
 // Setup: dinv (0 on fixed rows), r = f - A x0 on free rows (x0 = Dirichlet values at fixed DOFs and
@@ -238,20 +244,26 @@ __global__ void norm2_kernel(int n, const double* __restrict__ v, double* red, S
   }
 }
 
-int pick_lpr(double avg) { return avg >= 24 ? 32 : (avg >= 12 ? 16 : 8); }
+// lanes per row: FP64 rows use one thread each (the FP64 pipe is the bound); FP32 rows use few
+// lanes on short rows so several rows' loads are in flight per warp
+int pick_lpr(double avg, bool fp64) {
+  if (fp64) return 1;
+  return avg >= 96 ? 32 : (avg >= 48 ? 16 : 8);
+}
 
 template <typename TM, typename TV>
 void launch_spmv(int lpr, int grid, cudaStream_t s, int n, const int32_t* rp, const int32_t* ci, const TM* val,
                  const TV* p, TV* q, const uint8_t* fixed, double* red, Scalars* sc) {
   if (lpr == 32) cg_spmv<TM, TV, 32><<<grid, kThreads, 0, s>>>(n, rp, ci, val, p, q, fixed, red, sc);
   else if (lpr == 16) cg_spmv<TM, TV, 16><<<grid, kThreads, 0, s>>>(n, rp, ci, val, p, q, fixed, red, sc);
-  else cg_spmv<TM, TV, 8><<<grid, kThreads, 0, s>>>(n, rp, ci, val, p, q, fixed, red, sc);
+  else if (lpr == 8) cg_spmv<TM, TV, 8><<<grid, kThreads, 0, s>>>(n, rp, ci, val, p, q, fixed, red, sc);
+  else cg_spmv<TM, TV, 1><<<grid, kThreads, 0, s>>>(n, rp, ci, val, p, q, fixed, red, sc);
 }
 
 // Runs CG iterations (chunked, device-side convergence flag) on pre-started vectors.
 template <typename TM, typename TV, typename TX>
 int run_cg(cudaStream_t s, int n, const int32_t* rp, const int32_t* ci, const TM* val, const uint8_t* fixed,
-           const double* dinv, TX* x, TV* r, TV* z, TV* p, TV* q, double* red, double* red2, Scalars* sc,
+           const TV* dinv, TX* x, TV* r, TV* z, TV* p, TV* q, double* red, double* red2, Scalars* sc,
            Scalars* sc_host, int lpr, int grid, int max_iters, int chunk) {
   int launched = 0;
   while (launched < max_iters) {
@@ -289,7 +301,7 @@ extern "C" int gfe_csr_spmv(int32_t n_rows, const int32_t* row_ptr, const int32_
   rc = gfe::scratch_alloc((void**)&red, sizeof(double) * grid, s, "spmv partials");
   if (rc) { gfe::scratch_free(sc, s); return rc; }
   cudaMemsetAsync(sc, 0, sizeof(Scalars), s);
-  launch_spmv<double, double>(32, grid, s, n_rows, row_ptr, col_idx, values, x, y, fixed, red, sc);
+  launch_spmv<double, double>(1, grid, s, n_rows, row_ptr, col_idx, values, x, y, fixed, red, sc);
   gfe::scratch_free(red, s);
   gfe::scratch_free(sc, s);
   GFE_LAUNCH_CHECK("gfe_csr_spmv");
@@ -312,17 +324,17 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
   int32_t nnz1 = 0;
   GFE_CUDA_TRY(cudaMemcpyAsync(&nnz1, row_ptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   GFE_CUDA_TRY(cudaStreamSynchronize(s));
-  const int lpr = pick_lpr((double)(nnz1 - 1) / n);
+  const int lpr = pick_lpr((double)(nnz1 - 1) / n, precision == GFE_FP64);
   const int grid = 8 * sm_count();
-  const int chunk = 25;
+  const int chunk = 50;
 
-  // scratch: dinv, r64, then vector set (FP64 or FP32)
+  // scratch: dinv, r64, then vector set (FP64 or FP32) and an FP32 copy of dinv
   const size_t vbytes = precision == GFE_FP64 ? sizeof(double) : sizeof(float);
   char* buf = nullptr;
   const size_t nb = (size_t)n;
-  // ten carved pieces, each rounded up to 256 bytes
-  const size_t bytes = nb * sizeof(double) * 2 + nb * vbytes * 5 + sizeof(double) * grid * 2 + sizeof(Scalars) +
-                       11 * 256;
+  // eleven carved pieces, each rounded up to 256 bytes
+  const size_t bytes = nb * sizeof(double) * 2 + nb * vbytes * 6 + sizeof(double) * grid * 2 + sizeof(Scalars) +
+                       12 * 256;
   int rc = scratch_alloc((void**)&buf, bytes, s, "CG vectors");
   if (rc) return rc;
   auto carve = [&](size_t b) {
@@ -338,6 +350,7 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
   void* vp = carve(nb * vbytes);
   void* vq = carve(nb * vbytes);
   void* vd = carve(nb * vbytes);
+  void* vdinv = carve(nb * vbytes);
   double* red = (double*)carve(sizeof(double) * grid);
   double* red2 = (double*)carve(sizeof(double) * grid);
   Scalars* sc = (Scalars*)carve(sizeof(Scalars));
@@ -360,12 +373,26 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
   }
   if (precision == GFE_FP64) {
     double* r = (double*)vr; double* z = (double*)vz; double* p = (double*)vp; double* q = (double*)vq;
-    cg_start<double, double><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, x, false, red, red2, sc, rtol * rtol);
-    rc = run_cg<double, double, double>(s, n, row_ptr, col_idx, values, fixed, dinv, x, r, z, p, q, red, red2, sc,
-                                        &sh, lpr, grid, max_iters, chunk);
-    total_it = sh.it;
+    // The recurrence residual drifts from the true residual b - A x, so CG aims at half the target
+    // and restarts from the true residual (residual replacement) while the latter is above it.
+    double r2_start = b2;
+    for (int round = 0; round < 4 && rc == GFE_OK; ++round) {
+      cg_start<double, double><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, x, false, red, red2, sc,
+                                                         0.25 * rtol * rtol * b2 / r2_start);
+      rc = run_cg<double, double, double>(s, n, row_ptr, col_idx, values, fixed, dinv, x, r, z, p, q, red, red2, sc,
+                                          &sh, lpr, grid, max_iters - total_it, chunk);
+      total_it += sh.it;
+      if (rc || sh.bad || total_it >= max_iters) break;
+      cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
+      norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, sc, red2 + grid - 1);
+      GFE_CUDA_TRY(cudaMemcpyAsync(&r2_start, red2 + grid - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+      GFE_CUDA_TRY(cudaStreamSynchronize(s));
+      if (r2_start <= rtol * rtol * b2 || r2_start == 0.0) break;
+    }
   } else {
     float* r = (float*)vr; float* z = (float*)vz; float* p = (float*)vp; float* q = (float*)vq; float* d = (float*)vd;
+    float* dinv32 = (float*)vdinv;
+    to_float<<<grid, kThreads, 0, s>>>(n, dinv, dinv32);
     const double inner_rtol = 1e-4;
     for (int outer = 0; outer < 64 && rc == GFE_OK; ++outer) {
       if (outer > 0) {
@@ -378,7 +405,7 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
       }
       cg_start<float, float><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, d, true, red, red2, sc,
                                                        inner_rtol * inner_rtol);
-      rc = run_cg<float, float, float>(s, n, row_ptr, col_idx, values32, fixed, dinv, d, r, z, p, q, red, red2, sc,
+      rc = run_cg<float, float, float>(s, n, row_ptr, col_idx, values32, fixed, dinv32, d, r, z, p, q, red, red2, sc,
                                        &sh, lpr, grid, max_iters - total_it, chunk);
       total_it += sh.it;
       if (sh.bad) break;
@@ -460,7 +487,7 @@ extern "C" int gfe_cg_solve_noalloc(int32_t n, const int32_t* row_ptr, const int
   int32_t nnz1 = 0;
   GFE_CUDA_TRY(cudaMemcpyAsync(&nnz1, row_ptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   GFE_CUDA_TRY(cudaStreamSynchronize(s));
-  const int lpr = pick_lpr((double)(nnz1 - 1) / n);
+  const int lpr = pick_lpr((double)(nnz1 - 1) / n, true);
   const int grid = std::min<int>(8 * sm_count(), (int)kNoAllocGrid);
   const int chunk = 25;
   const size_t nb = (size_t)n;
@@ -492,14 +519,23 @@ extern "C" int gfe_cg_solve_noalloc(int32_t n, const int32_t* row_ptr, const int
     if (rel_host) *rel_host = 0.0;
     return GFE_OK;
   }
-  cg_start<double, double><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, x, false, red, red2, sc, rtol * rtol);
-  rc = run_cg<double, double, double>(s, n, row_ptr, col_idx, values, fixed, dinv, x, r, z, p, q, red, red2, sc, &sh,
-                                      lpr, grid, max_iters, chunk);
-  if (rc) return rc;
-  cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
-  norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, sc, red2 + grid - 1);
-  GFE_CUDA_TRY(cudaMemcpyAsync(&r2, red2 + grid - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
-  GFE_CUDA_TRY(cudaStreamSynchronize(s));
+  // same residual-replacement rounds as gfe_cg_solve
+  int total_it = 0;
+  r2 = b2;
+  for (int round = 0; round < 4; ++round) {
+    cg_start<double, double><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, x, false, red, red2, sc,
+                                                       0.25 * rtol * rtol * b2 / r2);
+    rc = run_cg<double, double, double>(s, n, row_ptr, col_idx, values, fixed, dinv, x, r, z, p, q, red, red2, sc,
+                                        &sh, lpr, grid, max_iters - total_it, chunk);
+    if (rc) return rc;
+    total_it += sh.it;
+    cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
+    norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, sc, red2 + grid - 1);
+    GFE_CUDA_TRY(cudaMemcpyAsync(&r2, red2 + grid - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GFE_CUDA_TRY(cudaStreamSynchronize(s));
+    if (sh.bad || total_it >= max_iters || r2 <= rtol * rtol * b2 || r2 == 0.0) break;
+  }
+  sh.it = total_it;
   const double rel = std::sqrt(r2 / b2);
   if (iters_host) *iters_host = sh.it;
   if (rel_host) *rel_host = rel;

@@ -17,7 +17,10 @@ import torch
 from . import _lib
 from ._lib import GFE_FP64, GFE_MIXED, GfeError
 
-PRECISIONS = {"fp64": GFE_FP64, "mixed": GFE_MIXED}
+GFE_MIXED_DF = 2
+# fp64: FP64 element arithmetic; mixed: FP32 element arithmetic (about 1e-6 relative), FP64
+# accumulation; mixed_df: float-float element arithmetic on the FP32 pipes (FP64-level accuracy)
+PRECISIONS = {"fp64": GFE_FP64, "mixed": GFE_MIXED, "mixed_df": GFE_MIXED_DF}
 
 
 def csr_structure(elem_dofs: torch.Tensor, n_dofs: int, stream=None):
@@ -81,24 +84,51 @@ class LaplaceAssembly:
         self.values = torch.empty(self.nnz, dtype=torch.float64, device=self.device)
         self.values32 = None
         self.rhs = torch.empty(self.n_nodes, dtype=torch.float64, device=self.device)
+        self.regular = None  # (nx, ny, nz) when the mesh is Iron's regular generated mesh
 
     @classmethod
     def from_regular_mesh(cls, mesh, kappa=None, device=None):
         order, ptr = mesh.colouring()
-        return cls(mesh.elem_nodes, mesh.coords, kappa=kappa, colour_elems=order, colour_ptr=ptr, device=device)
+        obj = cls(mesh.elem_nodes, mesh.coords, kappa=kappa, colour_elems=order, colour_ptr=ptr, device=device)
+        if mesh.order == 1:
+            nx, ny, nz = mesh.nelem
+            bad = C.c_int64(-1)
+            _lib.call("gfe_laplace_regular_check", nx, ny, nz, _lib.ptr(obj.row_ptr), _lib.ptr(obj.col_idx),
+                      C.byref(bad), _lib.stream_handle())
+            if bad.value == 0:
+                obj.regular = (nx, ny, nz)
+        return obj
 
-    def assemble(self, precision: str = "fp64", stream=None, check: bool = True) -> torch.Tensor:
-        """Assemble K (FP64 values in self.values); mixed precision also fills self.values32."""
+    def assemble(self, precision: str = "fp64", stream=None, check: bool = True, path: str = "auto",
+                 fp32_copy: bool | None = None) -> torch.Tensor:
+        """Assemble K into self.values (FP64).  path: 'auto' (regular-mesh kernel when the mesh is
+        Iron's regular generated mesh, else the colour-scatter kernel), 'regular' or 'general'.
+        fp32_copy (default: for the mixed precisions) also fills self.values32."""
         prec = PRECISIONS[precision]
-        if prec == GFE_MIXED and self.values32 is None:
+        if fp32_copy is None:
+            fp32_copy = prec != GFE_FP64
+        if fp32_copy and self.values32 is None:
             self.values32 = torch.empty(self.nnz, dtype=torch.float32, device=self.device)
-        v32 = self.values32 if prec == GFE_MIXED else None
-        cp = self.colour_ptr
-        _lib.call("gfe_laplace_assemble", self.n_elements, self.n_nodes, _lib.ptr(self.elem_nodes),
-                  _lib.ptr(self.coords), _lib.ptr(self.kappa), _lib.ptr(self.colour_elems),
-                  cp.ctypes.data_as(C.c_void_p), len(cp) - 1, _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx),
-                  self.nnz, _lib.ptr(self.values), _lib.ptr(v32), _lib.ptr(self.rhs), prec,
-                  _lib.stream_handle(stream))
+        v32 = self.values32 if fp32_copy else None
+        if path == "regular" and self.regular is None:
+            raise GfeError(-1, "the regular-mesh kernel needs Iron's regular generated mesh")
+        if path == "auto":
+            # FP64 element arithmetic is bound by GB300's FP64 pipe: the colour kernel computes each
+            # element once, while the tiled kernel recomputes its halo elements.  The FP32-pipe
+            # precisions are bound by memory traffic, which the tiled kernel minimises.
+            path = "general" if (prec == GFE_FP64 or self.regular is None) else "regular"
+        if path == "regular":
+            nx, ny, nz = self.regular
+            _lib.call("gfe_laplace_assemble_regular", nx, ny, nz, _lib.ptr(self.coords), _lib.ptr(self.kappa),
+                      _lib.ptr(self.row_ptr), _lib.ptr(self.values), _lib.ptr(v32), _lib.ptr(self.rhs), prec,
+                      _lib.stream_handle(stream))
+        else:
+            cp = self.colour_ptr
+            _lib.call("gfe_laplace_assemble", self.n_elements, self.n_nodes, _lib.ptr(self.elem_nodes),
+                      _lib.ptr(self.coords), _lib.ptr(self.kappa), _lib.ptr(self.colour_elems),
+                      cp.ctypes.data_as(C.c_void_p), len(cp) - 1, _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx),
+                      self.nnz, _lib.ptr(self.values), _lib.ptr(v32), _lib.ptr(self.rhs), prec,
+                      _lib.stream_handle(stream))
         if check:
             _lib.raise_device_errors("gfe_laplace_assemble", stream)
         return self.values
@@ -120,10 +150,11 @@ class LaplaceAssembly:
     def solve(self, fixed: torch.Tensor, x: torch.Tensor, f: torch.Tensor | None = None, rtol: float = 1e-12,
               max_iters: int = 200000, precision: str = "fp64", stream=None) -> SolveInfo:
         """Solve K x = f with x fixed (Dirichlet) where fixed != 0; x holds the fixed values on
-        entry and the solution on exit."""
-        prec = PRECISIONS[precision]
+        entry and the solution on exit.  precision 'fp64': FP64 CG; 'mixed' / 'mixed_df': FP32 CG on
+        self.values32 inside FP64 iterative refinement with the FP64 matrix."""
+        prec = GFE_FP64 if precision == "fp64" else GFE_MIXED
         if prec == GFE_MIXED and self.values32 is None:
-            raise GfeError(-1, "mixed-precision solve needs assemble(precision='mixed') first")
+            raise GfeError(-1, "mixed-precision solve needs the FP32 copy (assemble with fp32_copy=True)")
         fixed = fixed.to(device=self.device, dtype=torch.uint8).contiguous()
         it = C.c_int32(0)
         rel = C.c_double(0.0)

@@ -51,7 +51,7 @@ def test_structure_q2p1_bit_exact(gfe_cuda):
     assert np.array_equal(ci.cpu().numpy(), oci)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 2e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-13), ("mixed", 2e-6), ("mixed_df", 5e-13)])
 def test_element_matrices(gfe_cuda, precision, tol):
     m = _mesh((4, 3, 5), seed=1)
     kap = _kappa(m.n_elements, 2)
@@ -62,17 +62,50 @@ def test_element_matrices(gfe_cuda, precision, tol):
         assert np.abs(K[e] - Ko).max() <= tol * np.abs(Ko).max(), e
 
 
-@pytest.mark.parametrize("ne,seed", [((8, 8, 8), 0), ((8, 8, 8), 3), ((7, 3, 5), 1), ((1, 1, 1), 2)])
+@pytest.mark.parametrize("ne,seed", [((8, 8, 8), 0), ((8, 8, 8), 3), ((7, 3, 5), 1), ((1, 1, 1), 2),
+                                     ((33, 9, 40), 4)])
 @pytest.mark.parametrize("with_kappa", [False, True])
-def test_assembly_fp64(gfe_cuda, ne, seed, with_kappa):
+@pytest.mark.parametrize("path", ["regular", "general"])
+def test_assembly_fp64(gfe_cuda, ne, seed, with_kappa, path):
     m = _mesh(ne, seed)
     kap = _kappa(m.n_elements, seed + 10) if with_kappa else None
     A = LaplaceAssembly.from_regular_mesh(m, kappa=kap)
-    v = A.assemble("fp64").cpu().numpy()
+    assert A.regular == tuple(ne)
+    A.rhs.fill_(7.0)
+    v = A.assemble("fp64", path=path).cpu().numpy()
     rp, ci = oracle.csr_structure(m.elem_nodes, m.n_nodes)
     ov, orhs = oracle.laplace_assemble(3, [1, 1, 1], [2, 2, 2], m.elem_nodes, m.coords, kap, rp, ci)
     assert np.abs(v - ov).max() <= 1e-13 * np.abs(ov).max()
     assert torch.count_nonzero(A.rhs).item() == 0
+
+
+@pytest.mark.parametrize("path", ["regular", "general"])
+def test_assembly_mixed_df_is_fp64_accurate(gfe_cuda, path):
+    """Float-float element arithmetic on the FP32 pipes matches the FP64 oracle to 5e-13."""
+    m = _mesh((12, 10, 9), 5)
+    kap = _kappa(m.n_elements, 6)
+    A = LaplaceAssembly.from_regular_mesh(m, kappa=kap)
+    v = A.assemble("mixed_df", path=path).cpu().numpy()
+    rp, ci = oracle.csr_structure(m.elem_nodes, m.n_nodes)
+    ov, _ = oracle.laplace_assemble(3, [1, 1, 1], [2, 2, 2], m.elem_nodes, m.coords, kap, rp, ci)
+    assert np.abs(v - ov).max() <= 5e-13 * np.abs(ov).max()
+    assert np.array_equal(A.values32.cpu().numpy(), v.astype(np.float32))
+
+
+def test_regular_check_rejects_other_structures(gfe_cuda):
+    m = _mesh((4, 3, 2), 0)
+    perm = np.random.default_rng(0).permutation(m.n_elements)
+    A = LaplaceAssembly(m.elem_nodes[perm], m.coords)
+    assert A.regular is None
+    import ctypes as C
+    from iron_gb300 import _lib
+    bad = C.c_int64(0)
+    # the structure of a 4x3x2 mesh is not the one of a 3x4x2 mesh
+    _lib.call("gfe_laplace_regular_check", 3, 4, 2, _lib.ptr(A.row_ptr), _lib.ptr(A.col_idx), C.byref(bad),
+              _lib.stream_handle())
+    assert bad.value > 0
+    with pytest.raises(GfeError):
+        A.assemble("fp64", path="regular")
 
 
 def test_assembly_mixed_and_fp32_copy(gfe_cuda):
@@ -91,9 +124,11 @@ def test_assembly_mixed_and_fp32_copy(gfe_cuda):
 def test_assembly_deterministic(gfe_cuda):
     m = _mesh((9, 7, 6), 4)
     A = LaplaceAssembly.from_regular_mesh(m, kappa=_kappa(m.n_elements, 1))
-    a = A.assemble("fp64").clone()
-    b = A.assemble("fp64").clone()
-    assert torch.equal(a, b)
+    for path in ("regular", "general"):
+        for prec in ("fp64", "mixed_df"):
+            a = A.assemble(prec, path=path).clone()
+            b = A.assemble(prec, path=path).clone()
+            assert torch.equal(a, b)
 
 
 def test_greedy_colouring_permuted_mesh(gfe_cuda):
