@@ -172,7 +172,9 @@ int gfe_mr_slot_map(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int
 int gfe_mr_jacobian(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, int32_t n_lin,
                     const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
                     const double* dep, const double* cpar, const int32_t* slots, double* values, int64_t nnz,
-                    double* K_out, void* stream);
+                    double* K_out, int32_t precision, void* stream);
+/* precision: GFE_FP64 (FP64 contraction) or GFE_MIXED (FP32 contraction of the basis-gradient x
+ * material blocks; Gauss-point kinematics, det(F) and the assembled values stay FP64). */
 
 /* Consistent tangent: the exact derivative of the residual of gfe_mr_residual with respect to
  * the dependent vector (what Iron's finite-difference Jacobian, EquationsSet_FiniteElementJacobianEvaluateFD
@@ -181,7 +183,7 @@ int gfe_mr_jacobian(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int
 int gfe_mr_tangent(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, int32_t n_lin,
                    const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
                    const double* dep, const double* cpar, const int32_t* slots, double* values, int64_t nnz,
-                   double* K_out, void* stream);
+                   double* K_out, int32_t precision, void* stream);
 
 /* Adjoint of the residual (K6): for `batch` problems, du[b] = v[b]^T dR/d(dep) ([batch][ndof]) and
  * dc[b] = v[b]^T dR/d(c10, c01) ([batch][2]).  No counterpart routine in Iron (its gradients come

@@ -1,0 +1,157 @@
+"""Secondary benchmark workloads of bench.py (the default workload, Laplace assembly, lives there).
+
+mr:         Mooney-Rivlin mixed u-p (triquadratic u, trilinear p) residual, Iron's analytic
+            Jacobian and the consistent tangent assembled on a 32^3 mesh, c10 = 2, c01 = 6, at a 10 %
+            uniaxial stretch state with a small seeded perturbation.
+mr_adjoint: residual and its hand-written adjoint for a batch of 64 parameter sets on a 16^3 mesh
+            (c10, c01 log-uniform in [0.5, 10], displacement perturbation N(0, (0.01 h)^2), seeded).
+serve:      the request stream of iron_gb300.serving.
+
+Each prints one JSON line.
+"""
+from __future__ import annotations
+
+import json
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+from .elasticity import MooneyRivlinAssembly
+
+
+def _events_time(fn, steps, warmup, stream):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(steps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def stretched_state(A: MooneyRivlinAssembly, lam: float, c10: float, c01: float, seed: int, amp: float):
+    """z = uniaxial isochoric stretch of x plus N(0, (amp h)^2); p = traction-free lateral value."""
+    rng = np.random.default_rng(seed)
+    x = A.xg.cpu().numpy()
+    z = x * np.array([lam, lam ** -0.5, lam ** -0.5])[:, None]
+    h = 1.0 / A.mesh.nelem[0]
+    z = z + rng.normal(0.0, amp * h, z.shape)
+    F = np.diag([lam, lam ** -0.5, lam ** -0.5])
+    Cb = F.T @ F
+    S = -2 * c01 * Cb + 2 * (c10 + np.trace(Cb) * c01) * np.eye(3)
+    sb = F @ S @ F.T
+    p = np.trace(sb) / 3 - sb[1, 1]
+    return np.r_[z.ravel(), np.full(A.n_lin, p)]
+
+
+def bench_mr(args, log, clock_sampler):
+    n = 32 if args.n == 128 else args.n
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    log(f"MR Q2/Q1 mesh {n}^3: structure + slot map")
+    A = MooneyRivlinAssembly.from_regular_mesh((n, n, n), device=dev)
+    c = torch.tensor([2.0, 6.0], dtype=torch.float64, device=dev)
+    dep = torch.from_numpy(stretched_state(A, 1.10, 2.0, 6.0, 0, 0.01)).to(dev)
+    R = torch.empty_like(dep)
+    E, ndof, nnz = A.n_elements, A.ndof, A.nnz
+    res = {}
+    with clock_sampler(dev.index) as clk:
+        log("timing residual")
+        res["residual_ms"] = _events_time(lambda: A.residual(dep, c, out=R, check=False), args.steps, args.warmup,
+                                          stream)
+        for prec in ("fp64", "mixed"):
+            log(f"timing analytic Jacobian ({prec})")
+            res[f"jacobian_{prec}_ms"] = _events_time(lambda: A.jacobian(dep, c, precision=prec, check=False),
+                                                      args.steps, args.warmup, stream)
+            log(f"timing consistent tangent ({prec})")
+            res[f"tangent_{prec}_ms"] = _events_time(lambda: A.tangent(dep, c, precision=prec, check=False),
+                                                     args.steps, args.warmup, stream)
+        res["jacobian_ms"] = res["jacobian_fp64_ms"]
+        # accuracy of the mixed contraction against FP64
+        v64 = A.jacobian(dep, c, precision="fp64").clone()
+        vmx = A.jacobian(dep, c, precision="mixed")
+        res_err = float((vmx - v64).abs().max() / v64.abs().max())
+        del v64
+    _lib.raise_device_errors("bench mr")
+    nu = 3 * A.n_q2
+    jac_bytes = E * (27 * 4 + 8 * 4) + A.n_q2 * (3 * 8 * 2) + A.n_lin * 8 * 2 + nnz * 8
+    res_bytes = E * (27 * 4 + 8 * 4) + A.n_q2 * (3 * 8 * 2) + A.n_lin * 8 * 2 + ndof * 8
+    jac_flop = 27 * (2 * 81 * 81 * 9 + 2 * 81 * 36 + 4 * 81 * 8) * E
+    line = {
+        "metric": "mr_jacobian_assembled_elements_per_s", "value": E / (res["jacobian_ms"] * 1e-3),
+        "unit": "elements/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "mooney_rivlin_q2p1", "elements_per_side": n, "elements": E, "dofs": ndof,
+                   "jacobian_nnz": nnz, "gauss": "3x3x3", "c10": 2.0, "c01": 6.0,
+                   "state": "10% uniaxial stretch + N(0,(0.01h)^2), traction-free p"},
+        "times_ms": res,
+        "jacobian_mixed_rel_err_vs_fp64": res_err,
+        "elements_per_s": {k.replace("_ms", ""): E / (v * 1e-3) for k, v in res.items()},
+        "dofs_per_s": {k.replace("_ms", ""): ndof / (v * 1e-3) for k, v in res.items()},
+        "algorithmic": {"jacobian_bytes": jac_bytes, "residual_bytes": res_bytes, "jacobian_flop": jac_flop,
+                        "jacobian_GBps": jac_bytes / (res["jacobian_ms"] * 1e-3) / 1e9,
+                        "jacobian_fp64_gflops": jac_flop / (res["jacobian_ms"] * 1e-3) / 1e9},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def bench_mr_adjoint(args, log, clock_sampler):
+    n = 16 if args.n == 128 else args.n
+    B = 64
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    log(f"MR adjoint {n}^3 x {B}")
+    A = MooneyRivlinAssembly.from_regular_mesh((n, n, n), device=dev, build_jacobian=False)
+    rng = np.random.default_rng(7)
+    cs = np.exp(rng.uniform(np.log(0.5), np.log(10.0), (B, 2)))
+    deps = np.stack([stretched_state(A, 1.0, cs[b, 0], cs[b, 1], 100 + b, 0.01) for b in range(B)])
+    dep = torch.from_numpy(deps).to(dev)
+    c = torch.from_numpy(cs).to(dev)
+    v = torch.from_numpy(rng.normal(0, 1, deps.shape)).to(dev)
+    R = torch.empty_like(dep)
+    with clock_sampler(dev.index) as clk:
+        fwd = _events_time(lambda: A.residual(dep, c, out=R, check=False), args.steps, args.warmup, stream)
+        bwd = _events_time(lambda: A.residual_vjp(dep, c, v), args.steps, args.warmup, stream)
+    _lib.raise_device_errors("bench mr adjoint")
+    # directional check of one gradient against central differences (step 1e-6 relative)
+    du, dc = A.residual_vjp(dep[:1], c[:1], v[:1])
+    d = torch.from_numpy(rng.normal(0, 1, deps.shape[1])).to(dev)
+    h = 1e-6
+    Rp = A.residual(dep[0] + h * d, c[0])
+    Rm = A.residual(dep[0] - h * d, c[0])
+    fd = float((v[0] * (Rp - Rm)).sum() / (2 * h))
+    an = float((du[0] * d).sum())
+    items = A.n_elements * B
+    line = {
+        "metric": "mr_residual_adjoint_element_problems_per_s", "value": items / ((fwd + bwd) * 1e-3),
+        "unit": "element-problems/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "mooney_rivlin_q2p1_adjoint", "elements_per_side": n, "batch": B,
+                   "params": "c10,c01 log-uniform [0.5,10] kPa", "perturbation": "N(0,(0.01h)^2)"},
+        "forward_ms": fwd, "backward_ms": bwd,
+        "directional_check": {"adjoint": an, "central_fd": fd, "rel_diff": abs(an - fd) / max(abs(fd), 1e-300)},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run(args, log, clock_sampler):
+    _lib.load()
+    if args.workload == "mr":
+        return bench_mr(args, log, clock_sampler)
+    if args.workload == "mr_adjoint":
+        return bench_mr_adjoint(args, log, clock_sampler)
+    if args.workload == "serve":
+        from . import serving
+
+        return serving.bench(args, log, clock_sampler)
+    raise ValueError(args.workload)

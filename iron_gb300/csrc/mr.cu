@@ -316,187 +316,6 @@ mr_residual_kernel(const int32_t* __restrict__ elems, int32_t count, int32_t bat
   (void)ndof;
 }
 
-// ----------------------------------------------------------------------------------------------
-// Iron's analytic Jacobian
-// ----------------------------------------------------------------------------------------------
-constexpr int kJacThreads = 128;
-
-struct JacShared {
-  double x[81], z[81], p[8];
-  double dphidz[NG][NQ][3];  // spatial basis gradients
-  double sub[NG][6][9];      // J_z w (D + sigma) diagonal blocks 0..2; J_z w D off-diagonal (1,0),(2,0),(2,1)
-  double hyd[NG][9];         // J_z w push(C^-1)
-  double jgw[NG];
-  int dofs[ND];
-};
-
-__device__ void jacobian_point(const Tables& T, int g, JacShared& S, double c1, double c2, unsigned* err) {
-  GP q;
-  if (!gauss_point(T, g, S.z, S.x, S.p, q)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
-  const double J = q.Jz / q.Jx;
-  // unmodified right Cauchy-Green tensor and its inverse
-  double C[3][3], Ci[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) C[i][j] = q.F[0][i] * q.F[0][j] + q.F[1][i] * q.F[1][j] + q.F[2][i] * q.F[2][j];
-  const double I3 = inv3(C, Ci);
-  const double L[6] = {C[0][0], C[1][1], C[2][2], C[0][1], C[0][2], C[1][2]};
-  const double U[6] = {Ci[0][0], Ci[1][1], Ci[2][2], Ci[0][1], Ci[0][2], Ci[1][2]};
-  // I3EE as filled by Fortran RESHAPE (column j listed): I3EE[i][j] = col[j][i]
-  const double col[6][6] = {{0.0, 4 * L[2], 4 * L[1], 0.0, 0.0, -4 * L[5]},
-                            {4 * L[2], 0.0, 4 * L[0], 0.0, -4 * L[4], 0.0},
-                            {4 * L[1], 4 * L[0], 0.0, -2 * L[3], 0.0, 0.0},
-                            {0.0, 0.0, -4 * L[3], -2 * L[2], 2 * L[5], 2 * L[4]},
-                            {0.0, -4 * L[4], 0.0, 2 * L[5], -2 * L[1], 2 * L[3]},
-                            {-4 * L[5], 0.0, 0.0, 2 * L[4], 2 * L[3], -2 * L[0]}};
-  double D[6][6];
-#pragma unroll
-  for (int i = 0; i < 6; ++i)
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      double v = 0.0;
-      if (i < 3 && j < 3 && i != j) v = 4.0 * c2;
-      if (i >= 3 && i == j) v = -2.0 * c2;
-      D[i][j] = v + q.p * (-2.0 * U[i] * U[j] + 0.5 * col[j][i] / I3);
-    }
-  const double I1 = C[0][0] + C[1][1] + C[2][2];
-  const double t2 = 2.0 * (c1 + I1 * c2);
-  double Sv[6] = {-2 * c2 * C[0][0] + t2, -2 * c2 * C[1][1] + t2, -2 * c2 * C[2][2] + t2,
-                  -2 * c2 * C[1][0], -2 * c2 * C[2][0], -2 * c2 * C[2][1]};
-  double H[6] = {U[0], U[1], U[2], U[3], U[4], U[5]};
-  double t[6][6];
-  push_t(q.F, t);
-  push_vec(t, Sv, J);
-  push_vec(t, H, J);
-  double tD[6][6];
-#pragma unroll
-  for (int i = 0; i < 6; ++i)
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      double s = 0.0;
-#pragma unroll
-      for (int k = 0; k < 6; ++k) s += t[i][k] * D[k][j];
-      tD[i][j] = s;
-    }
-#pragma unroll
-  for (int i = 0; i < 6; ++i)
-#pragma unroll
-    for (int j = 0; j < 6; ++j) {
-      double s = 0.0;
-#pragma unroll
-      for (int k = 0; k < 6; ++k) s += tD[i][k] * t[j][k];
-      D[i][j] = s / J;
-    }
-  Sv[0] += q.p; Sv[1] += q.p; Sv[2] += q.p;
-  const double jgw = q.Jz * q.w;
-  S.jgw[g] = jgw;
-#pragma unroll
-  for (int nh = 0; nh < 3; ++nh)
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) S.sub[g][nh][i * 3 + j] = jgw * (D[kT2V[i][nh]][kT2V[j][nh]] + Sv[kT2V[i][j]]);
-  // off-diagonal blocks rows mh, columns nh: (mh,nh) = (1,0), (2,0), (2,1)
-  const int om[3] = {1, 2, 2}, on[3] = {0, 0, 1};
-#pragma unroll
-  for (int o = 0; o < 3; ++o)
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int j = 0; j < 3; ++j) S.sub[g][3 + o][i * 3 + j] = jgw * D[kT2V[i][om[o]]][kT2V[j][on[o]]];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) S.hyd[g][i * 3 + j] = jgw * H[kT2V[i][j]];
-  for (int ms = 0; ms < NQ; ++ms)
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-      S.dphidz[g][ms][k] =
-          q.Zi[0][k] * T.dphi[g][0][ms] + q.Zi[1][k] * T.dphi[g][1][ms] + q.Zi[2][k] * T.dphi[g][2][ms];
-}
-
-// Element Jacobian entry (row r, column c) of Iron's analytic tangent, 0 <= r, c < 89.
-__device__ __forceinline__ double jacobian_entry(const Tables& T, const JacShared& S, int r, int c) {
-  double s = 0.0;
-  if (r < 81 && c < 81) {
-    // use the lower triangle (Iron mirrors the lower u-u triangle to the upper)
-    int rr = r, cc = c;
-    if (rr < cc) { rr = c; cc = r; }
-    const int mh = rr / NQ, ms = rr % NQ, nh = cc / NQ, ns = cc % NQ;
-    int blk;
-    if (mh == nh) blk = mh;
-    else blk = 3 + (mh == 1 ? 0 : (nh == 0 ? 1 : 2));
-    for (int g = 0; g < NG; ++g) {
-      const double* B = S.sub[g][blk];
-      const double a0 = S.dphidz[g][ns][0], a1 = S.dphidz[g][ns][1], a2 = S.dphidz[g][ns][2];
-      const double t0 = B[0] * a0 + B[1] * a1 + B[2] * a2;
-      const double t1 = B[3] * a0 + B[4] * a1 + B[5] * a2;
-      const double t2 = B[6] * a0 + B[7] * a1 + B[8] * a2;
-      s += S.dphidz[g][ms][0] * t0 + S.dphidz[g][ms][1] * t1 + S.dphidz[g][ms][2] * t2;
-    }
-  } else if (r >= 81 && c < 81) {
-    const int ms = r - 81, nh = c / NQ, ns = c % NQ;
-    for (int g = 0; g < NG; ++g) s += S.jgw[g] * S.dphidz[g][ns][nh] * T.psi[g][ms];
-  } else if (r < 81 && c >= 81) {
-    const int mh = r / NQ, ms = r % NQ, ns = c - 81;
-    for (int g = 0; g < NG; ++g) {
-      const double* Hh = S.hyd[g];
-      const double tv = Hh[mh * 3 + 0] * S.dphidz[g][ms][0] + Hh[mh * 3 + 1] * S.dphidz[g][ms][1] +
-                        Hh[mh * 3 + 2] * S.dphidz[g][ms][2];
-      s += tv * T.psi[g][ns];
-    }
-  }
-  return s;
-}
-
-__global__ void __launch_bounds__(kJacThreads)
-mr_jacobian_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
-                   const int32_t* __restrict__ elin, int32_t nq2, int32_t nlin, const double* __restrict__ xg,
-                   const double* __restrict__ dep, const double* __restrict__ cpar, const Tables* __restrict__ Tg,
-                   const int32_t* __restrict__ slots, double* __restrict__ values, double* __restrict__ Kout,
-                   unsigned* err) {
-  extern __shared__ double smem[];
-  Tables& T = *reinterpret_cast<Tables*>(smem);
-  JacShared& S = *reinterpret_cast<JacShared*>(smem + sizeof(Tables) / sizeof(double));
-  {
-    const double* src = reinterpret_cast<const double*>(Tg);
-    for (int i = threadIdx.x; i < (int)(sizeof(Tables) / sizeof(double)); i += blockDim.x) smem[i] = src[i];
-  }
-  const double c1 = cpar[0], c2 = cpar[1];
-  for (int item = blockIdx.x; item < count; item += gridDim.x) {
-    const int e = __ldg(elems + item);
-    __syncthreads();
-    for (int i = threadIdx.x; i < NQ; i += blockDim.x) {
-      const int n = __ldg(eq2 + (size_t)e * NQ + i);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        S.x[c * NQ + i] = __ldg(xg + (size_t)c * nq2 + n);
-        S.z[c * NQ + i] = dep[(size_t)c * nq2 + n];
-      }
-    }
-    if (threadIdx.x < NL) S.p[threadIdx.x] = dep[(size_t)3 * nq2 + __ldg(elin + (size_t)e * NL + threadIdx.x)];
-    __syncthreads();
-    if (threadIdx.x < NG) jacobian_point(T, threadIdx.x, S, c1, c2, err);
-    __syncthreads();
-    const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
-    for (int k = threadIdx.x; k < ND * ND; k += blockDim.x) {
-      const int r = k / ND, c = k % ND;
-      if (r >= 81 && c >= 81) {
-        if (Kout) Kout[(size_t)e * ND * ND + k] = 0.0;
-        continue;
-      }
-      const double v = jacobian_entry(T, S, r, c);
-      if (Kout) Kout[(size_t)e * ND * ND + k] = v;
-      if (sl) {
-        const int pos = __ldg(sl + k);
-        if (pos < 0) gfe_raise(err, GFE_DEVERR_SLOT);
-        else values[pos] += v;
-      }
-    }
-  }
-}
-
 // slot map: for each element (in colour order) and each (r, c), the 0-based CSR position of
 // (dof_r, dof_c); -1 when absent.  One warp per (element, row).
 __global__ void mr_slot_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
@@ -728,39 +547,6 @@ __device__ void tangent_points(const Tables& T, TanShared& S, double c1, double 
   __syncthreads();
 }
 
-// exact element tangent entry (r, c)
-__device__ __forceinline__ double tangent_entry(const Tables& T, const TanShared& S, int r, int c) {
-  double s = 0.0;
-  if (r < 81 && c < 81) {
-    const int mh = r / NQ, ms = r % NQ, nh = c / NQ, ns = c % NQ;
-    for (int g = 0; g < NG; ++g) {
-      // sum_xi g_ms[xi] sum_zeta dP[xi][mh]/dZ[nh][zeta] g_ns[zeta]
-      double t = 0.0;
-#pragma unroll
-      for (int zeta = 0; zeta < 3; ++zeta) {
-        const double* d = S.dPdZ[g][nh * 3 + zeta];
-        t += (T.dphi[g][0][ms] * d[0 * 3 + mh] + T.dphi[g][1][ms] * d[1 * 3 + mh] + T.dphi[g][2][ms] * d[2 * 3 + mh]) *
-             T.dphi[g][zeta][ns];
-      }
-      s += t;
-    }
-  } else if (r < 81 && c >= 81) {
-    const int mh = r / NQ, ms = r % NQ, ns = c - 81;
-    for (int g = 0; g < NG; ++g) {
-      const double* d = S.dPdZ[g][9];
-      s += (T.dphi[g][0][ms] * d[mh] + T.dphi[g][1][ms] * d[3 + mh] + T.dphi[g][2][ms] * d[6 + mh]) * T.psi[g][ns];
-    }
-  } else if (r >= 81 && c < 81) {
-    const int ms = r - 81, nh = c / NQ, ns = c % NQ;
-    for (int g = 0; g < NG; ++g) {
-      const double* a = S.wJZi[g];
-      s += T.psi[g][ms] * (a[0 * 3 + nh] * T.dphi[g][0][ns] + a[1 * 3 + nh] * T.dphi[g][1][ns] +
-                           a[2 * 3 + nh] * T.dphi[g][2][ns]);
-    }
-  }
-  return s;
-}
-
 __device__ __forceinline__ void load_element_state(int e, const int32_t* eq2, const int32_t* elin, int nq2,
                                                    const double* xg, const double* dep, double* sx, double* sz,
                                                    double* sp, int* dofs) {
@@ -777,36 +563,6 @@ __device__ __forceinline__ void load_element_state(int e, const int32_t* eq2, co
     const int n = __ldg(elin + (size_t)e * NL + threadIdx.x);
     sp[threadIdx.x] = dep[(size_t)3 * nq2 + n];
     if (dofs) dofs[81 + threadIdx.x] = 3 * nq2 + n;
-  }
-}
-
-__global__ void __launch_bounds__(kTanThreads)
-mr_tangent_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
-                  const int32_t* __restrict__ elin, int32_t nq2, const double* __restrict__ xg,
-                  const double* __restrict__ dep, const double* __restrict__ cpar, const Tables* __restrict__ Tg,
-                  const int32_t* __restrict__ slots, double* __restrict__ values, double* __restrict__ Kout) {
-  extern __shared__ double smem[];
-  Tables& T = *reinterpret_cast<Tables*>(smem);
-  TanShared& S = *reinterpret_cast<TanShared*>(smem + sizeof(Tables) / sizeof(double));
-  for (int i = threadIdx.x; i < (int)(sizeof(Tables) / sizeof(double)); i += blockDim.x)
-    smem[i] = reinterpret_cast<const double*>(Tg)[i];
-  const double c1 = cpar[0], c2 = cpar[1];
-  for (int item = blockIdx.x; item < count; item += gridDim.x) {
-    const int e = __ldg(elems + item);
-    __syncthreads();
-    load_element_state(e, eq2, elin, nq2, xg, dep, S.x, S.z, S.p, nullptr);
-    __syncthreads();
-    tangent_points(T, S, c1, c2);
-    const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
-    for (int k = threadIdx.x; k < ND * ND; k += blockDim.x) {
-      const int r = k / ND, c = k % ND;
-      const double v = (r >= 81 && c >= 81) ? 0.0 : tangent_entry(T, S, r, c);
-      if (Kout) Kout[(size_t)e * ND * ND + k] = v;
-      if (sl && !(r >= 81 && c >= 81)) {
-        const int pos = __ldg(sl + k);
-        if (pos >= 0) values[pos] += v;
-      }
-    }
   }
 }
 
@@ -917,11 +673,323 @@ __global__ void sum_dc(const double* __restrict__ dc_elem, int32_t n_elem, int32
   dc[b * 2 + q] = s;
 }
 
-size_t tangent_smem() { return sizeof(Tables) + sizeof(TanShared); }
+// ----------------------------------------------------------------------------------------------
+// Element Jacobians: Iron's analytic tangent and the consistent tangent
+// ----------------------------------------------------------------------------------------------
+// Both are sums over Gauss points of  K(ms mh, ns nh) = g_ms^T D_g^(mh,nh) g_ns  (u-u block) with
+// the reference basis gradients g (constant tables) and 3x3 blocks D_g expressed in xi space, plus
+// the u-p / p-u blocks.  The work is split in two kernels:
+//  * mr_gp_kernel, one thread per (element, Gauss point): kinematics and material tangent in FP64,
+//    written as D_g (9 blocks x 9), Hv_g (u-p coefficients) and Pv_g (p-u coefficients);
+//  * mr_contract_kernel, one CTA per element: H_g = D_g G_g (per Gauss point, 3 x 81 x 81 values
+//    in shared memory), then the contraction K_mh^T = H_mh^T G^T against the constant table
+//    G[(g,xi)][ms] (a 81 x 27 x 81 product per displacement component), the u-p / p-u blocks, and
+//    the scatter into CSR through the per-element slot map.
+// The contraction runs in FP64 (GFE_FP64) or FP32 (GFE_MIXED; the kinematics and det(F) stay FP64,
+// the assembled values are accumulated in FP64).
+//
+// Iron's analytic tangent (src/finite_elasticity_routines.F90:1016-1274): the spatial blocks
+// J_z w (c + sigma) / J_z w c of FINITE_ELASTICITY_GAUSS_ELASTICITY_TENSOR (:649-795) mapped to xi
+// space with Z^-1 = dxi/dz (dphi/dz = Z^-T g), only the lower u-u triangle evaluated and mirrored
+// to the upper (:1269-1274), p-u = J_z w dphi_ns/dz_nh psi_ms, u-p = J_z w (push(C^-1) dphi_ms)_mh
+// psi_ns.  Consistent tangent: D_g^(mh,nh)[xi][zeta] = dP[xi][mh]/dZ[nh][zeta] from the forward-mode
+// passes of tangent_points, Hv = dP/dp, Pv = w J_z Z^-1.
+
+// Iron's per-Gauss-point tangent blocks in spatial coordinates (src/finite_elasticity_routines.F90:
+// 649-795 and 1072-1192): sub[0..2] = J_z w (c_sub + sigma) for the diagonal component blocks,
+// sub[3..5] = J_z w c_sub for the off-diagonal blocks (mh, nh) = (1,0), (2,0), (2,1);
+// hyd = J_z w push(C^-1).
+__device__ void iron_point_tensors(const GP& q, double c1, double c2, double sub[6][9], double hyd[9],
+                                   double& jgw) {
+  const double J = q.Jz / q.Jx;
+  // unmodified right Cauchy-Green tensor and its inverse
+  double C[3][3], Ci[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[i][j] = q.F[0][i] * q.F[0][j] + q.F[1][i] * q.F[1][j] + q.F[2][i] * q.F[2][j];
+  const double I3 = inv3(C, Ci);
+  const double L[6] = {C[0][0], C[1][1], C[2][2], C[0][1], C[0][2], C[1][2]};
+  const double U[6] = {Ci[0][0], Ci[1][1], Ci[2][2], Ci[0][1], Ci[0][2], Ci[1][2]};
+  // I3EE as filled by Fortran RESHAPE (column j listed): I3EE[i][j] = col[j][i]
+  const double col[6][6] = {{0.0, 4 * L[2], 4 * L[1], 0.0, 0.0, -4 * L[5]},
+                            {4 * L[2], 0.0, 4 * L[0], 0.0, -4 * L[4], 0.0},
+                            {4 * L[1], 4 * L[0], 0.0, -2 * L[3], 0.0, 0.0},
+                            {0.0, 0.0, -4 * L[3], -2 * L[2], 2 * L[5], 2 * L[4]},
+                            {0.0, -4 * L[4], 0.0, 2 * L[5], -2 * L[1], 2 * L[3]},
+                            {-4 * L[5], 0.0, 0.0, 2 * L[4], 2 * L[3], -2 * L[0]}};
+  double D[6][6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      double v = 0.0;
+      if (i < 3 && j < 3 && i != j) v = 4.0 * c2;
+      if (i >= 3 && i == j) v = -2.0 * c2;
+      D[i][j] = v + q.p * (-2.0 * U[i] * U[j] + 0.5 * col[j][i] / I3);
+    }
+  const double I1 = C[0][0] + C[1][1] + C[2][2];
+  const double t2 = 2.0 * (c1 + I1 * c2);
+  double Sv[6] = {-2 * c2 * C[0][0] + t2, -2 * c2 * C[1][1] + t2, -2 * c2 * C[2][2] + t2,
+                  -2 * c2 * C[1][0], -2 * c2 * C[2][0], -2 * c2 * C[2][1]};
+  double H[6] = {U[0], U[1], U[2], U[3], U[4], U[5]};
+  double t[6][6];
+  push_t(q.F, t);
+  push_vec(t, Sv, J);
+  push_vec(t, H, J);
+  double tD[6][6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += t[i][k] * D[k][j];
+      tD[i][j] = s;
+    }
+#pragma unroll
+  for (int i = 0; i < 6; ++i)
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      double s = 0.0;
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s += tD[i][k] * t[j][k];
+      D[i][j] = s / J;
+    }
+  Sv[0] += q.p; Sv[1] += q.p; Sv[2] += q.p;
+  jgw = q.Jz * q.w;
+#pragma unroll
+  for (int nh = 0; nh < 3; ++nh)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) sub[nh][i * 3 + j] = jgw * (D[kT2V[i][nh]][kT2V[j][nh]] + Sv[kT2V[i][j]]);
+  const int om[3] = {1, 2, 2}, on[3] = {0, 0, 1};
+#pragma unroll
+  for (int o = 0; o < 3; ++o)
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) sub[3 + o][i * 3 + j] = jgw * D[kT2V[i][om[o]]][kT2V[j][on[o]]];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) hyd[i * 3 + j] = jgw * H[kT2V[i][j]];
+}
+
+constexpr int kGPElems = 4;                // elements per CTA of mr_gp_kernel
+constexpr int kGPThreads = kGPElems * NG;  // 108
+constexpr int kGPOut = 81 + 9 + 9;         // D (9 blocks x 9), Hv, Pv per Gauss point
+
+struct GPShared {
+  double x[kGPElems][81], z[kGPElems][81], p[kGPElems][8];
+};
+
+// One thread per (element, Gauss point).  out[item][g][kGPOut] in the contraction type TO:
+// D[(mh*3+nh)*9 + xi*3+zeta], Hv[81 + xi*3+mh], Pv[90 + xi*3+nh].
+template <typename TO, bool EXACT>
+__global__ void __launch_bounds__(kGPThreads)
+mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
+             const int32_t* __restrict__ elin, int32_t nq2, const double* __restrict__ xg,
+             const double* __restrict__ dep, const double* __restrict__ cpar, const Tables* __restrict__ Tg,
+             TO* __restrict__ out, unsigned* err) {
+  extern __shared__ double smem[];
+  Tables& T = *reinterpret_cast<Tables*>(smem);
+  GPShared& S = *reinterpret_cast<GPShared*>(smem + sizeof(Tables) / sizeof(double));
+  for (int i = threadIdx.x; i < (int)(sizeof(Tables) / sizeof(double)); i += blockDim.x)
+    smem[i] = reinterpret_cast<const double*>(Tg)[i];
+  const int le = threadIdx.x / NG, g = threadIdx.x % NG;
+  const int item = blockIdx.x * kGPElems + le;
+  // cooperative load of the CTA's elements
+  for (int t = threadIdx.x; t < kGPElems * NQ; t += blockDim.x) {
+    const int l = t / NQ, i = t % NQ, it = blockIdx.x * kGPElems + l;
+    if (it >= count) continue;
+    const int e = __ldg(elems + it);
+    const int n = __ldg(eq2 + (size_t)e * NQ + i);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      S.x[l][c * NQ + i] = __ldg(xg + (size_t)c * nq2 + n);
+      S.z[l][c * NQ + i] = dep[(size_t)c * nq2 + n];
+    }
+  }
+  for (int t = threadIdx.x; t < kGPElems * NL; t += blockDim.x) {
+    const int l = t / NL, i = t % NL, it = blockIdx.x * kGPElems + l;
+    if (it >= count) continue;
+    const int e = __ldg(elems + it);
+    S.p[l][i] = dep[(size_t)3 * nq2 + __ldg(elin + (size_t)e * NL + i)];
+  }
+  __syncthreads();
+  if (item >= count) return;
+  const double c1 = cpar[0], c2 = cpar[1];
+  TO* o = out + ((size_t)item * NG + g) * kGPOut;
+  if (!EXACT) {
+    GP q;
+    if (!gauss_point(T, g, S.z[le], S.x[le], S.p[le], q)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+    double sub[6][9], hyd[9], jgw;
+    iron_point_tensors(q, c1, c2, sub, hyd, jgw);
+    // blocks to xi space: Dxi = Zi sub Zi^T (Zi = dxi/dz); upper blocks as transposes of the lower
+    for (int mh = 0; mh < 3; ++mh)
+      for (int nh = 0; nh < 3; ++nh) {
+        const int blk = mh == nh ? mh : (mh > nh ? 3 + (mh == 1 ? 0 : (nh == 0 ? 1 : 2))
+                                                 : 3 + (nh == 1 ? 0 : (mh == 0 ? 1 : 2)));
+        const bool tr = mh < nh;
+        double W[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int z = 0; z < 3; ++z) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) s += (tr ? sub[blk][j * 3 + i] : sub[blk][i * 3 + j]) * q.Zi[z][j];
+            W[i][z] = s;  // (sub Zi^T)[i][zeta]
+          }
+#pragma unroll
+        for (int xi = 0; xi < 3; ++xi)
+#pragma unroll
+          for (int z = 0; z < 3; ++z)
+            o[(mh * 3 + nh) * 9 + xi * 3 + z] =
+                (TO)(q.Zi[xi][0] * W[0][z] + q.Zi[xi][1] * W[1][z] + q.Zi[xi][2] * W[2][z]);
+      }
+#pragma unroll
+    for (int xi = 0; xi < 3; ++xi)
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        o[81 + xi * 3 + m] = (TO)(q.Zi[xi][0] * hyd[m * 3 + 0] + q.Zi[xi][1] * hyd[m * 3 + 1] +
+                                  q.Zi[xi][2] * hyd[m * 3 + 2]);
+        o[90 + xi * 3 + m] = (TO)(jgw * q.Zi[xi][m]);
+      }
+  } else {
+    GPIn in;
+    gauss_inputs(T, g, S.z[le], S.x[le], S.p[le], in);
+    for (int seed = 0; seed < 10; ++seed) {
+      double d[9], Jz;
+      point_dP(in, seed, c1, c2, d, &Jz);
+      if (seed < 9) {
+        const int nh = seed / 3, z = seed % 3;
+#pragma unroll
+        for (int xi = 0; xi < 3; ++xi)
+#pragma unroll
+          for (int mh = 0; mh < 3; ++mh) o[(mh * 3 + nh) * 9 + xi * 3 + z] = (TO)d[xi * 3 + mh];
+      } else {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) o[81 + k] = (TO)d[k];
+        double Zi[3][3];
+        const double dz = inv3(in.Z, Zi);
+        if (!(dz > 0.0) || !isfinite(dz)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+#pragma unroll
+        for (int xi = 0; xi < 3; ++xi)
+#pragma unroll
+          for (int nh = 0; nh < 3; ++nh) o[90 + xi * 3 + nh] = (TO)(in.w * Jz * Zi[xi][nh]);
+      }
+    }
+  }
+}
+
+constexpr int kCThreads = 256;
+
+// shared layout of mr_contract_kernel (in units of TS)
+template <typename TS>
+struct ContractShared {
+  TS G[81][28];        // G[(g,xi)][ms] (padded row)
+  TS psi[NG][NL];      // pressure basis at the Gauss points
+  TS Dg[NG][kGPOut];   // this element's Gauss-point blocks
+  TS H[81][81];        // H_mh[(g,xi)][(ns,nh)] of the current displacement component mh
+  TS Kuu[81][81];      // K_uu[(ms,mh)][(ns,nh)]
+  TS HvG[NG][81];      // sum_xi G[(g,xi)][ms] Hv[xi][mh]  -> [g][(mh,ms)]
+  TS PvG[NG][81];      // sum_xi G[(g,xi)][ns] Pv[xi][nh]  -> [g][(nh,ns)]
+};
+
+template <typename TS, bool EXACT>
+__global__ void __launch_bounds__(kCThreads)
+mr_contract_kernel(const int32_t* __restrict__ elems, int32_t count, const Tables* __restrict__ Tg,
+                   const TS* __restrict__ gp, const int32_t* __restrict__ slots, double* __restrict__ values,
+                   double* __restrict__ Kout, unsigned* err) {
+  extern __shared__ __align__(16) unsigned char craw[];
+  ContractShared<TS>& S = *reinterpret_cast<ContractShared<TS>*>(craw);
+  const int tid = threadIdx.x;
+  for (int t = tid; t < 81 * 27; t += blockDim.x) {
+    const int k = t / 27, ms = t % 27;
+    S.G[k][ms] = (TS)Tg->dphi[k / 3][k % 3][ms];
+  }
+  for (int t = tid; t < NG * NL; t += blockDim.x) S.psi[t / NL][t % NL] = (TS)Tg->psi[t / NL][t % NL];
+  for (int item = blockIdx.x; item < count; item += gridDim.x) {
+    __syncthreads();
+    const TS* src = gp + (size_t)item * NG * kGPOut;
+    for (int t = tid; t < NG * kGPOut; t += blockDim.x) (&S.Dg[0][0])[t] = src[t];
+    __syncthreads();
+    // u-p / p-u coefficients
+    for (int t = tid; t < 2 * NG * 81; t += blockDim.x) {
+      const int which = t / (NG * 81), r = t % (NG * 81), g = r / 81, c = r % 81, h = c / 27, s = c % 27;
+      const int off = which == 0 ? 81 : 90;
+      const TS v = S.G[g * 3 + 0][s] * S.Dg[g][off + 0 * 3 + h] + S.G[g * 3 + 1][s] * S.Dg[g][off + 1 * 3 + h] +
+                   S.G[g * 3 + 2][s] * S.Dg[g][off + 2 * 3 + h];
+      if (which == 0) S.HvG[g][c] = v; else S.PvG[g][c] = v;
+    }
+    // per displacement component mh: H_mh = D G, then K_mh^T = H_mh^T G^T with 3x3 thread tiles
+    const bool active = tid < 243;
+    const int rg = tid / 9, cg = tid % 9;
+    for (int mh = 0; mh < 3; ++mh) {
+      __syncthreads();
+      for (int t = tid; t < 81 * 81; t += blockDim.x) {
+        const int k = t / 81, c = t % 81;
+        const int g = k / 3, xi = k % 3, nh = c / 27, ns = c % 27;
+        const TS* D = &S.Dg[g][(mh * 3 + nh) * 9 + xi * 3];
+        S.H[k][c] = D[0] * S.G[g * 3 + 0][ns] + D[1] * S.G[g * 3 + 1][ns] + D[2] * S.G[g * 3 + 2][ns];
+      }
+      __syncthreads();
+      if (active) {
+        TS acc[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) acc[a][b] = TS(0);
+#pragma unroll 3
+        for (int k = 0; k < 81; ++k) {
+          const TS h0 = S.H[k][rg * 3 + 0], h1 = S.H[k][rg * 3 + 1], h2 = S.H[k][rg * 3 + 2];
+          const TS g0 = S.G[k][cg * 3 + 0], g1 = S.G[k][cg * 3 + 1], g2 = S.G[k][cg * 3 + 2];
+          acc[0][0] += h0 * g0; acc[0][1] += h0 * g1; acc[0][2] += h0 * g2;
+          acc[1][0] += h1 * g0; acc[1][1] += h1 * g1; acc[1][2] += h1 * g2;
+          acc[2][0] += h2 * g0; acc[2][1] += h2 * g1; acc[2][2] += h2 * g2;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) S.Kuu[mh * 27 + cg * 3 + b][rg * 3 + a] = acc[a][b];
+      }
+    }
+    __syncthreads();
+    TS(*Kuu)[81] = S.Kuu;
+    const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
+    const int e = Kout ? __ldg(elems + item) : 0;
+    for (int k = tid; k < ND * ND; k += blockDim.x) {
+      const int r = k / ND, c = k % ND;
+      TS v;
+      if (r < 81 && c < 81) {
+        v = (EXACT || r >= c) ? Kuu[r][c] : Kuu[c][r];  // Iron mirrors the lower u-u triangle
+      } else if (r < 81) {  // u rows, p columns
+        TS s = TS(0);
+        for (int g = 0; g < NG; ++g) s += S.HvG[g][r] * S.psi[g][c - 81];
+        v = s;
+      } else if (c < 81) {  // p rows, u columns
+        TS s = TS(0);
+        for (int g = 0; g < NG; ++g) s += S.psi[g][r - 81] * S.PvG[g][c];
+        v = s;
+      } else {
+        v = TS(0);
+      }
+      if (Kout) Kout[(size_t)e * ND * ND + k] = (double)v;
+      if (sl && !(r >= 81 && c >= 81)) {
+        const int pos = __ldg(sl + k);
+        if (pos < 0) gfe_raise(err, GFE_DEVERR_SLOT);
+        else values[pos] += (double)v;
+      }
+    }
+  }
+}
+
 size_t vjp_smem() { return sizeof(Tables) + sizeof(TanShared) + sizeof(double) * (ND + NG * 9 + NG + NG * 2); }
 
 size_t residual_smem() { return sizeof(Tables) + kResWarps * sizeof(double) * (81 + 81 + 8 + NG * 9 + NG + 48); }
-size_t jacobian_smem() { return sizeof(Tables) + sizeof(JacShared); }
 
 int check_mesh(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin, const double* xg,
                const char* fn) {
@@ -985,46 +1053,68 @@ extern "C" int gfe_mr_slot_map(int32_t n_elem, const int32_t* eq2, const int32_t
   return GFE_OK;
 }
 
-extern "C" int gfe_mr_jacobian(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
-                               const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host,
-                               int32_t n_colors, const double* dep, const double* cpar, const int32_t* slots,
-                               double* values, int64_t nnz, double* K_out, void* stream) {
-  const char* fn = "gfe_mr_jacobian";
-  int rc = check_mesh(n_elem, eq2, elin, nq2, nlin, xg, fn);
-  if (rc) return rc;
-  if (!dep || !cpar || (n_elem > 0 && (!color_elems || !color_ptr_host || n_colors <= 0)))
-    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
-  if (!K_out && (!slots || !values)) return gfe::set_error(GFE_ERR_ARG, "%s: need CSR values + slots or K_out", fn);
-  if (color_ptr_host[0] != 0 || color_ptr_host[n_colors] != n_elem)
-    return gfe::set_error(GFE_ERR_ARG, "%s: colour offsets must run from 0 to n_elem", fn);
+namespace {
+
+// Element Jacobians of one problem (mode 0: Iron's analytic tangent, 1: consistent tangent), in the
+// contraction precision `precision`, assembled into CSR values through the slot map and/or written
+// as dense element matrices.  Per colour: the Gauss-point kernel fills a scratch array, the
+// contraction kernel consumes it.
+template <typename TS>
+int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, const double* xg,
+                  const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors, const double* dep,
+                  const double* cpar, const int32_t* slots, double* values, int64_t nnz, double* K_out,
+                  cudaStream_t s, const char* fn) {
   const Tables* T = nullptr;
-  if ((rc = device_tables(&T))) return rc;
-  cudaStream_t s = gfe::as_stream(stream);
+  int rc = device_tables(&T);
+  if (rc) return rc;
+  int max_cnt = 0;
+  for (int c = 0; c < n_colors; ++c) max_cnt = std::max(max_cnt, color_ptr_host[c + 1] - color_ptr_host[c]);
+  TS* gpbuf = nullptr;
+  if ((rc = gfe::scratch_alloc((void**)&gpbuf, sizeof(TS) * (size_t)max_cnt * NG * kGPOut + 16, s,
+                               "Gauss-point tangent blocks")))
+    return rc;
   if (values) GFE_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)nnz, s));
-  const size_t sm = jacobian_smem();
-  if ((rc = set_smem((const void*)mr_jacobian_kernel, sm))) return rc;
+  const size_t gsm = sizeof(Tables) + sizeof(GPShared);
+  const size_t csm = sizeof(ContractShared<TS>);
+  const void* gk = mode == 0 ? (const void*)mr_gp_kernel<TS, false> : (const void*)mr_gp_kernel<TS, true>;
+  const void* ck = mode == 0 ? (const void*)mr_contract_kernel<TS, false> : (const void*)mr_contract_kernel<TS, true>;
+  if ((rc = set_smem(gk, gsm)) || (rc = set_smem(ck, csm))) {
+    gfe::scratch_free(gpbuf, s);
+    return rc;
+  }
   unsigned* err = gfe::device_error_word();
   void* prof = gfe::stage_begin(GFE_STAGE_MR_JACOBIAN, s);
   int launches = 0;
   for (int c = 0; c < n_colors; ++c) {
     const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
     if (cnt <= 0) continue;
-    const int grid = std::min(cnt, 8 * gfe::sm_count());
-    mr_jacobian_kernel<<<grid, kJacThreads, sm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, nlin, xg, dep, cpar, T,
-                                                      slots ? slots + (size_t)c0 * ND * ND : nullptr, values, K_out,
-                                                      err);
-    ++launches;
+    const int ggrid = (cnt + kGPElems - 1) / kGPElems;
+    const int cgrid = std::min(cnt, 8 * gfe::sm_count());
+    const int32_t* sl = slots ? slots + (size_t)c0 * ND * ND : nullptr;
+    if (mode == 0) {
+      mr_gp_kernel<TS, false><<<ggrid, kGPThreads, gsm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar, T,
+                                                             gpbuf, err);
+      mr_contract_kernel<TS, false><<<cgrid, kCThreads, csm, s>>>(color_elems + c0, cnt, T, gpbuf, sl, values,
+                                                                  K_out, err);
+    } else {
+      mr_gp_kernel<TS, true><<<ggrid, kGPThreads, gsm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar, T,
+                                                            gpbuf, err);
+      mr_contract_kernel<TS, true><<<cgrid, kCThreads, csm, s>>>(color_elems + c0, cnt, T, gpbuf, sl, values, K_out,
+                                                                 err);
+    }
+    launches += 2;
   }
   gfe::stage_end(GFE_STAGE_MR_JACOBIAN, prof, s, launches);
+  gfe::scratch_free(gpbuf, s);
   GFE_LAUNCH_CHECK(fn);
   return GFE_OK;
 }
 
-extern "C" int gfe_mr_tangent(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
-                              const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host,
-                              int32_t n_colors, const double* dep, const double* cpar, const int32_t* slots,
-                              double* values, int64_t nnz, double* K_out, void* stream) {
-  const char* fn = "gfe_mr_tangent";
+int jacobian_entry_point(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
+                         const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host,
+                         int32_t n_colors, const double* dep, const double* cpar, const int32_t* slots,
+                         double* values, int64_t nnz, double* K_out, int32_t precision, void* stream,
+                         const char* fn) {
   int rc = check_mesh(n_elem, eq2, elin, nq2, nlin, xg, fn);
   if (rc) return rc;
   if (!dep || !cpar || (n_elem > 0 && (!color_elems || !color_ptr_host || n_colors <= 0)))
@@ -1032,25 +1122,32 @@ extern "C" int gfe_mr_tangent(int32_t n_elem, const int32_t* eq2, const int32_t*
   if (!K_out && (!slots || !values)) return gfe::set_error(GFE_ERR_ARG, "%s: need CSR values + slots or K_out", fn);
   if (color_ptr_host[0] != 0 || color_ptr_host[n_colors] != n_elem)
     return gfe::set_error(GFE_ERR_ARG, "%s: colour offsets must run from 0 to n_elem", fn);
-  const Tables* T = nullptr;
-  if ((rc = device_tables(&T))) return rc;
+  if (precision != GFE_FP64 && precision != GFE_MIXED)
+    return gfe::set_error(GFE_ERR_ARG, "%s: precision must be GFE_FP64 or GFE_MIXED", fn);
   cudaStream_t s = gfe::as_stream(stream);
-  if (values) GFE_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)nnz, s));
-  const size_t sm = tangent_smem();
-  if ((rc = set_smem((const void*)mr_tangent_kernel, sm))) return rc;
-  void* prof = gfe::stage_begin(GFE_STAGE_MR_JACOBIAN, s);
-  int launches = 0;
-  for (int c = 0; c < n_colors; ++c) {
-    const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
-    if (cnt <= 0) continue;
-    const int grid = std::min(cnt, 8 * gfe::sm_count());
-    mr_tangent_kernel<<<grid, kTanThreads, sm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar, T,
-                                                     slots ? slots + (size_t)c0 * ND * ND : nullptr, values, K_out);
-    ++launches;
-  }
-  gfe::stage_end(GFE_STAGE_MR_JACOBIAN, prof, s, launches);
-  GFE_LAUNCH_CHECK(fn);
-  return GFE_OK;
+  if (precision == GFE_FP64)
+    return jacobian_impl<double>(mode, n_elem, eq2, elin, nq2, xg, color_elems, color_ptr_host, n_colors, dep, cpar,
+                                 slots, values, nnz, K_out, s, fn);
+  return jacobian_impl<float>(mode, n_elem, eq2, elin, nq2, xg, color_elems, color_ptr_host, n_colors, dep, cpar,
+                              slots, values, nnz, K_out, s, fn);
+}
+
+}  // namespace
+
+extern "C" int gfe_mr_jacobian(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
+                               const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host,
+                               int32_t n_colors, const double* dep, const double* cpar, const int32_t* slots,
+                               double* values, int64_t nnz, double* K_out, int32_t precision, void* stream) {
+  return jacobian_entry_point(0, n_elem, eq2, elin, nq2, nlin, xg, color_elems, color_ptr_host, n_colors, dep, cpar,
+                              slots, values, nnz, K_out, precision, stream, "gfe_mr_jacobian");
+}
+
+extern "C" int gfe_mr_tangent(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
+                              const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host,
+                              int32_t n_colors, const double* dep, const double* cpar, const int32_t* slots,
+                              double* values, int64_t nnz, double* K_out, int32_t precision, void* stream) {
+  return jacobian_entry_point(1, n_elem, eq2, elin, nq2, nlin, xg, color_elems, color_ptr_host, n_colors, dep, cpar,
+                              slots, values, nnz, K_out, precision, stream, "gfe_mr_tangent");
 }
 
 extern "C" int gfe_mr_residual_vjp(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2,

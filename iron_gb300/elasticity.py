@@ -96,55 +96,38 @@ class MooneyRivlinAssembly:
             _lib.raise_device_errors("gfe_mr_residual", stream)
         return R
 
-    def jacobian(self, dep: torch.Tensor, c, stream=None, check=True) -> torch.Tensor:
-        """Iron's analytic Jacobian assembled into the CSR values (self.values)."""
-        if self.slots is None:
+    def _element_jacobians(self, fn: str, dep, c, precision: str, dense: bool, stream, check: bool):
+        prec = {"fp64": _lib.GFE_FP64, "mixed": _lib.GFE_MIXED}[precision]
+        if not dense and self.slots is None:
             self.build_structure(stream)
         dep = dep.to(self.device, torch.float64).contiguous()
         cp = self._cpar(c, 1)
         cptr = self.colour_ptr
-        _lib.call("gfe_mr_jacobian", self.n_elements, _lib.ptr(self.eq2), _lib.ptr(self.elin), self.n_q2, self.n_lin,
+        K = torch.empty((self.n_elements, 89, 89), dtype=torch.float64, device=self.device) if dense else None
+        _lib.call(fn, self.n_elements, _lib.ptr(self.eq2), _lib.ptr(self.elin), self.n_q2, self.n_lin,
                   _lib.ptr(self.xg), _lib.ptr(self.colour_elems), cptr.ctypes.data_as(C.c_void_p), len(cptr) - 1,
-                  _lib.ptr(dep), _lib.ptr(cp), _lib.ptr(self.slots), _lib.ptr(self.values), self.nnz, None,
+                  _lib.ptr(dep), _lib.ptr(cp), None if dense else _lib.ptr(self.slots),
+                  None if dense else _lib.ptr(self.values), 0 if dense else self.nnz, _lib.ptr(K), prec,
                   _lib.stream_handle(stream))
         if check:
-            _lib.raise_device_errors("gfe_mr_jacobian", stream)
-        return self.values
+            _lib.raise_device_errors(fn, stream)
+        return K if dense else self.values
 
-    def element_jacobians(self, dep: torch.Tensor, c, stream=None) -> torch.Tensor:
+    def jacobian(self, dep: torch.Tensor, c, precision: str = "fp64", stream=None, check=True) -> torch.Tensor:
+        """Iron's analytic Jacobian assembled into the CSR values (self.values).  precision 'mixed'
+        runs the basis-gradient contraction in FP32 (kinematics and assembled values in FP64)."""
+        return self._element_jacobians("gfe_mr_jacobian", dep, c, precision, False, stream, check)
+
+    def element_jacobians(self, dep: torch.Tensor, c, precision: str = "fp64", stream=None) -> torch.Tensor:
         """Dense element Jacobians [E][89][89] (Iron's analytic form), for parity checks."""
-        dep = dep.to(self.device, torch.float64).contiguous()
-        cp = self._cpar(c, 1)
-        K = torch.empty((self.n_elements, 89, 89), dtype=torch.float64, device=self.device)
-        cptr = self.colour_ptr
-        _lib.call("gfe_mr_jacobian", self.n_elements, _lib.ptr(self.eq2), _lib.ptr(self.elin), self.n_q2, self.n_lin,
-                  _lib.ptr(self.xg), _lib.ptr(self.colour_elems), cptr.ctypes.data_as(C.c_void_p), len(cptr) - 1,
-                  _lib.ptr(dep), _lib.ptr(cp), None, None, 0, _lib.ptr(K), _lib.stream_handle(stream))
-        _lib.raise_device_errors("gfe_mr_jacobian", stream)
-        return K
+        return self._element_jacobians("gfe_mr_jacobian", dep, c, precision, True, stream, True)
 
-    def tangent(self, dep: torch.Tensor, c, stream=None) -> torch.Tensor:
+    def tangent(self, dep: torch.Tensor, c, precision: str = "fp64", stream=None, check=True) -> torch.Tensor:
         """Consistent tangent dR/d(dep) assembled into self.values (exact derivative of residual())."""
-        if self.slots is None:
-            self.build_structure(stream)
-        dep = dep.to(self.device, torch.float64).contiguous()
-        cp = self._cpar(c, 1)
-        cptr = self.colour_ptr
-        _lib.call("gfe_mr_tangent", self.n_elements, _lib.ptr(self.eq2), _lib.ptr(self.elin), self.n_q2, self.n_lin,
-                  _lib.ptr(self.xg), _lib.ptr(self.colour_elems), cptr.ctypes.data_as(C.c_void_p), len(cptr) - 1,
-                  _lib.ptr(dep), _lib.ptr(cp), _lib.ptr(self.slots), _lib.ptr(self.values), self.nnz, None,
-                  _lib.stream_handle(stream))
-        return self.values
+        return self._element_jacobians("gfe_mr_tangent", dep, c, precision, False, stream, check)
 
-    def element_tangents(self, dep: torch.Tensor, c, stream=None) -> torch.Tensor:
-        dep = dep.to(self.device, torch.float64).contiguous()
-        cp = self._cpar(c, 1)
-        K = torch.empty((self.n_elements, 89, 89), dtype=torch.float64, device=self.device)
-        cptr = self.colour_ptr
-        _lib.call("gfe_mr_tangent", self.n_elements, _lib.ptr(self.eq2), _lib.ptr(self.elin), self.n_q2, self.n_lin,
-                  _lib.ptr(self.xg), _lib.ptr(self.colour_elems), cptr.ctypes.data_as(C.c_void_p), len(cptr) - 1,
-                  _lib.ptr(dep), _lib.ptr(cp), None, None, 0, _lib.ptr(K), _lib.stream_handle(stream))
-        return K
+    def element_tangents(self, dep: torch.Tensor, c, precision: str = "fp64", stream=None) -> torch.Tensor:
+        return self._element_jacobians("gfe_mr_tangent", dep, c, precision, True, stream, True)
 
     def residual_vjp(self, dep: torch.Tensor, c, v: torch.Tensor, stream=None):
         """(v^T dR/d dep, v^T dR/d(c10, c01)) for one or a batch of problems."""
