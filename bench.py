@@ -41,9 +41,10 @@ def parse():
     ap.add_argument("--impl", default="gfe", choices=["gfe", "reference"])
     ap.add_argument("--n", type=int, default=128, help="elements per side")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed_df", "mixed"])
-    ap.add_argument("--workload", default="laplace", choices=["laplace", "mr", "mr_adjoint", "serve"],
+    ap.add_argument("--workload", default="laplace", choices=["laplace", "mr", "mr_newton", "mr_adjoint", "serve"],
                     help="laplace: the headline assembly workload; mr: Mooney-Rivlin Q2/Q1 residual + Jacobian "
-                         "assembly (32^3); mr_adjoint: batched residual adjoint (16^3 x 64); serve: request stream")
+                         "assembly (32^3); mr_newton: load-stepped Newton solve of the uniaxial stretch (32^3); "
+                         "mr_adjoint: batched residual adjoint (16^3 x 64); serve: request stream")
     ap.add_argument("--path", default="auto", choices=["auto", "regular", "general"],
                     help="assembly kernel: regular-mesh tiled kernel (auto for generated meshes) or colour scatter")
     ap.add_argument("--no-solve", action="store_true")

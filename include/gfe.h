@@ -231,6 +231,40 @@ int gfe_cg_solve_noalloc(int32_t n, const int32_t* row_ptr, const int32_t* col_i
                          const double* f, const uint8_t* fixed, double* x, double rtol, int32_t max_iters,
                          int32_t* iters_host, double* rel_host, void* stream);
 
+/* Solve K x = f for symmetric (possibly indefinite) K with Dirichlet conditions, by preconditioned
+ * MINRES: the linear solve of the Newton step for the mixed u-p Jacobian, whose p-p block is zero.
+ * Replaces the PETSc KSP solve Iron runs inside its Newton solver (GMRES + Jacobi by default,
+ * src/solver_routines.F90:11320-11369; SNES linear solve call in src/solver_routines.F90:18942-18991).
+ *  minv       [n] inverse of a symmetric positive definite diagonal preconditioner (> 0 on free
+ *             rows), or NULL for 1/|K_ii| with 1 where K_ii = 0
+ *  rtol       relative 2-norm residual target ||f - K x|| / ||f - K x0||, x0 = Dirichlet values
+ *             with zeros elsewhere; the other arguments as gfe_cg_solve (GFE_MIXED: FP64-residual
+ *             refinement around FP32 MINRES on values32).
+ * Synchronises `stream`.  Allocates and frees its scratch on `stream`. */
+int gfe_minres_solve(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const double* values,
+                     const float* values32, const double* minv, const double* f, const uint8_t* fixed, double* x,
+                     double rtol, int32_t max_iters, int32_t precision, int32_t* iters_host, double* rel_host,
+                     void* stream);
+
+/* Solve K x = f for general (non-symmetric) K with Dirichlet conditions by restarted GMRES(restart),
+ * right-preconditioned by the diagonal minv (as gfe_minres_solve; NULL = Jacobi with 1 for a zero
+ * diagonal), classical Gram-Schmidt.  Iron's default linear solver: PETSc GMRES, restart 30
+ * (src/solver_routines.F90:11320-11369); needed for Iron's analytic Mooney-Rivlin Jacobian, whose
+ * u-p and p-u blocks are not transposes of each other.  Each restart forms the residual in FP64;
+ * GFE_MIXED runs the Krylov cycles in FP32 on values32.  restart: 1..64.  Other arguments as
+ * gfe_minres_solve.  Synchronises `stream` once per cycle. */
+int gfe_gmres_solve(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const double* values,
+                    const float* values32, const double* minv, const double* f, const uint8_t* fixed, double* x,
+                    double rtol, int32_t max_iters, int32_t restart, int32_t precision, int32_t* iters_host,
+                    double* rel_host, void* stream);
+
+/* Diagonal SPD preconditioner for gfe_minres_solve on a u-p saddle-point matrix whose first n_u
+ * rows are the displacement block: minv[i] = 1/|K_ii| on u rows and, on p rows, the inverse of
+ * sum_{free j < n_u} K_ij^2 / |K_jj| (the diagonal of B diag(K_uu)^-1 B^T); 1 where either is zero,
+ * 0 on fixed rows.  Iron's default Jacobi preconditioner has no usable p-p diagonal (it is zero). */
+int gfe_saddle_preconditioner(int32_t n, int32_t n_u, const int32_t* row_ptr, const int32_t* col_idx,
+                              const double* values, const uint8_t* fixed, double* minv, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

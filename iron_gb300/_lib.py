@@ -68,6 +68,11 @@ SIGNATURES = {
                                C.POINTER(C.c_double), vp]),
     "gfe_cg_solve_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, f64, i32, C.POINTER(C.c_int32),
                                        C.POINTER(C.c_double), vp]),
+    "gfe_minres_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(C.c_int32),
+                                   C.POINTER(C.c_double), vp]),
+    "gfe_gmres_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, vp, f64, i32, i32, i32, C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_double), vp]),
+    "gfe_saddle_preconditioner":(C.c_int, [i32, i32, vp, vp, vp, vp, vp, vp]),
 }
 
 

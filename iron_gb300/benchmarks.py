@@ -144,10 +144,67 @@ def bench_mr_adjoint(args, log, clock_sampler):
     return 0
 
 
+def bench_mr_newton(args, log, clock_sampler):
+    """Uniaxial stretch of the Mooney-Rivlin box to lambda = 1.1 in 5 load steps (Iron's increment
+    rule), roller conditions, Newton with the consistent tangent and MINRES; FP64 plain against
+    mixed precision (FP32 contraction + FP32 MINRES inside FP64 refinement, FP64 residual)."""
+    from .newton import NewtonSolver, uniaxial_exact_state, uniaxial_roller_conditions
+
+    n = 32 if args.n == 128 else args.n
+    lam, steps = 1.10, 5
+    dev = torch.device("cuda", 0)
+    log(f"MR Newton {n}^3: structure + slot map")
+    A = MooneyRivlinAssembly.from_regular_mesh((n, n, n), device=dev)
+    fixed, full = uniaxial_roller_conditions(A, lam)
+    exact = uniaxial_exact_state(A, lam, 2.0, 6.0)
+    res, states = {}, {}
+    with clock_sampler(dev.index) as clk:
+        for prec in ("fp64", "mixed"):
+            dep = A.initial_state(0.0)
+            solver = NewtonSolver(A, [2.0, 6.0], precision=prec, absolute_tolerance=1e-12,
+                                  relative_tolerance=1e-12, solution_tolerance=0.0,
+                                  linear_relative_tolerance=1e-6)
+            log(f"Newton ({prec})")
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            infos = solver.solve(dep, fixed, full, load_increments=steps,
+                                 callback=lambda s, i: log(f"  step {s}: {i.iterations} its, "
+                                                           f"|R| {i.residual_norms[-1]:.3e}, "
+                                                           f"linear {i.linear_iterations}"))
+            torch.cuda.synchronize()
+            res[prec] = {"seconds": time.perf_counter() - t0,
+                         "newton_iterations": [i.iterations for i in infos],
+                         "linear_iterations": [i.linear_iterations for i in infos],
+                         "final_residual": infos[-1].residual_norms[-1]}
+            states[prec] = dep
+    _lib.raise_device_errors("bench mr newton")
+    scale = float(states["fp64"].abs().max())
+    err_mixed = float((states["mixed"] - states["fp64"]).abs().max()) / scale
+    err_exact = {p: float((states[p] - exact).abs().max()) / scale for p in states}
+    best = min(res, key=lambda p: res[p]["seconds"])
+    E = A.n_elements
+    line = {
+        "metric": "mr_newton_load_stepped_elements_per_s", "value": E * steps / res[best]["seconds"],
+        "unit": "element-load-steps/s", "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": True,
+        "dtype": "f64" if best == "fp64" else "f32/f64", "data": "synthetic",
+        "config": {"workload": "mooney_rivlin_q2p1_uniaxial_newton", "elements_per_side": n, "elements": E,
+                   "dofs": A.ndof, "jacobian_nnz": A.nnz, "lambda": lam, "load_steps": steps, "c10": 2.0,
+                   "c01": 6.0, "bcs": "rollers on x=0,y=0,z=0; z1=lambda on x=1",
+                   "jacobian": "consistent tangent", "linear_solver": "MINRES + saddle diagonal"},
+        "headline_precision": best, "runs": res,
+        "mixed_rel_err_vs_fp64": err_mixed, "rel_err_vs_exact": err_exact,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run(args, log, clock_sampler):
     _lib.load()
     if args.workload == "mr":
         return bench_mr(args, log, clock_sampler)
+    if args.workload == "mr_newton":
+        return bench_mr_newton(args, log, clock_sampler)
     if args.workload == "mr_adjoint":
         return bench_mr_adjoint(args, log, clock_sampler)
     if args.workload == "serve":

@@ -22,59 +22,20 @@
 #include <vector>
 
 #include "gfe_internal.cuh"
+#include "reduce.cuh"
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = gfe_red::kThreads;
 
 struct Scalars {
   double rz, pq, alpha, beta, rr, rr0, tol2;
   int done, it, ticket1, ticket2, bad;
 };
 
-// Deterministic block reduction of one double per thread into red[blockIdx.x]; returns true in
-// thread 0 of the last block to arrive, after which red[0..nblk) are all visible.
-__device__ __forceinline__ double block_sum(double v) {
-  __shared__ double sh[kThreads / 32];
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < kThreads / 32; ++i) s += sh[i];
-  __syncthreads();
-  return s;  // valid in thread 0
-}
-
-__device__ __forceinline__ bool last_block(int* ticket) {
-  __shared__ bool amlast;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    int t = atomicAdd(ticket, 1);
-    amlast = (t == (int)gridDim.x - 1);
-  }
-  __syncthreads();
-  return amlast;
-}
-
-// Sum red[0..n) in index order using the whole block; result valid in thread 0.
-__device__ __forceinline__ double ordered_sum(const double* red, int n) {
-  __shared__ double sh[kThreads];
-  // each thread sums a contiguous chunk, then thread 0 sums the chunk totals in order
-  const int per = (n + kThreads - 1) / kThreads;
-  double s = 0.0;
-  const int i0 = threadIdx.x * per;
-  for (int i = i0; i < i0 + per && i < n; ++i) s += __ldcg(red + i);
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < kThreads; ++i) t += sh[i];
-  __syncthreads();
-  return t;
-}
+using gfe_red::block_sum;
+using gfe_red::last_block;
+using gfe_red::ordered_sum;
 
 // q = A p on free rows (0 on fixed rows), partial <p, q>.  LPR lanes per row.  The arithmetic is
 // done in the vector type TV: GB300's FP64 pipe issues a warp instruction in 64 cycles, so the FP64
@@ -426,6 +387,745 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
   if (sh.bad) return set_error(GFE_ERR_NUMERIC, "%s: CG breakdown (non-positive curvature or non-finite value)", fn);
   if (!(rel <= rtol)) return set_error(GFE_ERR_NOCONV, "%s: relative residual %.3e above %.3e after %d iterations",
                                        fn, rel, rtol, total_it);
+  return GFE_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Preconditioned MINRES for symmetric indefinite systems
+// ---------------------------------------------------------------------------------------------
+// The consistent tangent of the mixed u-p Mooney-Rivlin residual is symmetric with a zero p-p
+// block, so CG does not apply.  Iron hands such systems to PETSc (GMRES + Jacobi by default,
+// src/solver_routines.F90:11320-11369, or a direct solver); here they are solved by MINRES with a
+// symmetric positive definite diagonal preconditioner M, in the Lanczos form of Elman, Silvester
+// and Wathen (Finite Elements and Fast Iterative Solvers, Algorithm 2.4):
+//   v_{j+1} = A z_j - (delta_j / gamma_j) v_j - (gamma_j / gamma_{j-1}) v_{j-1},  z = M^-1 v / gamma
+// with Givens rotations giving the update direction w and the M^-1-norm of the residual |eta|.
+// One iteration is two kernels: (A) the deferred w / x update of the previous iteration fused with
+// the SpMV q = A z_j and delta_j = <q, z_j>; (B) the Lanczos update, z_{j+1} = M^-1 v_{j+1},
+// gamma_{j+1} and, in the last block, the rotation scalars and the convergence flag.  Vector
+// buffers rotate between two copies on the host side; the kernels return at once after `done`, so
+// iterations are launched in chunks exactly like the CG.
+namespace {
+
+struct MinresScalars {
+  double gamma, gamma_old, delta, c, c_old, s, s_old, eta, tol;
+  double zs_prev, a1, a2, a3, ceta;
+  int done, pending, it, ticket1, ticket2, bad;
+};
+
+// (A): pending w / x update of the previous iteration, then q = A z / gamma (0 on fixed rows) and
+// delta = <q, z / gamma>.
+template <typename TM, typename TV, typename TX, int LPR>
+__global__ void __launch_bounds__(kThreads)
+minres_spmv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, const TM* __restrict__ val,
+            const TV* __restrict__ z, TV* __restrict__ q, const uint8_t* __restrict__ fixed,
+            const TV* __restrict__ zprev, TV* __restrict__ wold, const TV* __restrict__ wnew, TX* __restrict__ x,
+            double* red, MinresScalars* sc) {
+  const int pending = sc->pending, done = sc->done;
+  if (done && !pending) return;
+  if (pending) {
+    const TV zs = (TV)sc->zs_prev, a1i = (TV)(1.0 / sc->a1), a2 = (TV)sc->a2, a3 = (TV)sc->a3, ce = (TV)sc->ceta;
+    for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+      const TV w = (zprev[i] * zs - a3 * wold[i] - a2 * wnew[i]) * a1i;
+      wold[i] = w;
+      x[i] = x[i] + (TX)(ce * w);
+    }
+  }
+  TV dot = TV(0);
+  if (!done) {
+    const TV g = (TV)(1.0 / sc->gamma);
+    constexpr int RPB = kThreads / LPR;
+    const int sub = threadIdx.x % LPR, grp = threadIdx.x / LPR;
+    for (int base = blockIdx.x * RPB; base < n; base += gridDim.x * RPB) {
+      const int row = base + grp;
+      const bool valid = row < n;
+      const int k0 = valid ? __ldg(rp + row) - 1 : 0, k1 = valid ? __ldg(rp + row + 1) - 1 : 0;
+      TV acc = TV(0);
+#pragma unroll 4
+      for (int k = k0 + sub; k < k1; k += LPR) acc += (TV)__ldg(val + k) * z[__ldg(ci + k) - 1];
+#pragma unroll
+      for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LPR);
+      if (valid && sub == 0) {
+        const TV qv = (fixed && fixed[row]) ? TV(0) : acc * g;
+        q[row] = qv;
+        dot += z[row] * g * qv;
+      }
+    }
+  }
+  const double b = block_sum((double)dot);
+  if (threadIdx.x == 0) red[blockIdx.x] = b;
+  if (last_block(&sc->ticket1)) {
+    const double d = ordered_sum(red, gridDim.x);
+    if (threadIdx.x == 0) {
+      if (!done) {
+        sc->delta = d;
+        if (!isfinite(d)) { sc->bad = 1; sc->done = 1; }
+      }
+      sc->pending = 0;
+      sc->ticket1 = 0;
+    }
+  }
+}
+
+// (B): v_{j+1} (into vold), z_{j+1} = minv v_{j+1}, gamma_{j+1}; last block: rotation.
+template <typename TV>
+__global__ void __launch_bounds__(kThreads)
+minres_lanczos(int n, const TV* __restrict__ q, const TV* __restrict__ vcur, TV* __restrict__ vold,
+               const TV* __restrict__ minv, TV* __restrict__ znew, double* red, MinresScalars* sc) {
+  if (sc->done) return;
+  const TV a = (TV)(sc->delta / sc->gamma), b = (TV)(sc->gamma / sc->gamma_old);
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const TV vn = q[i] - a * vcur[i] - b * vold[i];
+    vold[i] = vn;
+    const TV zn = minv[i] * vn;
+    znew[i] = zn;
+    acc += (double)zn * (double)vn;
+  }
+  const double bs = block_sum(acc);
+  if (threadIdx.x == 0) red[blockIdx.x] = bs;
+  if (last_block(&sc->ticket2)) {
+    const double g2 = ordered_sum(red, gridDim.x);
+    if (threadIdx.x == 0) {
+      const double gn = sqrt(fmax(g2, 0.0)), g = sc->gamma, d = sc->delta;
+      const double a0 = sc->c * d - sc->c_old * sc->s * g;
+      const double a1 = hypot(a0, gn);
+      if (!(g2 >= 0.0) || !isfinite(g2) || !(a1 > 0.0)) {
+        sc->bad = 1;
+        sc->done = 1;
+      } else {
+        const double cn = a0 / a1, sn = gn / a1;
+        sc->a1 = a1;
+        sc->a2 = sc->s * d + sc->c_old * sc->c * g;
+        sc->a3 = sc->s_old * g;
+        sc->ceta = cn * sc->eta;
+        sc->zs_prev = 1.0 / g;
+        sc->eta = -sn * sc->eta;
+        sc->gamma_old = g;
+        sc->gamma = gn;
+        sc->c_old = sc->c;
+        sc->c = cn;
+        sc->s_old = sc->s;
+        sc->s = sn;
+        sc->pending = 1;
+        sc->it += 1;
+        if (fabs(sc->eta) <= sc->tol || gn == 0.0) sc->done = 2;
+      }
+      sc->ticket2 = 0;
+    }
+  }
+}
+
+// Start from the FP64 residual r64 (0 on fixed rows): v_1 = r64, v_0 = 0, z_1 = minv v_1,
+// w = 0, gamma_1 = sqrt(<z_1, v_1>), eta = gamma_1, tol = rtol_m gamma_1; optionally x = 0.
+template <typename TV, typename TX>
+__global__ void __launch_bounds__(kThreads)
+minres_start(int n, const double* __restrict__ r64, const TV* __restrict__ minv, TV* __restrict__ v1,
+             TV* __restrict__ v0, TV* __restrict__ z1, TV* __restrict__ w0, TV* __restrict__ w1, TX* __restrict__ x,
+             bool zero_x, double* red, MinresScalars* sc, double rtol_m) {
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const TV v = (TV)r64[i];
+    const TV z = minv[i] * v;
+    v1[i] = v; v0[i] = TV(0); z1[i] = z; w0[i] = TV(0); w1[i] = TV(0);
+    if (zero_x) x[i] = TX(0);
+    acc += (double)z * (double)v;
+  }
+  const double bs = block_sum(acc);
+  if (threadIdx.x == 0) red[blockIdx.x] = bs;
+  if (last_block(&sc->ticket2)) {
+    const double g2 = ordered_sum(red, gridDim.x);
+    if (threadIdx.x == 0) {
+      const double g = sqrt(fmax(g2, 0.0));
+      sc->gamma = g; sc->gamma_old = 1.0; sc->delta = 0.0;
+      sc->c = sc->c_old = 1.0; sc->s = sc->s_old = 0.0;
+      sc->eta = g; sc->tol = rtol_m * g;
+      sc->pending = 0; sc->it = 0; sc->ticket1 = 0; sc->ticket2 = 0;
+      sc->bad = (!(g2 >= 0.0) || !isfinite(g2)) ? 1 : 0;
+      sc->done = sc->bad ? 1 : (g == 0.0 ? 2 : 0);
+    }
+  }
+}
+
+// Effective preconditioner: the caller's minv (must be > 0 on free rows) or, when NULL,
+// 1/|a_ii| with 1 for a zero diagonal (PETSc's Jacobi convention); 0 on fixed rows.
+__global__ void minres_minv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                            const double* __restrict__ val, const double* __restrict__ user,
+                            const uint8_t* __restrict__ fixed, double* __restrict__ m64, float* __restrict__ m32,
+                            unsigned* err) {
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+    double m = 0.0;
+    if (!(fixed && fixed[row])) {
+      if (user) {
+        m = user[row];
+        if (!(m > 0.0) || !isfinite(m)) { gfe_raise(err, GFE_DEVERR_NONFINITE); m = 0.0; }
+      } else {
+        double d = 0.0;
+        for (int k = rp[row] - 1; k < rp[row + 1] - 1; ++k)
+          if (ci[k] == row + 1) { d = val[k]; break; }
+        m = (d != 0.0 && isfinite(d)) ? 1.0 / fabs(d) : 1.0;
+      }
+    }
+    m64[row] = m;
+    if (m32) m32[row] = (float)m;
+  }
+}
+
+template <typename TM, typename TV, typename TX>
+void launch_minres_spmv(int lpr, int grid, cudaStream_t s, int n, const int32_t* rp, const int32_t* ci,
+                        const TM* val, const TV* z, TV* q, const uint8_t* fixed, const TV* zprev, TV* wold,
+                        const TV* wnew, TX* x, double* red, MinresScalars* sc) {
+#define GFE_MINRES_SPMV(L) \
+  minres_spmv<TM, TV, TX, L><<<grid, kThreads, 0, s>>>(n, rp, ci, val, z, q, fixed, zprev, wold, wnew, x, red, sc)
+  if (lpr == 32) GFE_MINRES_SPMV(32);
+  else if (lpr == 16) GFE_MINRES_SPMV(16);
+  else if (lpr == 8) GFE_MINRES_SPMV(8);
+  else GFE_MINRES_SPMV(1);
+#undef GFE_MINRES_SPMV
+}
+
+// Runs MINRES iterations on started vectors (V[1] = v_1, V[0] = 0, Z[1] = z_1, W = 0).
+template <typename TM, typename TV, typename TX>
+int run_minres(cudaStream_t s, int n, const int32_t* rp, const int32_t* ci, const TM* val, const uint8_t* fixed,
+               const TV* minv, TX* x, TV* const V[2], TV* const Z[2], TV* const W[2], TV* q, double* red,
+               MinresScalars* sc, MinresScalars* sc_host, int lpr, int grid, int max_iters, int chunk) {
+  int j = 1;
+  while (j <= max_iters) {
+    const int k = std::min(chunk, max_iters - j + 1);
+    for (int t = 0; t < k; ++t, ++j) {
+      void* prof = gfe::stage_begin(GFE_STAGE_SPMV, s);
+      launch_minres_spmv<TM, TV, TX>(lpr, grid, s, n, rp, ci, val, Z[j & 1], q, fixed, Z[(j + 1) & 1], W[j & 1],
+                                     W[(j + 1) & 1], x, red, sc);
+      gfe::stage_end(GFE_STAGE_SPMV, prof, s, 1);
+      minres_lanczos<TV><<<grid, kThreads, 0, s>>>(n, q, V[j & 1], V[(j + 1) & 1], minv, Z[(j + 1) & 1], red, sc);
+    }
+    GFE_CUDA_TRY(cudaGetLastError());
+    GFE_CUDA_TRY(cudaMemcpyAsync(sc_host, sc, sizeof(MinresScalars), cudaMemcpyDeviceToHost, s));
+    GFE_CUDA_TRY(cudaStreamSynchronize(s));
+    if (sc_host->done) break;
+  }
+  // the update of the last completed iteration is deferred to the next (A) launch: flush it
+  launch_minres_spmv<TM, TV, TX>(lpr, grid, s, n, rp, ci, val, Z[j & 1], q, fixed, Z[(j + 1) & 1], W[j & 1],
+                                 W[(j + 1) & 1], x, red, sc);
+  GFE_CUDA_TRY(cudaGetLastError());
+  return GFE_OK;
+}
+
+// lanes per row of the MINRES SpMV: long rows (the u-p tangent has ~200 entries a row) use 8 lanes
+// in FP64, so the shuffle reduction adds little to the FP64-pipe work, and a full warp in FP32
+int minres_lpr(double avg, bool fp64) {
+  if (fp64) return avg >= 64 ? 8 : 1;
+  return avg >= 96 ? 32 : (avg >= 48 ? 16 : 8);
+}
+
+}  // namespace
+
+extern "C" int gfe_minres_solve(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const double* values,
+                                const float* values32, const double* minv, const double* f, const uint8_t* fixed,
+                                double* x, double rtol, int32_t max_iters, int32_t precision, int32_t* iters_host,
+                                double* rel_host, void* stream) {
+  using namespace gfe;
+  const char* fn = "gfe_minres_solve";
+  if (n <= 0 || !row_ptr || !col_idx || !values || !x || !(rtol > 0.0) || max_iters <= 0)
+    return set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (precision != GFE_FP64 && precision != GFE_MIXED) return set_error(GFE_ERR_ARG, "%s: unknown precision", fn);
+  if (precision == GFE_MIXED && !values32)
+    return set_error(GFE_ERR_ARG, "%s: mixed precision needs the FP32 copy of the matrix", fn);
+  cudaStream_t s = as_stream(stream);
+  unsigned* err = device_error_word();
+  int32_t nnz1 = 0;
+  GFE_CUDA_TRY(cudaMemcpyAsync(&nnz1, row_ptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  GFE_CUDA_TRY(cudaStreamSynchronize(s));
+  const bool fp64 = precision == GFE_FP64;
+  const int lpr = minres_lpr((double)(nnz1 - 1) / n, fp64);
+  const int grid = 8 * sm_count();
+  const int chunk = 50;
+  const size_t nb = (size_t)n, vbytes = fp64 ? sizeof(double) : sizeof(float);
+  // pieces: m64, m32, r64, eight vectors of the working type (V0 V1 Z0 Z1 W0 W1 q d), the block
+  // partials, the MINRES scalars, a Scalars block for the norm kernel and the norm result
+  const int pieces = 15;
+  const size_t bytes = nb * sizeof(double) * 2 + nb * sizeof(float) + nb * vbytes * 8 + sizeof(double) * grid +
+                       sizeof(MinresScalars) + sizeof(Scalars) + sizeof(double) + (pieces + 1) * 256;
+  char* buf = nullptr;
+  int rc = scratch_alloc((void**)&buf, bytes, s, "MINRES vectors");
+  if (rc) return rc;
+  char* base = buf;
+  auto carve = [&](size_t b) {
+    char* p = buf;
+    buf += (b + 255) & ~size_t(255);
+    return p;
+  };
+  double* m64 = (double*)carve(nb * sizeof(double));
+  float* m32 = (float*)carve(nb * sizeof(float));
+  double* r64 = (double*)carve(nb * sizeof(double));
+  void* vec[8];
+  for (int i = 0; i < 8; ++i) vec[i] = carve(nb * vbytes);
+  double* red = (double*)carve(sizeof(double) * grid);
+  MinresScalars* sc = (MinresScalars*)carve(sizeof(MinresScalars));
+  Scalars* nsc = (Scalars*)carve(sizeof(Scalars));
+  double* r2dev = (double*)carve(sizeof(double));
+  MinresScalars sh{};
+  double b2 = 0.0, r2 = 0.0;
+  int total_it = 0;
+  // r64 = f - A x on free rows and r2 = ||r64||^2
+  auto true_residual = [&]() -> int {
+    cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
+    norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, nsc, r2dev);
+    GFE_CUDA_TRY(cudaMemcpyAsync(&r2, r2dev, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GFE_CUDA_TRY(cudaStreamSynchronize(s));
+    return GFE_OK;
+  };
+  GFE_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(MinresScalars), s));
+  GFE_CUDA_TRY(cudaMemsetAsync(nsc, 0, sizeof(Scalars), s));
+  minres_minv<<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, minv, fixed, m64, fp64 ? nullptr : m32, err);
+  set_dirichlet<<<grid, kThreads, 0, s>>>(n, x, fixed, true);
+  rc = true_residual();
+  if (rc) { scratch_free(base, s); return rc; }
+  b2 = r2;
+  if (b2 == 0.0) {
+    if (iters_host) *iters_host = 0;
+    if (rel_host) *rel_host = 0.0;
+    scratch_free(base, s);
+    return GFE_OK;
+  }
+  if (fp64) {
+    double* V[2] = {(double*)vec[0], (double*)vec[1]};
+    double* Z[2] = {(double*)vec[2], (double*)vec[3]};
+    double* W[2] = {(double*)vec[4], (double*)vec[5]};
+    double* q = (double*)vec[6];
+    // MINRES minimises the M^-1-norm of the residual while the target is on the 2-norm: each round
+    // aims at half of the remaining factor and restarts from the true residual while that is above
+    // the target
+    for (int round = 0; round < 6 && rc == GFE_OK; ++round) {
+      minres_start<double, double><<<grid, kThreads, 0, s>>>(n, r64, m64, V[1], V[0], Z[1], W[0], W[1], x, false, red,
+                                                             sc, 0.5 * rtol * std::sqrt(b2 / r2));
+      rc = run_minres<double, double, double>(s, n, row_ptr, col_idx, values, fixed, m64, x, V, Z, W, q, red, sc, &sh,
+                                              lpr, grid, max_iters - total_it, chunk);
+      total_it += sh.it;
+      if (rc) break;
+      rc = true_residual();
+      if (rc || sh.bad || r2 <= rtol * rtol * b2 || r2 == 0.0 || total_it >= max_iters) break;
+    }
+  } else {
+    // iterative refinement: FP64 residual outside, FP32 MINRES on the FP32 matrix for the correction
+    float* V[2] = {(float*)vec[0], (float*)vec[1]};
+    float* Z[2] = {(float*)vec[2], (float*)vec[3]};
+    float* W[2] = {(float*)vec[4], (float*)vec[5]};
+    float* q = (float*)vec[6];
+    float* d = (float*)vec[7];
+    for (int outer = 0; outer < 64 && rc == GFE_OK; ++outer) {
+      // the reduction still needed, halved, but no tighter than FP32 MINRES reliably reaches
+      const double inner_rtol = std::max(0.5 * rtol * std::sqrt(b2 / r2), 2e-5);
+      minres_start<float, float><<<grid, kThreads, 0, s>>>(n, r64, m32, V[1], V[0], Z[1], W[0], W[1], d, true, red, sc,
+                                                           inner_rtol);
+      rc = run_minres<float, float, float>(s, n, row_ptr, col_idx, values32, fixed, m32, d, V, Z, W, q, red, sc, &sh,
+                                           lpr, grid, max_iters - total_it, chunk);
+      total_it += sh.it;
+      if (rc) break;
+      add_correction<<<grid, kThreads, 0, s>>>(n, x, d, fixed);
+      rc = true_residual();
+      if (rc || sh.bad || r2 <= rtol * rtol * b2 || total_it >= max_iters) break;
+    }
+  }
+  cudaError_t e = cudaStreamSynchronize(s);
+  scratch_free(base, s);
+  if (rc) return rc;
+  if (e != cudaSuccess) return set_error(GFE_ERR_CUDA, "%s: %s", fn, cudaGetErrorString(e));
+  const double rel = std::sqrt(r2 / b2);
+  if (iters_host) *iters_host = total_it;
+  if (rel_host) *rel_host = rel;
+  if (sh.bad)
+    return set_error(GFE_ERR_NUMERIC, "%s: breakdown (indefinite preconditioner, singular system or non-finite value)",
+                     fn);
+  if (!(rel <= rtol))
+    return set_error(GFE_ERR_NOCONV, "%s: relative residual %.3e above %.3e after %d iterations", fn, rel, rtol,
+                     total_it);
+  return GFE_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Restarted GMRES for non-symmetric systems
+// ---------------------------------------------------------------------------------------------
+// Iron's default linear solver inside Newton is PETSc GMRES with restart 30 and classical
+// Gram-Schmidt without refinement (src/solver_routines.F90:11320-11369); Iron's analytic Jacobian
+// of the mixed u-p Mooney-Rivlin element is not symmetric (its u-p and p-u blocks differ), so it
+// needs a non-symmetric Krylov method.  GMRES(m) with right preconditioning by a diagonal M^-1:
+// the Hessenberg residual estimate |g_{j+1}| is the true residual norm, every cycle starts from
+// the FP64 residual b - A x formed with the FP64 matrix, and the correction M^-1 V y is added to x
+// in FP64.  With precision GFE_MIXED the Krylov basis and the matrix of the cycle are FP32, which
+// makes each restart an FP64 iterative-refinement step.
+//
+// One iteration is three kernels, all reading the column index j from device memory so the host
+// launches whole cycles without synchronising: (1) w = s A M^-1 v_j (s = 1 / ||v_j|| pending);
+// (2) normalise v_j in place and h_kj = <w, v_k>, k <= j (a 2-D grid, one column k per blockIdx.y);
+// (3) w -= sum_k h_kj v_k into v_{j+1}, ||w|| and, in the last block, the Givens rotations and the
+// convergence / end-of-cycle flags.  At the end of a cycle one thread solves H y = g and a kernel
+// adds M^-1 V y to x.
+namespace {
+
+constexpr int kGmresMaxRestart = 64;
+
+struct GmresScalars {
+  double H[(kGmresMaxRestart + 1) * kGmresMaxRestart];  // column-major, leading dimension m + 1
+  double cs[kGmresMaxRestart], sn[kGmresMaxRestart], g[kGmresMaxRestart + 1], y[kGmresMaxRestart];
+  double vscale, tol;
+  int j, cols, done, bad, it, ticket1, ticket2;
+};
+
+template <typename TM, typename TV, int LPR>
+__global__ void __launch_bounds__(kThreads)
+gmres_spmv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, const TM* __restrict__ val,
+           const TV* __restrict__ minv, const TV* __restrict__ V, size_t ldv, TV* __restrict__ w,
+           const uint8_t* __restrict__ fixed, GmresScalars* sc) {
+  if (sc->done) return;
+  const TV* __restrict__ v = V + (size_t)sc->j * ldv;
+  const TV s = (TV)sc->vscale;
+  constexpr int RPB = kThreads / LPR;
+  const int sub = threadIdx.x % LPR, grp = threadIdx.x / LPR;
+  for (int base = blockIdx.x * RPB; base < n; base += gridDim.x * RPB) {
+    const int row = base + grp;
+    const bool valid = row < n;
+    const int k0 = valid ? __ldg(rp + row) - 1 : 0, k1 = valid ? __ldg(rp + row + 1) - 1 : 0;
+    TV acc = TV(0);
+#pragma unroll 4
+    for (int k = k0 + sub; k < k1; k += LPR) {
+      const int c = __ldg(ci + k) - 1;
+      acc += (TV)__ldg(val + k) * (minv[c] * v[c]);
+    }
+#pragma unroll
+    for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LPR);
+    if (valid && sub == 0) w[row] = (fixed && fixed[row]) ? TV(0) : acc * s;
+  }
+}
+
+// blockIdx.y = k: partial <w, v_k> for k <= j; the k == j blocks normalise v_j first.
+template <typename TV>
+__global__ void __launch_bounds__(kThreads)
+gmres_dots(int n, TV* __restrict__ V, size_t ldv, const TV* __restrict__ w, double* red, GmresScalars* sc) {
+  if (sc->done) return;
+  const int j = sc->j, k = blockIdx.y;
+  if (k > j) return;
+  TV* __restrict__ v = V + (size_t)k * ldv;
+  double acc = 0.0;
+  if (k == j) {
+    const TV s = (TV)sc->vscale;
+    for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+      const TV vi = v[i] * s;
+      v[i] = vi;
+      acc += (double)vi * (double)w[i];
+    }
+  } else {
+    for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads)
+      acc += (double)v[i] * (double)w[i];
+  }
+  const double b = block_sum(acc);
+  if (threadIdx.x == 0) red[(size_t)k * gridDim.x + blockIdx.x] = b;
+  // ticket over the (j + 1) * gridDim.x active blocks
+  __shared__ bool amlast;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const int t = atomicAdd(&sc->ticket1, 1);
+    amlast = (t == (j + 1) * (int)gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!amlast) return;
+  const int ldh = kGmresMaxRestart + 1;
+  for (int kk = 0; kk <= j; ++kk) {
+    const double h = ordered_sum(red + (size_t)kk * gridDim.x, gridDim.x);
+    if (threadIdx.x == 0) sc->H[(size_t)j * ldh + kk] = h;
+  }
+  if (threadIdx.x == 0) sc->ticket1 = 0;
+}
+
+// w -= sum_{k<=j} h_kj v_k, stored into v_{j+1}; ||w||^2; last block: rotations and flags.
+template <typename TV>
+__global__ void __launch_bounds__(kThreads)
+gmres_orth(int n, TV* __restrict__ V, size_t ldv, const TV* __restrict__ w, double* red, GmresScalars* sc, int m) {
+  if (sc->done) return;
+  const int j = sc->j;
+  const int ldh = kGmresMaxRestart + 1;
+  __shared__ TV hs[kGmresMaxRestart + 1];
+  for (int k = threadIdx.x; k <= j; k += kThreads) hs[k] = (TV)sc->H[(size_t)j * ldh + k];
+  __syncthreads();
+  TV* __restrict__ vn = V + (size_t)(j + 1) * ldv;
+  double acc = 0.0;
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    TV wi = w[i];
+    for (int k = 0; k <= j; ++k) wi -= hs[k] * V[(size_t)k * ldv + i];
+    vn[i] = wi;
+    acc += (double)wi * (double)wi;
+  }
+  const double b = block_sum(acc);
+  if (threadIdx.x == 0) red[blockIdx.x] = b;
+  if (last_block(&sc->ticket2)) {
+    const double hn2 = ordered_sum(red, gridDim.x);
+    if (threadIdx.x == 0) {
+      double* h = sc->H + (size_t)j * ldh;
+      const double hn = sqrt(fmax(hn2, 0.0));
+      h[j + 1] = hn;
+      for (int k = 0; k < j; ++k) {
+        const double t = sc->cs[k] * h[k] + sc->sn[k] * h[k + 1];
+        h[k + 1] = -sc->sn[k] * h[k] + sc->cs[k] * h[k + 1];
+        h[k] = t;
+      }
+      const double den = hypot(h[j], h[j + 1]);
+      if (!isfinite(hn2) || !(den > 0.0)) {
+        sc->bad = 1;
+        sc->done = 1;
+      } else {
+        sc->cs[j] = h[j] / den;
+        sc->sn[j] = h[j + 1] / den;
+        h[j] = den;
+        h[j + 1] = 0.0;
+        sc->g[j + 1] = -sc->sn[j] * sc->g[j];
+        sc->g[j] = sc->cs[j] * sc->g[j];
+        sc->cols = j + 1;
+        sc->it += 1;
+        sc->vscale = hn > 0.0 ? 1.0 / hn : 0.0;
+        if (fabs(sc->g[j + 1]) <= sc->tol || hn == 0.0) sc->done = 2;
+        else if (j + 1 == m) sc->done = 3;
+        sc->j = j + 1;
+      }
+      sc->ticket2 = 0;
+    }
+  }
+}
+
+// back substitution H y = g on the cols x cols upper triangle (one thread)
+__global__ void gmres_solve_y(GmresScalars* sc) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int c = sc->cols, ldh = kGmresMaxRestart + 1;
+  for (int r = c - 1; r >= 0; --r) {
+    double s = sc->g[r];
+    for (int k = r + 1; k < c; ++k) s -= sc->H[(size_t)k * ldh + r] * sc->y[k];
+    sc->y[r] = s / sc->H[(size_t)r * ldh + r];
+  }
+}
+
+template <typename TV>
+__global__ void __launch_bounds__(kThreads)
+gmres_update_x(int n, const TV* __restrict__ V, size_t ldv, const TV* __restrict__ minv, double* __restrict__ x,
+               const GmresScalars* sc) {
+  __shared__ double ys[kGmresMaxRestart];
+  const int c = sc->cols;
+  for (int k = threadIdx.x; k < c; k += kThreads) ys[k] = sc->y[k];
+  __syncthreads();
+  for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    double s = 0.0;
+    for (int k = 0; k < c; ++k) s += ys[k] * (double)V[(size_t)k * ldv + i];
+    x[i] += (double)minv[i] * s;
+  }
+}
+
+// cycle start: v_0 = r64 (raw; its norm is applied by the first dots kernel), g = beta e_1
+template <typename TV>
+__global__ void gmres_start(int n, const double* __restrict__ r64, TV* __restrict__ v0, GmresScalars* sc,
+                            double beta, double tol) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v0[i] = (TV)r64[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    for (int k = 0; k <= kGmresMaxRestart; ++k) sc->g[k] = 0.0;
+    sc->g[0] = beta;
+    sc->vscale = 1.0 / beta;
+    sc->tol = tol;
+    sc->j = 0; sc->cols = 0; sc->done = 0; sc->bad = 0; sc->it = 0; sc->ticket1 = 0; sc->ticket2 = 0;
+  }
+}
+
+template <typename TM, typename TV>
+void launch_gmres_spmv(int lpr, int grid, cudaStream_t s, int n, const int32_t* rp, const int32_t* ci, const TM* val,
+                       const TV* minv, const TV* V, size_t ldv, TV* w, const uint8_t* fixed, GmresScalars* sc) {
+#define GFE_GMRES_SPMV(L) gmres_spmv<TM, TV, L><<<grid, kThreads, 0, s>>>(n, rp, ci, val, minv, V, ldv, w, fixed, sc)
+  if (lpr == 32) GFE_GMRES_SPMV(32);
+  else if (lpr == 16) GFE_GMRES_SPMV(16);
+  else if (lpr == 8) GFE_GMRES_SPMV(8);
+  else GFE_GMRES_SPMV(1);
+#undef GFE_GMRES_SPMV
+}
+
+// one GMRES cycle of at most m iterations from r64 (||r64|| = beta); adds the correction to x
+template <typename TM, typename TV>
+int gmres_cycle(cudaStream_t s, int n, const int32_t* rp, const int32_t* ci, const TM* val, const uint8_t* fixed,
+                const TV* minv, double* x, const double* r64, double beta, double tol_abs, TV* V, size_t ldv, TV* w,
+                double* red, GmresScalars* sc, int* it_host, int* flag_host, int lpr, int grid, int m) {
+  gmres_start<TV><<<grid, kThreads, 0, s>>>(n, r64, V, sc, beta, tol_abs);
+  for (int t = 0; t < m; ++t) {
+    void* prof = gfe::stage_begin(GFE_STAGE_SPMV, s);
+    launch_gmres_spmv<TM, TV>(lpr, grid, s, n, rp, ci, val, minv, V, ldv, w, fixed, sc);
+    gfe::stage_end(GFE_STAGE_SPMV, prof, s, 1);
+    gmres_dots<TV><<<dim3(grid, t + 1), kThreads, 0, s>>>(n, V, ldv, w, red, sc);
+    gmres_orth<TV><<<grid, kThreads, 0, s>>>(n, V, ldv, w, red, sc, m);
+  }
+  gmres_solve_y<<<1, 32, 0, s>>>(sc);
+  gmres_update_x<TV><<<grid, kThreads, 0, s>>>(n, V, ldv, minv, x, sc);
+  GFE_CUDA_TRY(cudaGetLastError());
+  int hv[2];
+  GFE_CUDA_TRY(cudaMemcpyAsync(hv, &sc->done, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+  int itv = 0;
+  GFE_CUDA_TRY(cudaMemcpyAsync(&itv, &sc->it, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GFE_CUDA_TRY(cudaStreamSynchronize(s));
+  *flag_host = hv[1] ? -1 : hv[0];
+  *it_host = itv;
+  return GFE_OK;
+}
+
+}  // namespace
+
+extern "C" int gfe_gmres_solve(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const double* values,
+                               const float* values32, const double* minv, const double* f, const uint8_t* fixed,
+                               double* x, double rtol, int32_t max_iters, int32_t restart, int32_t precision,
+                               int32_t* iters_host, double* rel_host, void* stream) {
+  using namespace gfe;
+  const char* fn = "gfe_gmres_solve";
+  if (n <= 0 || !row_ptr || !col_idx || !values || !x || !(rtol > 0.0) || max_iters <= 0)
+    return set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (restart < 1 || restart > kGmresMaxRestart)
+    return set_error(GFE_ERR_ARG, "%s: restart %d outside 1..%d", fn, restart, kGmresMaxRestart);
+  if (precision != GFE_FP64 && precision != GFE_MIXED) return set_error(GFE_ERR_ARG, "%s: unknown precision", fn);
+  if (precision == GFE_MIXED && !values32)
+    return set_error(GFE_ERR_ARG, "%s: mixed precision needs the FP32 copy of the matrix", fn);
+  cudaStream_t s = as_stream(stream);
+  unsigned* err = device_error_word();
+  int32_t nnz1 = 0;
+  GFE_CUDA_TRY(cudaMemcpyAsync(&nnz1, row_ptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  GFE_CUDA_TRY(cudaStreamSynchronize(s));
+  const bool fp64 = precision == GFE_FP64;
+  const int lpr = minres_lpr((double)(nnz1 - 1) / n, fp64);
+  const int grid = 2 * sm_count();
+  const int m = restart;
+  const size_t nb = (size_t)n, vbytes = fp64 ? sizeof(double) : sizeof(float);
+  const size_t ldv = (nb + 63) & ~size_t(63);
+  // pieces: m64, m32, r64, basis (m + 1 columns), w, partials (m + 1 columns of grid), scalars,
+  // norm-kernel scalars, norm result
+  const int pieces = 9;
+  const size_t bytes = nb * sizeof(double) * 2 + nb * sizeof(float) + ldv * vbytes * (m + 1) + nb * vbytes +
+                       sizeof(double) * grid * (m + 1) + sizeof(GmresScalars) + sizeof(Scalars) + sizeof(double) +
+                       (pieces + 1) * 256;
+  char* buf = nullptr;
+  int rc = scratch_alloc((void**)&buf, bytes, s, "GMRES vectors");
+  if (rc) return rc;
+  char* base = buf;
+  auto carve = [&](size_t b) {
+    char* p = buf;
+    buf += (b + 255) & ~size_t(255);
+    return p;
+  };
+  double* m64 = (double*)carve(nb * sizeof(double));
+  float* m32 = (float*)carve(nb * sizeof(float));
+  double* r64 = (double*)carve(nb * sizeof(double));
+  void* Vb = carve(ldv * vbytes * (m + 1));
+  void* wb = carve(nb * vbytes);
+  double* red = (double*)carve(sizeof(double) * grid * (m + 1));
+  GmresScalars* sc = (GmresScalars*)carve(sizeof(GmresScalars));
+  Scalars* nsc = (Scalars*)carve(sizeof(Scalars));
+  double* r2dev = (double*)carve(sizeof(double));
+  double b2 = 0.0, r2 = 0.0;
+  int total_it = 0, flag = 0, bad = 0;
+  auto true_residual = [&]() -> int {
+    cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
+    norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, nsc, r2dev);
+    GFE_CUDA_TRY(cudaMemcpyAsync(&r2, r2dev, sizeof(double), cudaMemcpyDeviceToHost, s));
+    GFE_CUDA_TRY(cudaStreamSynchronize(s));
+    return GFE_OK;
+  };
+  GFE_CUDA_TRY(cudaMemsetAsync(sc, 0, sizeof(GmresScalars), s));
+  GFE_CUDA_TRY(cudaMemsetAsync(nsc, 0, sizeof(Scalars), s));
+  minres_minv<<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, minv, fixed, m64, fp64 ? nullptr : m32, err);
+  set_dirichlet<<<grid, kThreads, 0, s>>>(n, x, fixed, true);
+  rc = true_residual();
+  if (rc) { scratch_free(base, s); return rc; }
+  b2 = r2;
+  if (b2 == 0.0) {
+    if (iters_host) *iters_host = 0;
+    if (rel_host) *rel_host = 0.0;
+    scratch_free(base, s);
+    return GFE_OK;
+  }
+  const double target2 = rtol * rtol * b2;
+  while (total_it < max_iters && rc == GFE_OK) {
+    const double beta = std::sqrt(r2);
+    // aim each cycle at half the target so the true residual (which the FP64 check below
+    // measures) lands under it despite rounding in the recurrence
+    const double tol_abs = 0.5 * rtol * std::sqrt(b2);
+    const int mm = std::min(m, max_iters - total_it);
+    int it = 0;
+    if (fp64)
+      rc = gmres_cycle<double, double>(s, n, row_ptr, col_idx, values, fixed, m64, x, r64, beta, tol_abs, (double*)Vb,
+                                       ldv, (double*)wb, red, sc, &it, &flag, lpr, grid, mm);
+    else
+      rc = gmres_cycle<float, float>(s, n, row_ptr, col_idx, values32, fixed, m32, x, r64, beta, tol_abs, (float*)Vb,
+                                     ldv, (float*)wb, red, sc, &it, &flag, lpr, grid, mm);
+    total_it += it;
+    if (rc) break;
+    if (flag < 0) { bad = 1; break; }
+    rc = true_residual();
+    if (rc || r2 <= target2) break;
+    if (!isfinite(r2)) { bad = 1; break; }
+  }
+  cudaError_t e = cudaStreamSynchronize(s);
+  scratch_free(base, s);
+  if (rc) return rc;
+  if (e != cudaSuccess) return set_error(GFE_ERR_CUDA, "%s: %s", fn, cudaGetErrorString(e));
+  const double rel = std::sqrt(r2 / b2);
+  if (iters_host) *iters_host = total_it;
+  if (rel_host) *rel_host = rel;
+  if (bad) return set_error(GFE_ERR_NUMERIC, "%s: breakdown (zero Hessenberg diagonal or non-finite value)", fn);
+  if (!(rel <= rtol))
+    return set_error(GFE_ERR_NOCONV, "%s: relative residual %.3e above %.3e after %d iterations", fn, rel, rtol,
+                     total_it);
+  return GFE_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Diagonal preconditioner for the u-p saddle-point matrix [K_uu B^T; B 0]
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+// u rows (row < n_u): 1/|K_ii| (1 when K_ii = 0); fixed rows 0
+__global__ void saddle_minv_u(int n_u, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                              const double* __restrict__ val, const uint8_t* __restrict__ fixed,
+                              double* __restrict__ minv) {
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n_u; row += gridDim.x * blockDim.x) {
+    double d = 0.0;
+    for (int k = rp[row] - 1; k < rp[row + 1] - 1; ++k)
+      if (ci[k] == row + 1) { d = val[k]; break; }
+    minv[row] = (fixed && fixed[row]) ? 0.0 : ((d != 0.0 && isfinite(d)) ? 1.0 / fabs(d) : 1.0);
+  }
+}
+
+// p rows (row >= n_u), one warp each: 1 / sum_{free j < n_u} B_pj^2 / |K_jj| (the diagonal of the
+// Schur complement B diag(K_uu)^-1 B^T); 1 when that sum is 0; fixed rows 0.  minv of the u rows
+// must already be set (it is |K_jj|^-1 there, 0 on fixed u rows).
+__global__ void saddle_minv_p(int n, int n_u, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                              const double* __restrict__ val, const uint8_t* __restrict__ fixed,
+                              double* __restrict__ minv) {
+  const int lane = threadIdx.x & 31;
+  for (int row = n_u + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); row < n;
+       row += (gridDim.x * blockDim.x) >> 5) {
+    const int k0 = rp[row] - 1, k1 = rp[row + 1] - 1;
+    double s = 0.0;
+    for (int k = k0 + lane; k < k1; k += 32) {
+      const int j = ci[k] - 1;
+      if (j < n_u) s += val[k] * val[k] * minv[j];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) minv[row] = (fixed && fixed[row]) ? 0.0 : ((s > 0.0 && isfinite(s)) ? 1.0 / s : 1.0);
+  }
+}
+
+}  // namespace
+
+extern "C" int gfe_saddle_preconditioner(int32_t n, int32_t n_u, const int32_t* row_ptr, const int32_t* col_idx,
+                                         const double* values, const uint8_t* fixed, double* minv, void* stream) {
+  using namespace gfe;
+  if (n <= 0 || n_u < 0 || n_u > n || !row_ptr || !col_idx || !values || !minv)
+    return set_error(GFE_ERR_ARG, "gfe_saddle_preconditioner: invalid arguments");
+  cudaStream_t s = as_stream(stream);
+  const int grid = 4 * sm_count();
+  if (n_u > 0) saddle_minv_u<<<grid, kThreads, 0, s>>>(n_u, row_ptr, col_idx, values, fixed, minv);
+  if (n > n_u) saddle_minv_p<<<grid, kThreads, 0, s>>>(n, n_u, row_ptr, col_idx, values, fixed, minv);
+  GFE_LAUNCH_CHECK("gfe_saddle_preconditioner");
   return GFE_OK;
 }
 
