@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--path", default="auto", choices=["auto", "regular", "general"],
                     help="assembly kernel: regular-mesh tiled kernel (auto for generated meshes) or colour scatter")
     ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=2000, help="serve workload: requests in the stream")
+    ap.add_argument("--serve-workers", type=int, default=8, help="serve workload: concurrent request slots")
     ap.add_argument("--cpu-sample-n", type=int, default=96, help="side of the CPU-baseline sample mesh")
     return ap.parse_args()
 

@@ -56,6 +56,13 @@ int gfe_last_error(char* buf, int len);
 /* Read and clear the device error word (bit set of GFE_DEVERR_* raised by kernels). */
 int gfe_device_errors(uint32_t* bits_host, void* stream);
 
+/* Route this host thread's kernels to the caller's device error word (a zeroed uint32 in device
+ * memory), or back to the library's per-device word with NULL.  A host that runs independent work
+ * from several threads (a serving loop) gives each thread its own word, so that one request's
+ * errors are neither reported for nor cleared by another.  Kernels captured into a CUDA graph keep
+ * the word that was current at capture. */
+int gfe_set_thread_error_word(uint32_t* dev_word);
+
 #define GFE_DEVERR_SLOT 1u     /* CSR slot not found during a scatter */
 #define GFE_DEVERR_JACOBIAN 2u /* non-positive Jacobian / det(F) at a Gauss point */
 #define GFE_DEVERR_NONFINITE 4u
@@ -130,6 +137,15 @@ int gfe_laplace_assemble(int32_t n_elem, int32_t n_nodes, const int32_t* elem_no
 int gfe_laplace_assemble_regular(int32_t nx, int32_t ny, int32_t nz, const double* coords, const double* kappa,
                                  const int32_t* row_ptr, double* values, float* values32, double* rhs,
                                  int32_t precision, void* stream);
+
+/* The same assembly with a caller-owned device workspace (16-byte aligned) of
+ * gfe_laplace_regular_workspace_bytes(nx, ny, nz, precision) bytes for the converted coordinates,
+ * so that nothing is allocated: the form to capture into a CUDA graph.  workspace may be NULL
+ * (then it is allocated on `stream`, as gfe_laplace_assemble_regular does). */
+int64_t gfe_laplace_regular_workspace_bytes(int32_t nx, int32_t ny, int32_t nz, int32_t precision);
+int gfe_laplace_assemble_regular_ws(int32_t nx, int32_t ny, int32_t nz, const double* coords, const double* kappa,
+                                    const int32_t* row_ptr, double* values, float* values32, double* rhs,
+                                    int32_t precision, void* workspace, void* stream);
 
 /* Number of CSR rows/entries that differ from the clipped 27-point stencil of the regular mesh
  * (0 = the structure is the one gfe_laplace_assemble_regular writes).  Synchronises `stream`. */
@@ -231,15 +247,41 @@ int gfe_cg_solve_noalloc(int32_t n, const int32_t* row_ptr, const int32_t* col_i
                          const double* f, const uint8_t* fixed, double* x, double rtol, int32_t max_iters,
                          int32_t* iters_host, double* rel_host, void* stream);
 
+/* Graph-capturable FP64 Jacobi-CG (the solve of gfe_cg_solve split into enqueue-only steps, for a
+ * serving loop that captures its launches into CUDA graphs).  The caller allocates a 256-byte
+ * aligned device workspace of gfe_cg_workspace_bytes(n) bytes per concurrent solve.
+ *  gfe_cg_begin   Jacobi inverse, x0 (Dirichlet values, zeros elsewhere), r0 = f - K x0 and the
+ *                 first direction; converged when ||r_k||^2 <= rtol^2 ||r_0||^2 (recurrence residual)
+ *  gfe_cg_steps   `steps` CG iterations; iterations after convergence or breakdown do nothing
+ *  gfe_cg_status  copies the state to state_host (pinned memory when captured); the copy is
+ *                 complete when `stream` reaches this point
+ * None of them allocates or synchronises. */
+typedef struct gfe_cg_state {
+  double rr;          /* ||r_k||^2 */
+  double rr0;         /* ||r_0||^2 */
+  int32_t done;       /* 0 running, 2 converged, 1 breakdown */
+  int32_t iterations;
+  int32_t breakdown;
+  int32_t reserved;
+} gfe_cg_state;
+int64_t gfe_cg_workspace_bytes(int32_t n);
+int gfe_cg_begin(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const double* values, const double* f,
+                 const uint8_t* fixed, double* x, double rtol, void* workspace, void* stream);
+int gfe_cg_steps(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const double* values,
+                 const uint8_t* fixed, double* x, int32_t steps, void* workspace, void* stream);
+int gfe_cg_status(int32_t n, void* workspace, gfe_cg_state* state_host, void* stream);
+
 /* Solve K x = f for symmetric (possibly indefinite) K with Dirichlet conditions, by preconditioned
  * MINRES: the linear solve of the Newton step for the mixed u-p Jacobian, whose p-p block is zero.
  * Replaces the PETSc KSP solve Iron runs inside its Newton solver (GMRES + Jacobi by default,
  * src/solver_routines.F90:11320-11369; SNES linear solve call in src/solver_routines.F90:18942-18991).
  *  minv       [n] inverse of a symmetric positive definite diagonal preconditioner (> 0 on free
  *             rows), or NULL for 1/|K_ii| with 1 where K_ii = 0
- *  rtol       relative 2-norm residual target ||f - K x|| / ||f - K x0||, x0 = Dirichlet values
- *             with zeros elsewhere; the other arguments as gfe_cg_solve (GFE_MIXED: FP64-residual
- *             refinement around FP32 MINRES on values32).
+ *  rtol       relative residual target in the preconditioner's norm, ||f - K x||_{M^-1} /
+ *             ||f - K x0||_{M^-1} with ||r||_{M^-1}^2 = sum_i minv_i r_i^2 (the norm MINRES
+ *             minimises, PETSc's default for KSPMINRES), x0 = Dirichlet values with zeros
+ *             elsewhere; rel_host returns that ratio for the final FP64 residual.  Other arguments
+ *             as gfe_cg_solve (GFE_MIXED: FP64-residual refinement around FP32 MINRES on values32).
  * Synchronises `stream`.  Allocates and frees its scratch on `stream`. */
 int gfe_minres_solve(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const double* values,
                      const float* values32, const double* minv, const double* f, const uint8_t* fixed, double* x,

@@ -50,6 +50,7 @@ SIGNATURES = {
     "gfe_version": (C.c_int, []),
     "gfe_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "gfe_device_errors": (C.c_int, [C.POINTER(C.c_uint32), vp]),
+    "gfe_set_thread_error_word": (C.c_int, [vp]),
     "gfe_profile_enable": (C.c_int, [C.c_int]),
     "gfe_profile_read": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int]),
     "gfe_probe_fma_rate": (C.c_int, [i32, C.POINTER(C.c_double), vp]),
@@ -57,6 +58,8 @@ SIGNATURES = {
     "gfe_laplace_assemble": (C.c_int, [i32, i32, vp, vp, vp, vp, vp, i32, vp, vp, i64, vp, vp, vp, i32, vp]),
     "gfe_laplace_element_matrices": (C.c_int, [i32, i32, vp, vp, vp, vp, i32, vp]),
     "gfe_laplace_assemble_regular": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp]),
+    "gfe_laplace_regular_workspace_bytes": (C.c_int64, [i32, i32, i32, i32]),
+    "gfe_laplace_assemble_regular_ws": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp, vp]),
     "gfe_laplace_regular_check": (C.c_int, [i32, i32, i32, vp, vp, C.POINTER(C.c_int64), vp]),
     "gfe_csr_spmv": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "gfe_mr_residual": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp]),
@@ -68,11 +71,15 @@ SIGNATURES = {
                                C.POINTER(C.c_double), vp]),
     "gfe_cg_solve_noalloc": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, f64, i32, C.POINTER(C.c_int32),
                                        C.POINTER(C.c_double), vp]),
+    "gfe_cg_workspace_bytes": (C.c_int64, [i32]),
+    "gfe_cg_begin": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, f64, vp, vp]),
+    "gfe_cg_steps": (C.c_int, [i32, vp, vp, vp, vp, vp, i32, vp, vp]),
+    "gfe_cg_status": (C.c_int, [i32, vp, vp, vp]),
     "gfe_minres_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(C.c_int32),
                                    C.POINTER(C.c_double), vp]),
     "gfe_gmres_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, vp, f64, i32, i32, i32, C.POINTER(C.c_int32),
                                   C.POINTER(C.c_double), vp]),
-    "gfe_saddle_preconditioner":(C.c_int, [i32, i32, vp, vp, vp, vp, vp, vp]),
+    "gfe_saddle_preconditioner": (C.c_int, [i32, i32, vp, vp, vp, vp, vp, vp]),
 }
 
 
@@ -163,6 +170,12 @@ def device_errors(stream=None) -> int:
     bits = C.c_uint32(0)
     check(L.gfe_device_errors(C.byref(bits), stream_handle(stream)))
     return int(bits.value)
+
+
+def set_thread_error_word(word: torch.Tensor | None) -> None:
+    """Route this thread's kernel error reports to `word` (a zeroed CUDA int32/uint32 scalar), or
+    back to the library's per-device word with None."""
+    check(load().gfe_set_thread_error_word(ptr(word) if word is not None else None))
 
 
 def raise_device_errors(what: str, stream=None) -> None:

@@ -6,6 +6,7 @@
 
 namespace {
 thread_local std::string t_last_error;
+thread_local unsigned* t_err_word = nullptr;  // gfe_set_thread_error_word override
 std::mutex g_mu;
 unsigned* g_err_word[64] = {nullptr};
 int g_sm_count[64] = {0};
@@ -24,6 +25,7 @@ int set_error(int code, const char* fmt, ...) {
 }
 
 unsigned* device_error_word() {
+  if (t_err_word) return t_err_word;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
   std::lock_guard<std::mutex> lk(g_mu);
@@ -75,6 +77,13 @@ extern "C" int gfe_last_error(char* buf, int len) {
     buf[k] = 0;
   }
   return n;
+}
+
+extern "C" int gfe_set_thread_error_word(uint32_t* dev_word) {
+  if (dev_word && (reinterpret_cast<uintptr_t>(dev_word) & 3))
+    return gfe::set_error(GFE_ERR_ARG, "gfe_set_thread_error_word: word must be 4-byte aligned");
+  t_err_word = reinterpret_cast<unsigned*>(dev_word);
+  return GFE_OK;
 }
 
 extern "C" int gfe_device_errors(uint32_t* bits_host, void* stream) {

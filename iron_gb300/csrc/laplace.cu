@@ -252,7 +252,7 @@ laplace_assemble_color(const int32_t* __restrict__ elems, int32_t count, int32_t
       const int col = nd[j] + 1;
       int lo = lo0, hi = hi0;  // lower_bound of col in ci[lo0, hi0)
       while (lo < hi) {
-        int mid = (lo + hi) >> 1;
+        int mid = lo + ((hi - lo) >> 1);  // no int32 overflow past 2^30 entries
         if (__ldg(ci + mid) < col) lo = mid + 1; else hi = mid;
       }
       if (lo < hi0 && __ldg(ci + lo) == col) {
@@ -514,26 +514,35 @@ int check_device_errors(cudaStream_t s, const char* fn, bool sync) {
   return GFE_OK;
 }
 
+// bytes of the converted-coordinate array the FP32-pipe precisions read (0 for FP64)
+size_t regular_workspace_bytes(int32_t nx, int32_t ny, int32_t nz, int precision) {
+  const size_t n3 = 3ull * (nx + 1) * (ny + 1) * (nz + 1);
+  if (precision == GFE_FP64) return 0;
+  return n3 * (precision == GFE_MIXED ? sizeof(float) : sizeof(f2));
+}
+
+// ws: caller workspace of regular_workspace_bytes(), or NULL to allocate it on the stream
 template <typename T>
 int launch_regular(dim3 grid, cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const double* coords,
                    const double* kappa, const int32_t* rp, double* values, float* values32, double* rhs,
-                   unsigned* err) {
+                   unsigned* err, void* ws) {
   const size_t smem = 2 * 36 * kRThreads * sizeof(typename StoreOf<T>::type);
   GFE_CUDA_TRY(cudaFuncSetAttribute((const void*)laplace_regular_kernel<T>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long long n3 = 3ll * (nx + 1) * (ny + 1) * (nz + 1);
-  T* ct = nullptr;
-  if (int rc = gfe::scratch_alloc((void**)&ct, sizeof(T) * n3, s, "split coordinates")) return rc;
+  T* ct = static_cast<T*>(ws);
+  if (!ct)
+    if (int rc = gfe::scratch_alloc((void**)&ct, sizeof(T) * n3, s, "split coordinates")) return rc;
   split_coords<T><<<4 * gfe::sm_count(), 256, 0, s>>>(n3, coords, ct);
   laplace_regular_kernel<T><<<grid, kRThreads, smem, s>>>(nx, ny, nz, ct, kappa, rp, values, values32, rhs, err);
-  gfe::scratch_free(ct, s);
+  if (!ws) gfe::scratch_free(ct, s);
   return GFE_OK;
 }
 
 template <>
 int launch_regular<double>(dim3 grid, cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const double* coords,
                            const double* kappa, const int32_t* rp, double* values, float* values32, double* rhs,
-                           unsigned* err) {
+                           unsigned* err, void*) {
   const size_t smem = 2 * 36 * kRThreads * sizeof(double);
   GFE_CUDA_TRY(cudaFuncSetAttribute((const void*)laplace_regular_kernel<double>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -592,24 +601,39 @@ extern "C" int gfe_laplace_assemble(int32_t n_elem, int32_t n_nodes, const int32
   return GFE_OK;
 }
 
+extern "C" int64_t gfe_laplace_regular_workspace_bytes(int32_t nx, int32_t ny, int32_t nz, int32_t precision) {
+  if (nx <= 0 || ny <= 0 || nz <= 0) return 0;
+  return (int64_t)regular_workspace_bytes(nx, ny, nz, precision);
+}
+
 extern "C" int gfe_laplace_assemble_regular(int32_t nx, int32_t ny, int32_t nz, const double* coords,
                                             const double* kappa, const int32_t* row_ptr, double* values,
                                             float* values32, double* rhs, int32_t precision, void* stream) {
+  return gfe_laplace_assemble_regular_ws(nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, precision,
+                                         nullptr, stream);
+}
+
+extern "C" int gfe_laplace_assemble_regular_ws(int32_t nx, int32_t ny, int32_t nz, const double* coords,
+                                               const double* kappa, const int32_t* row_ptr, double* values,
+                                               float* values32, double* rhs, int32_t precision, void* workspace,
+                                               void* stream) {
   const char* fn = "gfe_laplace_assemble_regular";
   if (nx <= 0 || ny <= 0 || nz <= 0 || !coords || !row_ptr || !values)
     return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
   if (int rc = check_precision(precision, fn)) return rc;
+  if (workspace && (reinterpret_cast<uintptr_t>(workspace) & 15))
+    return gfe::set_error(GFE_ERR_ARG, "%s: workspace must be 16-byte aligned", fn);
   cudaStream_t s = gfe::as_stream(stream);
   unsigned* err = gfe::device_error_word();
   const dim3 grid((nx + 1 + kRTX - 1) / kRTX, (ny + 1 + kRTY - 1) / kRTY, (nz + 1 + kRZ - 1) / kRZ);
   void* prof = gfe::stage_begin(GFE_STAGE_LAPLACE_ELEMENTS, s);
   int rc;
   if (precision == GFE_FP64)
-    rc = launch_regular<double>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err);
+    rc = launch_regular<double>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace);
   else if (precision == GFE_MIXED)
-    rc = launch_regular<float>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err);
+    rc = launch_regular<float>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace);
   else
-    rc = launch_regular<f2>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err);
+    rc = launch_regular<f2>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace);
   gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, 1);
   if (rc) return rc;
   GFE_LAUNCH_CHECK(fn);

@@ -336,7 +336,7 @@ __global__ void mr_slot_kernel(const int32_t* __restrict__ elems, int32_t count,
       const int col = dof(c) + 1;
       int lo = lo0, hi = hi0;
       while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
+        const int mid = lo + ((hi - lo) >> 1);  // no int32 overflow past 2^30 entries
         if (ci[mid] < col) lo = mid + 1; else hi = mid;
       }
       slots[((size_t)item * ND + r) * ND + c] = (lo < hi0 && ci[lo] == col) ? lo : -1;

@@ -1,0 +1,714 @@
+"""Serving loop: a persistent engine for a stream of assembly + solve requests.
+
+Requests are Laplace/diffusion problems (trilinear hexahedra, per-element conductivity, u = 0 at
+x = 0 and u = 1 at x = 1, solved to a relative residual of 1e-10) or Mooney-Rivlin problems
+(triquadratic u / trilinear p, per-request c10 and c01 and stretch lambda: the first Newton step
+of a uniaxial load step from the affine predictor -- residual, consistent tangent, MINRES
+correction to 1e-3, updated residual) on jittered regular meshes of different sizes.  The engine
+
+* admits requests in arrival order as soon as a worker slot is free and the request's device
+  memory fits the HBM budget (a request that does not fit yet may be overtaken by later ones that
+  do; least-recently-used resident state that no running request holds is evicted to make room);
+* keeps per-size state resident: mesh connectivity, colouring, the Iron-identical CSR structure,
+  the MR slot map, and per-worker value/vector buffers;
+* runs each worker on its own CUDA stream, so requests admitted while others are on the GPU
+  overlap with them (continuous batching);
+* replays CUDA graphs for the launch-bound Laplace requests: per (worker, mesh size) one graph for
+  "assemble + CG start" and one for "25 CG iterations + status copy", replayed until the device
+  says the solve has converged.  Mooney-Rivlin requests (milliseconds-long kernels and host-side
+  Krylov control) run eagerly on their worker's stream.
+
+Kernels are deterministic (coloured scatters, fixed-order reductions), so a request's result does
+not depend on what runs beside it.  `plain_fp64` is the baseline: the FP64 drop-in path run one
+request at a time, building each request's structure from scratch as Iron does per problem.
+"""
+from __future__ import annotations
+
+import copy
+import ctypes as C
+import math
+import threading
+import time
+from collections import OrderedDict, deque
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import GfeError
+from .elasticity import MooneyRivlinAssembly
+from .laplace import LaplaceAssembly
+from .mesh import RegularMesh, linear_component
+from .newton import minres_solve, saddle_preconditioner, uniaxial_roller_conditions
+
+LAPLACE_RTOL = 1e-10
+MR_LINEAR_RTOL = 1e-3
+MR_STRETCH = (1.0, 1.1)
+CG_CHUNK = 25
+
+
+# torch registers every captured graph with the process-wide CUDA generator state, which is not
+# safe against concurrent capture or destruction from several threads.  Capture, destruction and
+# the building of resident state all happen under this lock, taken before the engine's own lock
+# whenever both are held.
+_GRAPH_LOCK = threading.RLock()
+
+
+class _CgState(C.Structure):
+    _fields_ = [("rr", C.c_double), ("rr0", C.c_double), ("done", C.c_int32), ("iterations", C.c_int32),
+                ("breakdown", C.c_int32), ("reserved", C.c_int32)]
+
+
+# ---- requests -----------------------------------------------------------------------------------
+
+@dataclass
+class Request:
+    rid: int
+    kind: str  # "laplace" | "mr"
+    n: int
+    seed: int
+    arrival: float = 0.0
+    # client-side inputs (host, pinned once generated)
+    inputs: dict = field(default_factory=dict, repr=False)
+    # filled by the engine
+    t_admit: float = math.nan
+    t_done: float = math.nan
+    result: np.ndarray | None = field(default=None, repr=False)
+    info: dict = field(default_factory=dict)
+
+    @property
+    def elements(self) -> int:
+        return self.n ** 3
+
+    @property
+    def latency(self) -> float:
+        return self.t_done - self.arrival
+
+
+def request_stream(n_requests: int = 2000, rate: float = 200.0, laplace_fraction: float = 0.7, n_lo: int = 4,
+                   n_hi: int = 64, seed: int = 0) -> list[Request]:
+    """Poisson arrivals (exponential inter-arrival times at `rate` per second), kind Laplace with
+    probability laplace_fraction else Mooney-Rivlin, side n = round(exp(U(ln n_lo, ln n_hi)))."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    kinds = np.where(rng.random(n_requests) < laplace_fraction, "laplace", "mr")
+    ns = np.rint(np.exp(rng.uniform(math.log(n_lo), math.log(n_hi), n_requests))).astype(int)
+    seeds = rng.integers(0, 2 ** 31 - 1, n_requests)
+    return [Request(i, str(kinds[i]), int(ns[i]), int(seeds[i]), float(t[i] - t[0])) for i in range(n_requests)]
+
+
+def _pinned(a: np.ndarray) -> torch.Tensor:
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    return t.pin_memory() if torch.cuda.is_available() else t
+
+
+def make_inputs(req: Request, pin: bool = True) -> None:
+    """The client's data for a request (host memory): jittered coordinates and conductivity
+    (Laplace) or coordinates, material and stretch (Mooney-Rivlin)."""
+    rng = np.random.default_rng(req.seed)
+    conv = _pinned if pin else (lambda a: torch.from_numpy(np.ascontiguousarray(a)))
+    if req.kind == "laplace":
+        m = RegularMesh((req.n,) * 3)
+        m.jitter_interior(int(rng.integers(2 ** 31)))
+        kappa = np.exp(rng.uniform(math.log(0.1), math.log(10.0), m.n_elements))
+        req.inputs = {"coords": conv(m.coords), "kappa": conv(kappa)}
+    else:
+        m = RegularMesh((req.n,) * 3, order=2)
+        m.jitter_interior(int(rng.integers(2 ** 31)))
+        c = np.exp(rng.uniform(math.log(0.5), math.log(10.0), 2))
+        lam = rng.uniform(*MR_STRETCH)
+        req.inputs = {"coords": conv(m.coords), "c": conv(c), "lam": float(lam)}
+
+
+def _laplace_bcs(m: RegularMesh):
+    fixed = np.zeros(m.n_nodes, np.uint8)
+    x0 = np.zeros(m.n_nodes)
+    fixed[m.face_nodes(0, 0)] = 1
+    right = m.face_nodes(0, 1)
+    fixed[right] = 1
+    x0[right] = 1.0
+    return fixed, x0
+
+
+# ---- resident state --------------------------------------------------------------------------------
+
+class _LaplaceMesh:
+    """Per-size resident Laplace state: connectivity, colouring, CSR structure, BCs."""
+
+    def __init__(self, n: int, dev):
+        m = RegularMesh((n, n, n))
+        self.mesh = m
+        base = LaplaceAssembly.from_regular_mesh(m, device=dev)
+        if base.regular is None:
+            raise GfeError(-3, "generated mesh failed the regular-structure check")
+        self.base = base
+        fixed, x0 = _laplace_bcs(m)
+        self.fixed = torch.from_numpy(fixed).to(dev)
+        self.x0 = torch.from_numpy(x0).to(dev)
+        base.values = None  # the base object holds structure only
+
+
+class _LaplaceSlot:
+    """A worker's buffers and captured graphs for one Laplace mesh size."""
+
+    def __init__(self, lm: _LaplaceMesh, dev, use_graphs: bool):
+        b = lm.base
+        self.lm = lm
+        self.asm = copy.copy(b)
+        # valid data for the warm-up run before capture: the undeformed mesh, unit conductivity
+        self.asm.coords = b.coords.clone()
+        self.asm.kappa = torch.ones(b.n_elements, dtype=torch.float64, device=dev)
+        self.asm.values = torch.empty(b.nnz, dtype=torch.float64, device=dev)
+        self.asm.values32 = torch.empty(b.nnz, dtype=torch.float32, device=dev)
+        self.asm.rhs = torch.empty(b.n_nodes, dtype=torch.float64, device=dev)
+        self.x = torch.empty(b.n_nodes, dtype=torch.float64, device=dev)
+        L = _lib.load()
+        wsb = int(L.gfe_cg_workspace_bytes(b.n_nodes))
+        self.ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+        nx, ny, nz = b.regular
+        awb = int(L.gfe_laplace_regular_workspace_bytes(nx, ny, nz, 2))
+        self.asm_ws = torch.empty(max(awb, 16), dtype=torch.uint8, device=dev)
+        self.state = torch.zeros(C.sizeof(_CgState), dtype=torch.uint8).pin_memory()
+        self.use_graphs = use_graphs
+        self.g_begin = self.g_chunk = None
+
+    # the two launch sequences (also what the graphs capture)
+    def _begin(self, stream):
+        a = self.asm
+        nx, ny, nz = a.regular
+        st = _lib.stream_handle(stream)
+        self.x.copy_(self.lm.x0)
+        _lib.call("gfe_laplace_assemble_regular_ws", nx, ny, nz, _lib.ptr(a.coords), _lib.ptr(a.kappa),
+                  _lib.ptr(a.row_ptr), _lib.ptr(a.values), _lib.ptr(a.values32), _lib.ptr(a.rhs), 2,
+                  _lib.ptr(self.asm_ws), st)
+        _lib.call("gfe_cg_begin", a.n_nodes, _lib.ptr(a.row_ptr), _lib.ptr(a.col_idx), _lib.ptr(a.values), None,
+                  _lib.ptr(self.lm.fixed), _lib.ptr(self.x), LAPLACE_RTOL, _lib.ptr(self.ws), st)
+
+    def _chunk(self, stream):
+        a = self.asm
+        st = _lib.stream_handle(stream)
+        _lib.call("gfe_cg_steps", a.n_nodes, _lib.ptr(a.row_ptr), _lib.ptr(a.col_idx), _lib.ptr(a.values),
+                  _lib.ptr(self.lm.fixed), _lib.ptr(self.x), CG_CHUNK, _lib.ptr(self.ws), st)
+        _lib.call("gfe_cg_status", a.n_nodes, _lib.ptr(self.ws), C.c_void_p(self.state.data_ptr()), st)
+
+    def capture(self, stream):
+        """Warm up once eagerly, then capture both sequences on `stream`.  Capture is thread-local
+        (other workers keep launching and allocating meanwhile) and, unlike torch.cuda.graph,
+        does not synchronise the whole device first."""
+        with torch.cuda.stream(stream):
+            self._begin(stream)
+            self._chunk(stream)
+            stream.synchronize()
+            graphs = []
+            with _GRAPH_LOCK:
+                for fn in (self._begin, self._chunk):
+                    g = torch.cuda.CUDAGraph()
+                    g.capture_begin(capture_error_mode="thread_local")
+                    try:
+                        fn(stream)
+                    finally:
+                        g.capture_end()
+                    graphs.append(g)
+            self.g_begin, self.g_chunk = graphs
+        stream.synchronize()
+
+    def release(self):
+        with _GRAPH_LOCK:
+            self.g_begin = self.g_chunk = None
+
+    def run(self, req: Request, stream) -> None:
+        a = self.asm
+        with torch.cuda.stream(stream):
+            a.coords.copy_(req.inputs["coords"], non_blocking=True)
+            a.kappa.copy_(req.inputs["kappa"], non_blocking=True)
+            if self.use_graphs:
+                self.g_begin.replay()
+            else:
+                self._begin(stream)
+            st = _CgState.from_address(self.state.data_ptr())
+            chunks = 0
+            while True:
+                if self.use_graphs:
+                    self.g_chunk.replay()
+                else:
+                    self._chunk(stream)
+                chunks += 1
+                stream.synchronize()
+                if st.done or chunks * CG_CHUNK > 200000:
+                    break
+            out = torch.empty(a.n_nodes, dtype=torch.float64, pin_memory=True)
+            out.copy_(self.x, non_blocking=True)
+            stream.synchronize()
+        bits = _lib.device_errors(stream)
+        if bits or st.done != 2:
+            raise GfeError(-5, f"request {req.rid}: Laplace solve ended with state {st.done}, device bits {bits:#x}")
+        req.result = out.numpy()
+        req.info = {"iterations": int(st.iterations), "rel_residual": math.sqrt(st.rr / st.rr0) if st.rr0 else 0.0}
+
+
+class _MRMesh:
+    """Per-size resident Mooney-Rivlin state: connectivity, colouring, CSR structure, slot map."""
+
+    def __init__(self, n: int, dev):
+        self.base = MooneyRivlinAssembly.from_regular_mesh((n, n, n), device=dev)
+        b = self.base
+        b.values = None
+        # the Dirichlet DOFs (rollers and the pulled face): boundary nodes are never jittered, so
+        # the mask holds for every request of this size
+        self.fixed, _ = uniaxial_roller_conditions(b, 1.0)
+        self.fixed_b = self.fixed.bool()
+
+
+class _MRSlot:
+    def __init__(self, mm: _MRMesh, dev):
+        b = mm.base
+        self.mm = mm
+        self.asm = copy.copy(b)
+        self.asm.xg = torch.empty_like(b.xg)
+        self.asm.values = torch.empty(b.nnz, dtype=torch.float64, device=dev)
+        self.values32 = torch.empty(b.nnz, dtype=torch.float32, device=dev)
+        n = b.ndof
+        self.dep = torch.empty(n, dtype=torch.float64, device=dev)
+        self.R = torch.empty(n, dtype=torch.float64, device=dev)
+        self.du = torch.empty(n, dtype=torch.float64, device=dev)
+        self.minv = torch.empty(n, dtype=torch.float64, device=dev)
+
+    def run(self, req: Request, stream, precision: str = "mixed") -> None:
+        a = self.asm
+        with torch.cuda.stream(stream):
+            a.xg.copy_(req.inputs["coords"], non_blocking=True)
+            c = req.inputs["c"].to(a.device, non_blocking=True)
+            mm = self.mm
+            _mr_start_state(a.xg, req.inputs["lam"], self.dep)
+            info = _mr_newton_step(a, self.dep, c, mm.fixed, mm.fixed_b, self.R, self.du, self.minv, self.values32,
+                                   precision, stream)
+            out = torch.empty(a.ndof, dtype=torch.float64, pin_memory=True)
+            out.copy_(self.dep, non_blocking=True)
+            stream.synchronize()
+        req.result = out.numpy()
+        req.info = info
+
+
+def _mr_start_state(xg: torch.Tensor, lam: float, dep: torch.Tensor) -> None:
+    """The load step's predictor: the affine isochoric stretch z = diag(lam, lam^-1/2, lam^-1/2) x
+    with p = 0.  It meets the roller and pulled-face conditions exactly (those boundary nodes are not
+    jittered) and keeps every element valid, unlike moving the pulled face alone."""
+    nq = xg.shape[1]
+    scale = torch.tensor([lam, lam ** -0.5, lam ** -0.5], dtype=xg.dtype, device=xg.device)
+    torch.mul(xg, scale[:, None], out=dep[: 3 * nq].view(3, nq))
+    dep[3 * nq:] = 0.0
+
+
+def _mr_newton_step(a, dep, c, fixed_u8, fixed_b, R, du, minv, values32, precision, stream) -> dict:
+    """One Newton correction of the MR problem: R, consistent tangent, MINRES to MR_LINEAR_RTOL,
+    dep += du, the new residual norm."""
+    a.residual(dep, c, out=R, stream=stream)
+    R.masked_fill_(fixed_b, 0.0)
+    r0 = float(torch.linalg.vector_norm(R))
+    vals = a.tangent(dep, c, precision=precision, stream=stream)
+    saddle_preconditioner(a.row_ptr, a.col_idx, vals, 3 * a.n_q2, fixed_u8, out=minv, stream=stream)
+    v32 = None
+    if precision == "mixed":
+        values32.copy_(vals)
+        v32 = values32
+    du.zero_()
+    R.neg_()
+    li = minres_solve(a.row_ptr, a.col_idx, vals, R, fixed_u8, du, minv=minv, values32=v32, rtol=MR_LINEAR_RTOL,
+                      max_iters=100000, precision=precision, stream=stream)
+    dep.add_(du)
+    a.residual(dep, c, out=R, stream=stream)
+    R.masked_fill_(fixed_b, 0.0)
+    r1 = float(torch.linalg.vector_norm(R))
+    return {"linear_iterations": li.iterations, "residual_before": r0, "residual_after": r1}
+
+
+# ---- the engine ------------------------------------------------------------------------------------
+
+def estimate_bytes(kind: str, n: int) -> tuple[int, int]:
+    """(resident bytes per mesh size, working bytes per slot) used for admission: upper estimates
+    of the device memory the engine allocates (torch tensors plus the library's stream-ordered
+    scratch), so the accounted total never falls below what is in use."""
+    E = n ** 3
+    if kind == "laplace":
+        N = (n + 1) ** 3
+        nnz = (3 * n + 1) ** 3  # exact for the regular trilinear mesh
+        resident = 4 * (N + 1) + 4 * nnz + 36 * E + 41 * N
+        work = 12 * nnz + 56 * N + 8 * E + 40 * N + 24 * N + 16 * 2048 + 4096
+    else:
+        Nq, Np = (2 * n + 1) ** 3, (n + 1) ** 3
+        ndof = 3 * Nq + Np
+        # interior rows: a u node couples with 64 u nodes and 15.6 p nodes on average, a p node
+        # with 125 u nodes and 27 p nodes; boundary rows have fewer
+        nnz = 3 * Nq * 208 + Np * 402
+        resident = 4 * (ndof + 1) + 4 * nnz + 4 * 89 * 89 * E + 4 * (27 + 8 + 89 + 1) * E + 24 * Nq + 10 * ndof
+        work = 12 * nnz + 24 * Nq + 32 * ndof + 84 * ndof + 27 * 99 * 8 * ((E + 7) // 8)
+    return int(1.05 * resident) + (1 << 20), int(1.05 * work) + (1 << 20)
+
+
+class HbmLedger:
+    """Device-memory bookkeeping of the serving engine (host logic only, no CUDA).
+
+    Charges, against `budget` bytes: resident per-size state (charged when a request for a new size
+    is admitted, kept until evicted), Laplace per-(worker, size) slots (kept with their size's
+    resident state), and Mooney-Rivlin per-request working memory (released when the request
+    ends).  Eviction frees least-recently-used sizes that no admitted request holds, together with
+    their slots."""
+
+    def __init__(self, budget: int):
+        self.budget = int(budget)
+        self.in_use = 0
+        self.resident: OrderedDict = OrderedDict()  # (kind, n) -> bytes, LRU order (built or building)
+        self.slots: dict = {}  # (worker, kind, n) -> bytes
+        self.users: dict = {}  # (kind, n) -> admitted requests holding it
+        self.work: dict = {}  # rid -> per-request bytes
+        self.evictions = 0
+
+    def _free_for(self, need: int, keep) -> tuple[bool, list, list]:
+        evicted, dropped = [], []
+        for key in list(self.resident.keys()):
+            if self.in_use + need <= self.budget:
+                break
+            if key == keep or self.users.get(key, 0) > 0:
+                continue
+            self.in_use -= self.resident.pop(key)
+            for sk in [k for k in self.slots if k[1:] == key]:
+                self.in_use -= self.slots.pop(sk)
+                dropped.append(sk)
+            evicted.append(key)
+            self.evictions += 1
+        return self.in_use + need <= self.budget, evicted, dropped
+
+    def admit(self, rid: int, kind: str, n: int, worker: int):
+        """Charge a request; returns (admitted, evicted size keys, dropped slot keys)."""
+        key = (kind, n)
+        res_b, work_b = estimate_bytes(kind, n)
+        need = 0 if key in self.resident else res_b
+        if kind == "laplace":
+            need += 0 if (worker,) + key in self.slots else work_b
+        else:
+            need += work_b
+        ok, evicted, dropped = self._free_for(need, key)
+        if not ok:
+            return False, evicted, dropped
+        if key in self.resident:
+            self.resident.move_to_end(key)
+        else:
+            self.resident[key] = res_b
+        if kind == "laplace":
+            self.slots.setdefault((worker,) + key, work_b)
+        else:
+            self.work[rid] = work_b
+        self.in_use += need
+        self.users[key] = self.users.get(key, 0) + 1
+        return True, evicted, dropped
+
+    def finish(self, rid: int, kind: str, n: int) -> None:
+        key = (kind, n)
+        self.users[key] -= 1
+        self.in_use -= self.work.pop(rid, 0)
+
+    def check(self) -> None:
+        total = sum(self.resident.values()) + sum(self.slots.values()) + sum(self.work.values())
+        assert total == self.in_use, (total, self.in_use)
+        assert all(sk[1:] in self.resident for sk in self.slots)
+
+
+class ServingEngine:
+    """Persistent request loop over `workers` CUDA streams with an HBM budget (bytes; default 60 % of
+    the free device memory, leaving room for allocator caching and the library's stream-ordered
+    scratch, which the estimates do not itemise)."""
+
+    def __init__(self, device=None, workers: int = 8, hbm_budget: int | None = None, use_graphs: bool = True,
+                 mr_precision: str = "mixed"):
+        self.dev = torch.device(device) if device is not None else _lib.require_cuda()
+        _lib.load()
+        free, _total = torch.cuda.mem_get_info(self.dev)
+        self.ledger = HbmLedger(hbm_budget if hbm_budget is not None else 0.6 * free)
+        self.workers = workers
+        self.use_graphs = use_graphs
+        self.mr_precision = mr_precision
+        self.streams = [torch.cuda.Stream(self.dev) for _ in range(workers)]
+        # one device error word per worker: a request's kernel errors stay with that request
+        self.err_words = [torch.zeros(1, dtype=torch.int32, device=self.dev) for _ in range(workers)]
+        self.meshes: dict = {}  # (kind, n) -> resident mesh state
+        self.slots: dict = {}  # (worker, "laplace", n) -> slot
+        self.lock = threading.Lock()
+        self.cv = threading.Condition(self.lock)
+        self.stats = {"evictions": 0, "graphs_captured": 0, "max_concurrent": 0}
+        self._graveyard: list = []
+
+    @property
+    def budget(self) -> int:
+        return self.ledger.budget
+
+    @property
+    def in_use(self) -> int:
+        return self.ledger.in_use
+
+    def _drop(self, evicted, dropped) -> None:
+        """Forget evicted state (lock held); slots with graphs are destroyed later, under the
+        capture lock."""
+        for key in evicted:
+            self.meshes.pop(key, None)
+        for sk in dropped:
+            slot = self.slots.pop(sk, None)
+            if slot is not None:
+                self._graveyard.append(slot)
+        self.stats["evictions"] = self.ledger.evictions
+
+    def _prepare(self, req: Request, worker: int):
+        """Resident mesh and, for Laplace, the worker's slot (built on first use, one build at a
+        time); a Mooney-Rivlin request gets working buffers of its own."""
+        key = (req.kind, req.n)
+        sk = (worker,) + key
+        with _GRAPH_LOCK:
+            with self.lock:
+                dead, self._graveyard = self._graveyard, []
+                mesh = self.meshes.get(key)
+                slot = self.slots.get(sk)
+            for d in dead:
+                if hasattr(d, "release"):
+                    d.release()
+            del dead
+            if mesh is None:
+                mesh = _LaplaceMesh(req.n, self.dev) if req.kind == "laplace" else _MRMesh(req.n, self.dev)
+                with self.lock:
+                    self.meshes[key] = mesh
+            if req.kind == "mr":
+                return _MRSlot(mesh, self.dev)
+            if slot is None:
+                slot = _LaplaceSlot(mesh, self.dev, self.use_graphs)
+                if self.use_graphs:
+                    slot.capture(self.streams[worker])
+                    self.stats["graphs_captured"] += 2
+                with self.lock:
+                    self.slots[sk] = slot
+        return slot
+
+    # run ------------------------------------------------------------------------------------------
+    def serve(self, requests: list[Request], realtime: bool = True, log=None) -> dict:
+        """Serve `requests` (arrival times in seconds from the start).  With realtime, a request
+        is not admitted before its arrival time.  Returns summary statistics; per-request results
+        and times are stored on the requests.  Raises GfeError after the running requests have
+        finished if a request failed or cannot fit the budget at all."""
+        order = sorted(requests, key=lambda r: r.arrival)
+        pending: deque = deque()
+        free_workers = list(range(self.workers))
+        running = 0
+        errors = []
+        t0 = time.perf_counter()
+        clock = (lambda: time.perf_counter() - t0) if realtime else (lambda: math.inf)
+        nxt = 0
+        done_count = 0
+        fatal = None
+
+        def work(req: Request, worker: int):
+            nonlocal running, done_count
+            stream = self.streams[worker]
+            try:
+                _lib.set_thread_error_word(self.err_words[worker])
+                with torch.cuda.stream(stream):
+                    slot = self._prepare(req, worker)
+                if req.kind == "laplace":
+                    slot.run(req, stream)
+                else:
+                    slot.run(req, stream, self.mr_precision)
+                    del slot  # per-request working memory
+            except Exception as e:  # reported after the loop
+                errors.append((req.rid, repr(e)))
+            finally:
+                req.t_done = time.perf_counter() - t0
+                with self.cv:
+                    running -= 1
+                    done_count += 1
+                    self.ledger.finish(req.rid, req.kind, req.n)
+                    free_workers.append(worker)
+                    self.cv.notify_all()
+
+        threads = []
+        with self.cv:
+            while done_count < len(order) and fatal is None:
+                now = clock()
+                while nxt < len(order) and order[nxt].arrival <= now:
+                    pending.append(order[nxt])
+                    nxt += 1
+                # admit in arrival order; a request that does not fit may be overtaken
+                i = 0
+                while i < len(pending) and free_workers:
+                    req = pending[i]
+                    w = free_workers[-1]
+                    ok, evicted, dropped = self.ledger.admit(req.rid, req.kind, req.n, w)
+                    self._drop(evicted, dropped)
+                    if ok:
+                        free_workers.pop()
+                        del pending[i]
+                        req.t_admit = clock() if realtime else time.perf_counter() - t0
+                        running += 1
+                        self.stats["max_concurrent"] = max(self.stats["max_concurrent"], running)
+                        th = threading.Thread(target=work, args=(req, w), daemon=True)
+                        threads.append(th)
+                        th.start()
+                    else:
+                        i += 1
+                if pending and running == 0:
+                    # nothing running and the head still does not fit: the budget is too small
+                    req = pending[0]
+                    fatal = GfeError(-7, f"request {req.rid} ({req.kind} n={req.n}) does not fit the HBM budget "
+                                         f"of {self.budget} bytes")
+                    break
+                if done_count >= len(order):
+                    break
+                wait = None
+                if nxt < len(order) and realtime:
+                    wait = max(0.0, order[nxt].arrival - clock())
+                self.cv.wait(timeout=wait if wait is not None else 0.5)
+        for th in threads:
+            th.join()
+        if fatal is not None:
+            raise fatal
+        if errors:
+            raise GfeError(-4, f"{len(errors)} request(s) failed, first: {errors[0]}")
+        return summarize(order)
+
+    def close(self):
+        """Drop every resident mesh and slot (graphs are destroyed under the capture lock)."""
+        with _GRAPH_LOCK:
+            with self.lock:
+                dead = list(self.slots.values()) + self._graveyard
+                self.slots.clear()
+                self.meshes.clear()
+                self._graveyard = []
+                self.ledger = HbmLedger(self.ledger.budget)
+            for slot in dead:
+                if hasattr(slot, "release"):
+                    slot.release()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def summarize(reqs: list[Request]) -> dict:
+    lat = np.array([r.latency for r in reqs]) * 1e3
+    t_end = max(r.t_done for r in reqs)
+    t_first = min(r.arrival for r in reqs)
+    span = t_end - t_first
+    E = sum(r.elements for r in reqs)
+    out = {"requests": len(reqs), "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "span_s": span,
+           "requests_per_s": len(reqs) / span, "elements_per_s": E / span}
+    for kind in ("laplace", "mr"):
+        rk = [r for r in reqs if r.kind == kind]
+        if not rk:
+            continue
+        lk = np.array([r.latency for r in rk]) * 1e3
+        sk = np.array([r.t_done - r.t_admit for r in rk]) * 1e3
+        out[f"{kind}_p50_ms"] = float(np.percentile(lk, 50))
+        out[f"{kind}_p99_ms"] = float(np.percentile(lk, 99))
+        out[f"{kind}_service_mean_ms"] = float(sk.mean())
+        its = [r.info.get("linear_iterations", r.info.get("iterations")) for r in rk]
+        its = [i for i in its if i is not None]
+        if its:
+            out[f"{kind}_solver_iterations_mean"] = float(np.mean(its))
+    return out
+
+
+# ---- the baseline: the plain FP64 path, one request at a time ------------------------------------
+
+def plain_fp64(requests: list[Request], realtime: bool = True) -> dict:
+    """Each request from scratch (mesh, structure, FP64 colour-scatter assembly, FP64 solve), one
+    at a time in arrival order, on the default stream."""
+    order = sorted(requests, key=lambda r: r.arrival)
+    dev = _lib.require_cuda()
+    t0 = time.perf_counter()
+    for req in order:
+        if realtime:
+            wait = req.arrival - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+        req.t_admit = time.perf_counter() - t0
+        if req.kind == "laplace":
+            m = RegularMesh((req.n,) * 3)
+            A = LaplaceAssembly(m.elem_nodes, req.inputs["coords"].numpy(), kappa=req.inputs["kappa"].numpy(),
+                                colour_elems=m.colouring()[0], colour_ptr=m.colouring()[1], device=dev)
+            A.assemble("fp64", path="general")
+            fixed, x0 = _laplace_bcs(m)
+            x = torch.from_numpy(x0).to(dev)
+            info = A.solve(torch.from_numpy(fixed).to(dev), x, rtol=LAPLACE_RTOL, precision="fp64")
+            req.result = x.cpu().numpy()
+            req.info = {"iterations": info.iterations, "rel_residual": info.relative_residual}
+        else:
+            m = RegularMesh((req.n,) * 3, order=2)
+            elin, lin2g = linear_component(m.elem_nodes, 2)
+            order_c, ptr = m.colouring()
+            A = MooneyRivlinAssembly(m.elem_nodes, elin, req.inputs["coords"].numpy(), order_c, ptr, len(lin2g),
+                                     device=dev)
+            c = req.inputs["c"].to(dev)
+            fixed, _full = uniaxial_roller_conditions(A, req.inputs["lam"])
+            fb = fixed.bool()
+            dep = torch.empty(A.ndof, dtype=torch.float64, device=dev)
+            _mr_start_state(A.xg, req.inputs["lam"], dep)
+            n = A.ndof
+            R, du, minv = (torch.empty(n, dtype=torch.float64, device=dev) for _ in range(3))
+            req.info = _mr_newton_step(A, dep, c, fixed, fb, R, du, minv, None, "fp64", None)
+            req.result = dep.cpu().numpy()
+        torch.cuda.synchronize()
+        req.t_done = time.perf_counter() - t0
+    return summarize(order)
+
+
+# ---- bench entry -----------------------------------------------------------------------------------
+
+def bench(args, log, clock_sampler):
+    import json
+
+    n_req = getattr(args, "serve_requests", 2000)
+    reqs = request_stream(n_requests=n_req, seed=0)
+    log(f"serve: generating inputs for {len(reqs)} requests")
+    for r in reqs:
+        make_inputs(r)
+    dev = torch.device("cuda", 0)
+    eng = ServingEngine(dev, workers=getattr(args, "serve_workers", 8))
+    # warm-up: one small request of each kind (library load, kernel attributes)
+    warm = request_stream(n_requests=4, seed=99, n_lo=4, n_hi=5)
+    for r in warm:
+        make_inputs(r)
+    eng.serve(warm, realtime=False)
+    log("serve: engine")
+    with clock_sampler(dev.index) as clk:
+        s_eng = eng.serve(reqs, realtime=True)
+    res_engine = {r.rid: r.result for r in reqs}
+    info_engine = {r.rid: dict(r.info) for r in reqs}
+    log(f"serve: engine p50 {s_eng['p50_ms']:.1f} ms p99 {s_eng['p99_ms']:.1f} ms; plain FP64 baseline")
+    for r in reqs:
+        r.result = None
+    with clock_sampler(dev.index) as clk2:
+        s_plain = plain_fp64(reqs, realtime=True)
+    # agreement with the plain FP64 path: Laplace solutions; MR post-step residual norms
+    lap_err, mr_ratio = 0.0, []
+    for r in reqs:
+        if r.kind == "laplace":
+            lap_err = max(lap_err, float(np.abs(res_engine[r.rid] - r.result).max()))
+        else:
+            a, b = info_engine[r.rid]["residual_after"], r.info["residual_after"]
+            mr_ratio.append(a / b if b > 0 else 1.0)
+    line = {
+        "metric": "serve_p99_latency_ms", "value": s_eng["p99_ms"], "unit": "ms", "n_gpus": 1, "steps": 1,
+        "warmup": 1, "higher_is_better": False, "dtype": "f64 (Laplace mixed_df assembly), f32/f64 (MR)",
+        "data": "synthetic",
+        "config": {"workload": "serve_stream", "requests": len(reqs), "arrivals": "Poisson 200/s", "laplace": 0.7,
+                   "side": "round(exp(U(ln 4, ln 64)))", "laplace_solve": f"CG rtol {LAPLACE_RTOL}",
+                   "mr_request": f"one Newton step, MINRES rtol {MR_LINEAR_RTOL}", "workers": eng.workers,
+                   "hbm_budget_GB": eng.budget / 1e9},
+        "engine": s_eng, "plain_fp64_one_at_a_time": s_plain,
+        "p99_speedup_vs_plain": s_plain["p99_ms"] / s_eng["p99_ms"],
+        "throughput_speedup_vs_plain": s_eng["requests_per_s"] / s_plain["requests_per_s"],
+        "laplace_max_abs_diff_vs_plain": lap_err,
+        "mr_residual_after_ratio_vs_plain": [float(np.min(mr_ratio)), float(np.max(mr_ratio))] if mr_ratio else None,
+        "engine_stats": eng.stats, "clocks": clk.summary(), "clocks_plain": clk2.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0

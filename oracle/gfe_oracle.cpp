@@ -195,7 +195,7 @@ int csr_values_add(const int32_t* rp, const int32_t* ci, double* data, int nr, c
       if (col <= prev) lo = rp[row - 1]; else up = rp[row];
       prev = col;
       while (up - lo > kBisectionToLinear) {
-        int mid = (up + lo) / 2;
+        int mid = lo + (up - lo) / 2;
         if (ci[mid - 1] > col) up = mid; else lo = mid;
       }
       for (int k = lo; k <= up && k < rp[row]; ++k) {
@@ -346,7 +346,7 @@ int64_t orc_csr_location(const int32_t* rp, const int32_t* ci, int row, int col)
   if (up <= lo) return 0;
   if (col < ci[lo - 1] || col > ci[up - 2]) return 0;
   while (up - lo > kBisectionToLinear) {
-    int mid = (up + lo) / 2;
+    int mid = lo + (up - lo) / 2;
     if (ci[mid - 1] > col) up = mid; else lo = mid;
   }
   for (int k = lo; k < up; ++k)

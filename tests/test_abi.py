@@ -11,7 +11,7 @@ ROOT = Path(__file__).resolve().parent.parent
 def header_functions():
     text = (ROOT / "include" / "gfe.h").read_text()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"^\s*int\s+(gfe_\w+)\s*\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t)\s+(gfe_\w+)\s*\(", text, flags=re.M)))
 
 
 def test_header_declares_entry_points():

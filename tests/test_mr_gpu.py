@@ -85,3 +85,29 @@ def test_assembled_jacobian_matches_oracle(gfe_cuda, ne):
     vo = oracle.mr_assemble_jacobian(A.mesh.elem_nodes, A.elin.cpu().numpy(), A.n_q2, A.n_lin, A.xg.cpu().numpy(),
                                      dep, [C1, C2], orp, oci)
     assert np.abs(v - vo).max() <= 1e-12 * np.abs(vo).max()
+
+
+def test_slot_map_beyond_2pow30_entries(gfe_cuda):
+    """59^3 Q2/Q1 mesh: the Jacobian has more than 2^30 non-zeros, so the bisection midpoint of
+    rows near the end would overflow int32 if computed as (lo + hi) / 2.  Sampled slot-map entries
+    of the last elements in colour order point at their (row, column) in the CSR."""
+    A = MooneyRivlinAssembly.from_regular_mesh((59, 59, 59))
+    assert A.nnz > 2 ** 30
+    torch.cuda.synchronize()
+    rp = A.row_ptr
+    ce = A.colour_elems
+    dofs = A.elem_dofs
+    for item in (A.n_elements - 1, A.n_elements - 2, A.colour_ptr[-2]):
+        e = int(ce[item])
+        d = dofs[e].cpu().numpy()
+        sl = A.slots[item].cpu().numpy()
+        for r in (0, 40, 80, 81, 88):
+            lo, hi = int(rp[d[r]]) - 1, int(rp[d[r] + 1]) - 1
+            cols = A.col_idx[lo:hi].cpu().numpy()
+            for c in range(89):
+                if r >= 81 and c >= 81:
+                    continue
+                pos = lo + int(np.searchsorted(cols, d[c] + 1))
+                assert sl[r, c] == pos, (item, r, c)
+    del A
+    torch.cuda.empty_cache()

@@ -77,8 +77,8 @@ def test_minres_on_spd_system_matches_cg(gfe_cuda):
     x1 = torch.from_numpy(x0).cuda()
     x2 = torch.from_numpy(x0).cuda()
     L.solve(fixed_t, x1, rtol=1e-12)
-    info = minres_solve(L.row_ptr, L.col_idx, L.values, None, fixed_t, x2, rtol=1e-12)
-    assert info.relative_residual <= 1e-12
+    info = minres_solve(L.row_ptr, L.col_idx, L.values, None, fixed_t, x2, rtol=1e-13)
+    assert info.relative_residual <= 1e-13
     assert (x1 - x2).abs().max().item() <= 1e-10
 
 
@@ -139,20 +139,43 @@ def test_newton_mixed_precision_matches_fp64(gfe_cuda):
     assert np.abs(res["mixed"] - res["fp64"]).max() <= 1e-10 * np.abs(res["fp64"]).max()
 
 
-def test_newton_with_iron_analytic_jacobian(gfe_cuda):
-    """Iron's analytic Jacobian is not the exact derivative of its residual, so Newton converges
-    linearly with it, but to the same state."""
+def test_newton_direction_with_iron_analytic_jacobian(gfe_cuda):
+    """Iron's analytic Jacobian (as restated from finite_elasticity_routines.F90) is not the
+    derivative of the residual: its u-u block is about 14 % off even in the undeformed state, so a
+    full Newton step with it does not reduce the residual (the oracle's dense Newton shows the same),
+    while the consistent tangent's step does.  The GPU direction (GMRES on the assembled analytic
+    Jacobian) matches the oracle's dense solve of the same system."""
+    from iron_gb300.newton import gmres_solve
+
     lam = 1.05
     A = MooneyRivlinAssembly.from_regular_mesh((2, 2, 2))
     fixed, full = uniaxial_roller_conditions(A, lam)
+    fb = fixed.bool()
     dep = A.initial_state(0.0)
-    s = NewtonSolver(A, [C1, C2], jacobian="analytic", absolute_tolerance=1e-12, relative_tolerance=1e-14,
-                     solution_tolerance=0.0, maximum_iterations=100, linear_relative_tolerance=1e-10)
-    s.solve(dep, fixed, full, load_increments=2)
-    exact = uniaxial_exact_state(A, lam, C1, C2).cpu().numpy()
-    d = dep.cpu().numpy()
-    nu = 3 * A.n_q2
-    assert np.abs(d[:nu] - exact[:nu]).max() <= 1e-9 * np.abs(exact[:nu]).max()
+    dep[fb] = full[fb]
+    c = [C1, C2]
+    R = A.residual(dep, c).clone()
+    R[fb] = 0.0
+    steps = {}
+    for kind in ("analytic", "consistent"):
+        vals = (A.jacobian(dep, c) if kind == "analytic" else A.tangent(dep, c)).clone()
+        minv = saddle_preconditioner(A.row_ptr, A.col_idx, vals, 3 * A.n_q2, fixed)
+        du = torch.zeros_like(dep)
+        gmres_solve(A.row_ptr, A.col_idx, vals, -R, fixed, du, minv=minv, rtol=1e-12)
+        steps[kind] = du
+        if kind == "analytic":
+            K = _dense(A.row_ptr.cpu().numpy(), A.col_idx.cpu().numpy(), vals.cpu().numpy(), A.ndof)
+            free = fixed.cpu().numpy() == 0
+            ref = np.zeros(A.ndof)
+            ref[free] = np.linalg.solve(K[np.ix_(free, free)], -R.cpu().numpy()[free])
+            assert np.abs(du.cpu().numpy() - ref).max() <= 1e-8 * np.abs(ref).max()
+    r0 = float(R.norm())
+    r_an = A.residual(dep + steps["analytic"], c)
+    r_an[fb] = 0.0
+    r_co = A.residual(dep + steps["consistent"], c)
+    r_co[fb] = 0.0
+    assert float(r_co.norm()) < 0.1 * r0
+    assert float(r_an.norm()) > r0
 
 
 @pytest.mark.parametrize("precision,rtol", [("fp64", 1e-11), ("mixed", 1e-9)])
