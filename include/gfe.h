@@ -43,6 +43,8 @@ extern "C" {
 #define GFE_FP64 0  /* plain: element arithmetic and storage in FP64 */
 #define GFE_MIXED 1 /* FP32 element arithmetic, FP64 accumulation */
 #define GFE_MIXED_DF 2 /* float-float element arithmetic on the FP32 pipes (~48-bit), FP64 accumulation */
+#define GFE_TC_TF32X3 3 /* MR Jacobian: tensor-core (tcgen05) TF32 contraction, 3-pass split (~FP32 accuracy) */
+#define GFE_TC_TF32 4   /* MR Jacobian: tensor-core (tcgen05) TF32 contraction, one pass (~1e-3 relative) */
 
 /* ---- library -------------------------------------------------------------------------- */
 
@@ -189,8 +191,10 @@ int gfe_mr_jacobian(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int
                     const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
                     const double* dep, const double* cpar, const int32_t* slots, double* values, int64_t nnz,
                     double* K_out, int32_t precision, void* stream);
-/* precision: GFE_FP64 (FP64 contraction) or GFE_MIXED (FP32 contraction of the basis-gradient x
- * material blocks; Gauss-point kinematics, det(F) and the assembled values stay FP64). */
+/* precision: GFE_FP64 (FP64 contraction), GFE_MIXED (FP32 CUDA-core contraction of the
+ * basis-gradient x material blocks), GFE_TC_TF32X3 / GFE_TC_TF32 (the same contraction on the
+ * tensor cores, tcgen05 kind::tf32 with FP32 accumulation in tensor memory, three-pass split or one
+ * pass).  In every mode the Gauss-point kinematics, det(F) and the assembled values stay FP64. */
 
 /* Consistent tangent: the exact derivative of the residual of gfe_mr_residual with respect to
  * the dependent vector (what Iron's finite-difference Jacobian, EquationsSet_FiniteElementJacobianEvaluateFD

@@ -26,6 +26,7 @@
 #include <mutex>
 
 #include "gfe_internal.cuh"
+#include "tcgen05.cuh"
 
 namespace {
 
@@ -987,6 +988,184 @@ mr_contract_kernel(const int32_t* __restrict__ elems, int32_t count, const Table
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Tensor-core (tcgen05, TF32) basis-gradient contraction of the element Jacobian
+// ---------------------------------------------------------------------------------------------
+// For every (mh, nh) displacement-component pair the u-u block is
+//   K[(ms,mh),(ns,nh)] = sum_{g,zeta} A[(mh,nh,ms)][(g,zeta)] G[(g,zeta)][ns],
+//   A[(mh,nh,ms)][(g,zeta)] = sum_xi G[(g,xi)][ms] D_g[(mh,nh)][xi][zeta],
+// i.e. one 243 x 81 by 81 x 27 product per element.  A is formed on the CUDA cores (FP32) straight
+// into shared memory in the tensor cores' operand layout; the product runs as two M = 128 halves of
+// tcgen05.mma kind::tf32 (N = 32, K = 88 in 11 steps of 8) accumulating in tensor memory.  With
+// SPLIT3 each operand is split into a TF32 head and a TF32 tail and the three products
+// hi*hi + lo*hi + hi*lo recover about FP32 accuracy; without it the contraction is plain TF32
+// (about 1e-3 relative).  u-p / p-u blocks, Iron's lower-triangle mirror and the scatter through the
+// slot map are as in mr_contract_kernel.
+constexpr int kTCThreads = 256;
+constexpr int kTK = 88;                        // K = 27 Gauss points x 3, padded to 11 steps of 8
+constexpr int kTKC = kTK / 4;                  // core-matrix columns along K (4 TF32 = 16 bytes)
+constexpr int kTABytes = 16 * kTKC * 128;      // one M = 128 operand tile
+constexpr int kTBBytes = 4 * kTKC * 128;       // the N = 32 operand
+constexpr uint32_t kTLbo = 128, kTSbo = kTKC * 128;
+constexpr int kTKRow = 33;                     // padded row of the staged product (no bank conflicts)
+constexpr uint32_t kTWaitPolls = 1u << 24;     // bounded mbarrier wait
+
+struct __align__(128) TCShared {
+  unsigned char A[2][kTABytes];  // head, tail of the current M half
+  unsigned char B[2][kTBBytes];  // G head, tail: B[ns][(g,zeta)]
+  float G[81][28];               // G[(g,xi)][ms]
+  float psi[NG][NL];
+  float Dg[NG][kGPOut];
+  float K[256][kTKRow];          // product rows (mh,nh,ms), columns ns
+  float HvG[NG][81];
+  float PvG[NG][81];
+  uint64_t mbar;
+  uint32_t tmem;
+  int abort;
+};
+
+// byte offset of element (row, k) in a no-swizzle K-major operand with kTKC core columns
+__device__ __forceinline__ uint32_t tc_offset(int row, int k) {
+  return (uint32_t)((((row >> 3) * kTKC + (k >> 2)) * 8 + (row & 7)) * 16 + (k & 3) * 4);
+}
+
+template <bool EXACT, bool SPLIT3>
+__global__ void __launch_bounds__(kTCThreads, 1)
+mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Tables* __restrict__ Tg,
+                      const float* __restrict__ gp, const int32_t* __restrict__ slots, double* __restrict__ values,
+                      double* __restrict__ Kout, unsigned* err) {
+  extern __shared__ __align__(1024) unsigned char traw[];
+  TCShared& S = *reinterpret_cast<TCShared*>(traw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // constant operands: G (FP32, for forming A) and B = G^T split into TF32 head / tail
+  for (int t = tid; t < 81 * 27; t += blockDim.x) {
+    const int k = t / 27, ms = t % 27;
+    S.G[k][ms] = (float)Tg->dphi[k / 3][k % 3][ms];
+  }
+  for (int t = tid; t < NG * NL; t += blockDim.x) S.psi[t / NL][t % NL] = (float)Tg->psi[t / NL][t % NL];
+  for (int t = tid; t < 32 * kTK; t += blockDim.x) {
+    const int n = t / kTK, k = t % kTK;
+    const float v = (n < 27 && k < 81) ? (float)Tg->dphi[k / 3][k % 3][n] : 0.0f;
+    const float hi = tc::to_tf32(v);
+    *reinterpret_cast<float*>(S.B[0] + tc_offset(n, k)) = hi;
+    *reinterpret_cast<float*>(S.B[1] + tc_offset(n, k)) = tc::to_tf32(v - hi);
+  }
+  if (warp == 0) tc::tmem_alloc(&S.tmem, 64);
+  if (tid == 0) {
+    tc::mbar_init(&S.mbar, 1);
+    S.abort = 0;
+  }
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = S.tmem;
+  constexpr uint32_t idesc = tc::idesc_tf32(128, 32);
+  const uint32_t a_hi = tc::smem_u32(S.A[0]), a_lo = tc::smem_u32(S.A[1]);
+  const uint32_t b_hi = tc::smem_u32(S.B[0]), b_lo = tc::smem_u32(S.B[1]);
+  uint32_t parity = 0;
+
+  for (int item = blockIdx.x; item < count; item += gridDim.x) {
+    __syncthreads();
+    const float* src = gp + (size_t)item * NG * kGPOut;
+    for (int t = tid; t < NG * kGPOut; t += blockDim.x) (&S.Dg[0][0])[t] = src[t];
+    __syncthreads();
+    for (int t = tid; t < 2 * NG * 81; t += blockDim.x) {
+      const int which = t / (NG * 81), r = t % (NG * 81), g = r / 81, c = r % 81, h = c / 27, s = c % 27;
+      const int off = which == 0 ? 81 : 90;
+      const float v = S.G[g * 3 + 0][s] * S.Dg[g][off + 0 * 3 + h] + S.G[g * 3 + 1][s] * S.Dg[g][off + 1 * 3 + h] +
+                      S.G[g * 3 + 2][s] * S.Dg[g][off + 2 * 3 + h];
+      if (which == 0) S.HvG[g][c] = v; else S.PvG[g][c] = v;
+    }
+    for (int half = 0; half < 2; ++half) {
+      // A rows [128 half, 128 half + 128): one core matrix (8 rows x 4 k) per warp step, so each
+      // warp writes 128 contiguous bytes
+      for (int cm = warp; cm < 16 * kTKC; cm += kTCThreads / 32) {
+        const int rg = cm / kTKC, kc = cm % kTKC;
+        const int row = half * 128 + rg * 8 + (lane >> 2), k = kc * 4 + (lane & 3);
+        float v = 0.0f;
+        if (row < 243 && k < 81) {
+          const int pair = row / 27, ms = row % 27, g = k / 3, zeta = k % 3;
+          const float* D = &S.Dg[g][pair * 9 + zeta];
+          v = S.G[g * 3 + 0][ms] * D[0] + S.G[g * 3 + 1][ms] * D[3] + S.G[g * 3 + 2][ms] * D[6];
+        }
+        const float hi = tc::to_tf32(v);
+        const uint32_t o = (uint32_t)(cm * 128 + lane * 4);
+        *reinterpret_cast<float*>(S.A[0] + o) = hi;
+        if (SPLIT3) *reinterpret_cast<float*>(S.A[1] + o) = tc::to_tf32(v - hi);
+      }
+      tc::fence_proxy_async();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        const uint32_t d = tmem + (uint32_t)(half * 32);
+#pragma unroll 1
+        for (int s = 0; s < kTK / 8; ++s) {
+          const uint32_t ko = (uint32_t)(s * 256);
+          tc::mma_tf32(d, tc::smem_desc(a_hi + ko, kTLbo, kTSbo), tc::smem_desc(b_hi + ko, kTLbo, kTSbo), idesc,
+                       s > 0 ? 1u : 0u);
+          if (SPLIT3) {
+            tc::mma_tf32(d, tc::smem_desc(a_lo + ko, kTLbo, kTSbo), tc::smem_desc(b_hi + ko, kTLbo, kTSbo), idesc, 1u);
+            tc::mma_tf32(d, tc::smem_desc(a_hi + ko, kTLbo, kTSbo), tc::smem_desc(b_lo + ko, kTLbo, kTSbo), idesc, 1u);
+          }
+        }
+        tc::commit(&S.mbar);
+      }
+      // the A tile is rewritten by the next half: wait for this half's products
+      if (!tc::mbar_wait(&S.mbar, parity, kTWaitPolls)) {
+        gfe_raise(err, GFE_DEVERR_TIMEOUT);
+        S.abort = 1;
+      }
+      parity ^= 1u;
+      tc::fence_after_sync();
+      __syncthreads();
+      if (S.abort) break;
+    }
+    if (S.abort) break;
+    // tensor memory -> staged product: warp w reads lanes 32 (w % 4) .. of half w / 4
+    {
+      const int half = warp >> 2, q = warp & 3;
+      float v[32];
+      tc::tmem_ld_32x32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(half * 32), v);
+      const int row = half * 128 + q * 32 + lane;
+#pragma unroll
+      for (int n = 0; n < 27; ++n) S.K[row][n] = v[n];
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
+    const int e = Kout ? __ldg(elems + item) : 0;
+    for (int k = tid; k < ND * ND; k += blockDim.x) {
+      const int r = k / ND, c = k % ND;
+      float v;
+      if (r < 81 && c < 81) {
+        const int rr = (EXACT || r >= c) ? r : c, cc = (EXACT || r >= c) ? c : r;  // Iron mirrors the lower triangle
+        const int mh = rr / 27, ms = rr % 27, nh = cc / 27, ns = cc % 27;
+        v = S.K[(mh * 3 + nh) * 27 + ms][ns];
+      } else if (r < 81) {
+        float s = 0.0f;
+        for (int g = 0; g < NG; ++g) s += S.HvG[g][r] * S.psi[g][c - 81];
+        v = s;
+      } else if (c < 81) {
+        float s = 0.0f;
+        for (int g = 0; g < NG; ++g) s += S.psi[g][r - 81] * S.PvG[g][c];
+        v = s;
+      } else {
+        v = 0.0f;
+      }
+      if (Kout) Kout[(size_t)e * ND * ND + k] = (double)v;
+      if (sl && !(r >= 81 && c >= 81)) {
+        const int pos = __ldg(sl + k);
+        if (pos < 0) gfe_raise(err, GFE_DEVERR_SLOT);
+        else values[pos] += (double)v;
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+}
+
 size_t vjp_smem() { return sizeof(Tables) + sizeof(TanShared) + sizeof(double) * (ND + NG * 9 + NG + NG * 2); }
 
 size_t residual_smem() { return sizeof(Tables) + kResWarps * sizeof(double) * (81 + 81 + 8 + NG * 9 + NG + 48); }
@@ -1059,11 +1238,18 @@ namespace {
 // contraction precision `precision`, assembled into CSR values through the slot map and/or written
 // as dense element matrices.  Per colour: the Gauss-point kernel fills a scratch array, the
 // contraction kernel consumes it.
+template <bool EXACT, bool SPLIT3>
+void launch_contract_tc(int grid, cudaStream_t s, const int32_t* elems, int cnt, const Tables* T, const float* gp,
+                        const int32_t* sl, double* values, double* K_out, unsigned* err) {
+  mr_contract_tc_kernel<EXACT, SPLIT3><<<grid, kTCThreads, sizeof(TCShared), s>>>(elems, cnt, T, gp, sl, values,
+                                                                                 K_out, err);
+}
+
 template <typename TS>
 int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, const double* xg,
                   const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors, const double* dep,
                   const double* cpar, const int32_t* slots, double* values, int64_t nnz, double* K_out,
-                  cudaStream_t s, const char* fn) {
+                  cudaStream_t s, const char* fn, int tc_mode = 0) {
   const Tables* T = nullptr;
   int rc = device_tables(&T);
   if (rc) return rc;
@@ -1082,6 +1268,15 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
     gfe::scratch_free(gpbuf, s);
     return rc;
   }
+  if (tc_mode) {
+    const void* tk[4] = {(const void*)mr_contract_tc_kernel<false, false>, (const void*)mr_contract_tc_kernel<false, true>,
+                         (const void*)mr_contract_tc_kernel<true, false>, (const void*)mr_contract_tc_kernel<true, true>};
+    for (const void* k : tk)
+      if ((rc = set_smem(k, sizeof(TCShared)))) {
+        gfe::scratch_free(gpbuf, s);
+        return rc;
+      }
+  }
   unsigned* err = gfe::device_error_word();
   void* prof = gfe::stage_begin(GFE_STAGE_MR_JACOBIAN, s);
   int launches = 0;
@@ -1091,7 +1286,26 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
     const int ggrid = (cnt + kGPElems - 1) / kGPElems;
     const int cgrid = std::min(cnt, 8 * gfe::sm_count());
     const int32_t* sl = slots ? slots + (size_t)c0 * ND * ND : nullptr;
-    if (mode == 0) {
+    if (tc_mode) {
+      // TS is float here: the Gauss-point coefficients feed the tensor-core contraction
+      const float* gpf = reinterpret_cast<const float*>(gpbuf);
+      const int tgrid = std::min(cnt, gfe::sm_count());
+      if (mode == 0) {
+        mr_gp_kernel<TS, false><<<ggrid, kGPThreads, gsm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar,
+                                                               T, gpbuf, err);
+        if (tc_mode == GFE_TC_TF32X3)
+          launch_contract_tc<false, true>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
+        else
+          launch_contract_tc<false, false>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
+      } else {
+        mr_gp_kernel<TS, true><<<ggrid, kGPThreads, gsm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar,
+                                                              T, gpbuf, err);
+        if (tc_mode == GFE_TC_TF32X3)
+          launch_contract_tc<true, true>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
+        else
+          launch_contract_tc<true, false>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
+      }
+    } else if (mode == 0) {
       mr_gp_kernel<TS, false><<<ggrid, kGPThreads, gsm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar, T,
                                                              gpbuf, err);
       mr_contract_kernel<TS, false><<<cgrid, kCThreads, csm, s>>>(color_elems + c0, cnt, T, gpbuf, sl, values,
@@ -1122,14 +1336,14 @@ int jacobian_entry_point(int mode, int32_t n_elem, const int32_t* eq2, const int
   if (!K_out && (!slots || !values)) return gfe::set_error(GFE_ERR_ARG, "%s: need CSR values + slots or K_out", fn);
   if (color_ptr_host[0] != 0 || color_ptr_host[n_colors] != n_elem)
     return gfe::set_error(GFE_ERR_ARG, "%s: colour offsets must run from 0 to n_elem", fn);
-  if (precision != GFE_FP64 && precision != GFE_MIXED)
-    return gfe::set_error(GFE_ERR_ARG, "%s: precision must be GFE_FP64 or GFE_MIXED", fn);
+  if (precision != GFE_FP64 && precision != GFE_MIXED && precision != GFE_TC_TF32X3 && precision != GFE_TC_TF32)
+    return gfe::set_error(GFE_ERR_ARG, "%s: precision must be GFE_FP64, GFE_MIXED, GFE_TC_TF32X3 or GFE_TC_TF32", fn);
   cudaStream_t s = gfe::as_stream(stream);
   if (precision == GFE_FP64)
     return jacobian_impl<double>(mode, n_elem, eq2, elin, nq2, xg, color_elems, color_ptr_host, n_colors, dep, cpar,
                                  slots, values, nnz, K_out, s, fn);
   return jacobian_impl<float>(mode, n_elem, eq2, elin, nq2, xg, color_elems, color_ptr_host, n_colors, dep, cpar,
-                              slots, values, nnz, K_out, s, fn);
+                              slots, values, nnz, K_out, s, fn, precision == GFE_MIXED ? 0 : precision);
 }
 
 }  // namespace

@@ -21,6 +21,9 @@ from ._lib import GfeError
 from .laplace import csr_structure
 from .mesh import RegularMesh, linear_component
 
+# tensor-core contraction of the Jacobian (tcgen05 kind::tf32): three-pass split / one pass
+GFE_TC_TF32X3, GFE_TC_TF32 = 3, 4
+
 
 class MooneyRivlinAssembly:
     def __init__(self, eq2, elin, xg, colour_elems, colour_ptr, n_lin: int, device=None, build_jacobian=True):
@@ -97,7 +100,7 @@ class MooneyRivlinAssembly:
         return R
 
     def _element_jacobians(self, fn: str, dep, c, precision: str, dense: bool, stream, check: bool):
-        prec = {"fp64": _lib.GFE_FP64, "mixed": _lib.GFE_MIXED}[precision]
+        prec = {"fp64": _lib.GFE_FP64, "mixed": _lib.GFE_MIXED, "tf32x3": GFE_TC_TF32X3, "tf32": GFE_TC_TF32}[precision]
         if not dense and self.slots is None:
             self.build_structure(stream)
         dep = dep.to(self.device, torch.float64).contiguous()
@@ -115,7 +118,8 @@ class MooneyRivlinAssembly:
 
     def jacobian(self, dep: torch.Tensor, c, precision: str = "fp64", stream=None, check=True) -> torch.Tensor:
         """Iron's analytic Jacobian assembled into the CSR values (self.values).  precision 'mixed'
-        runs the basis-gradient contraction in FP32 (kinematics and assembled values in FP64)."""
+        runs the basis-gradient contraction in FP32 on the CUDA cores, 'tf32x3' / 'tf32' on the
+        tensor cores (kinematics and assembled values in FP64 in every mode)."""
         return self._element_jacobians("gfe_mr_jacobian", dep, c, precision, False, stream, check)
 
     def element_jacobians(self, dep: torch.Tensor, c, precision: str = "fp64", stream=None) -> torch.Tensor:

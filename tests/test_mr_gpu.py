@@ -57,10 +57,11 @@ def test_undeformed_residual_zero(gfe_cuda):
     assert np.abs(R).max() < 1e-13
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 2e-5)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 2e-5), ("tf32x3", 2e-5), ("tf32", 4e-3)])
 def test_element_jacobians_match_oracle(gfe_cuda, precision, tol):
     """Iron's analytic element Jacobian; 'mixed' = FP32 basis-gradient contraction (FP64 kinematics),
-    tolerance 2e-5 x max|K|."""
+    'tf32x3' / 'tf32' = the contraction on the tensor cores (three-pass split / one TF32 pass);
+    tolerances relative to max|K|."""
     A = MooneyRivlinAssembly.from_regular_mesh((2, 2, 1), build_jacobian=False)
     dep = _state(A, 1)
     K = A.element_jacobians(torch.from_numpy(dep).cuda(), [C1, C2], precision=precision).cpu().numpy()
@@ -111,3 +112,15 @@ def test_slot_map_beyond_2pow30_entries(gfe_cuda):
                 assert sl[r, c] == pos, (item, r, c)
     del A
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("precision,tol", [("tf32x3", 2e-5), ("tf32", 4e-3)])
+def test_tensor_core_assembly_matches_fp64(gfe_cuda, precision, tol):
+    """CSR assembly (slot-map scatter) of the analytic Jacobian and the consistent tangent with the
+    tensor-core contraction against the FP64 contraction, on a mesh with several elements per colour."""
+    A = MooneyRivlinAssembly.from_regular_mesh((5, 4, 3))
+    dep = torch.from_numpy(_state(A, 4)).cuda()
+    for fn in ("jacobian", "tangent"):
+        ref = getattr(A, fn)(dep, [C1, C2], precision="fp64").clone()
+        got = getattr(A, fn)(dep, [C1, C2], precision=precision)
+        assert (got - ref).abs().max().item() <= tol * ref.abs().max().item(), fn
