@@ -145,14 +145,19 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic_per_unit():
-    """DRAM bytes per element of the colour kernel from the committed ncu summary, if present."""
-    p = ROOT / "profiles" / "laplace_assemble_color_traffic.txt"
+def profile_traffic_per_unit(kernel: str):
+    """DRAM bytes (read + write) per element of `kernel` (e.g. "laplace_regular_kernel<f2>") from
+    the committed ncu summary profiles/laplace_kernels_traffic.txt, if it lists the kernel."""
+    p = ROOT / "profiles" / "laplace_kernels_traffic.txt"
     if not p.exists():
         return None
     for ln in p.read_text().splitlines():
-        if ln.startswith("dram_bytes_per_element:"):
-            return float(ln.split(":", 1)[1])
+        parts = ln.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
     return None
 
 
@@ -267,19 +272,31 @@ def run_gfe(args):
     vals_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
     e2e = {}
     for prec in precisions:
+        # the regular-mesh precisions use the slab pipeline (device-to-host copies overlap the
+        # next slab's assembly); the colour-scatter FP64 assembly copies after the whole matrix
+        pipelined = A.regular is not None and (path == "regular" or (path == "auto" and prec != "fp64"))
         for i in range(args.warmup + args.steps):
             if i == args.warmup:
                 torch.cuda.synchronize()
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-            A.coords.copy_(coords_h, non_blocking=True)
-            A.kappa.copy_(kappa_h, non_blocking=True)
-            A.assemble(prec, check=False, path=path)
-            vals_h.copy_(A.values, non_blocking=True)
+            if pipelined:
+                A.assemble_to_host(vals_h, prec, coords_host=coords_h, kappa_host=kappa_h, stream=stream)
+            else:
+                A.coords.copy_(coords_h, non_blocking=True)
+                A.kappa.copy_(kappa_h, non_blocking=True)
+                A.assemble(prec, check=False, path=path)
+                vals_h.copy_(A.values, non_blocking=True)
         e1.record(stream)
         torch.cuda.synchronize()
         e2e[prec] = e0.elapsed_time(e1) / args.steps
+        if pipelined:
+            # the host copy equals the device-resident assembly of the same precision
+            A.assemble(prec, check=False, path=path)
+            torch.cuda.synchronize()
+            if not torch.equal(vals_h, A.values.cpu()):
+                raise RuntimeError(f"slab-pipelined host values differ from the device assembly ({prec})")
     _lib.raise_device_errors("bench e2e")
     h2d = int(coords_h.numel() * 8 + kappa_h.numel() * 8)
     d2h = int(nnz * 8)
@@ -331,7 +348,9 @@ def run_gfe(args):
     bytes_per_elem = algorithmic_bytes(E, N, nnz) / E
     achieved = bytes_per_elem * units_per_launch / (per_launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    tpu = profile_traffic_per_unit()
+    kname = ("laplace_regular_kernel" if used_path == "regular" else "laplace_assemble_color") + \
+        "<%s>" % {"fp64": "double", "mixed_df": "f2", "mixed": "float"}[head]
+    tpu = profile_traffic_per_unit(kname)
     line = {
         "metric": "assembled_elements_per_s", "value": value, "unit": "elements/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": T["ms_per_step"], "higher_is_better": True,
@@ -351,9 +370,7 @@ def run_gfe(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": peak_kind,
                      "traffic": None if tpu is None else tpu * units_per_launch,
-                     "kernel": ("laplace_regular_kernel" if used_path == "regular"
-                                else "laplace_assemble_color") + "<%s>" % {"fp64": "double", "mixed_df": "f2",
-                                                                          "mixed": "float"}[head],
+                     "kernel": kname,
                      "per_launch_ms": per_launch_ms, "units_per_launch": units_per_launch,
                      "algorithmic_bytes_per_element": bytes_per_elem},
         "precisions": {p: {"ms_per_step": timings[p]["ms_per_step"],

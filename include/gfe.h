@@ -149,6 +149,16 @@ int gfe_laplace_assemble_regular_ws(int32_t nx, int32_t ny, int32_t nz, const do
                                     const int32_t* row_ptr, double* values, float* values32, double* rhs,
                                     int32_t precision, void* workspace, void* stream);
 
+/* The rows of node layers [layer_begin, layer_end) only (layer = node index along xi3; layer_begin a
+ * multiple of 8): those rows form one contiguous range of the CSR values, so an assembly split into
+ * layer slabs can copy each slab's values to the host while the next slab computes.
+ * convert_coords: convert the coordinates into the workspace first (needed in the first call of an
+ * assembly; later calls of the same assembly pass 0 and reuse it; requires a workspace). */
+int gfe_laplace_assemble_regular_layers(int32_t nx, int32_t ny, int32_t nz, const double* coords, const double* kappa,
+                                        const int32_t* row_ptr, double* values, float* values32, double* rhs,
+                                        int32_t precision, void* workspace, int32_t layer_begin, int32_t layer_end,
+                                        int32_t convert_coords, void* stream);
+
 /* Number of CSR rows/entries that differ from the clipped 27-point stencil of the regular mesh
  * (0 = the structure is the one gfe_laplace_assemble_regular writes).  Synchronises `stream`. */
 int gfe_laplace_regular_check(int32_t nx, int32_t ny, int32_t nz, const int32_t* row_ptr, const int32_t* col_idx,

@@ -60,6 +60,8 @@ SIGNATURES = {
     "gfe_laplace_assemble_regular": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp]),
     "gfe_laplace_regular_workspace_bytes": (C.c_int64, [i32, i32, i32, i32]),
     "gfe_laplace_assemble_regular_ws": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp, vp]),
+    "gfe_laplace_assemble_regular_layers": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp, i32, i32, i32,
+                                                      vp]),
     "gfe_laplace_regular_check": (C.c_int, [i32, i32, i32, vp, vp, C.POINTER(C.c_int64), vp]),
     "gfe_csr_spmv": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "gfe_mr_residual": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp]),

@@ -358,15 +358,17 @@ template <typename T>
 __global__ void __launch_bounds__(kRThreads)
 laplace_regular_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ coords,
                        const double* __restrict__ kappa, const int32_t* __restrict__ rp, double* __restrict__ values,
-                       float* __restrict__ values32, double* __restrict__ rhs, unsigned* err) {
+                       float* __restrict__ values32, double* __restrict__ rhs, unsigned* err,
+                       int32_t layer0 = 0, int32_t layer_end = 0x7fffffff) {
   using S = typename StoreOf<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S(*sK)[36][kRThreads] = reinterpret_cast<S(*)[36][kRThreads]>(smem_raw);  // [layer buffer][entry][element]
   const int tid = threadIdx.x;
-  const int x0 = blockIdx.x * kRTX, y0 = blockIdx.y * kRTY, k0 = blockIdx.z * kRZ;
+  // node layers [layer0, layer_end) of the mesh; layer0 is a multiple of kRZ
+  const int x0 = blockIdx.x * kRTX, y0 = blockIdx.y * kRTY, k0 = layer0 + blockIdx.z * kRZ;
   const int NX = nx + 1, NY = ny + 1, NZ = nz + 1;
   const long long NXY = (long long)NX * NY;
-  const int k1 = min(k0 + kRZ, NZ);
+  const int k1 = min(min(k0 + kRZ, NZ), layer_end);
   // element owned by this thread in each element layer
   const int ex = x0 - 1 + (tid % kREX), ey = y0 - 1 + (tid / kREX);
   const bool e_in_xy = ex >= 0 && ex < nx && ey >= 0 && ey < ny;
@@ -521,11 +523,13 @@ size_t regular_workspace_bytes(int32_t nx, int32_t ny, int32_t nz, int precision
   return n3 * (precision == GFE_MIXED ? sizeof(float) : sizeof(f2));
 }
 
-// ws: caller workspace of regular_workspace_bytes(), or NULL to allocate it on the stream
+// Node layers [l0, l1) (l0 a multiple of kRZ).  ws: caller workspace of regular_workspace_bytes(),
+// or NULL to allocate it on the stream; split: convert the coordinates into it first (the later
+// layer calls of one assembly reuse the converted array).
 template <typename T>
 int launch_regular(dim3 grid, cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const double* coords,
                    const double* kappa, const int32_t* rp, double* values, float* values32, double* rhs,
-                   unsigned* err, void* ws) {
+                   unsigned* err, void* ws, int32_t l0, int32_t l1, bool split) {
   const size_t smem = 2 * 36 * kRThreads * sizeof(typename StoreOf<T>::type);
   GFE_CUDA_TRY(cudaFuncSetAttribute((const void*)laplace_regular_kernel<T>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -533,8 +537,9 @@ int launch_regular(dim3 grid, cudaStream_t s, int32_t nx, int32_t ny, int32_t nz
   T* ct = static_cast<T*>(ws);
   if (!ct)
     if (int rc = gfe::scratch_alloc((void**)&ct, sizeof(T) * n3, s, "split coordinates")) return rc;
-  split_coords<T><<<4 * gfe::sm_count(), 256, 0, s>>>(n3, coords, ct);
-  laplace_regular_kernel<T><<<grid, kRThreads, smem, s>>>(nx, ny, nz, ct, kappa, rp, values, values32, rhs, err);
+  if (split || !ws) split_coords<T><<<4 * gfe::sm_count(), 256, 0, s>>>(n3, coords, ct);
+  laplace_regular_kernel<T><<<grid, kRThreads, smem, s>>>(nx, ny, nz, ct, kappa, rp, values, values32, rhs, err, l0,
+                                                           l1);
   if (!ws) gfe::scratch_free(ct, s);
   return GFE_OK;
 }
@@ -542,12 +547,12 @@ int launch_regular(dim3 grid, cudaStream_t s, int32_t nx, int32_t ny, int32_t nz
 template <>
 int launch_regular<double>(dim3 grid, cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const double* coords,
                            const double* kappa, const int32_t* rp, double* values, float* values32, double* rhs,
-                           unsigned* err, void*) {
+                           unsigned* err, void*, int32_t l0, int32_t l1, bool) {
   const size_t smem = 2 * 36 * kRThreads * sizeof(double);
   GFE_CUDA_TRY(cudaFuncSetAttribute((const void*)laplace_regular_kernel<double>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   laplace_regular_kernel<double><<<grid, kRThreads, smem, s>>>(nx, ny, nz, coords, kappa, rp, values, values32, rhs,
-                                                               err);
+                                                               err, l0, l1);
   return GFE_OK;
 }
 
@@ -617,23 +622,42 @@ extern "C" int gfe_laplace_assemble_regular_ws(int32_t nx, int32_t ny, int32_t n
                                                const double* kappa, const int32_t* row_ptr, double* values,
                                                float* values32, double* rhs, int32_t precision, void* workspace,
                                                void* stream) {
+  return gfe_laplace_assemble_regular_layers(nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, precision,
+                                             workspace, 0, nz + 1, 1, stream);
+}
+
+extern "C" int gfe_laplace_assemble_regular_layers(int32_t nx, int32_t ny, int32_t nz, const double* coords,
+                                                   const double* kappa, const int32_t* row_ptr, double* values,
+                                                   float* values32, double* rhs, int32_t precision, void* workspace,
+                                                   int32_t layer_begin, int32_t layer_end, int32_t convert_coords,
+                                                   void* stream) {
   const char* fn = "gfe_laplace_assemble_regular";
   if (nx <= 0 || ny <= 0 || nz <= 0 || !coords || !row_ptr || !values)
     return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
   if (int rc = check_precision(precision, fn)) return rc;
   if (workspace && (reinterpret_cast<uintptr_t>(workspace) & 15))
     return gfe::set_error(GFE_ERR_ARG, "%s: workspace must be 16-byte aligned", fn);
+  if (layer_begin < 0 || layer_end > nz + 1 || layer_begin >= layer_end || layer_begin % kRZ != 0)
+    return gfe::set_error(GFE_ERR_ARG, "%s: node layers [%d, %d) must lie in [0, %d) and start at a multiple of %d",
+                          fn, layer_begin, layer_end, nz + 1, kRZ);
+  if (!workspace && !convert_coords)
+    return gfe::set_error(GFE_ERR_ARG, "%s: without a workspace the coordinates are converted every call", fn);
   cudaStream_t s = gfe::as_stream(stream);
   unsigned* err = gfe::device_error_word();
-  const dim3 grid((nx + 1 + kRTX - 1) / kRTX, (ny + 1 + kRTY - 1) / kRTY, (nz + 1 + kRZ - 1) / kRZ);
+  const dim3 grid((nx + 1 + kRTX - 1) / kRTX, (ny + 1 + kRTY - 1) / kRTY, (layer_end - layer_begin + kRZ - 1) / kRZ);
   void* prof = gfe::stage_begin(GFE_STAGE_LAPLACE_ELEMENTS, s);
   int rc;
+  const int32_t l0 = layer_begin, l1 = layer_end;
+  const bool cv = convert_coords != 0;
   if (precision == GFE_FP64)
-    rc = launch_regular<double>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace);
+    rc = launch_regular<double>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace,
+                                l0, l1, cv);
   else if (precision == GFE_MIXED)
-    rc = launch_regular<float>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace);
+    rc = launch_regular<float>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace,
+                               l0, l1, cv);
   else
-    rc = launch_regular<f2>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace);
+    rc = launch_regular<f2>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace, l0,
+                            l1, cv);
   gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, 1);
   if (rc) return rc;
   GFE_LAUNCH_CHECK(fn);

@@ -889,6 +889,38 @@ mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __
 constexpr int kCThreads = 256;
 
 // shared layout of mr_contract_kernel (in units of TS)
+// Adds one element's 89 x 89 matrix into the CSR values through its slot-map row block (and/or
+// writes it densely to Kout_e).  val(r, c) gives entry (r, c).  Positions within one element are
+// distinct, so each thread first reads kBatch slots and old values and then writes them all back:
+// kBatch independent read-modify-writes in flight instead of a chain of dependent ones.
+template <int kBatch, typename F>
+__device__ __forceinline__ void scatter_element(const int32_t* __restrict__ sl, double* __restrict__ values,
+                                                double* __restrict__ Kout_e, F val, unsigned* err) {
+  for (int k0 = threadIdx.x; k0 < ND * ND; k0 += kBatch * blockDim.x) {
+    int pos[kBatch];
+    double v[kBatch], old[kBatch];
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int k = k0 + j * blockDim.x;
+      pos[j] = -2;  // nothing to add
+      v[j] = 0.0;
+      if (k < ND * ND) {
+        const int r = k / ND, c = k % ND;
+        v[j] = (double)val(r, c);
+        if (Kout_e) Kout_e[k] = v[j];
+        if (sl && !(r >= 81 && c >= 81)) pos[j] = __ldg(sl + k);  // -1: absent from the structure
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) old[j] = pos[j] >= 0 ? values[pos[j]] : 0.0;
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      if (pos[j] >= 0) values[pos[j]] = old[j] + v[j];
+      else if (pos[j] == -1) gfe_raise(err, GFE_DEVERR_SLOT);
+    }
+  }
+}
+
 template <typename TS>
 struct ContractShared {
   TS G[81][28];        // G[(g,xi)][ms] (padded row)
@@ -961,30 +993,17 @@ mr_contract_kernel(const int32_t* __restrict__ elems, int32_t count, const Table
     __syncthreads();
     TS(*Kuu)[81] = S.Kuu;
     const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
-    const int e = Kout ? __ldg(elems + item) : 0;
-    for (int k = tid; k < ND * ND; k += blockDim.x) {
-      const int r = k / ND, c = k % ND;
-      TS v;
-      if (r < 81 && c < 81) {
-        v = (EXACT || r >= c) ? Kuu[r][c] : Kuu[c][r];  // Iron mirrors the lower u-u triangle
-      } else if (r < 81) {  // u rows, p columns
-        TS s = TS(0);
+    double* Ke = Kout ? Kout + (size_t)__ldg(elems + item) * ND * ND : nullptr;
+    scatter_element<8>(sl, values, Ke, [&](int r, int c) -> TS {
+      if (r < 81 && c < 81) return (EXACT || r >= c) ? Kuu[r][c] : Kuu[c][r];  // Iron mirrors the lower u-u triangle
+      TS s = TS(0);
+      if (r < 81) {  // u rows, p columns
         for (int g = 0; g < NG; ++g) s += S.HvG[g][r] * S.psi[g][c - 81];
-        v = s;
       } else if (c < 81) {  // p rows, u columns
-        TS s = TS(0);
         for (int g = 0; g < NG; ++g) s += S.psi[g][r - 81] * S.PvG[g][c];
-        v = s;
-      } else {
-        v = TS(0);
       }
-      if (Kout) Kout[(size_t)e * ND * ND + k] = (double)v;
-      if (sl && !(r >= 81 && c >= 81)) {
-        const int pos = __ldg(sl + k);
-        if (pos < 0) gfe_raise(err, GFE_DEVERR_SLOT);
-        else values[pos] += (double)v;
-      }
-    }
+      return s;
+    }, err);
   }
 }
 
@@ -1134,32 +1153,20 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
     tc::fence_before_sync();
     __syncthreads();
     const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
-    const int e = Kout ? __ldg(elems + item) : 0;
-    for (int k = tid; k < ND * ND; k += blockDim.x) {
-      const int r = k / ND, c = k % ND;
-      float v;
+    double* Ke = Kout ? Kout + (size_t)__ldg(elems + item) * ND * ND : nullptr;
+    scatter_element<8>(sl, values, Ke, [&](int r, int c) -> float {
       if (r < 81 && c < 81) {
         const int rr = (EXACT || r >= c) ? r : c, cc = (EXACT || r >= c) ? c : r;  // Iron mirrors the lower triangle
-        const int mh = rr / 27, ms = rr % 27, nh = cc / 27, ns = cc % 27;
-        v = S.K[(mh * 3 + nh) * 27 + ms][ns];
-      } else if (r < 81) {
-        float s = 0.0f;
+        return S.K[(rr / 27 * 3 + cc / 27) * 27 + rr % 27][cc % 27];
+      }
+      float s = 0.0f;
+      if (r < 81) {
         for (int g = 0; g < NG; ++g) s += S.HvG[g][r] * S.psi[g][c - 81];
-        v = s;
       } else if (c < 81) {
-        float s = 0.0f;
         for (int g = 0; g < NG; ++g) s += S.psi[g][r - 81] * S.PvG[g][c];
-        v = s;
-      } else {
-        v = 0.0f;
       }
-      if (Kout) Kout[(size_t)e * ND * ND + k] = (double)v;
-      if (sl && !(r >= 81 && c >= 81)) {
-        const int pos = __ldg(sl + k);
-        if (pos < 0) gfe_raise(err, GFE_DEVERR_SLOT);
-        else values[pos] += (double)v;
-      }
-    }
+      return s;
+    }, err);
   }
   tc::fence_before_sync();
   __syncthreads();

@@ -133,6 +133,58 @@ class LaplaceAssembly:
             _lib.raise_device_errors("gfe_laplace_assemble", stream)
         return self.values
 
+    def assemble_to_host(self, values_host: torch.Tensor, precision: str = "mixed_df", coords_host=None,
+                         kappa_host=None, slabs: int | None = None, stream=None) -> torch.Tensor:
+        """End-to-end assembly with host buffers on Iron's regular generated mesh: copy the geometry
+        and conductivity in (pinned host tensors, optional), assemble in node-layer slabs, and copy
+        each slab's CSR values (one contiguous range) to values_host (pinned float64 [nnz]) on a
+        second stream while the next slab computes.  slabs: number of slabs (default: slabs of 16
+        node layers, two of the kernel's 8-layer blocks, which measured best at 128^3).  Returns
+        values_host; the copies are ordered before later work on `stream`."""
+        if self.regular is None:
+            raise GfeError(-1, "the slab pipeline needs Iron's regular generated mesh")
+        if values_host.numel() != self.nnz or values_host.dtype != torch.float64 or values_host.is_cuda:
+            raise GfeError(-1, f"values_host must be a host float64 tensor of {self.nnz} entries")
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        L = _lib.load()
+        nx, ny, nz = self.regular
+        prec = PRECISIONS[precision]
+        if getattr(self, "_copy_stream", None) is None:
+            self._copy_stream = torch.cuda.Stream(self.device)
+            self._row_ptr_host = self.row_ptr.cpu().numpy()
+        if getattr(self, "_asm_ws_prec", None) != prec:
+            wb = int(L.gfe_laplace_regular_workspace_bytes(nx, ny, nz, prec))
+            self._asm_ws = torch.empty(max(wb, 16), dtype=torch.uint8, device=self.device)
+            self._asm_ws_prec = prec
+        cs = self._copy_stream
+        rp = self._row_ptr_host
+        NZ, NXY = nz + 1, (nx + 1) * (ny + 1)
+        step = 16 if slabs is None else -(-NZ // max(int(slabs), 1))
+        step = -(-step // 8) * 8  # slabs start at multiples of the kernel's 8-layer blocks
+        with torch.cuda.stream(st):
+            if coords_host is not None:
+                self.coords.copy_(coords_host, non_blocking=True)
+            if kappa_host is not None:
+                self.kappa.copy_(kappa_host, non_blocking=True)
+            l0 = 0
+            while l0 < NZ:
+                l1 = min(l0 + step, NZ)
+                _lib.call("gfe_laplace_assemble_regular_layers", nx, ny, nz, _lib.ptr(self.coords),
+                          _lib.ptr(self.kappa), _lib.ptr(self.row_ptr), _lib.ptr(self.values), None,
+                          _lib.ptr(self.rhs), prec, _lib.ptr(self._asm_ws), l0, l1, 1 if l0 == 0 else 0,
+                          _lib.stream_handle(st))
+                ev = torch.cuda.Event()
+                ev.record(st)
+                cs.wait_event(ev)
+                a, b = int(rp[l0 * NXY]) - 1, int(rp[l1 * NXY]) - 1
+                with torch.cuda.stream(cs):
+                    values_host[a:b].copy_(self.values[a:b], non_blocking=True)
+                l0 = l1
+            done = torch.cuda.Event()
+            done.record(cs)
+            st.wait_event(done)
+        return values_host
+
     def element_matrices(self, precision: str = "fp64", stream=None) -> torch.Tensor:
         K = torch.empty((self.n_elements, 8, 8), dtype=torch.float64, device=self.device)
         _lib.call("gfe_laplace_element_matrices", self.n_elements, self.n_nodes, _lib.ptr(self.elem_nodes),

@@ -201,3 +201,20 @@ def test_kappa_solve_fp64_and_mixed(gfe_cuda):
     info2 = A.solve(torch.from_numpy(fixed).cuda(), x2, rtol=1e-12, precision="mixed")
     assert info2.relative_residual <= 1e-12
     assert np.abs(x2.cpu().numpy() - uo).max() <= 1e-10 * np.abs(uo).max(), info2
+
+
+@pytest.mark.parametrize("precision,slabs", [("mixed_df", 3), ("mixed", 1), ("fp64", 4), ("mixed_df", None)])
+def test_slab_pipelined_host_assembly_equals_device(gfe_cuda, precision, slabs):
+    """assemble_to_host (node-layer slabs, device-to-host copies overlapping the next slab) gives
+    exactly the values of the one-shot regular-mesh assembly."""
+    m = _mesh((9, 7, 21), 5)
+    kap = _kappa(m.n_elements, 6)
+    A = LaplaceAssembly.from_regular_mesh(m, kappa=kap)
+    ref = A.assemble(precision, path="regular").cpu().clone()
+    host = torch.zeros(A.nnz, dtype=torch.float64).pin_memory()
+    A.values.zero_()
+    coords_h = torch.from_numpy(m.coords).pin_memory()
+    kappa_h = torch.from_numpy(kap).pin_memory()
+    A.assemble_to_host(host, precision, coords_host=coords_h, kappa_host=kappa_h, slabs=slabs)
+    torch.cuda.synchronize()
+    assert torch.equal(host, ref)
