@@ -153,7 +153,9 @@ int gfe_laplace_assemble_regular_ws(int32_t nx, int32_t ny, int32_t nz, const do
  * multiple of 8): those rows form one contiguous range of the CSR values, so an assembly split into
  * layer slabs can copy each slab's values to the host while the next slab computes.
  * convert_coords: convert the coordinates into the workspace first (needed in the first call of an
- * assembly; later calls of the same assembly pass 0 and reuse it; requires a workspace). */
+ * assembly; later calls of the same assembly pass 0 and reuse it; requires a workspace).  An empty
+ * range (layer_begin == layer_end) with convert_coords only converts, so that slab calls on
+ * several streams can all start once the conversion is done. */
 int gfe_laplace_assemble_regular_layers(int32_t nx, int32_t ny, int32_t nz, const double* coords, const double* kappa,
                                         const int32_t* row_ptr, double* values, float* values32, double* rhs,
                                         int32_t precision, void* workspace, int32_t layer_begin, int32_t layer_end,

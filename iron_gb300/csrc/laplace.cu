@@ -637,12 +637,22 @@ extern "C" int gfe_laplace_assemble_regular_layers(int32_t nx, int32_t ny, int32
   if (int rc = check_precision(precision, fn)) return rc;
   if (workspace && (reinterpret_cast<uintptr_t>(workspace) & 15))
     return gfe::set_error(GFE_ERR_ARG, "%s: workspace must be 16-byte aligned", fn);
-  if (layer_begin < 0 || layer_end > nz + 1 || layer_begin >= layer_end || layer_begin % kRZ != 0)
+  if (layer_begin < 0 || layer_end > nz + 1 || layer_begin > layer_end || layer_begin % kRZ != 0)
     return gfe::set_error(GFE_ERR_ARG, "%s: node layers [%d, %d) must lie in [0, %d) and start at a multiple of %d",
                           fn, layer_begin, layer_end, nz + 1, kRZ);
   if (!workspace && !convert_coords)
     return gfe::set_error(GFE_ERR_ARG, "%s: without a workspace the coordinates are converted every call", fn);
   cudaStream_t s = gfe::as_stream(stream);
+  if (layer_begin == layer_end) {
+    // an empty range only converts the coordinates into the workspace
+    if (!workspace || !convert_coords)
+      return gfe::set_error(GFE_ERR_ARG, "%s: an empty layer range needs a workspace and convert_coords", fn);
+    const long long n3 = 3ll * (nx + 1) * (ny + 1) * (nz + 1);
+    if (precision == GFE_MIXED) split_coords<float><<<4 * gfe::sm_count(), 256, 0, s>>>(n3, coords, (float*)workspace);
+    else if (precision == GFE_MIXED_DF) split_coords<f2><<<4 * gfe::sm_count(), 256, 0, s>>>(n3, coords, (f2*)workspace);
+    GFE_LAUNCH_CHECK(fn);
+    return GFE_OK;
+  }
   unsigned* err = gfe::device_error_word();
   const dim3 grid((nx + 1 + kRTX - 1) / kRTX, (ny + 1 + kRTY - 1) / kRTY, (layer_end - layer_begin + kRZ - 1) / kRZ);
   void* prof = gfe::stage_begin(GFE_STAGE_LAPLACE_ELEMENTS, s);

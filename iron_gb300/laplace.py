@@ -137,10 +137,11 @@ class LaplaceAssembly:
                          kappa_host=None, slabs: int | None = None, stream=None) -> torch.Tensor:
         """End-to-end assembly with host buffers on Iron's regular generated mesh: copy the geometry
         and conductivity in (pinned host tensors, optional), assemble in node-layer slabs, and copy
-        each slab's CSR values (one contiguous range) to values_host (pinned float64 [nnz]) on a
-        second stream while the next slab computes.  slabs: number of slabs (default: slabs of 16
-        node layers, two of the kernel's 8-layer blocks, which measured best at 128^3).  Returns
-        values_host; the copies are ordered before later work on `stream`."""
+        each slab's CSR values (one contiguous range) to values_host (pinned float64 [nnz]) on a copy
+        stream while the next slab computes.  Consecutive slabs alternate between `stream` and a
+        second compute stream, so the last wave of one slab's grid overlaps the first wave of the
+        next.  slabs: number of slabs (default: slabs of 16 node layers, two of the kernel's 8-layer
+        blocks).  Returns values_host; all work is ordered before later work on `stream`."""
         if self.regular is None:
             raise GfeError(-1, "the slab pipeline needs Iron's regular generated mesh")
         if values_host.numel() != self.nnz or values_host.dtype != torch.float64 or values_host.is_cuda:
@@ -151,6 +152,7 @@ class LaplaceAssembly:
         prec = PRECISIONS[precision]
         if getattr(self, "_copy_stream", None) is None:
             self._copy_stream = torch.cuda.Stream(self.device)
+            self._compute_stream2 = torch.cuda.Stream(self.device)
             self._row_ptr_host = self.row_ptr.cpu().numpy()
         if getattr(self, "_asm_ws_prec", None) != prec:
             wb = int(L.gfe_laplace_regular_workspace_bytes(nx, ny, nz, prec))
@@ -161,28 +163,39 @@ class LaplaceAssembly:
         NZ, NXY = nz + 1, (nx + 1) * (ny + 1)
         step = 16 if slabs is None else -(-NZ // max(int(slabs), 1))
         step = -(-step // 8) * 8  # slabs start at multiples of the kernel's 8-layer blocks
+        st2 = self._compute_stream2
         with torch.cuda.stream(st):
             if coords_host is not None:
                 self.coords.copy_(coords_host, non_blocking=True)
             if kappa_host is not None:
                 self.kappa.copy_(kappa_host, non_blocking=True)
-            l0 = 0
+            args = (nx, ny, nz, _lib.ptr(self.coords), _lib.ptr(self.kappa), _lib.ptr(self.row_ptr),
+                    _lib.ptr(self.values), None, _lib.ptr(self.rhs), prec, _lib.ptr(self._asm_ws))
+            # the FP32-pipe kernels read a converted copy of the coordinates, made once here; the
+            # FP64 kernel reads them directly
+            converted = prec != GFE_FP64
+            if converted:
+                _lib.call("gfe_laplace_assemble_regular_layers", *args, 0, 0, 1, _lib.stream_handle(st))
+            ready = torch.cuda.Event()
+            ready.record(st)
+            st2.wait_event(ready)
+            l0, i = 0, 0
             while l0 < NZ:
                 l1 = min(l0 + step, NZ)
-                _lib.call("gfe_laplace_assemble_regular_layers", nx, ny, nz, _lib.ptr(self.coords),
-                          _lib.ptr(self.kappa), _lib.ptr(self.row_ptr), _lib.ptr(self.values), None,
-                          _lib.ptr(self.rhs), prec, _lib.ptr(self._asm_ws), l0, l1, 1 if l0 == 0 else 0,
-                          _lib.stream_handle(st))
+                sk = st if i % 2 == 0 else st2
+                _lib.call("gfe_laplace_assemble_regular_layers", *args, l0, l1, 0 if converted else 1,
+                          _lib.stream_handle(sk))
                 ev = torch.cuda.Event()
-                ev.record(st)
+                ev.record(sk)
                 cs.wait_event(ev)
                 a, b = int(rp[l0 * NXY]) - 1, int(rp[l1 * NXY]) - 1
                 with torch.cuda.stream(cs):
                     values_host[a:b].copy_(self.values[a:b], non_blocking=True)
-                l0 = l1
-            done = torch.cuda.Event()
-            done.record(cs)
-            st.wait_event(done)
+                l0, i = l1, i + 1
+            for other in (st2, cs):
+                done = torch.cuda.Event()
+                done.record(other)
+                st.wait_event(done)
         return values_host
 
     def element_matrices(self, precision: str = "fp64", stream=None) -> torch.Tensor:
