@@ -205,7 +205,7 @@ def run_reference(args):
 def run_gfe(args):
     import torch
 
-    from iron_gb300 import _lib
+    from iron_gb300 import _lib, replicas
     from iron_gb300.laplace import LaplaceAssembly
 
     ws, rank, local = dist_env()
@@ -243,8 +243,7 @@ def run_gfe(args):
         torch.cuda.synchronize()
         _lib.profile_enable(True)
         _lib.profile_read(_lib.STAGE_LAPLACE_ELEMENTS, reset=True)
-        if ws > 1:
-            torch.distributed.barrier()
+        replicas.barrier()
         with ClockSampler(dev.index) as clk:
             torch.cuda.synchronize()
             t0 = torch.cuda.Event(enable_timing=True)
@@ -257,11 +256,7 @@ def run_gfe(args):
         _lib.profile_enable(False)
         kern_ms, launches = _lib.profile_read(_lib.STAGE_LAPLACE_ELEMENTS, reset=True)
         _lib.raise_device_errors("bench assembly")
-        ms = t0.elapsed_time(t1) / args.steps
-        if ws > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = replicas.max_over_replicas(t0.elapsed_time(t1) / args.steps, dev)
         timings[prec] = {"ms_per_step": ms, "kernel_ms_total": kern_ms, "launches": launches,
                          "clocks": clk.summary()}
 
@@ -278,6 +273,7 @@ def run_gfe(args):
         for i in range(args.warmup + args.steps):
             if i == args.warmup:
                 torch.cuda.synchronize()
+                replicas.barrier()
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
@@ -290,7 +286,7 @@ def run_gfe(args):
                 vals_h.copy_(A.values, non_blocking=True)
         e1.record(stream)
         torch.cuda.synchronize()
-        e2e[prec] = e0.elapsed_time(e1) / args.steps
+        e2e[prec] = replicas.max_over_replicas(e0.elapsed_time(e1) / args.steps, dev)
         if pipelined:
             # the host copy equals the device-resident assembly of the same precision
             A.assemble(prec, check=False, path=path)
@@ -341,7 +337,7 @@ def run_gfe(args):
         used_path = "general" if (head == "fp64" or A.regular is None) else "regular"
     else:
         used_path = path
-    value = ws * E / (T["ms_per_step"] * 1e-3)
+    value = replicas.job_throughput(E, T["ms_per_step"], ws)
     per_launch_ms = T["kernel_ms_total"] / max(T["launches"], 1)
     n_launch_step = max(T["launches"] // max(args.steps, 1), 1)
     units_per_launch = E / n_launch_step
@@ -362,7 +358,7 @@ def run_gfe(args):
                    "precision": head, "l2": "inputs larger than L2 (CSR values %.0f MB > 129 MB)" % (nnz * 8 / 1e6),
                    "parallelism": "replicas" if ws > 1 else "single"},
         "clocks": T["clocks"],
-        "e2e": {"value": ws * E / (e2e[head] * 1e-3), "unit": "elements/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": replicas.job_throughput(E, e2e[head], ws), "unit": "elements/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         # element kernel launches + one coordinate split (regular path) or FP32 copy (colour path)
         # per step for the FP32-pipe precisions
@@ -374,7 +370,7 @@ def run_gfe(args):
                      "per_launch_ms": per_launch_ms, "units_per_launch": units_per_launch,
                      "algorithmic_bytes_per_element": bytes_per_elem},
         "precisions": {p: {"ms_per_step": timings[p]["ms_per_step"],
-                           "elements_per_s": ws * E / (timings[p]["ms_per_step"] * 1e-3),
+                           "elements_per_s": replicas.job_throughput(E, timings[p]["ms_per_step"], ws),
                            "e2e_ms": e2e[p], "kernel_ms_per_launch": timings[p]["kernel_ms_total"] /
                            max(timings[p]["launches"], 1)} for p in precisions},
         "assembly_rel_err_vs_fp64": asm_err,
