@@ -382,6 +382,16 @@ def run_gfe(args):
         line["fp32_pipe_gflops"] = _lib.probe_fma_rate(_lib.GFE_MIXED)
         fl = algorithmic_flops(E) / (T["ms_per_step"] * 1e-3) / 1e9
         line["flops"] = {"algorithmic_gflops_per_s": fl, "formula": "E*8*(18*8+45+18*8+6*64)"}
+        # the element arithmetic, not memory, bounds the headline kernel: its algorithmic flops are
+        # FP64-accurate (float-float on the FP32 pipes), so the natural roof is GB300's FP64 pipe
+        fp64_peak = line["fp64_pipe_gflops"]
+        line["compute_roofline"] = {
+            "bound": "fp32_pipe" if head != "fp64" else "fp64_pipe",
+            "achieved_fp64_equivalent_gflops": fl,
+            "fp64_pipe_peak_gflops": fp64_peak, "vs_fp64_pipe_peak": fl / fp64_peak if fp64_peak else None,
+            "fp32_pipe_peak_gflops": line["fp32_pipe_gflops"],
+            "note": "algorithmic flops per second against the probed FMA-chain rates; float-float "
+                    "costs several FP32 instructions per FP64-accurate flop"}
     except Exception as exc:  # diagnostic only
         line["probe_error"] = str(exc)
     if solve is not None:
