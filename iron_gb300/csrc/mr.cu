@@ -24,7 +24,9 @@
 // then form the lower u-u triangle and the u-p / p-u blocks and add them into the CSR values
 // through a precomputed per-element slot map (u-u upper triangle mirrored, p-p structurally zero).
 #include <mutex>
+#include <type_traits>
 
+#include "df.cuh"
 #include "gfe_internal.cuh"
 #include "tcgen05.cuh"
 
@@ -35,11 +37,14 @@ constexpr int NL = 8;    // linear (pressure) element nodes
 constexpr int NG = 27;   // Gauss points (3x3x3)
 constexpr int ND = 89;   // element DOFs
 
-struct Tables {
-  double dphi[NG][3][NQ];  // d phi_ns / d xi_k at Gauss point g (quadratic basis)
-  double w[NG];
-  double psi[NG][NL];      // linear basis values at the Gauss points
+template <typename S>
+struct TablesT {
+  S dphi[NG][3][NQ];  // d phi_ns / d xi_k at Gauss point g (quadratic basis)
+  S w[NG];
+  S psi[NG][NL];      // linear basis values at the Gauss points
 };
+using Tables = TablesT<double>;
+using TablesF = TablesT<float>;  // FP32 copy read by the FP32 Gauss-point kernel
 
 // Host construction of the tables (Gauss-Legendre 3-point rule on [0,1], Lagrange bases),
 // src/basis_routines.F90:3720-4090, 6804-6890, 7969-8090.
@@ -94,14 +99,43 @@ int device_tables(const Tables** out) {
   return GFE_OK;
 }
 
-__device__ __constant__ int kT2V[3][3] = {{0, 3, 4}, {3, 1, 5}, {4, 5, 2}};
-__device__ __constant__ int kV2T[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+TablesF* g_tables_f[64] = {nullptr};
+
+int device_tables_f(const TablesF** out) {
+  int dev = 0;
+  GFE_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_tab_mu);
+  if (!g_tables_f[dev]) {
+    Tables h;
+    build_tables(h);
+    TablesF f;
+    for (int g = 0; g < NG; ++g) {
+      f.w[g] = (float)h.w[g];
+      for (int k = 0; k < 3; ++k)
+        for (int n = 0; n < NQ; ++n) f.dphi[g][k][n] = (float)h.dphi[g][k][n];
+      for (int m = 0; m < NL; ++m) f.psi[g][m] = (float)h.psi[g][m];
+    }
+    void* p = nullptr;
+    GFE_CUDA_TRY(cudaMalloc(&p, sizeof(TablesF)));
+    GFE_CUDA_TRY(cudaMemcpy(p, &f, sizeof(TablesF), cudaMemcpyHostToDevice));
+    g_tables_f[dev] = static_cast<TablesF*>(p);
+  }
+  *out = g_tables_f[dev];
+  return GFE_OK;
+}
+
+// Voigt index of tensor entry (i, j) and the tensor entries of Voigt index v, as arithmetic so that
+// unrolled loops index register arrays with constants: 11 22 33 12 13 23.
+__host__ __device__ constexpr int t2v(int i, int j) { return i == j ? i : i + j + 2; }
+__host__ __device__ constexpr int v2t_a(int v) { return v < 3 ? v : (v == 5 ? 1 : 0); }
+__host__ __device__ constexpr int v2t_b(int v) { return v < 3 ? v : (v == 3 ? 1 : 2); }
 
 // Inverse and determinant with Iron's cofactor formulas (src/maths.F90:2807-2868).
-__device__ __forceinline__ double inv3(const double A[3][3], double B[3][3]) {
-  const double det = A[0][0] * A[1][1] * A[2][2] + A[0][1] * A[1][2] * A[2][0] + A[0][2] * A[1][0] * A[2][1] -
-                     A[0][0] * A[2][1] * A[1][2] - A[1][0] * A[0][1] * A[2][2] - A[2][0] * A[1][1] * A[0][2];
-  const double r = 1.0 / det;
+template <typename S>
+__device__ __forceinline__ S inv3(const S A[3][3], S B[3][3]) {
+  const S det = A[0][0] * A[1][1] * A[2][2] + A[0][1] * A[1][2] * A[2][0] + A[0][2] * A[1][0] * A[2][1] -
+                A[0][0] * A[2][1] * A[1][2] - A[1][0] * A[0][1] * A[2][2] - A[2][0] * A[1][1] * A[0][2];
+  const S r = S(1) / det;
   B[0][0] = (A[1][1] * A[2][2] - A[2][1] * A[1][2]) * r;
   B[1][0] = (A[1][2] * A[2][0] - A[2][2] * A[1][0]) * r;
   B[2][0] = (A[1][0] * A[2][1] - A[2][0] * A[1][1]) * r;
@@ -114,7 +148,8 @@ __device__ __forceinline__ double inv3(const double A[3][3], double B[3][3]) {
   return det;
 }
 
-__device__ __forceinline__ double det3(const double A[3][3]) {
+template <typename S>
+__device__ __forceinline__ S det3(const S A[3][3]) {
   return A[0][0] * A[1][1] * A[2][2] + A[0][1] * A[1][2] * A[2][0] + A[0][2] * A[1][0] * A[2][1] -
          A[0][0] * A[2][1] * A[1][2] - A[1][0] * A[0][1] * A[2][2] - A[2][0] * A[1][1] * A[0][2];
 }
@@ -128,25 +163,39 @@ __device__ __forceinline__ double vol_jacobian(const double M[3][3]) {
     for (int j = 0; j < 3; ++j) G[i][j] = M[0][i] * M[0][j] + M[1][i] * M[1][j] + M[2][i] * M[2][j];
   return sqrt(fabs(det3(G)));
 }
+// The FP32 path keeps the volume Jacobian in FP64: the gradient matrix is widened exactly (integer
+// re-packing, no FP64-pipe conversion) and |det M| (= sqrt(det(M^T M)) for a square M) is taken
+// directly, which also avoids the Gram product and the square root.
+__device__ __forceinline__ float vol_jacobian(const float M[3][3]) {
+  double D[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) D[i][j] = f32_to_f64_exact(M[i][j]);
+  return (float)fabs(det3(D));
+}
 
 // Per-Gauss-point kinematics shared by residual and Jacobian.
-struct GP {
-  double Zi[3][3];  // dxi/dz
-  double F[3][3];   // dz/dnu
-  double Jz, Jx, p, w;
+template <typename S>
+struct GPT {
+  S Zi[3][3];  // dxi/dz
+  S F[3][3];   // dz/dnu
+  S Jz, Jx, p, w;
 };
+using GP = GPT<double>;
 
-__device__ __forceinline__ bool gauss_point(const Tables& T, int g, const double* sz, const double* sx,
-                                            const double* sp, GP& o) {
-  double Z[3][3], X[3][3];
+template <typename S>
+__device__ __forceinline__ bool gauss_point(const TablesT<S>& T, int g, const S* sz, const S* sx, const S* sp,
+                                            GPT<S>& o) {
+  S Z[3][3], X[3][3];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      double a = 0.0, b = 0.0;
+      S a = S(0), b = S(0);
 #pragma unroll 9
       for (int ns = 0; ns < NQ; ++ns) {
-        const double d = T.dphi[g][k][ns];
+        const S d = T.dphi[g][k][ns];
         a += d * sz[c * NQ + ns];
         b += d * sx[c * NQ + ns];
       }
@@ -155,12 +204,12 @@ __device__ __forceinline__ bool gauss_point(const Tables& T, int g, const double
     }
   o.Jz = vol_jacobian(Z);
   o.Jx = vol_jacobian(X);
-  const double dz = inv3(Z, o.Zi);
+  const S dz = inv3(Z, o.Zi);
   // material frame without fibres: dX/dNu columns = normalised DX_DXI columns
-  double N[3][3], NX[3][3], A[3][3];
+  S N[3][3], NX[3][3], A[3][3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const double n = sqrt(X[0][k] * X[0][k] + X[1][k] * X[1][k] + X[2][k] * X[2][k]);
+    const S n = sqrt(X[0][k] * X[0][k] + X[1][k] * X[1][k] + X[2][k] * X[2][k]);
 #pragma unroll
     for (int c = 0; c < 3; ++c) N[c][k] = X[c][k] / n;
   }
@@ -173,32 +222,34 @@ __device__ __forceinline__ bool gauss_point(const Tables& T, int g, const double
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) o.F[i][j] = Z[i][0] * A[0][j] + Z[i][1] * A[1][j] + Z[i][2] * A[2][j];
-  double p = 0.0;
+  S p = S(0);
 #pragma unroll
   for (int m = 0; m < NL; ++m) p += T.psi[g][m] * sp[m];
   o.p = p;
   o.w = T.w[g];
-  return dz > 0.0 && o.Jx > 0.0 && isfinite(dz);
+  return dz > S(0) && o.Jx > S(0) && isfinite(dz);
 }
 
 // push-forward matrix t (src/finite_elasticity_routines.F90:1343-1375)
-__device__ __forceinline__ void push_t(const double F[3][3], double t[6][6]) {
+template <typename S>
+__device__ __forceinline__ void push_t(const S F[3][3], S t[6][6]) {
 #pragma unroll
   for (int j = 0; j < 6; ++j)
 #pragma unroll
     for (int i = 0; i < 6; ++i) {
-      const int ai = kV2T[i][0], bi = kV2T[i][1], aj = kV2T[j][0], bj = kV2T[j][1];
-      double v = F[ai][aj] * F[bi][bj];
+      const int ai = v2t_a(i), bi = v2t_b(i), aj = v2t_a(j), bj = v2t_b(j);
+      S v = F[ai][aj] * F[bi][bj];
       if (j >= 3) v += F[ai][bj] * F[bi][aj];
       t[i][j] = v;
     }
 }
 
-__device__ __forceinline__ void push_vec(const double t[6][6], double S[6], double J) {
-  double o[6];
+template <typename R>
+__device__ __forceinline__ void push_vec(const R t[6][6], R S[6], R J) {
+  R o[6];
 #pragma unroll
   for (int i = 0; i < 6; ++i) {
-    double s = 0.0;
+    R s = R(0);
 #pragma unroll
     for (int j = 0; j < 6; ++j) s += t[i][j] * S[j];
     o[i] = s / J;
@@ -292,8 +343,8 @@ mr_residual_kernel(const int32_t* __restrict__ elems, int32_t count, int32_t bat
       for (int k = 0; k < 3; ++k)
 #pragma unroll
         for (int mh = 0; mh < 3; ++mh)
-          sP[lane * 9 + k * 3 + mh] = jgw * (q.Zi[k][0] * sig[kT2V[0][mh]] + q.Zi[k][1] * sig[kT2V[1][mh]] +
-                                             q.Zi[k][2] * sig[kT2V[2][mh]]);
+          sP[lane * 9 + k * 3 + mh] = jgw * (q.Zi[k][0] * sig[t2v(0, mh)] + q.Zi[k][1] * sig[t2v(1, mh)] +
+                                             q.Zi[k][2] * sig[t2v(2, mh)]);
       stp[lane] = q.Jx * q.w * (q.Jz / q.Jx - 1.0);
     }
     __syncwarp();
@@ -700,50 +751,51 @@ __global__ void sum_dc(const double* __restrict__ dc_elem, int32_t n_elem, int32
 // 649-795 and 1072-1192): sub[0..2] = J_z w (c_sub + sigma) for the diagonal component blocks,
 // sub[3..5] = J_z w c_sub for the off-diagonal blocks (mh, nh) = (1,0), (2,0), (2,1);
 // hyd = J_z w push(C^-1).
-__device__ void iron_point_tensors(const GP& q, double c1, double c2, double sub[6][9], double hyd[9],
-                                   double& jgw) {
-  const double J = q.Jz / q.Jx;
+template <typename S>
+__device__ void iron_point_tensors(const GPT<S>& q, S c1, S c2, S sub[6][9], S hyd[9], S& jgw) {
+  const S J = q.Jz / q.Jx;
   // unmodified right Cauchy-Green tensor and its inverse
-  double C[3][3], Ci[3][3];
+  S C[3][3], Ci[3][3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) C[i][j] = q.F[0][i] * q.F[0][j] + q.F[1][i] * q.F[1][j] + q.F[2][i] * q.F[2][j];
-  const double I3 = inv3(C, Ci);
-  const double L[6] = {C[0][0], C[1][1], C[2][2], C[0][1], C[0][2], C[1][2]};
-  const double U[6] = {Ci[0][0], Ci[1][1], Ci[2][2], Ci[0][1], Ci[0][2], Ci[1][2]};
+  const S I3 = inv3(C, Ci);
+  const S L[6] = {C[0][0], C[1][1], C[2][2], C[0][1], C[0][2], C[1][2]};
+  const S U[6] = {Ci[0][0], Ci[1][1], Ci[2][2], Ci[0][1], Ci[0][2], Ci[1][2]};
   // I3EE as filled by Fortran RESHAPE (column j listed): I3EE[i][j] = col[j][i]
-  const double col[6][6] = {{0.0, 4 * L[2], 4 * L[1], 0.0, 0.0, -4 * L[5]},
-                            {4 * L[2], 0.0, 4 * L[0], 0.0, -4 * L[4], 0.0},
-                            {4 * L[1], 4 * L[0], 0.0, -2 * L[3], 0.0, 0.0},
-                            {0.0, 0.0, -4 * L[3], -2 * L[2], 2 * L[5], 2 * L[4]},
-                            {0.0, -4 * L[4], 0.0, 2 * L[5], -2 * L[1], 2 * L[3]},
-                            {-4 * L[5], 0.0, 0.0, 2 * L[4], 2 * L[3], -2 * L[0]}};
-  double D[6][6];
+  const S z0 = S(0), f4 = S(4), f2 = S(2);
+  const S col[6][6] = {{z0, f4 * L[2], f4 * L[1], z0, z0, -f4 * L[5]},
+                       {f4 * L[2], z0, f4 * L[0], z0, -f4 * L[4], z0},
+                       {f4 * L[1], f4 * L[0], z0, -f2 * L[3], z0, z0},
+                       {z0, z0, -f4 * L[3], -f2 * L[2], f2 * L[5], f2 * L[4]},
+                       {z0, -f4 * L[4], z0, f2 * L[5], -f2 * L[1], f2 * L[3]},
+                       {-f4 * L[5], z0, z0, f2 * L[4], f2 * L[3], -f2 * L[0]}};
+  S D[6][6];
 #pragma unroll
   for (int i = 0; i < 6; ++i)
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
-      double v = 0.0;
-      if (i < 3 && j < 3 && i != j) v = 4.0 * c2;
-      if (i >= 3 && i == j) v = -2.0 * c2;
-      D[i][j] = v + q.p * (-2.0 * U[i] * U[j] + 0.5 * col[j][i] / I3);
+      S v = S(0);
+      if (i < 3 && j < 3 && i != j) v = f4 * c2;
+      if (i >= 3 && i == j) v = -f2 * c2;
+      D[i][j] = v + q.p * (-f2 * U[i] * U[j] + S(0.5) * col[j][i] / I3);
     }
-  const double I1 = C[0][0] + C[1][1] + C[2][2];
-  const double t2 = 2.0 * (c1 + I1 * c2);
-  double Sv[6] = {-2 * c2 * C[0][0] + t2, -2 * c2 * C[1][1] + t2, -2 * c2 * C[2][2] + t2,
-                  -2 * c2 * C[1][0], -2 * c2 * C[2][0], -2 * c2 * C[2][1]};
-  double H[6] = {U[0], U[1], U[2], U[3], U[4], U[5]};
-  double t[6][6];
+  const S I1 = C[0][0] + C[1][1] + C[2][2];
+  const S t2 = f2 * (c1 + I1 * c2);
+  S Sv[6] = {-f2 * c2 * C[0][0] + t2, -f2 * c2 * C[1][1] + t2, -f2 * c2 * C[2][2] + t2,
+             -f2 * c2 * C[1][0], -f2 * c2 * C[2][0], -f2 * c2 * C[2][1]};
+  S H[6] = {U[0], U[1], U[2], U[3], U[4], U[5]};
+  S t[6][6];
   push_t(q.F, t);
   push_vec(t, Sv, J);
   push_vec(t, H, J);
-  double tD[6][6];
+  S tD[6][6];
 #pragma unroll
   for (int i = 0; i < 6; ++i)
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
-      double s = 0.0;
+      S s = S(0);
 #pragma unroll
       for (int k = 0; k < 6; ++k) s += t[i][k] * D[k][j];
       tD[i][j] = s;
@@ -752,7 +804,7 @@ __device__ void iron_point_tensors(const GP& q, double c1, double c2, double sub
   for (int i = 0; i < 6; ++i)
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
-      double s = 0.0;
+      S s = S(0);
 #pragma unroll
       for (int k = 0; k < 6; ++k) s += tD[i][k] * t[j][k];
       D[i][j] = s / J;
@@ -764,41 +816,47 @@ __device__ void iron_point_tensors(const GP& q, double c1, double c2, double sub
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j) sub[nh][i * 3 + j] = jgw * (D[kT2V[i][nh]][kT2V[j][nh]] + Sv[kT2V[i][j]]);
+      for (int j = 0; j < 3; ++j) sub[nh][i * 3 + j] = jgw * (D[t2v(i, nh)][t2v(j, nh)] + Sv[t2v(i, j)]);
   const int om[3] = {1, 2, 2}, on[3] = {0, 0, 1};
 #pragma unroll
   for (int o = 0; o < 3; ++o)
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-      for (int j = 0; j < 3; ++j) sub[3 + o][i * 3 + j] = jgw * D[kT2V[i][om[o]]][kT2V[j][on[o]]];
+      for (int j = 0; j < 3; ++j) sub[3 + o][i * 3 + j] = jgw * D[t2v(i, om[o])][t2v(j, on[o])];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) hyd[i * 3 + j] = jgw * H[kT2V[i][j]];
+    for (int j = 0; j < 3; ++j) hyd[i * 3 + j] = jgw * H[t2v(i, j)];
 }
 
 constexpr int kGPElems = 4;                // elements per CTA of mr_gp_kernel
 constexpr int kGPThreads = kGPElems * NG;  // 108
 constexpr int kGPOut = 81 + 9 + 9;         // D (9 blocks x 9), Hv, Pv per Gauss point
 
+template <typename KS>
 struct GPShared {
-  double x[kGPElems][81], z[kGPElems][81], p[kGPElems][8];
+  KS x[kGPElems][81], z[kGPElems][81], p[kGPElems][8];
 };
 
 // One thread per (element, Gauss point).  out[item][g][kGPOut] in the contraction type TO:
-// D[(mh*3+nh)*9 + xi*3+zeta], Hv[81 + xi*3+mh], Pv[90 + xi*3+nh].
-template <typename TO, bool EXACT>
+// D[(mh*3+nh)*9 + xi*3+zeta], Hv[81 + xi*3+mh], Pv[90 + xi*3+nh].  KS is the kinematics type:
+// double, or float for Iron's analytic tangent on the FP32 paths (element data rounded once per
+// node when staged, the volume Jacobians det(Z), det(X) still evaluated in FP64 from the exactly
+// widened gradients).  The consistent tangent (EXACT) always runs its dual numbers in FP64.
+template <typename TO, bool EXACT, typename KS = double>
 __global__ void __launch_bounds__(kGPThreads)
 mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
              const int32_t* __restrict__ elin, int32_t nq2, const double* __restrict__ xg,
-             const double* __restrict__ dep, const double* __restrict__ cpar, const Tables* __restrict__ Tg,
+             const double* __restrict__ dep, const double* __restrict__ cpar, const TablesT<KS>* __restrict__ Tg,
              TO* __restrict__ out, unsigned* err) {
-  extern __shared__ double smem[];
-  Tables& T = *reinterpret_cast<Tables*>(smem);
-  GPShared& S = *reinterpret_cast<GPShared*>(smem + sizeof(Tables) / sizeof(double));
-  for (int i = threadIdx.x; i < (int)(sizeof(Tables) / sizeof(double)); i += blockDim.x)
-    smem[i] = reinterpret_cast<const double*>(Tg)[i];
+  static_assert(!EXACT || std::is_same<KS, double>::value, "the consistent tangent runs in FP64");
+  extern __shared__ double smem_d[];
+  KS* smem = reinterpret_cast<KS*>(smem_d);
+  constexpr int kTabWords = (int)(sizeof(TablesT<KS>) / sizeof(KS));
+  TablesT<KS>& T = *reinterpret_cast<TablesT<KS>*>(smem);
+  GPShared<KS>& S = *reinterpret_cast<GPShared<KS>*>(smem + kTabWords);
+  for (int i = threadIdx.x; i < kTabWords; i += blockDim.x) smem[i] = reinterpret_cast<const KS*>(Tg)[i];
   const int le = threadIdx.x / NG, g = threadIdx.x % NG;
   const int item = blockIdx.x * kGPElems + le;
   // cooperative load of the CTA's elements
@@ -809,37 +867,39 @@ mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __
     const int n = __ldg(eq2 + (size_t)e * NQ + i);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      S.x[l][c * NQ + i] = __ldg(xg + (size_t)c * nq2 + n);
-      S.z[l][c * NQ + i] = dep[(size_t)c * nq2 + n];
+      S.x[l][c * NQ + i] = (KS)__ldg(xg + (size_t)c * nq2 + n);
+      S.z[l][c * NQ + i] = (KS)dep[(size_t)c * nq2 + n];
     }
   }
   for (int t = threadIdx.x; t < kGPElems * NL; t += blockDim.x) {
     const int l = t / NL, i = t % NL, it = blockIdx.x * kGPElems + l;
     if (it >= count) continue;
     const int e = __ldg(elems + it);
-    S.p[l][i] = dep[(size_t)3 * nq2 + __ldg(elin + (size_t)e * NL + i)];
+    S.p[l][i] = (KS)dep[(size_t)3 * nq2 + __ldg(elin + (size_t)e * NL + i)];
   }
   __syncthreads();
   if (item >= count) return;
-  const double c1 = cpar[0], c2 = cpar[1];
   TO* o = out + ((size_t)item * NG + g) * kGPOut;
-  if (!EXACT) {
-    GP q;
+  if constexpr (!EXACT) {
+    const KS c1 = (KS)cpar[0], c2 = (KS)cpar[1];
+    GPT<KS> q;
     if (!gauss_point(T, g, S.z[le], S.x[le], S.p[le], q)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
-    double sub[6][9], hyd[9], jgw;
+    KS sub[6][9], hyd[9], jgw;
     iron_point_tensors(q, c1, c2, sub, hyd, jgw);
     // blocks to xi space: Dxi = Zi sub Zi^T (Zi = dxi/dz); upper blocks as transposes of the lower
+#pragma unroll
     for (int mh = 0; mh < 3; ++mh)
+#pragma unroll
       for (int nh = 0; nh < 3; ++nh) {
         const int blk = mh == nh ? mh : (mh > nh ? 3 + (mh == 1 ? 0 : (nh == 0 ? 1 : 2))
                                                  : 3 + (nh == 1 ? 0 : (mh == 0 ? 1 : 2)));
         const bool tr = mh < nh;
-        double W[3][3];
+        KS W[3][3];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
           for (int z = 0; z < 3; ++z) {
-            double s = 0.0;
+            KS s = KS(0);
 #pragma unroll
             for (int j = 0; j < 3; ++j) s += (tr ? sub[blk][j * 3 + i] : sub[blk][i * 3 + j]) * q.Zi[z][j];
             W[i][z] = s;  // (sub Zi^T)[i][zeta]
@@ -860,6 +920,7 @@ mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __
         o[90 + xi * 3 + m] = (TO)(jgw * q.Zi[xi][m]);
       }
   } else {
+    const double c1 = cpar[0], c2 = cpar[1];
     GPIn in;
     gauss_inputs(T, g, S.z[le], S.x[le], S.p[le], in);
     for (int seed = 0; seed < 10; ++seed) {
@@ -1260,18 +1321,28 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
   const Tables* T = nullptr;
   int rc = device_tables(&T);
   if (rc) return rc;
+  // Iron's analytic tangent on the FP32 paths: FP32 kinematics from the FP32 tables
+  using KF = typename std::conditional<std::is_same<TS, float>::value, float, double>::type;
+  const TablesT<KF>* TK = nullptr;
+  if constexpr (std::is_same<KF, float>::value) {
+    if ((rc = device_tables_f(&TK))) return rc;
+  } else {
+    TK = T;
+  }
+  const size_t gsm = sizeof(Tables) + sizeof(GPShared<double>);
+  const size_t gsm_k = sizeof(TablesT<KF>) + sizeof(GPShared<KF>);
+  const size_t csm = sizeof(ContractShared<TS>);
+  const void* gk = mode == 0 ? (const void*)mr_gp_kernel<TS, false, KF> : (const void*)mr_gp_kernel<TS, true>;
+  if ((rc = set_smem(gk, mode == 0 ? gsm_k : gsm))) return rc;
   int max_cnt = 0;
   for (int c = 0; c < n_colors; ++c) max_cnt = std::max(max_cnt, color_ptr_host[c + 1] - color_ptr_host[c]);
+  if (values) GFE_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)nnz, s));
   TS* gpbuf = nullptr;
   if ((rc = gfe::scratch_alloc((void**)&gpbuf, sizeof(TS) * (size_t)max_cnt * NG * kGPOut + 16, s,
                                "Gauss-point tangent blocks")))
     return rc;
-  if (values) GFE_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)nnz, s));
-  const size_t gsm = sizeof(Tables) + sizeof(GPShared);
-  const size_t csm = sizeof(ContractShared<TS>);
-  const void* gk = mode == 0 ? (const void*)mr_gp_kernel<TS, false> : (const void*)mr_gp_kernel<TS, true>;
   const void* ck = mode == 0 ? (const void*)mr_contract_kernel<TS, false> : (const void*)mr_contract_kernel<TS, true>;
-  if ((rc = set_smem(gk, gsm)) || (rc = set_smem(ck, csm))) {
+  if ((rc = set_smem(ck, csm))) {
     gfe::scratch_free(gpbuf, s);
     return rc;
   }
@@ -1298,8 +1369,8 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
       const float* gpf = reinterpret_cast<const float*>(gpbuf);
       const int tgrid = std::min(cnt, gfe::sm_count());
       if (mode == 0) {
-        mr_gp_kernel<TS, false><<<ggrid, kGPThreads, gsm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar,
-                                                               T, gpbuf, err);
+        mr_gp_kernel<TS, false, KF><<<ggrid, kGPThreads, gsm_k, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg,
+                                                                     dep, cpar, TK, gpbuf, err);
         if (tc_mode == GFE_TC_TF32X3)
           launch_contract_tc<false, true>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
         else
@@ -1313,8 +1384,8 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
           launch_contract_tc<true, false>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
       }
     } else if (mode == 0) {
-      mr_gp_kernel<TS, false><<<ggrid, kGPThreads, gsm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar, T,
-                                                             gpbuf, err);
+      mr_gp_kernel<TS, false, KF><<<ggrid, kGPThreads, gsm_k, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep,
+                                                                   cpar, TK, gpbuf, err);
       mr_contract_kernel<TS, false><<<cgrid, kCThreads, csm, s>>>(color_elems + c0, cnt, T, gpbuf, sl, values,
                                                                   K_out, err);
     } else {
