@@ -206,7 +206,9 @@ int gfe_mr_jacobian(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int
 /* precision: GFE_FP64 (FP64 contraction), GFE_MIXED (FP32 CUDA-core contraction of the
  * basis-gradient x material blocks), GFE_TC_TF32X3 / GFE_TC_TF32 (the same contraction on the
  * tensor cores, tcgen05 kind::tf32 with FP32 accumulation in tensor memory, three-pass split or one
- * pass).  In every mode the Gauss-point kinematics, det(F) and the assembled values stay FP64. */
+ * pass).  GFE_FP64 runs the Gauss-point kinematics in FP64; the other modes run them in FP32 from
+ * FP32 basis tables with the volume Jacobians det(Z), det(X) evaluated in FP64 on exactly widened
+ * gradients.  The assembled values are FP64 in every mode. */
 
 /* Consistent tangent: the exact derivative of the residual of gfe_mr_residual with respect to
  * the dependent vector (what Iron's finite-difference Jacobian, EquationsSet_FiniteElementJacobianEvaluateFD

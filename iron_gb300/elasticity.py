@@ -119,7 +119,8 @@ class MooneyRivlinAssembly:
     def jacobian(self, dep: torch.Tensor, c, precision: str = "fp64", stream=None, check=True) -> torch.Tensor:
         """Iron's analytic Jacobian assembled into the CSR values (self.values).  precision 'mixed'
         runs the basis-gradient contraction in FP32 on the CUDA cores, 'tf32x3' / 'tf32' on the
-        tensor cores (kinematics and assembled values in FP64 in every mode)."""
+        tensor cores; those three run the Gauss-point kinematics in FP32 with FP64 volume Jacobians.
+        The assembled values are FP64 in every mode."""
         return self._element_jacobians("gfe_mr_jacobian", dep, c, precision, False, stream, check)
 
     def element_jacobians(self, dep: torch.Tensor, c, precision: str = "fp64", stream=None) -> torch.Tensor:

@@ -59,7 +59,7 @@ def test_undeformed_residual_zero(gfe_cuda):
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed", 2e-5), ("tf32x3", 2e-5), ("tf32", 4e-3)])
 def test_element_jacobians_match_oracle(gfe_cuda, precision, tol):
-    """Iron's analytic element Jacobian; 'mixed' = FP32 basis-gradient contraction (FP64 kinematics),
+    """Iron's analytic element Jacobian; 'mixed' = FP32 kinematics (FP64 volume Jacobians) and FP32 basis-gradient contraction,
     'tf32x3' / 'tf32' = the contraction on the tensor cores (three-pass split / one TF32 pass);
     tolerances relative to max|K|."""
     A = MooneyRivlinAssembly.from_regular_mesh((2, 2, 1), build_jacobian=False)
