@@ -161,6 +161,27 @@ int gfe_laplace_assemble_regular_layers(int32_t nx, int32_t ny, int32_t nz, cons
                                         int32_t precision, void* workspace, int32_t layer_begin, int32_t layer_end,
                                         int32_t convert_coords, void* stream);
 
+/* End-to-end assembly with host buffers: the regular-mesh assembly above with the geometry and
+ * conductivity uploaded from host memory and the FP64 CSR values returned to host memory, as
+ * Iron's caller sees the element loop (host arrays in, the assembled matrix in host memory out).
+ * The work is pipelined over slabs of node layers (the first of 8 layers, then slab_layers each;
+ * 0 = 16): per slab, the coordinate and conductivity layers it reads are copied in and converted
+ * on an input stream, the slab is assembled on one of two alternating compute streams, and its
+ * rows -- one contiguous range of the CSR values -- are copied to values_host on an output
+ * stream while later slabs compute.  coords [3][N] / kappa [n_elem] are the device copies the
+ * uploads fill (coords_host / kappa_host NULL: the device copy is already current; kappa NULL:
+ * unit conductivity); values [nnz] is the device CSR value array.  Host buffers should be pinned
+ * for the copies to overlap.  The FP32-pipe precisions need a 16-byte aligned workspace of
+ * gfe_laplace_regular_workspace_bytes bytes; nothing is allocated.  Asynchronous: the pipeline's
+ * own streams start after the work already on `stream`, and `stream` waits for all of them, so
+ * values_host is complete once `stream` has reached this point.  Slab boundaries come from the
+ * closed-form entry count of the clipped 27-point stencil, so row_ptr must be the structure of the
+ * regular mesh (gfe_laplace_regular_check). */
+int gfe_laplace_assemble_regular_host(int32_t nx, int32_t ny, int32_t nz, const double* coords_host,
+                                      const double* kappa_host, double* coords, double* kappa,
+                                      const int32_t* row_ptr, double* values, double* values_host, double* rhs,
+                                      int32_t precision, void* workspace, int32_t slab_layers, void* stream);
+
 /* Number of CSR rows/entries that differ from the clipped 27-point stencil of the regular mesh
  * (0 = the structure is the one gfe_laplace_assemble_regular writes).  Synchronises `stream`. */
 int gfe_laplace_regular_check(int32_t nx, int32_t ny, int32_t nz, const int32_t* row_ptr, const int32_t* col_idx,

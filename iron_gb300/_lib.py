@@ -62,6 +62,8 @@ SIGNATURES = {
     "gfe_laplace_assemble_regular_ws": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp, vp]),
     "gfe_laplace_assemble_regular_layers": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp, i32, i32, i32,
                                                       vp]),
+    "gfe_laplace_assemble_regular_host": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp, i32,
+                                                    vp]),
     "gfe_laplace_regular_check": (C.c_int, [i32, i32, i32, vp, vp, C.POINTER(C.c_int64), vp]),
     "gfe_csr_spmv": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "gfe_mr_residual": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp]),
@@ -129,6 +131,17 @@ def ptr(t: torch.Tensor | None):
         return None
     if not t.is_cuda:
         raise GfeError(-1, "expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise GfeError(-1, "expected a contiguous tensor")
+    return C.c_void_p(t.data_ptr())
+
+
+def host_ptr(t: torch.Tensor | None):
+    """Address of a contiguous host tensor (None -> NULL)."""
+    if t is None:
+        return None
+    if t.is_cuda:
+        raise GfeError(-1, "expected a host tensor")
     if not t.is_contiguous():
         raise GfeError(-1, "expected a contiguous tensor")
     return C.c_void_p(t.data_ptr())

@@ -29,6 +29,7 @@
 //    column indices.
 #include <cmath>
 #include <type_traits>
+#include <vector>
 
 #include "df.cuh"
 #include "gfe_internal.cuh"
@@ -670,6 +671,158 @@ extern "C" int gfe_laplace_assemble_regular_layers(int32_t nx, int32_t ny, int32
                             l1, cv);
   gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, 1);
   if (rc) return rc;
+  GFE_LAUNCH_CHECK(fn);
+  return GFE_OK;
+}
+
+namespace {
+
+// Node layers [a, a + n) of each coordinate component (component-major [3][NXY * NZ], layers
+// contiguous) converted into the workspace: the slab-wise form of split_coords.
+template <typename T>
+__global__ void split_coords_layers(long long per_comp, long long a, long long n, const double* __restrict__ in,
+                                    T* __restrict__ out) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < 3 * n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long j = (i / n) * per_comp + a + i % n;
+    out[j] = from_double<T>(in[j]);
+  }
+}
+
+// CSR entries in the rows of node layers [0, L) of the regular mesh: every row holds its clipped
+// 27-point stencil, so the count factorises into (3 NX - 2)(3 NY - 2) times the clipped widths
+// along xi3.  Equals row_ptr[L * NX * NY] - 1 for the structure gfe_laplace_regular_check accepts.
+long long regular_entries_before(int32_t nx, int32_t ny, int32_t nz, int32_t L) {
+  const long long NX = nx + 1, NY = ny + 1, NZ = nz + 1;
+  long long w = 0;
+  for (long long l = 0; l < L; ++l) w += 3 - (l == 0) - (l == NZ - 1);
+  return (3 * NX - 2) * (3 * NY - 2) * w;
+}
+
+// Streams and events of the host-buffer pipeline, one set per host thread and device, created on
+// first use and kept for the thread's lifetime (the driver releases them at process exit).
+struct HostPipe {
+  int dev = -1;
+  cudaStream_t in = nullptr, comp[2] = {nullptr, nullptr}, out = nullptr;
+  std::vector<cudaEvent_t> ev;
+};
+thread_local std::vector<HostPipe> t_pipes;
+
+int host_pipe(HostPipe** out, size_t n_events) {
+  int dev = 0;
+  GFE_CUDA_TRY(cudaGetDevice(&dev));
+  HostPipe* hp = nullptr;
+  for (auto& p : t_pipes)
+    if (p.dev == dev) hp = &p;
+  if (!hp) {
+    HostPipe p;
+    p.dev = dev;
+    GFE_CUDA_TRY(cudaStreamCreateWithFlags(&p.in, cudaStreamNonBlocking));
+    GFE_CUDA_TRY(cudaStreamCreateWithFlags(&p.comp[0], cudaStreamNonBlocking));
+    GFE_CUDA_TRY(cudaStreamCreateWithFlags(&p.comp[1], cudaStreamNonBlocking));
+    GFE_CUDA_TRY(cudaStreamCreateWithFlags(&p.out, cudaStreamNonBlocking));
+    t_pipes.push_back(p);
+    hp = &t_pipes.back();
+  }
+  while (hp->ev.size() < n_events) {
+    cudaEvent_t e;
+    GFE_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    hp->ev.push_back(e);
+  }
+  *out = hp;
+  return GFE_OK;
+}
+
+}  // namespace
+
+extern "C" int gfe_laplace_assemble_regular_host(int32_t nx, int32_t ny, int32_t nz, const double* coords_host,
+                                                 const double* kappa_host, double* coords, double* kappa,
+                                                 const int32_t* row_ptr, double* values, double* values_host,
+                                                 double* rhs, int32_t precision, void* workspace,
+                                                 int32_t slab_layers, void* stream) {
+  const char* fn = "gfe_laplace_assemble_regular_host";
+  if (nx <= 0 || ny <= 0 || nz <= 0 || !coords || !row_ptr || !values || !values_host)
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (int rc = check_precision(precision, fn)) return rc;
+  if (kappa_host && !kappa) return gfe::set_error(GFE_ERR_ARG, "%s: kappa_host needs a device kappa array", fn);
+  if (precision != GFE_FP64 && (!workspace || (reinterpret_cast<uintptr_t>(workspace) & 15)))
+    return gfe::set_error(GFE_ERR_ARG, "%s: the FP32-pipe precisions need a 16-byte aligned workspace", fn);
+  if (slab_layers == 0) slab_layers = 2 * kRZ;
+  if (slab_layers < 0 || slab_layers % kRZ != 0)
+    return gfe::set_error(GFE_ERR_ARG, "%s: slab_layers must be a positive multiple of %d", fn, kRZ);
+  const long long NX = nx + 1, NY = ny + 1, NZ = nz + 1, NXY = NX * NY, N = NXY * NZ, EXY = (long long)nx * ny;
+  // slabs of node layers: [0, kRZ) first, so the first copy-out starts early, then slab_layers each
+  std::vector<int32_t> cut{0};
+  for (long long l = std::min<long long>(kRZ, NZ); cut.back() < NZ; l = std::min<long long>(l + slab_layers, NZ))
+    cut.push_back((int32_t)l);
+  const int n_slabs = (int)cut.size() - 1;
+  HostPipe* hp = nullptr;
+  if (int rc = host_pipe(&hp, 2 * (size_t)n_slabs + 4)) return rc;
+  cudaStream_t s = gfe::as_stream(stream);
+  cudaEvent_t* ev = hp->ev.data();
+  unsigned* err = gfe::device_error_word();
+  void* prof = gfe::stage_begin(GFE_STAGE_LAPLACE_ELEMENTS, s);
+  // every pipeline stream starts after the work already on `stream`
+  GFE_CUDA_TRY(cudaEventRecord(ev[0], s));
+  for (cudaStream_t t : {hp->in, hp->comp[0], hp->comp[1], hp->out}) GFE_CUDA_TRY(cudaStreamWaitEvent(t, ev[0], 0));
+  long long node_hi = 0, elem_hi = 0;  // node / element layers uploaded so far
+  const int cvt_grid = 2 * gfe::sm_count();
+  for (int i = 0; i < n_slabs; ++i) {
+    const int32_t l0 = cut[i], l1 = cut[i + 1];
+    cudaEvent_t ev_in = ev[1 + 2 * i], ev_c = ev[2 + 2 * i];
+    // inputs: the node layers [l0 - 1, l1] and element layers [l0 - 1, l1 - 1] this slab reads
+    const long long nh = std::min<long long>(l1 + 1, NZ), eh = std::min<long long>(l1, nz);
+    if (nh > node_hi) {
+      if (coords_host)
+        for (int c = 0; c < 3; ++c) {
+          const long long o = c * N + node_hi * NXY;
+          GFE_CUDA_TRY(cudaMemcpyAsync(coords + o, coords_host + o, sizeof(double) * (nh - node_hi) * NXY,
+                                       cudaMemcpyHostToDevice, hp->in));
+        }
+      if (precision == GFE_MIXED)
+        split_coords_layers<float><<<cvt_grid, 256, 0, hp->in>>>(N, node_hi * NXY, (nh - node_hi) * NXY, coords,
+                                                                 static_cast<float*>(workspace));
+      else if (precision == GFE_MIXED_DF)
+        split_coords_layers<f2><<<cvt_grid, 256, 0, hp->in>>>(N, node_hi * NXY, (nh - node_hi) * NXY, coords,
+                                                              static_cast<f2*>(workspace));
+      node_hi = nh;
+    }
+    if (kappa_host && eh > elem_hi) {
+      GFE_CUDA_TRY(cudaMemcpyAsync(kappa + elem_hi * EXY, kappa_host + elem_hi * EXY,
+                                   sizeof(double) * (eh - elem_hi) * EXY, cudaMemcpyHostToDevice, hp->in));
+      elem_hi = eh;
+    }
+    GFE_CUDA_TRY(cudaEventRecord(ev_in, hp->in));
+    // the slab on alternating compute streams: one slab's last wave overlaps the next one's first
+    cudaStream_t cs = hp->comp[i & 1];
+    GFE_CUDA_TRY(cudaStreamWaitEvent(cs, ev_in, 0));
+    const dim3 grid((unsigned)((NX + kRTX - 1) / kRTX), (unsigned)((NY + kRTY - 1) / kRTY),
+                    (unsigned)((l1 - l0 + kRZ - 1) / kRZ));
+    int rc;
+    if (precision == GFE_FP64)
+      rc = launch_regular<double>(grid, cs, nx, ny, nz, coords, kappa, row_ptr, values, nullptr, rhs, err, nullptr,
+                                  l0, l1, false);
+    else if (precision == GFE_MIXED)
+      rc = launch_regular<float>(grid, cs, nx, ny, nz, coords, kappa, row_ptr, values, nullptr, rhs, err, workspace,
+                                 l0, l1, false);
+    else
+      rc = launch_regular<f2>(grid, cs, nx, ny, nz, coords, kappa, row_ptr, values, nullptr, rhs, err, workspace,
+                              l0, l1, false);
+    if (rc) return rc;
+    GFE_CUDA_TRY(cudaEventRecord(ev_c, cs));
+    // the slab's rows are one contiguous range of the CSR values
+    GFE_CUDA_TRY(cudaStreamWaitEvent(hp->out, ev_c, 0));
+    const long long a = regular_entries_before(nx, ny, nz, l0), b = regular_entries_before(nx, ny, nz, l1);
+    GFE_CUDA_TRY(cudaMemcpyAsync(values_host + a, values + a, sizeof(double) * (b - a), cudaMemcpyDeviceToHost,
+                                 hp->out));
+  }
+  // `stream` resumes after the copies (which follow every slab) and the input stream
+  cudaEvent_t ev_out = ev[1 + 2 * n_slabs], ev_in_end = ev[2 + 2 * n_slabs];
+  GFE_CUDA_TRY(cudaEventRecord(ev_out, hp->out));
+  GFE_CUDA_TRY(cudaEventRecord(ev_in_end, hp->in));
+  GFE_CUDA_TRY(cudaStreamWaitEvent(s, ev_out, 0));
+  GFE_CUDA_TRY(cudaStreamWaitEvent(s, ev_in_end, 0));
+  gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, n_slabs);
   GFE_LAUNCH_CHECK(fn);
   return GFE_OK;
 }

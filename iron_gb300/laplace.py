@@ -134,68 +134,36 @@ class LaplaceAssembly:
         return self.values
 
     def assemble_to_host(self, values_host: torch.Tensor, precision: str = "mixed_df", coords_host=None,
-                         kappa_host=None, slabs: int | None = None, stream=None) -> torch.Tensor:
-        """End-to-end assembly with host buffers on Iron's regular generated mesh: copy the geometry
-        and conductivity in (pinned host tensors, optional), assemble in node-layer slabs, and copy
-        each slab's CSR values (one contiguous range) to values_host (pinned float64 [nnz]) on a copy
-        stream while the next slab computes.  Consecutive slabs alternate between `stream` and a
-        second compute stream, so the last wave of one slab's grid overlaps the first wave of the
-        next.  slabs: number of slabs (default: slabs of 16 node layers, two of the kernel's 8-layer
-        blocks).  Returns values_host; all work is ordered before later work on `stream`."""
+                         kappa_host=None, slab_layers: int = 16, stream=None) -> torch.Tensor:
+        """End-to-end assembly with host buffers on Iron's regular generated mesh
+        (gfe_laplace_assemble_regular_host): the geometry and conductivity are copied in from the
+        pinned host tensors coords_host [3][N] / kappa_host [n_elements] (optional: None keeps the
+        device copies), assembled in node-layer slabs (8 layers first, then slab_layers each, a
+        multiple of 8), and each slab's CSR values, one contiguous range, are copied to values_host
+        (pinned float64 [nnz]) while later slabs compute.  Inputs are uploaded and converted slab
+        by slab, so the first copy-out starts after one 8-layer slab.  Returns values_host; all
+        work is ordered before later work on `stream`."""
         if self.regular is None:
             raise GfeError(-1, "the slab pipeline needs Iron's regular generated mesh")
         if values_host.numel() != self.nnz or values_host.dtype != torch.float64 or values_host.is_cuda:
             raise GfeError(-1, f"values_host must be a host float64 tensor of {self.nnz} entries")
+        for name, h, d in (("coords_host", coords_host, self.coords), ("kappa_host", kappa_host, self.kappa)):
+            if h is None:
+                continue
+            if d is None or h.is_cuda or h.dtype != torch.float64 or h.numel() != d.numel() or not h.is_contiguous():
+                raise GfeError(-1, f"{name} must be a contiguous host float64 tensor like the device copy")
         st = stream if stream is not None else torch.cuda.current_stream(self.device)
         L = _lib.load()
         nx, ny, nz = self.regular
         prec = PRECISIONS[precision]
-        if getattr(self, "_copy_stream", None) is None:
-            self._copy_stream = torch.cuda.Stream(self.device)
-            self._compute_stream2 = torch.cuda.Stream(self.device)
-            self._row_ptr_host = self.row_ptr.cpu().numpy()
         if getattr(self, "_asm_ws_prec", None) != prec:
             wb = int(L.gfe_laplace_regular_workspace_bytes(nx, ny, nz, prec))
             self._asm_ws = torch.empty(max(wb, 16), dtype=torch.uint8, device=self.device)
             self._asm_ws_prec = prec
-        cs = self._copy_stream
-        rp = self._row_ptr_host
-        NZ, NXY = nz + 1, (nx + 1) * (ny + 1)
-        step = 16 if slabs is None else -(-NZ // max(int(slabs), 1))
-        step = -(-step // 8) * 8  # slabs start at multiples of the kernel's 8-layer blocks
-        st2 = self._compute_stream2
-        with torch.cuda.stream(st):
-            if coords_host is not None:
-                self.coords.copy_(coords_host, non_blocking=True)
-            if kappa_host is not None:
-                self.kappa.copy_(kappa_host, non_blocking=True)
-            args = (nx, ny, nz, _lib.ptr(self.coords), _lib.ptr(self.kappa), _lib.ptr(self.row_ptr),
-                    _lib.ptr(self.values), None, _lib.ptr(self.rhs), prec, _lib.ptr(self._asm_ws))
-            # the FP32-pipe kernels read a converted copy of the coordinates, made once here; the
-            # FP64 kernel reads them directly
-            converted = prec != GFE_FP64
-            if converted:
-                _lib.call("gfe_laplace_assemble_regular_layers", *args, 0, 0, 1, _lib.stream_handle(st))
-            ready = torch.cuda.Event()
-            ready.record(st)
-            st2.wait_event(ready)
-            l0, i = 0, 0
-            while l0 < NZ:
-                l1 = min(l0 + step, NZ)
-                sk = st if i % 2 == 0 else st2
-                _lib.call("gfe_laplace_assemble_regular_layers", *args, l0, l1, 0 if converted else 1,
-                          _lib.stream_handle(sk))
-                ev = torch.cuda.Event()
-                ev.record(sk)
-                cs.wait_event(ev)
-                a, b = int(rp[l0 * NXY]) - 1, int(rp[l1 * NXY]) - 1
-                with torch.cuda.stream(cs):
-                    values_host[a:b].copy_(self.values[a:b], non_blocking=True)
-                l0, i = l1, i + 1
-            for other in (st2, cs):
-                done = torch.cuda.Event()
-                done.record(other)
-                st.wait_event(done)
+        _lib.call("gfe_laplace_assemble_regular_host", nx, ny, nz, _lib.host_ptr(coords_host),
+                  _lib.host_ptr(kappa_host), _lib.ptr(self.coords), _lib.ptr(self.kappa), _lib.ptr(self.row_ptr),
+                  _lib.ptr(self.values), _lib.host_ptr(values_host), _lib.ptr(self.rhs), prec, _lib.ptr(self._asm_ws), int(slab_layers),
+                  _lib.stream_handle(st))
         return values_host
 
     def element_matrices(self, precision: str = "fp64", stream=None) -> torch.Tensor:

@@ -203,18 +203,38 @@ def test_kappa_solve_fp64_and_mixed(gfe_cuda):
     assert np.abs(x2.cpu().numpy() - uo).max() <= 1e-10 * np.abs(uo).max(), info2
 
 
-@pytest.mark.parametrize("precision,slabs", [("mixed_df", 3), ("mixed", 1), ("fp64", 4), ("mixed_df", None)])
-def test_slab_pipelined_host_assembly_equals_device(gfe_cuda, precision, slabs):
-    """assemble_to_host (node-layer slabs, device-to-host copies overlapping the next slab) gives
-    exactly the values of the one-shot regular-mesh assembly."""
+@pytest.mark.parametrize("precision,slab_layers", [("mixed_df", 8), ("mixed", 24), ("fp64", 16), ("mixed_df", 16),
+                                                   ("mixed_df", 64)])
+def test_slab_pipelined_host_assembly_equals_device(gfe_cuda, precision, slab_layers):
+    """gfe_laplace_assemble_regular_host (inputs uploaded and converted slab by slab, device-to-host
+    copies overlapping later slabs) gives exactly the values of the one-shot regular-mesh assembly;
+    the device copies of the inputs are cleared first, so every layer a slab reads must have been
+    uploaded before it runs, and every CSR entry must come back."""
     m = _mesh((9, 7, 21), 5)
     kap = _kappa(m.n_elements, 6)
     A = LaplaceAssembly.from_regular_mesh(m, kappa=kap)
     ref = A.assemble(precision, path="regular").cpu().clone()
-    host = torch.zeros(A.nnz, dtype=torch.float64).pin_memory()
+    host = torch.full((A.nnz,), float("nan"), dtype=torch.float64).pin_memory()
     A.values.zero_()
+    A.coords.zero_()
+    A.kappa.zero_()
     coords_h = torch.from_numpy(m.coords).pin_memory()
     kappa_h = torch.from_numpy(kap).pin_memory()
-    A.assemble_to_host(host, precision, coords_host=coords_h, kappa_host=kappa_h, slabs=slabs)
+    A.assemble_to_host(host, precision, coords_host=coords_h, kappa_host=kappa_h, slab_layers=slab_layers)
     torch.cuda.synchronize()
     assert torch.equal(host, ref)
+    # inputs already resident: the device copies are used as they are
+    host2 = torch.zeros(A.nnz, dtype=torch.float64).pin_memory()
+    A.assemble_to_host(host2, precision, slab_layers=slab_layers)
+    torch.cuda.synchronize()
+    assert torch.equal(host2, ref)
+
+
+def test_host_pipeline_rejects_bad_arguments(gfe_cuda):
+    m = _mesh((3, 3, 3), 1)
+    A = LaplaceAssembly.from_regular_mesh(m)
+    host = torch.zeros(A.nnz, dtype=torch.float64)
+    with pytest.raises(GfeError, match="multiple of 8"):
+        A.assemble_to_host(host, "mixed_df", slab_layers=12)
+    with pytest.raises(GfeError, match="coords_host"):
+        A.assemble_to_host(host, "mixed_df", coords_host=torch.zeros(5, dtype=torch.float64))
