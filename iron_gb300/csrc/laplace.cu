@@ -27,6 +27,7 @@
 //    writes the row exactly once.  CSR slot positions follow from the 27-point stencil
 //    (verified once against the structure by gfe_laplace_regular_check), so the kernel reads no
 //    column indices.
+#include <atomic>
 #include <cmath>
 #include <type_traits>
 #include <vector>
@@ -295,14 +296,29 @@ __global__ void to_fp32(const double* __restrict__ v, float* __restrict__ v32, l
 // ---------------------------------------------------------------------------------------------
 // Iron's regular generated mesh: tiled, row-owning assembly
 // ---------------------------------------------------------------------------------------------
-// Node tile TX x TY in x-y; the element tile is (TX+1) x (TY+1) = 16 x 8 = 128 elements, one per
+// Node tile TX x TY in x-y; the element tile is (TX+1) x (TY+1) = 16 x 12 = 192 elements, one per
 // thread.  Element matrices are kept in shared memory in the element arithmetic type; the row sums
 // are accumulated in FP64 (GFE_FP64) or float-float (the FP32-pipe precisions), so the FP32 paths
 // issue FP64 instructions only for the final conversion of each written entry.
-constexpr int kRTX = 15, kRTY = 7;
-constexpr int kREX = kRTX + 1, kREY = kRTY + 1;  // 16 x 8 elements
-constexpr int kRThreads = kREX * kREY;           // 128
-constexpr int kRZ = 8;                           // node layers per CTA
+// The kernel is persistent: the work, (tile column) x (node layer), is linearised column by
+// column and cut into one contiguous, equal share per CTA; a CTA walks its share as runs of
+// consecutive node layers, recomputing only the element layer below each run.  So the grid is
+// sized to the resident CTAs (no tail wave) and runs are long (little recomputation in z).
+constexpr int kRTX = 15, kRTY = 11;
+constexpr int kREX = kRTX + 1, kREY = kRTY + 1;  // 16 x 12 elements
+constexpr int kRThreads = kREX * kREY;           // 192
+constexpr int kRZ = 8;                           // alignment of the layer ranges of the slab API
+constexpr int kRMinRun = 8;                      // node layers per CTA at least, when work is scarce
+// Resident CTAs per SM the register allocation must allow: two 192-thread CTAs fill the shared
+// memory with float-float or FP64 element matrices; FP32 matrices take half of it.
+template <typename T>
+struct RMinBlocks {
+  static constexpr int value = 2;
+};
+template <>
+struct RMinBlocks<float> {
+  static constexpr int value = 3;
+};
 
 template <typename T>
 struct StoreOf {
@@ -348,6 +364,11 @@ __global__ void split_coords(long long n, const double* __restrict__ in, T* __re
     out[i] = from_double<T>(in[i]);
 }
 
+template <typename P>
+__device__ __forceinline__ void prefetch_l1(const P* p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ double load_coord(const double* p) { return __ldg(p); }
 __device__ __forceinline__ float load_coord(const float* p) { return __ldg(p); }
 __device__ __forceinline__ f2 load_coord(const f2* p) {
@@ -356,109 +377,159 @@ __device__ __forceinline__ f2 load_coord(const f2* p) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kRThreads)
+__global__ void __launch_bounds__(kRThreads, RMinBlocks<T>::value)
 laplace_regular_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ coords,
                        const double* __restrict__ kappa, const int32_t* __restrict__ rp, double* __restrict__ values,
-                       float* __restrict__ values32, double* __restrict__ rhs, unsigned* err,
-                       int32_t layer0 = 0, int32_t layer_end = 0x7fffffff) {
+                       float* __restrict__ values32, double* __restrict__ rhs, unsigned* err, int32_t layer0,
+                       int32_t layer_end) {
   using S = typename StoreOf<T>::type;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   S(*sK)[36][kRThreads] = reinterpret_cast<S(*)[36][kRThreads]>(smem_raw);  // [layer buffer][entry][element]
   const int tid = threadIdx.x;
-  // node layers [layer0, layer_end) of the mesh; layer0 is a multiple of kRZ
-  const int x0 = blockIdx.x * kRTX, y0 = blockIdx.y * kRTY, k0 = layer0 + blockIdx.z * kRZ;
   const int NX = nx + 1, NY = ny + 1, NZ = nz + 1;
   const long long NXY = (long long)NX * NY;
-  const int k1 = min(min(k0 + kRZ, NZ), layer_end);
-  // element owned by this thread in each element layer
-  const int ex = x0 - 1 + (tid % kREX), ey = y0 - 1 + (tid / kREX);
-  const bool e_in_xy = ex >= 0 && ex < nx && ey >= 0 && ey < ny;
-  // node owned by this thread (threads 0 .. TX*TY-1)
-  const int ni = x0 + tid % kRTX, nj = y0 + tid / kRTX;
-  const bool owns_node = tid < kRTX * kRTY && ni < NX && nj < NY;
+  // node layers [layer0, layer_end) of every tile column; this CTA's share [s, e) of the
+  // linearised (column, layer) work
+  const int tiles_x = (NX + kRTX - 1) / kRTX, tiles_y = (NY + kRTY - 1) / kRTY;
+  const long long nl = layer_end - layer0;
+  const long long W = (long long)tiles_x * tiles_y * nl;
+  long long s = W * blockIdx.x / gridDim.x;
+  const long long e_share = W * (blockIdx.x + 1) / gridDim.x;
   T p, q;
   gauss_pq(p, q);
   bool bad = false;
+  while (s < e_share) {  // uniform across the CTA
+    const long long col = s / nl;
+    const int off = (int)(s - col * nl);
+    const int run = (int)min(nl - off, e_share - s);
+    s += run;
+    const int k0 = layer0 + off, k1 = k0 + run;
+    const int x0 = (int)(col % tiles_x) * kRTX, y0 = (int)(col / tiles_x) * kRTY;
+    // element owned by this thread in each element layer
+    const int ex = x0 - 1 + (tid % kREX), ey = y0 - 1 + (tid / kREX);
+    const bool e_in_xy = ex >= 0 && ex < nx && ey >= 0 && ey < ny;
+    // node owned by this thread (threads 0 .. TX*TY-1)
+    const int ni = x0 + tid % kRTX, nj = y0 + tid / kRTX;
+    const bool owns_node = tid < kRTX * kRTY && ni < NX && nj < NY;
 
-  auto compute_layer = [&](int ez, int buf) {
-    if (e_in_xy && ez >= 0 && ez < nz) {
-      T x[3][8];
+    auto compute_layer = [&](int ez, int buf) {
+      if (e_in_xy && ez >= 0 && ez < nz) {
+        T x[3][8];
 #pragma unroll
-      for (int m = 0; m < 8; ++m) {
-        const long long n = (long long)(ex + (m & 1)) + (long long)(ey + ((m >> 1) & 1)) * NX + (ez + (m >> 2)) * NXY;
+        for (int m = 0; m < 8; ++m) {
+          const long long n = (long long)(ex + (m & 1)) + (long long)(ey + ((m >> 1) & 1)) * NX + (ez + (m >> 2)) * NXY;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) x[c][m] = load_coord(coords + c * NXY * NZ + n);
+          for (int c = 0; c < 3; ++c) x[c][m] = load_coord(coords + c * NXY * NZ + n);
+        }
+        const long long e = (long long)ex + (long long)ey * nx + (long long)ez * nx * ny;
+        const T kap = from_double<T>(kappa ? __ldg(kappa + e) : 1.0);
+        T K[36];
+        if (!laplace_hex8<T>(x, kap, p, q, K)) bad = true;
+#pragma unroll
+        for (int k = 0; k < 36; ++k) sK[buf][k][tid] = K[k];
       }
-      const long long e = (long long)ex + (long long)ey * nx + (long long)ez * nx * ny;
-      const T kap = from_double<T>(kappa ? __ldg(kappa + e) : 1.0);
-      T K[36];
-      if (!laplace_hex8<T>(x, kap, p, q, K)) bad = true;
+    };
+    // The next element layer's new node plane (z = ez + 1) and conductivities are prefetched into
+    // L1 before the node phase of the current layer, so that phase hides their latency; the lower
+    // plane is the one the current layer has just read.
+    auto prefetch_layer = [&](int ez) {
+      if (e_in_xy && ez >= 0 && ez < nz) {
 #pragma unroll
-      for (int k = 0; k < 36; ++k) sK[buf][k][tid] = K[k];
-    }
-  };
-  using A = typename AccOf<T>::type;
+        for (int m = 4; m < 8; ++m) {
+          const long long n = (long long)(ex + (m & 1)) + (long long)(ey + ((m >> 1) & 1)) * NX + (ez + 1) * NXY;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) prefetch_l1(coords + c * NXY * NZ + n);
+        }
+        if (kappa) prefetch_l1(kappa + (long long)ex + (long long)ey * nx + (long long)ez * nx * ny);
+      }
+    };
+    using A = typename AccOf<T>::type;
 
-  compute_layer(k0 - 1, (k0 - 1) & 1);
-  for (int k = k0; k < k1; ++k) {
-    compute_layer(k, k & 1);
-    __syncthreads();
-    if (owns_node) {
-      A acc[27];
+    // element layer k0 - 1 (below the first node layer) is computed in the first pass; the element
+    // routine has a single call site, so its code is not duplicated
+#pragma unroll 1
+    for (int k = k0 - 1; k < k1; ++k) {
+      compute_layer(k, k & 1);
+      if (k + 1 < k1) prefetch_layer(k + 1);
+      if (k < k0) continue;  // uniform across the CTA
+      __syncthreads();
+      if (owns_node) {
+        A acc[27];
 #pragma unroll
-      for (int s = 0; s < 27; ++s) acc[s] = from_double<A>(0.0);
-      // surrounding elements (i-1+a, j-1+b, k-1+c) in the fixed order c, b, a
+        for (int s = 0; s < 27; ++s) acc[s] = from_double<A>(0.0);
+        // surrounding elements (i-1+a, j-1+b, k-1+c) in the fixed order c, b, a
 #pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        const int ez = k - 1 + c;
-        if (ez < 0 || ez >= nz) continue;
-        const int buf = ez & 1;
+        for (int c = 0; c < 2; ++c) {
+          const int ez = k - 1 + c;
+          if (ez < 0 || ez >= nz) continue;
+          const int buf = ez & 1;
 #pragma unroll
-        for (int b = 0; b < 2; ++b) {
-          const int ey2 = nj - 1 + b;
-          if (ey2 < 0 || ey2 >= ny) continue;
+          for (int b = 0; b < 2; ++b) {
+            const int ey2 = nj - 1 + b;
+            if (ey2 < 0 || ey2 >= ny) continue;
 #pragma unroll
-          for (int a = 0; a < 2; ++a) {
-            const int ex2 = ni - 1 + a;
-            if (ex2 < 0 || ex2 >= nx) continue;
-            const int slot = (ex2 - (x0 - 1)) + (ey2 - (y0 - 1)) * kREX;
-            const int li = (1 - a) + 2 * (1 - b) + 4 * (1 - c);
+            for (int a = 0; a < 2; ++a) {
+              const int ex2 = ni - 1 + a;
+              if (ex2 < 0 || ex2 >= nx) continue;
+              const int slot = (ex2 - (x0 - 1)) + (ey2 - (y0 - 1)) * kREX;
+              const int li = (1 - a) + 2 * (1 - b) + 4 * (1 - c);
 #pragma unroll
-            for (int lj = 0; lj < 8; ++lj) {
-              const int di = a - 1 + (lj & 1), dj = b - 1 + ((lj >> 1) & 1), dk = c - 1 + (lj >> 2);
-              const int m = li < lj ? li : lj, n = li < lj ? lj : li;
-              const int q = (dk + 1) * 9 + (dj + 1) * 3 + (di + 1);
-              acc[q] = acc_add(acc[q], sK[buf][tri(m, n)][slot]);
+              for (int lj = 0; lj < 8; ++lj) {
+                const int di = a - 1 + (lj & 1), dj = b - 1 + ((lj >> 1) & 1), dk = c - 1 + (lj >> 2);
+                const int m = li < lj ? li : lj, n = li < lj ? lj : li;
+                const int q = (dk + 1) * 9 + (dj + 1) * 3 + (di + 1);
+                acc[q] = acc_add(acc[q], sK[buf][tri(m, n)][slot]);
+              }
             }
           }
         }
-      }
-      // write the row: the 27-point stencil clipped to the mesh, in ascending column order
-      const long long r = (long long)ni + (long long)nj * NX + (long long)k * NXY;
-      long long pos = (long long)__ldg(rp + r) - 1;
+        // write the row: the 27-point stencil clipped to the mesh, in ascending column order
+        const long long r = (long long)ni + (long long)nj * NX + (long long)k * NXY;
+        long long pos = (long long)__ldg(rp + r) - 1;
 #pragma unroll
-      for (int dk = -1; dk <= 1; ++dk) {
-        if (k + dk < 0 || k + dk >= NZ) continue;
+        for (int dk = -1; dk <= 1; ++dk) {
+          if (k + dk < 0 || k + dk >= NZ) continue;
 #pragma unroll
-        for (int dj = -1; dj <= 1; ++dj) {
-          if (nj + dj < 0 || nj + dj >= NY) continue;
+          for (int dj = -1; dj <= 1; ++dj) {
+            if (nj + dj < 0 || nj + dj >= NY) continue;
 #pragma unroll
-          for (int di = -1; di <= 1; ++di) {
-            if (ni + di < 0 || ni + di >= NX) continue;
-            double v;
-            float v32;
-            entry_out(acc[(dk + 1) * 9 + (dj + 1) * 3 + (di + 1)], !std::is_same<T, float>::value, v, v32);
-            values[pos] = v;
-            if (values32) values32[pos] = v32;
-            ++pos;
+            for (int di = -1; di <= 1; ++di) {
+              if (ni + di < 0 || ni + di >= NX) continue;
+              double v;
+              float v32;
+              entry_out(acc[(dk + 1) * 9 + (dj + 1) * 3 + (di + 1)], !std::is_same<T, float>::value, v, v32);
+              values[pos] = v;
+              if (values32) values32[pos] = v32;
+              ++pos;
+            }
           }
         }
+        if (rhs) rhs[r] = 0.0;
       }
-      if (rhs) rhs[r] = 0.0;
+      __syncthreads();
     }
-    __syncthreads();
   }
   if (bad) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+}
+
+// Persistent grid of the regular-mesh kernel: the resident CTAs, but no more than one CTA per
+// kRMinRun layers of one tile column.
+template <typename T>
+int regular_grid(int32_t nx, int32_t ny, int32_t l0, int32_t l1, size_t smem, int* grid) {
+  static std::atomic<int> cached[64];  // resident CTAs per SM, per device (0: not yet queried)
+  int dev = 0;
+  GFE_CUDA_TRY(cudaGetDevice(&dev));
+  int per_sm = dev < 64 ? cached[dev].load(std::memory_order_relaxed) : 0;
+  if (per_sm == 0) {
+    GFE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, laplace_regular_kernel<T>, kRThreads, smem));
+    if (dev < 64) cached[dev].store(per_sm, std::memory_order_relaxed);
+  }
+  const long long cols = (long long)((nx + 1 + kRTX - 1) / kRTX) * ((ny + 1 + kRTY - 1) / kRTY);
+  const long long W = cols * (l1 - l0);
+  const long long g = std::min<long long>((long long)std::max(per_sm, 1) * gfe::sm_count(),
+                                          std::max<long long>(1, (W + kRMinRun - 1) / kRMinRun));
+  *grid = (int)g;
+  return GFE_OK;
 }
 
 // Structure check: every row of the CSR is the clipped 27-point stencil of a regular mesh.
@@ -528,12 +599,14 @@ size_t regular_workspace_bytes(int32_t nx, int32_t ny, int32_t nz, int precision
 // or NULL to allocate it on the stream; split: convert the coordinates into it first (the later
 // layer calls of one assembly reuse the converted array).
 template <typename T>
-int launch_regular(dim3 grid, cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const double* coords,
+int launch_regular(cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const double* coords,
                    const double* kappa, const int32_t* rp, double* values, float* values32, double* rhs,
                    unsigned* err, void* ws, int32_t l0, int32_t l1, bool split) {
   const size_t smem = 2 * 36 * kRThreads * sizeof(typename StoreOf<T>::type);
   GFE_CUDA_TRY(cudaFuncSetAttribute((const void*)laplace_regular_kernel<T>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int grid = 0;
+  if (int rc = regular_grid<T>(nx, ny, l0, l1, smem, &grid)) return rc;
   const long long n3 = 3ll * (nx + 1) * (ny + 1) * (nz + 1);
   T* ct = static_cast<T*>(ws);
   if (!ct)
@@ -546,12 +619,14 @@ int launch_regular(dim3 grid, cudaStream_t s, int32_t nx, int32_t ny, int32_t nz
 }
 
 template <>
-int launch_regular<double>(dim3 grid, cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const double* coords,
+int launch_regular<double>(cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const double* coords,
                            const double* kappa, const int32_t* rp, double* values, float* values32, double* rhs,
                            unsigned* err, void*, int32_t l0, int32_t l1, bool) {
   const size_t smem = 2 * 36 * kRThreads * sizeof(double);
   GFE_CUDA_TRY(cudaFuncSetAttribute((const void*)laplace_regular_kernel<double>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int grid = 0;
+  if (int rc = regular_grid<double>(nx, ny, l0, l1, smem, &grid)) return rc;
   laplace_regular_kernel<double><<<grid, kRThreads, smem, s>>>(nx, ny, nz, coords, kappa, rp, values, values32, rhs,
                                                                err, l0, l1);
   return GFE_OK;
@@ -655,19 +730,18 @@ extern "C" int gfe_laplace_assemble_regular_layers(int32_t nx, int32_t ny, int32
     return GFE_OK;
   }
   unsigned* err = gfe::device_error_word();
-  const dim3 grid((nx + 1 + kRTX - 1) / kRTX, (ny + 1 + kRTY - 1) / kRTY, (layer_end - layer_begin + kRZ - 1) / kRZ);
   void* prof = gfe::stage_begin(GFE_STAGE_LAPLACE_ELEMENTS, s);
   int rc;
   const int32_t l0 = layer_begin, l1 = layer_end;
   const bool cv = convert_coords != 0;
   if (precision == GFE_FP64)
-    rc = launch_regular<double>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace,
+    rc = launch_regular<double>(s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace,
                                 l0, l1, cv);
   else if (precision == GFE_MIXED)
-    rc = launch_regular<float>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace,
+    rc = launch_regular<float>(s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace,
                                l0, l1, cv);
   else
-    rc = launch_regular<f2>(grid, s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace, l0,
+    rc = launch_regular<f2>(s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace, l0,
                             l1, cv);
   gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, 1);
   if (rc) return rc;
@@ -796,17 +870,15 @@ extern "C" int gfe_laplace_assemble_regular_host(int32_t nx, int32_t ny, int32_t
     // the slab on alternating compute streams: one slab's last wave overlaps the next one's first
     cudaStream_t cs = hp->comp[i & 1];
     GFE_CUDA_TRY(cudaStreamWaitEvent(cs, ev_in, 0));
-    const dim3 grid((unsigned)((NX + kRTX - 1) / kRTX), (unsigned)((NY + kRTY - 1) / kRTY),
-                    (unsigned)((l1 - l0 + kRZ - 1) / kRZ));
     int rc;
     if (precision == GFE_FP64)
-      rc = launch_regular<double>(grid, cs, nx, ny, nz, coords, kappa, row_ptr, values, nullptr, rhs, err, nullptr,
+      rc = launch_regular<double>(cs, nx, ny, nz, coords, kappa, row_ptr, values, nullptr, rhs, err, nullptr,
                                   l0, l1, false);
     else if (precision == GFE_MIXED)
-      rc = launch_regular<float>(grid, cs, nx, ny, nz, coords, kappa, row_ptr, values, nullptr, rhs, err, workspace,
+      rc = launch_regular<float>(cs, nx, ny, nz, coords, kappa, row_ptr, values, nullptr, rhs, err, workspace,
                                  l0, l1, false);
     else
-      rc = launch_regular<f2>(grid, cs, nx, ny, nz, coords, kappa, row_ptr, values, nullptr, rhs, err, workspace,
+      rc = launch_regular<f2>(cs, nx, ny, nz, coords, kappa, row_ptr, values, nullptr, rhs, err, workspace,
                               l0, l1, false);
     if (rc) return rc;
     GFE_CUDA_TRY(cudaEventRecord(ev_c, cs));
