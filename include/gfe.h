@@ -103,6 +103,41 @@ int gfe_probe_fma_rate(int32_t precision, double* gflops_host, void* stream);
 int gfe_csr_structure(int32_t n_elem, int32_t dofs_per_elem, const int32_t* elem_dofs, int32_t n_dofs,
                       int32_t* row_ptr, int32_t* col_idx, int64_t col_capacity, int64_t* nnz_host, void* stream);
 
+/* ---- solver system: Dirichlet elimination -------------------------------------------------- */
+
+/* The reduced system Iron hands to its linear solver for one linear equations set with Dirichlet
+ * conditions on one rank: rows and columns of fixed DOFs removed, their coupling moved to the
+ * right-hand side.  Replaces, for that case, the solver mapping (src/solver_mapping_routines.F90:
+ * 398-520), SOLVER_MATRIX_STRUCTURE_CALCULATE (src/solver_matrices_routines.F90:1612-2431),
+ * SOLVER_MATRIX_EQUATIONS_MATRIX_ADD (:806-1023) and the linear branch of
+ * SOLVER_MATRICES_STATIC_ASSEMBLE (src/solver_routines.F90:14025-15050); structure, values and
+ * right-hand side are bit-identical to Iron's.  Equations CSR 1-based (n rows), fixed[n] != 0
+ * marks a Dirichlet DOF.
+ *
+ * gfe_solver_structure: solver_of_dof[n] out (0-based solver number, -1 for a fixed DOF; free
+ * DOFs numbered in ascending order), s_row_ptr[n_free + 1] out (capacity n + 1), s_col_idx out
+ * (1-based; may be NULL to query nnz only), n_free_host / nnz_host out.  Synchronises `stream`. */
+int gfe_solver_structure(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const uint8_t* fixed,
+                         int32_t* solver_of_dof, int32_t* s_row_ptr, int32_t* s_col_idx, int64_t col_capacity,
+                         int32_t* n_free_host, int64_t* nnz_host, void* stream);
+/* Solver matrix values from the equations matrix values: every free-free entry, 0 + K(i, j), into
+ * s_values, and/or rounded to FP32 into s_values32 (for mixed-precision solves); either may be NULL. */
+int gfe_solver_matrix(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const double* values,
+                      const int32_t* solver_of_dof, const int32_t* s_row_ptr, double* s_values, float* s_values32,
+                      void* stream);
+/* Solver right-hand side: for free row i, in ascending order of the contributing equations row r,
+ * f(i) at r = i and -1 * K(i, r) * u(r) for each fixed column r with |u(r)| and |K(i, r)| at least
+ * ZERO_TOLERANCE = 5 EPSILON(1.0_DP).  f (equations RHS) may be NULL (zero).  u holds the
+ * Dirichlet values at fixed DOFs.  col_listed (may be NULL = all): the fixed columns whose
+ * coupling Iron moves to the right-hand side -- its Dirichlet column lists hold only DOFs on
+ * boundary nodes (src/equations_matrices_routines.F90:4531-4561). */
+int gfe_solver_rhs(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, const double* values, const double* f,
+                   const double* u, const uint8_t* fixed, const uint8_t* col_listed, const int32_t* solver_of_dof,
+                   double* s_rhs, void* stream);
+/* Copy a solver solution back into the dependent vector: u[i] = x[solver_of_dof[i]] for free i
+ * (the update of the dependent field from the solver variables, coupling coefficient 1). */
+int gfe_solver_update_dependent(int32_t n, const int32_t* solver_of_dof, const double* x, double* u, void* stream);
+
 /* ---- Laplace / diffusion assembly (K1 + K2) -------------------------------------------- */
 
 /* Assemble the global stiffness matrix of the Laplace equation on trilinear-Lagrange hexahedra

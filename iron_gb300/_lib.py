@@ -66,6 +66,11 @@ SIGNATURES = {
                                                     vp]),
     "gfe_laplace_regular_check": (C.c_int, [i32, i32, i32, vp, vp, C.POINTER(C.c_int64), vp]),
     "gfe_csr_spmv": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
+    "gfe_solver_structure": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, C.c_int64, C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_int64), vp]),
+    "gfe_solver_matrix": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "gfe_solver_rhs": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "gfe_solver_update_dependent": (C.c_int, [i32, vp, vp, vp, vp]),
     "gfe_mr_residual": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp]),
     "gfe_mr_slot_map": (C.c_int, [i32, vp, vp, i32, vp, vp, vp, vp, vp]),
     "gfe_mr_jacobian": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, vp, vp, vp, vp, i64, vp, i32, vp]),

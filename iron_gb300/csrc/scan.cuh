@@ -4,6 +4,8 @@
 #include "gfe_internal.cuh"
 
 namespace gfe {
+// internal linkage: every translation unit that includes this header gets its own kernels
+namespace {
 
 constexpr int kScanBlock = 1024;
 constexpr int kScanItems = 4;  // items per thread
@@ -102,4 +104,5 @@ int exclusive_scan(const TIn* in, long long n, long long* out, long long* total_
   return GFE_OK;
 }
 
+}  // namespace
 }  // namespace gfe

@@ -197,6 +197,46 @@ class LaplaceAssembly:
                   _lib.stream_handle(stream))
         return SolveInfo(int(it.value), float(rel.value), precision)
 
+    def solver_system(self, fixed: torch.Tensor, col_listed="boundary", stream=None):
+        """Iron's solver system (Dirichlet DOFs `fixed` removed, their coupling moved to the
+        right-hand side) for this matrix structure; see iron_gb300.solver_system.SolverSystem.
+        col_listed: "boundary" (the fixed DOFs on boundary nodes, as Iron's Dirichlet column lists
+        record them; on Iron's regular generated mesh), None (all fixed DOFs) or a mask."""
+        from .mesh import boundary_node_mask
+        from .solver_system import SolverSystem
+
+        if isinstance(col_listed, str):
+            if col_listed != "boundary":
+                raise GfeError(-1, f"unknown col_listed {col_listed!r}")
+            if self.regular is None:
+                raise GfeError(-1, "col_listed='boundary' needs Iron's regular generated mesh; pass a mask")
+            col_listed = torch.from_numpy(boundary_node_mask(self.regular, 1).astype("uint8")).to(self.device)
+        return SolverSystem(self.row_ptr, self.col_idx, fixed, col_listed, stream=stream)
+
+    def solve_reduced(self, fixed: torch.Tensor, x: torch.Tensor, f: torch.Tensor | None = None, rtol: float = 1e-12,
+                      max_iters: int = 200000, precision: str = "fp64", system=None, stream=None) -> SolveInfo:
+        """Iron's solve path: build the solver system (SOLVER_MATRICES_STATIC_ASSEMBLE), solve it by
+        Jacobi-preconditioned CG (FP64, or FP32 inner solves inside FP64 refinement for the mixed
+        precisions), and copy the solution into the free DOFs of x (the dependent-field update).
+        x holds the Dirichlet values at fixed DOFs on entry.  system: a SolverSystem of `fixed` to
+        reuse (its structure is built once per set of fixed DOFs)."""
+        S = system if system is not None else self.solver_system(fixed, stream=stream)
+        prec = GFE_FP64 if precision == "fp64" else GFE_MIXED
+        if prec == GFE_MIXED:
+            sv, sv32 = S.matrix(self.values, fp32=True, stream=stream)
+        else:
+            sv, sv32 = S.matrix(self.values, stream=stream), None
+        b = S.rhs(self.values, x, f, stream=stream)
+        xs = torch.zeros(max(S.n_free, 1), dtype=torch.float64, device=self.device)
+        it = C.c_int32(0)
+        rel = C.c_double(0.0)
+        if S.n_free > 0:
+            _lib.call("gfe_cg_solve", S.n_free, _lib.ptr(S.row_ptr), _lib.ptr(S.col_idx), _lib.ptr(sv), _lib.ptr(sv32),
+                      _lib.ptr(b), None, _lib.ptr(xs), float(rtol), int(max_iters), prec, C.byref(it), C.byref(rel),
+                      _lib.stream_handle(stream))
+            S.update_dependent(xs, x, stream=stream)
+        return SolveInfo(int(it.value), float(rel.value), precision)
+
     def to_iron_csr(self):
         """Host copy of the CSR matrix exactly as Iron stores it: (row_ptr 1-based, col_idx 1-based,
         values).  Analogue of cmfe_DistributedMatrix_StorageLocationsGet / DataGet

@@ -41,6 +41,9 @@ def lib():
         L.orc_laplace_assemble.argtypes = [C.c_int, i32p, i32p, C.c_int, C.c_int, i32p, f64p, C.c_void_p,
                                            i32p, i32p, f64p, C.c_void_p, C.c_int]
         L.orc_csr_spmv.argtypes = [C.c_int, i32p, i32p, f64p, f64p, f64p]
+        L.orc_solver_system.argtypes = [C.c_int, i32p, i32p, f64p, C.c_void_p, u8p, C.c_void_p, f64p, i32p, i32p,
+                                        i32p, f64p, f64p, C.c_int64, C.POINTER(C.c_int32)]
+        L.orc_solver_system.restype = C.c_int64
         L.orc_cg_dirichlet.argtypes = [C.c_int, i32p, i32p, f64p, C.c_void_p, u8p, f64p, C.c_double, C.c_int,
                                        C.POINTER(C.c_double)]
         _register_mr(L)
@@ -218,3 +221,28 @@ def cg_dirichlet(rp, ci, vals, f, fixed, x_fixed, rtol=1e-12, max_it=100000):
     if it < 0:
         raise RuntimeError("oracle CG did not converge")
     return x, it, rel.value
+
+
+def solver_system(rp, ci, vals, f, fixed, u, col_listed=None):
+    """Iron's solver system (reduced CSR, values and right-hand side) of a linear equations set
+    with Dirichlet DOFs `fixed` at values u; see orc_solver_system."""
+    n = len(rp) - 1
+    rp, ci, vals, u = _i32(rp), _i32(ci), _f64(vals), _f64(u)
+    fixed = np.ascontiguousarray(fixed, dtype=np.uint8)
+    fv = None if f is None else _f64(f)
+    cl = None if col_listed is None else np.ascontiguousarray(col_listed, dtype=np.uint8)
+    cap = int(rp[-1] - 1)
+    sod = np.empty(n, np.int32)
+    s_rp = np.empty(n + 1, np.int32)
+    s_ci = np.empty(max(cap, 1), np.int32)
+    s_v = np.empty(max(cap, 1), np.float64)
+    s_rhs = np.empty(max(n, 1), np.float64)
+    nf = C.c_int32(0)
+    nnz = lib().orc_solver_system(n, rp, ci, vals, None if fv is None else fv.ctypes.data, fixed,
+                                  None if cl is None else cl.ctypes.data, u, sod, s_rp, s_ci, s_v, s_rhs, cap,
+                                  C.byref(nf))
+    if nnz < 0:
+        raise RuntimeError("oracle solver system failed")
+    k = nf.value
+    return {"solver_of_dof": sod, "row_ptr": s_rp[:k + 1].copy(), "col_idx": s_ci[:nnz].copy(),
+            "values": s_v[:nnz].copy(), "rhs": s_rhs[:k].copy(), "n_free": k}

@@ -463,6 +463,90 @@ void orc_csr_spmv(int n, const int32_t* rp, const int32_t* ci, const double* v, 
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Solver system of one linear equations set with Dirichlet conditions on one rank.
+//  * Solver mapping, src/solver_mapping_routines.F90:398-520: an equations row is a solver row
+//    iff its dependent DOF is free; solver rows (and, for the square system, columns) are
+//    numbered in ascending global order.
+//  * Structure, SOLVER_MATRIX_STRUCTURE_CALCULATE src/solver_matrices_routines.F90:1612-2431
+//    (compressed-row branch): per solver row, the solver columns of the equations row's free
+//    columns, then LIST_REMOVE_DUPLICATES (sort + unique), stored 1-based.
+//  * Values, SOLVER_MATRIX_EQUATIONS_MATRIX_ADD src/solver_matrices_routines.F90:806-1023
+//    (compressed-row branch): the zeroed solver matrix receives
+//    ALPHA * K(row, col) * row_coupling * column_coupling at (solver row, solver column), found
+//    by the CSR search of MATRIX_VALUES_ADD_DP2, with ALPHA = coupling coefficients = 1.
+//  * Right-hand side, SOLVER_MATRICES_STATIC_ASSEMBLE src/solver_routines.F90:14025-15050 (the
+//    linear branch of the RHS loop): the zeroed solver RHS receives, for each equations row r in
+//    ascending order, f(r) on r's solver row (the RHS variable is free everywhere here), and, if
+//    r's dependent DOF is fixed with |u(r)| >= ZERO_TOLERANCE, -1 * K(i, r) * u(r) on the solver
+//    row of every row i of column r's list with |K(i, r)| >= ZERO_TOLERANCE.  Column lists hold
+//    the rows of the column in ascending order, and only for columns on boundary nodes
+//    (src/equations_matrices_routines.F90:4531-4561, src/boundary_condition_routines.F90:459-500);
+//    col_listed (optional) marks those columns, NULL lists every column.
+//  ZERO_TOLERANCE = 5 * EPSILON(1.0_DP) (src/constants.F90:69).
+// rp/ci 1-based (n rows); f may be NULL (a zero equations RHS).  Outputs: solver_of_dof[n]
+// (0-based solver number or -1), s_rp[n_free + 1], s_ci, s_v (capacity cap), s_rhs[n_free].
+// Returns the solver nnz, or -1 if cap is too small.
+// ---------------------------------------------------------------------------------------
+int64_t orc_solver_system(int n, const int32_t* rp, const int32_t* ci, const double* v, const double* f,
+                          const uint8_t* fixed, const uint8_t* col_listed, const double* u, int32_t* solver_of_dof,
+                          int32_t* s_rp, int32_t* s_ci, double* s_v, double* s_rhs, int64_t cap, int32_t* n_free) {
+  const double zero_tol = 5.0 * 2.220446049250313e-16;
+  int nf = 0;
+  for (int r = 0; r < n; ++r) solver_of_dof[r] = fixed[r] ? -1 : nf++;
+  *n_free = nf;
+  // structure
+  int64_t nnz = 0;
+  s_rp[0] = 1;
+  std::vector<int32_t> cols;
+  for (int r = 0; r < n; ++r) {
+    if (fixed[r]) continue;
+    cols.clear();
+    for (int k = rp[r] - 1; k < rp[r + 1] - 1; ++k) {
+      const int c = ci[k] - 1;
+      if (!fixed[c]) cols.push_back(solver_of_dof[c] + 1);
+    }
+    std::sort(cols.begin(), cols.end());
+    cols.erase(std::unique(cols.begin(), cols.end()), cols.end());
+    if (nnz + (int64_t)cols.size() > cap) return -1;
+    for (int32_t c : cols) s_ci[nnz++] = c;
+    s_rp[solver_of_dof[r] + 1] = (int32_t)(nnz + 1);
+  }
+  // values
+  std::fill(s_v, s_v + nnz, 0.0);
+  for (int r = 0; r < n; ++r) {
+    if (fixed[r]) continue;
+    const int sr = solver_of_dof[r] + 1;
+    for (int k = rp[r] - 1; k < rp[r + 1] - 1; ++k) {
+      const int c = ci[k] - 1;
+      if (fixed[c]) continue;
+      const double value = 1.0 * v[k] * 1.0 * 1.0;
+      const int64_t loc = orc_csr_location(s_rp, s_ci, sr, solver_of_dof[c] + 1);
+      if (loc == 0) return -1;
+      s_v[loc - 1] += value;
+    }
+  }
+  // right-hand side: column lists (rows ascending) of the listed fixed columns
+  std::vector<std::vector<int32_t>> lists(n);
+  for (int i = 0; i < n; ++i)
+    for (int k = rp[i] - 1; k < rp[i + 1] - 1; ++k) {
+      const int c = ci[k] - 1;
+      if (fixed[c] && (!col_listed || col_listed[c])) lists[c].push_back(i);
+    }
+  std::fill(s_rhs, s_rhs + nf, 0.0);
+  for (int r = 0; r < n; ++r) {
+    if (!fixed[r]) s_rhs[solver_of_dof[r]] += (f ? f[r] : 0.0) * 1.0;
+    if (!fixed[r] || !(std::fabs(u[r]) >= zero_tol)) continue;
+    for (int32_t i : lists[r]) {
+      const int64_t loc = orc_csr_location(rp, ci, i + 1, r + 1);
+      const double kv = loc ? v[loc - 1] : 0.0;
+      if (!(std::fabs(kv) >= zero_tol) || fixed[i]) continue;
+      s_rhs[solver_of_dof[i]] += -1.0 * kv * u[r] * 1.0;
+    }
+  }
+  return nnz;
+}
+
 // Dirichlet-eliminated Jacobi-preconditioned conjugate gradients in FP64.
 // The solver matrix of src/solver_routines.F90:14025-15050 (SOLVER_MATRICES_STATIC_ASSEMBLE)
 // removes the rows and columns of fixed DOFs and moves K_FD u_D to the right-hand side; the
