@@ -10,12 +10,16 @@ Sources:
       2x2 bilinear Lagrange elements, origin (-pi/2, -pi/2) with pi = 3.141592653579, extent 2x2,
       u = cos(x) cosh(y) on the boundary (Laplace_equations_routines.F90 TWO_DIM_2), iterative solve
       to 1e-12).  Nodal numerical / analytic values and the integral errors of variable 1.
+  tests/FiniteElasticity/output_cantilever/{linear_3x2x2,cubic_2x1x1}/Cantilever.part0.{exnode,exelem}
+      Iron's exported results of the Cantilever finite-elasticity test (FieldExport.c formats):
+      copied verbatim into exfile/ to pin the exnode/exelem reader and writer by round trip.
 """
 from __future__ import annotations
 
 import json
 import os
 import re
+import shutil
 from pathlib import Path
 
 REF = Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
@@ -47,6 +51,13 @@ def main():
     data = parse_opanal_variable1(src)
     (OUT / "analytic_laplace_linear_lagrange.json").write_text(json.dumps(data, indent=1) + "\n")
     print("wrote", OUT / "analytic_laplace_linear_lagrange.json", len(data["nodes"]), "nodes")
+    (OUT / "exfile").mkdir(exist_ok=True)
+    for case in ("linear_3x2x2", "cubic_2x1x1"):
+        for ext in ("exnode", "exelem"):
+            src = REF / "tests/FiniteElasticity/output_cantilever" / case / f"Cantilever.part0.{ext}"
+            dst = OUT / "exfile" / f"cantilever_{case}.{ext}"
+            shutil.copyfile(src, dst)
+            print("copied", src.relative_to(REF), "->", dst.name)
 
 
 if __name__ == "__main__":
