@@ -1,0 +1,327 @@
+// laplace_tp.cu -- Laplace assembly on tensor-product Lagrange hexahedra of any order 1..3.
+//
+// Iron's Laplace element routine (LaplaceEquation_FiniteElementCalculate,
+// src/Laplace_equations_routines.F90:433-747) works for every tensor-product Lagrange basis:
+// per Gauss point it interpolates the geometry with first derivatives, forms the metrics
+// (COORDINATE_METRICS_CALCULATE, src/coordinate_routines.F90:639-1026: GL = J^T J, GU = GL^-1,
+// Jacobian = sqrt|det GL|) and adds
+//   K(ms, ns) += sum_{mi,ni} dphi_ms/dxi_mi GU(mi,ni) dphi_ns/dxi_ni * Jacobian * w   (x kappa)
+// and EquationsMatrices_ElementAdd / MATRIX_VALUES_ADD_DP2 add it into the CSR matrix.  The
+// trilinear case has its own sum-factorised kernels (laplace.cu); this file covers
+// (order1+1)(order2+1)(order3+1)-node elements with n1 x n2 x n3 Gauss points:
+//  * basis tables (Gauss-Legendre points and weights on [0,1], closed forms for n <= 4 as in
+//    Gauss_Legendre src/basis_routines.F90:6804-6890; equally spaced Lagrange polynomials as in
+//    LAGRANGE_*_EVALUATE :7969-8090, node and Gauss-point numbering xi1 fastest, :3820) are built
+//    on the host once per configuration, in the element arithmetic type;
+//  * one CTA per element: Gauss-point threads form M_g = adj(GL) kappa w / sqrt(det GL) (= GU
+//    Jacobian w kappa), then pair threads form K(m, n), m <= n, as sum_g dphi_g(m)^T M_g dphi_g(n);
+//  * each pair is added at (node m, node n) and (node n, node m) of the CSR values through Iron's
+//    row search (bisection to a width of 10, then a linear scan, src/matrix_vector.F90:3202-3240),
+//    colour by colour, so no two elements of a launch share a row and the result is deterministic.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <type_traits>
+#include <vector>
+
+#include "df.cuh"
+#include "gfe_internal.cuh"
+
+namespace {
+
+constexpr int kTPThreads = 256;
+constexpr int kMaxNns = 64;  // (3+1)^3
+constexpr int kMaxNg = 64;   // 4^3
+
+// Gauss-Legendre points and weights on [0, 1], n = 1..4 (closed forms of the Legendre roots).
+void gauss01(int n, double* x, double* w) {
+  switch (n) {
+    case 1:
+      x[0] = 0.5;
+      w[0] = 1.0;
+      break;
+    case 2: {
+      const double d = 0.5 / std::sqrt(3.0);
+      x[0] = 0.5 - d; x[1] = 0.5 + d;
+      w[0] = w[1] = 0.5;
+      break;
+    }
+    case 3: {
+      const double d = 0.5 * std::sqrt(0.6);
+      x[0] = 0.5 - d; x[1] = 0.5; x[2] = 0.5 + d;
+      w[0] = w[2] = 5.0 / 18.0;
+      w[1] = 8.0 / 18.0;
+      break;
+    }
+    default: {  // 4
+      const double a = 0.5 * std::sqrt(3.0 / 7.0 - 2.0 / 7.0 * std::sqrt(1.2));
+      const double b = 0.5 * std::sqrt(3.0 / 7.0 + 2.0 / 7.0 * std::sqrt(1.2));
+      const double wa = (18.0 + std::sqrt(30.0)) / 72.0, wb = (18.0 - std::sqrt(30.0)) / 72.0;
+      x[0] = 0.5 - b; x[1] = 0.5 - a; x[2] = 0.5 + a; x[3] = 0.5 + b;
+      w[0] = w[3] = wb;
+      w[1] = w[2] = wa;
+      break;
+    }
+  }
+}
+
+// 1D Lagrange polynomial k of order p on the nodes j/p and its derivative, at t.
+void lagrange1d(int p, int k, double t, double* val, double* der) {
+  double v = 1.0, d = 0.0;
+  const double tk = (double)k / p;
+  for (int j = 0; j <= p; ++j) {
+    if (j == k) continue;
+    const double tj = (double)j / p, f = (t - tj) / (tk - tj), df = 1.0 / (tk - tj);
+    d = d * f + v * df;  // product rule, accumulated factor by factor
+    v *= f;
+  }
+  *val = v;
+  *der = d;
+}
+
+template <typename T>
+T to_elem(double v);
+template <>
+double to_elem<double>(double v) { return v; }
+template <>
+float to_elem<float>(double v) { return (float)v; }
+template <>
+f2 to_elem<f2>(double v) {
+  const float h = (float)v;
+  return {h, (float)(v - (double)h)};
+}
+
+struct TPConfig {
+  int nns, ng, npairs;
+};
+
+template <typename T>
+struct TPTables {
+  T* dphi = nullptr;       // [ng][3][nns]
+  T* w = nullptr;          // [ng]
+  int32_t* pairs = nullptr;  // [npairs]: m | n << 16, m <= n
+  TPConfig cfg{};
+};
+
+std::mutex g_tp_mu;
+
+template <typename T>
+int tp_tables(const int32_t* order, const int32_t* ngauss, const TPTables<T>** out) {
+  static std::map<std::tuple<int, int, int, int, int, int, int>, TPTables<T>> cache;
+  int dev = 0;
+  GFE_CUDA_TRY(cudaGetDevice(&dev));
+  const auto key = std::make_tuple(dev, order[0], order[1], order[2], ngauss[0], ngauss[1], ngauss[2]);
+  std::lock_guard<std::mutex> lk(g_tp_mu);
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    *out = &it->second;
+    return GFE_OK;
+  }
+  const int n1 = order[0] + 1, n2 = order[1] + 1, n3 = order[2] + 1;
+  const int nns = n1 * n2 * n3, ng = ngauss[0] * ngauss[1] * ngauss[2];
+  double gx[3][4], gw[3][4];
+  for (int d = 0; d < 3; ++d) gauss01(ngauss[d], gx[d], gw[d]);
+  std::vector<T> dphi((size_t)ng * 3 * nns), w(ng);
+  for (int g3 = 0; g3 < ngauss[2]; ++g3)
+    for (int g2 = 0; g2 < ngauss[1]; ++g2)
+      for (int g1 = 0; g1 < ngauss[0]; ++g1) {
+        const int g = g1 + ngauss[0] * (g2 + ngauss[1] * g3);
+        w[g] = to_elem<T>(gw[0][g1] * gw[1][g2] * gw[2][g3]);
+        for (int k3 = 0; k3 < n3; ++k3)
+          for (int k2 = 0; k2 < n2; ++k2)
+            for (int k1 = 0; k1 < n1; ++k1) {
+              const int n = k1 + n1 * (k2 + n2 * k3);
+              double v[3], dv[3];
+              lagrange1d(order[0], k1, gx[0][g1], &v[0], &dv[0]);
+              lagrange1d(order[1], k2, gx[1][g2], &v[1], &dv[1]);
+              lagrange1d(order[2], k3, gx[2][g3], &v[2], &dv[2]);
+              dphi[((size_t)g * 3 + 0) * nns + n] = to_elem<T>(dv[0] * v[1] * v[2]);
+              dphi[((size_t)g * 3 + 1) * nns + n] = to_elem<T>(v[0] * dv[1] * v[2]);
+              dphi[((size_t)g * 3 + 2) * nns + n] = to_elem<T>(v[0] * v[1] * dv[2]);
+            }
+      }
+  std::vector<int32_t> pairs;
+  for (int m = 0; m < nns; ++m)
+    for (int n = m; n < nns; ++n) pairs.push_back(m | (n << 16));
+  TPTables<T> t;
+  t.cfg = {nns, ng, (int)pairs.size()};
+  GFE_CUDA_TRY(cudaMalloc(&t.dphi, sizeof(T) * dphi.size()));
+  GFE_CUDA_TRY(cudaMalloc(&t.w, sizeof(T) * w.size()));
+  GFE_CUDA_TRY(cudaMalloc(&t.pairs, sizeof(int32_t) * pairs.size()));
+  GFE_CUDA_TRY(cudaMemcpy(t.dphi, dphi.data(), sizeof(T) * dphi.size(), cudaMemcpyHostToDevice));
+  GFE_CUDA_TRY(cudaMemcpy(t.w, w.data(), sizeof(T) * w.size(), cudaMemcpyHostToDevice));
+  GFE_CUDA_TRY(cudaMemcpy(t.pairs, pairs.data(), sizeof(int32_t) * pairs.size(), cudaMemcpyHostToDevice));
+  *out = &(cache[key] = t);
+  return GFE_OK;
+}
+
+// Iron's CSR search (MATRIX_VALUES_ADD_DP2): bisection until at most 10 candidates, then a
+// linear scan.  0-based position, or -1 if the column is absent.
+__device__ __forceinline__ long long csr_find(const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                             int row, int col1) {
+  long long lo = (long long)rp[row] - 1, hi = (long long)rp[row + 1] - 1;
+  while (hi - lo > 10) {
+    const long long mid = lo + (hi - lo) / 2;
+    if (ci[mid] > col1) hi = mid; else lo = mid;
+  }
+  for (long long k = lo; k < hi; ++k)
+    if (ci[k] == col1) return k;
+  return -1;
+}
+
+template <typename T>
+__device__ __forceinline__ T tp_rsqrt(T a) {
+  return rsqrt(a);
+}
+template <>
+__device__ __forceinline__ float tp_rsqrt<float>(float a) {
+  return rsqrtf(a);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kTPThreads)
+laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, const int32_t* __restrict__ en,
+                  const double* __restrict__ coords, const double* __restrict__ kappa, const T* __restrict__ dphi,
+                  const T* __restrict__ wg, const int32_t* __restrict__ pairs, TPConfig cfg,
+                  const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, double* __restrict__ values,
+                  unsigned* err) {
+  __shared__ T sx[3][kMaxNns];
+  __shared__ T sM[kMaxNg][6];
+  __shared__ int32_t snode[kMaxNns];
+  const int nns = cfg.nns, ng = cfg.ng;
+  for (int item = blockIdx.x; item < cnt; item += gridDim.x) {
+    const int e = ce[item];
+    for (int n = threadIdx.x; n < nns; n += blockDim.x) {
+      const int node = en[(size_t)e * nns + n];
+      snode[n] = node;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) sx[c][n] = from_double<T>(coords[(size_t)c * n_nodes + node]);
+    }
+    const T kap = from_double<T>(kappa ? kappa[e] : 1.0);
+    __syncthreads();
+    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+      T J[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          T s = from_double<T>(0.0);
+          for (int n = 0; n < nns; ++n) s = s + sx[c][n] * dphi[((size_t)g * 3 + a) * nns + n];
+          J[c][a] = s;
+        }
+      const T G00 = J[0][0] * J[0][0] + J[1][0] * J[1][0] + J[2][0] * J[2][0];
+      const T G11 = J[0][1] * J[0][1] + J[1][1] * J[1][1] + J[2][1] * J[2][1];
+      const T G22 = J[0][2] * J[0][2] + J[1][2] * J[1][2] + J[2][2] * J[2][2];
+      const T G01 = J[0][0] * J[0][1] + J[1][0] * J[1][1] + J[2][0] * J[2][1];
+      const T G02 = J[0][0] * J[0][2] + J[1][0] * J[1][2] + J[2][0] * J[2][2];
+      const T G12 = J[0][1] * J[0][2] + J[1][1] * J[1][2] + J[2][1] * J[2][2];
+      const T A00 = G11 * G22 - G12 * G12, A11 = G00 * G22 - G02 * G02, A22 = G00 * G11 - G01 * G01;
+      const T A01 = G02 * G12 - G01 * G22, A02 = G01 * G12 - G02 * G11, A12 = G01 * G02 - G00 * G12;
+      const T det = G00 * A00 + G01 * A01 + G02 * A02;
+      if (!(det > from_double<T>(0.0))) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+      // GU * Jacobian * w * kappa = adj(GL) / det * sqrt(det) * w * kappa
+      const T sc = kap * wg[g] * tp_rsqrt(det);
+      sM[g][0] = A00 * sc; sM[g][1] = A11 * sc; sM[g][2] = A22 * sc;
+      sM[g][3] = A01 * sc; sM[g][4] = A02 * sc; sM[g][5] = A12 * sc;
+    }
+    __syncthreads();
+    using Acc = typename std::conditional<std::is_same<T, double>::value, double, f2>::type;
+    for (int p = threadIdx.x; p < cfg.npairs; p += blockDim.x) {
+      const int32_t mn = pairs[p];
+      const int m = mn & 0xffff, n = mn >> 16;
+      Acc acc = from_double<Acc>(0.0);
+      for (int g = 0; g < ng; ++g) {
+        const T* dg = dphi + (size_t)g * 3 * nns;
+        const T am0 = dg[m], am1 = dg[nns + m], am2 = dg[2 * nns + m];
+        const T an0 = dg[n], an1 = dg[nns + n], an2 = dg[2 * nns + n];
+        // (M an)_a, then dm . (M an)
+        const T b0 = sM[g][0] * an0 + sM[g][3] * an1 + sM[g][4] * an2;
+        const T b1 = sM[g][3] * an0 + sM[g][1] * an1 + sM[g][5] * an2;
+        const T b2 = sM[g][4] * an0 + sM[g][5] * an1 + sM[g][2] * an2;
+        const T t = am0 * b0 + am1 * b1 + am2 * b2;
+        if constexpr (std::is_same<T, float>::value) accum(acc, f2{t, 0.0f});
+        else accum(acc, t);
+      }
+      finish(acc);
+      const double v = to_double(acc);
+      const int rm = snode[m], rn = snode[n];
+      const long long pmn = csr_find(rp, ci, rm, rn + 1);
+      if (pmn < 0) gfe_raise(err, GFE_DEVERR_SLOT);
+      else values[pmn] += v;
+      if (m != n) {
+        const long long pnm = csr_find(rp, ci, rn, rm + 1);
+        if (pnm < 0) gfe_raise(err, GFE_DEVERR_SLOT);
+        else values[pnm] += v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void values_to_fp32(const double* __restrict__ v, float* __restrict__ v32, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    v32[i] = (float)v[i];
+}
+
+template <typename T>
+int launch_tp(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, const int32_t* en, const double* coords,
+              const double* kappa, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
+              const int32_t* rp, const int32_t* ci, double* values, cudaStream_t s, int* launches) {
+  const TPTables<T>* t = nullptr;
+  if (int rc = tp_tables<T>(order, ngauss, &t)) return rc;
+  unsigned* err = gfe::device_error_word();
+  for (int c = 0; c < n_colors; ++c) {
+    const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
+    if (cnt <= 0) continue;
+    const int grid = std::min(cnt, 8 * gfe::sm_count());
+    laplace_tp_kernel<T><<<grid, kTPThreads, 0, s>>>(color_elems + c0, cnt, n_nodes, en, coords, kappa, t->dphi,
+                                                     t->w, t->pairs, t->cfg, rp, ci, values, err);
+    ++*launches;
+  }
+  return GFE_OK;
+}
+
+}  // namespace
+
+extern "C" int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_gauss, int32_t n_elem, int32_t n_nodes,
+                                       const int32_t* elem_nodes, const double* coords, const double* kappa,
+                                       const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
+                                       const int32_t* row_ptr, const int32_t* col_idx, int64_t nnz, double* values,
+                                       float* values32, double* rhs, int32_t precision, void* stream) {
+  const char* fn = "gfe_laplace_assemble_tp";
+  if (!order || !n_gauss) return gfe::set_error(GFE_ERR_ARG, "%s: order and n_gauss are required", fn);
+  for (int d = 0; d < 3; ++d) {
+    if (order[d] < 1 || order[d] > 3)
+      return gfe::set_error(GFE_ERR_ARG, "%s: Lagrange order %d in xi%d (1..3 supported)", fn, order[d], d + 1);
+    if (n_gauss[d] < 1 || n_gauss[d] > 4)
+      return gfe::set_error(GFE_ERR_ARG, "%s: %d Gauss points in xi%d (1..4 supported)", fn, n_gauss[d], d + 1);
+  }
+  if (n_elem < 0 || n_nodes <= 0 || !coords || !row_ptr || !col_idx || !values || nnz < 0 ||
+      (n_elem > 0 && (!elem_nodes || !color_elems || !color_ptr_host || n_colors <= 0)))
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (color_ptr_host && n_colors > 0 && (color_ptr_host[0] != 0 || color_ptr_host[n_colors] != n_elem))
+    return gfe::set_error(GFE_ERR_ARG, "%s: colour offsets must run from 0 to n_elem", fn);
+  if (precision != GFE_FP64 && precision != GFE_MIXED && precision != GFE_MIXED_DF)
+    return gfe::set_error(GFE_ERR_ARG, "%s: unknown precision %d", fn, precision);
+  cudaStream_t s = gfe::as_stream(stream);
+  GFE_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)nnz, s));
+  if (rhs) GFE_CUDA_TRY(cudaMemsetAsync(rhs, 0, sizeof(double) * (size_t)n_nodes, s));
+  void* prof = gfe::stage_begin(GFE_STAGE_LAPLACE_ELEMENTS, s);
+  int launches = 0, rc;
+  if (precision == GFE_FP64)
+    rc = launch_tp<double>(order, n_gauss, n_nodes, elem_nodes, coords, kappa, color_elems, color_ptr_host, n_colors,
+                           row_ptr, col_idx, values, s, &launches);
+  else if (precision == GFE_MIXED)
+    rc = launch_tp<float>(order, n_gauss, n_nodes, elem_nodes, coords, kappa, color_elems, color_ptr_host, n_colors,
+                          row_ptr, col_idx, values, s, &launches);
+  else
+    rc = launch_tp<f2>(order, n_gauss, n_nodes, elem_nodes, coords, kappa, color_elems, color_ptr_host, n_colors,
+                       row_ptr, col_idx, values, s, &launches);
+  gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, launches);
+  if (rc) return rc;
+  if (values32 && nnz > 0) values_to_fp32<<<4 * gfe::sm_count(), 256, 0, s>>>(values, values32, nnz);
+  GFE_LAUNCH_CHECK(fn);
+  return GFE_OK;
+}

@@ -46,21 +46,30 @@ class SolveInfo:
 
 
 class LaplaceAssembly:
-    """Device-resident Laplace problem on a trilinear hexahedral mesh.
+    """Device-resident Laplace problem on a hexahedral mesh of tensor-product Lagrange elements.
 
-    elem_nodes: [E][8] int (0-based, Iron local node order); coords: [3][N] float64;
+    elem_nodes: [E][nns] int (0-based, Iron local node order, xi1 fastest); coords: [3][N] float64;
     kappa: [E] element conductivity or None (standard Laplace subtype);
-    colour_elems / colour_ptr: an element colouring (elements of one colour share no node).
+    colour_elems / colour_ptr: an element colouring (elements of one colour share no node);
+    order: Lagrange order per direction (1..3, an int or three), nns = prod(order + 1);
+    n_gauss: Gauss points per direction (1..4; default order + 1).
+    Trilinear elements with 2x2x2 Gauss points use the sum-factorised kernels (and, on Iron's
+    regular generated mesh, the row-owning one); every other basis uses gfe_laplace_assemble_tp.
     """
 
     def __init__(self, elem_nodes, coords, kappa=None, colour_elems=None, colour_ptr=None, device=None,
-                 structure=None):
+                 structure=None, order=1, n_gauss=None):
         dev = device if device is not None else _lib.require_cuda()
         _lib.load()
         self.device = torch.device(dev)
+        self.order = tuple(int(o) for o in (order if np.ndim(order) else (order,) * 3))
+        self.n_gauss = tuple(int(g) for g in (n_gauss if n_gauss is not None and np.ndim(n_gauss) else
+                                              ((n_gauss,) * 3 if n_gauss is not None else [o + 1 for o in self.order])))
+        nns = int(np.prod([o + 1 for o in self.order]))
+        self.tensor_product = self.order != (1, 1, 1) or self.n_gauss != (2, 2, 2)
         en = np.ascontiguousarray(elem_nodes, dtype=np.int32)
-        if en.ndim != 2 or en.shape[1] != 8:
-            raise GfeError(-1, "trilinear hexahedra need [E][8] connectivity")
+        if en.ndim != 2 or en.shape[1] != nns:
+            raise GfeError(-1, f"Lagrange order {self.order} needs [E][{nns}] connectivity")
         xyz = np.ascontiguousarray(coords, dtype=np.float64)
         if xyz.ndim != 2 or xyz.shape[0] != 3:
             raise GfeError(-1, "coords must be [3][N] (separated components)")
@@ -84,13 +93,16 @@ class LaplaceAssembly:
         self.values = torch.empty(self.nnz, dtype=torch.float64, device=self.device)
         self.values32 = None
         self.rhs = torch.empty(self.n_nodes, dtype=torch.float64, device=self.device)
-        self.regular = None  # (nx, ny, nz) when the mesh is Iron's regular generated mesh
+        self.regular = None  # (nx, ny, nz) when the mesh is Iron's trilinear regular generated mesh
+        self.grid = None     # (nelem, order) of a regular generated mesh of any order
 
     @classmethod
-    def from_regular_mesh(cls, mesh, kappa=None, device=None):
+    def from_regular_mesh(cls, mesh, kappa=None, device=None, n_gauss=None):
         order, ptr = mesh.colouring()
-        obj = cls(mesh.elem_nodes, mesh.coords, kappa=kappa, colour_elems=order, colour_ptr=ptr, device=device)
-        if mesh.order == 1:
+        obj = cls(mesh.elem_nodes, mesh.coords, kappa=kappa, colour_elems=order, colour_ptr=ptr, device=device,
+                  order=mesh.order, n_gauss=n_gauss)
+        obj.grid = (tuple(mesh.nelem), mesh.order)
+        if mesh.order == 1 and not obj.tensor_product:
             nx, ny, nz = mesh.nelem
             bad = C.c_int64(-1)
             _lib.call("gfe_laplace_regular_check", nx, ny, nz, _lib.ptr(obj.row_ptr), _lib.ptr(obj.col_idx),
@@ -110,6 +122,18 @@ class LaplaceAssembly:
         if fp32_copy and self.values32 is None:
             self.values32 = torch.empty(self.nnz, dtype=torch.float32, device=self.device)
         v32 = self.values32 if fp32_copy else None
+        if self.tensor_product:
+            if path == "regular":
+                raise GfeError(-1, "the regular-mesh kernel is trilinear with 2x2x2 Gauss points")
+            cp = self.colour_ptr
+            _lib.call("gfe_laplace_assemble_tp", (C.c_int32 * 3)(*self.order), (C.c_int32 * 3)(*self.n_gauss),
+                      self.n_elements, self.n_nodes, _lib.ptr(self.elem_nodes), _lib.ptr(self.coords),
+                      _lib.ptr(self.kappa), _lib.ptr(self.colour_elems), cp.ctypes.data_as(C.c_void_p), len(cp) - 1,
+                      _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx), self.nnz, _lib.ptr(self.values), _lib.ptr(v32),
+                      _lib.ptr(self.rhs), prec, _lib.stream_handle(stream))
+            if check:
+                _lib.raise_device_errors("gfe_laplace_assemble_tp", stream)
+            return self.values
         if path == "regular" and self.regular is None:
             raise GfeError(-1, "the regular-mesh kernel needs Iron's regular generated mesh")
         if path == "auto":
@@ -167,6 +191,8 @@ class LaplaceAssembly:
         return values_host
 
     def element_matrices(self, precision: str = "fp64", stream=None) -> torch.Tensor:
+        if self.tensor_product:
+            raise GfeError(-1, "element matrices are available for trilinear elements with 2x2x2 Gauss points")
         K = torch.empty((self.n_elements, 8, 8), dtype=torch.float64, device=self.device)
         _lib.call("gfe_laplace_element_matrices", self.n_elements, self.n_nodes, _lib.ptr(self.elem_nodes),
                   _lib.ptr(self.coords), _lib.ptr(self.kappa), _lib.ptr(K), PRECISIONS[precision],
@@ -208,9 +234,10 @@ class LaplaceAssembly:
         if isinstance(col_listed, str):
             if col_listed != "boundary":
                 raise GfeError(-1, f"unknown col_listed {col_listed!r}")
-            if self.regular is None:
+            if self.grid is None:
                 raise GfeError(-1, "col_listed='boundary' needs Iron's regular generated mesh; pass a mask")
-            col_listed = torch.from_numpy(boundary_node_mask(self.regular, 1).astype("uint8")).to(self.device)
+            nelem, order = self.grid
+            col_listed = torch.from_numpy(boundary_node_mask(nelem, order).astype("uint8")).to(self.device)
         return SolverSystem(self.row_ptr, self.col_idx, fixed, col_listed, stream=stream)
 
     def solve_reduced(self, fixed: torch.Tensor, x: torch.Tensor, f: torch.Tensor | None = None, rtol: float = 1e-12,

@@ -21,7 +21,7 @@ def _grid_nodes(nelem, order):
 
 
 def regular_elements(nelem, order: int) -> np.ndarray:
-    """elem_nodes[E][(order+1)^3] (0-based) of a 3D regular mesh of Lagrange order 1 or 2."""
+    """elem_nodes[E][(order+1)^3] (0-based) of a 3D regular mesh of Lagrange order 1, 2 or 3."""
     nx, ny, nz = nelem
     tx, ty, _ = _grid_nodes(nelem, order)
     e1, e2, e3 = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")

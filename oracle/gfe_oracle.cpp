@@ -47,7 +47,8 @@ bool gauss_legendre(int n, double* x, double* w) {
 }
 
 // 1D Lagrange basis on [0,1]; node index a is 0-based.  deriv 0 = value, 1 = first derivative.
-// src/basis_routines.F90:7969-8020 (LAGRANGE_LINEAR_EVALUATE), :8027-8090 (QUADRATIC).
+// src/basis_routines.F90:7969-8020 (LAGRANGE_LINEAR_EVALUATE), :8027-8090 (QUADRATIC),
+// :7899-7962 (CUBIC).
 double lagrange1d(int order, int a, int deriv, double xi) {
   if (order == 1) {
     if (deriv == 0) return a == 0 ? 1.0 - xi : xi;
@@ -62,6 +63,18 @@ double lagrange1d(int order, int a, int deriv, double xi) {
     if (a == 0) return 4.0 * xi - 3.0;
     if (a == 1) return 4.0 - 8.0 * xi;
     return 4.0 * xi - 1.0;
+  }
+  if (order == 3) {
+    if (deriv == 0) {
+      if (a == 0) return 0.5 * (3.0 * xi - 1.0) * (3.0 * xi - 2.0) * (1.0 - xi);
+      if (a == 1) return 4.5 * xi * (3.0 * xi - 2.0) * (xi - 1.0);
+      if (a == 2) return 4.5 * xi * (3.0 * xi - 1.0) * (1.0 - xi);
+      return 0.5 * xi * (3.0 * xi - 1.0) * (3.0 * xi - 2.0);
+    }
+    if (a == 0) return -13.5 * xi * xi + 18.0 * xi - 5.5;
+    if (a == 1) return 40.5 * xi * xi - 45.0 * xi + 9.0;
+    if (a == 2) return -40.5 * xi * xi + 36.0 * xi - 4.5;
+    return 13.5 * xi * xi - 9.0 * xi + 1.0;
   }
   return 0.0;
 }
@@ -87,7 +100,7 @@ bool make_tp_basis(int nxi, const int* order, const int* ngauss, TPBasis& b) {
     gx[d][0] = 0.5; gw[d][0] = 1.0;
   }
   for (int d = 0; d < nxi; ++d) {
-    if (order[d] < 1 || order[d] > 2) return false;
+    if (order[d] < 1 || order[d] > 3) return false;
     b.order[d] = order[d];
     b.nnx[d] = order[d] + 1;
     b.ngx[d] = ngauss[d];
