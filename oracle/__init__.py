@@ -16,7 +16,19 @@ import numpy as np
 from . import build as _build
 
 _HERE = Path(__file__).resolve().parent
-_lib = None
+_libs = {}
+_variant = "parity"
+
+
+def use_build(variant: str) -> str:
+    """Select the library behind every oracle call: "parity" (no FMA contraction, bit-stable across
+    hosts; the default) or "timing" (the compiler's default contraction, for the CPU baseline).
+    Returns the previous selection."""
+    global _variant
+    if variant not in ("parity", "timing"):
+        raise ValueError(variant)
+    prev, _variant = _variant, variant
+    return prev
 
 i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -24,9 +36,9 @@ u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 
 
 def lib():
-    global _lib
-    if _lib is None:
-        path = _build.build()
+    if _variant not in _libs:
+        _build.build()
+        path = _build.LIB if _variant == "parity" else _build.LIB_TIMING
         L = C.CDLL(str(path))
         L.orc_gauss_legendre.argtypes = [C.c_int, f64p, f64p]
         L.orc_tp_basis.argtypes = [C.c_int, i32p, i32p, C.c_void_p, C.c_void_p]
@@ -47,8 +59,8 @@ def lib():
         L.orc_cg_dirichlet.argtypes = [C.c_int, i32p, i32p, f64p, C.c_void_p, u8p, f64p, C.c_double, C.c_int,
                                        C.POINTER(C.c_double)]
         _register_mr(L)
-        _lib = L
-    return _lib
+        _libs[_variant] = L
+    return _libs[_variant]
 
 
 def _register_mr(L):
