@@ -217,18 +217,28 @@ int gfe_laplace_assemble_regular_host(int32_t nx, int32_t ny, int32_t nz, const 
                                       const int32_t* row_ptr, double* values, double* values_host, double* rhs,
                                       int32_t precision, void* workspace, int32_t slab_layers, void* stream);
 
-/* The Laplace assembly of gfe_laplace_assemble on hexahedra of any tensor-product Lagrange basis of
- * order 1..3 per direction with 1..4 Gauss points per direction (Iron's element routine is
- * basis-generic: LaplaceEquation_FiniteElementCalculate, src/Laplace_equations_routines.F90:433-747,
- * with the quadrature of BASIS_QUADRATURE_CREATE, src/basis_routines.F90:3720-4090).
- *  order[3], n_gauss[3]  host arrays; elements have (order1+1)(order2+1)(order3+1) nodes, xi1 fastest
- *  elem_nodes [n_elem][nns] 0-based; colouring and CSR as for gfe_laplace_assemble
+/* The Laplace assembly of gfe_laplace_assemble on hexahedra of any tensor-product basis of Lagrange
+ * order 1..3 or cubic Hermite per direction, with 1..4 Gauss points per direction (Iron's element
+ * routine is basis-generic: LaplaceEquation_FiniteElementCalculate,
+ * src/Laplace_equations_routines.F90:433-747, with the quadrature of BASIS_QUADRATURE_CREATE,
+ * src/basis_routines.F90:3720-4090).
+ *  order[3]   host array of Iron's interpolation specification per xi (INTERPOLATION_XI):
+ *             1, 2, 3 = linear / quadratic / cubic Lagrange, 4 = cubic Hermite
+ *  n_gauss[3] host array of Gauss points per xi
+ *  elem_nodes [n_elem][nns] 0-based element parameter DOFs in Iron's order (local nodes xi1 fastest,
+ *             then each node's derivatives: value, d/ds1, d/ds2, d2/ds1ds2, d/ds3, ... over the
+ *             Hermite directions); n_nodes = number of DOFs; coords [3][n_nodes] geometric
+ *             parameters per DOF (positions and, for Hermite, derivatives)
+ *  scale      optional [n_elem][nns] element parameter scale factors: the geometric parameters are
+ *             interpolated scaled and the element matrix is scaled as K(m,n) SF(m) SF(n)
+ *             (src/Laplace_equations_routines.F90:555-579); NULL = unscaled
+ *  colouring and CSR as for gfe_laplace_assemble
  *  values32 (optional) FP32 copy of the assembled values
  * precision GFE_FP64, GFE_MIXED (FP32 element arithmetic) or GFE_MIXED_DF (float-float).  The
  * matrix and rhs are zeroed first; each pair of element nodes is added through Iron's CSR search.
  * Asynchronous; device-side failures are reported through gfe_device_errors(). */
 int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_gauss, int32_t n_elem, int32_t n_nodes,
-                            const int32_t* elem_nodes, const double* coords, const double* kappa,
+                            const int32_t* elem_nodes, const double* coords, const double* scale, const double* kappa,
                             const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
                             const int32_t* row_ptr, const int32_t* col_idx, int64_t nnz, double* values,
                             float* values32, double* rhs, int32_t precision, void* stream);

@@ -19,6 +19,7 @@
 //    row search (bisection to a width of 10, then a linear scan, src/matrix_vector.F90:3202-3240),
 //    colour by colour, so no two elements of a launch share a row and the result is deterministic.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <map>
 #include <mutex>
@@ -65,6 +66,15 @@ void gauss01(int n, double* x, double* w) {
       break;
     }
   }
+}
+
+// 1D cubic Hermite function of node a (0 or 1) and node derivative k (0 value, 1 slope) and its
+// derivative, at t (the four cubics of HERMITE_CUBIC_EVALUATE, src/basis_routines.F90:7607-7701).
+void hermite1d(int a, int k, double t, double* val, double* der) {
+  if (a == 0 && k == 0) { *val = (2.0 * t - 3.0) * t * t + 1.0; *der = 6.0 * t * (t - 1.0); }
+  else if (a == 0) { *val = ((t - 2.0) * t + 1.0) * t; *der = (3.0 * t - 4.0) * t + 1.0; }
+  else if (k == 0) { *val = t * t * (3.0 - 2.0 * t); *der = 6.0 * t * (1.0 - t); }
+  else { *val = t * t * (t - 1.0); *der = t * (3.0 * t - 2.0); }
 }
 
 // 1D Lagrange polynomial k of order p on the nodes j/p and its derivative, at t.
@@ -119,8 +129,25 @@ int tp_tables(const int32_t* order, const int32_t* ngauss, const TPTables<T>** o
     *out = &it->second;
     return GFE_OK;
   }
-  const int n1 = order[0] + 1, n2 = order[1] + 1, n3 = order[2] + 1;
-  const int nns = n1 * n2 * n3, ng = ngauss[0] * ngauss[1] * ngauss[2];
+  // element parameters in Iron's order: local nodes xi1 fastest, then each node's derivatives,
+  // whose count doubles for every Hermite direction in xi order (src/basis_routines.F90:2633-2662)
+  int nn[3], nder = 1;
+  for (int d = 0; d < 3; ++d) {
+    nn[d] = order[d] == 4 ? 2 : order[d] + 1;
+    if (order[d] == 4) nder *= 2;
+  }
+  std::vector<std::array<int, 6>> par;  // node position and node derivative per direction
+  for (int a3 = 0; a3 < nn[2]; ++a3)
+    for (int a2 = 0; a2 < nn[1]; ++a2)
+      for (int a1 = 0; a1 < nn[0]; ++a1)
+        for (int k = 0; k < nder; ++k) {
+          std::array<int, 6> q = {a1, a2, a3, 0, 0, 0};
+          int bit = 0;
+          for (int d = 0; d < 3; ++d)
+            if (order[d] == 4) q[3 + d] = (k >> bit++) & 1;
+          par.push_back(q);
+        }
+  const int nns = (int)par.size(), ng = ngauss[0] * ngauss[1] * ngauss[2];
   double gx[3][4], gw[3][4];
   for (int d = 0; d < 3; ++d) gauss01(ngauss[d], gx[d], gw[d]);
   std::vector<T> dphi((size_t)ng * 3 * nns), w(ng);
@@ -128,19 +155,18 @@ int tp_tables(const int32_t* order, const int32_t* ngauss, const TPTables<T>** o
     for (int g2 = 0; g2 < ngauss[1]; ++g2)
       for (int g1 = 0; g1 < ngauss[0]; ++g1) {
         const int g = g1 + ngauss[0] * (g2 + ngauss[1] * g3);
+        const double t[3] = {gx[0][g1], gx[1][g2], gx[2][g3]};
         w[g] = to_elem<T>(gw[0][g1] * gw[1][g2] * gw[2][g3]);
-        for (int k3 = 0; k3 < n3; ++k3)
-          for (int k2 = 0; k2 < n2; ++k2)
-            for (int k1 = 0; k1 < n1; ++k1) {
-              const int n = k1 + n1 * (k2 + n2 * k3);
-              double v[3], dv[3];
-              lagrange1d(order[0], k1, gx[0][g1], &v[0], &dv[0]);
-              lagrange1d(order[1], k2, gx[1][g2], &v[1], &dv[1]);
-              lagrange1d(order[2], k3, gx[2][g3], &v[2], &dv[2]);
-              dphi[((size_t)g * 3 + 0) * nns + n] = to_elem<T>(dv[0] * v[1] * v[2]);
-              dphi[((size_t)g * 3 + 1) * nns + n] = to_elem<T>(v[0] * dv[1] * v[2]);
-              dphi[((size_t)g * 3 + 2) * nns + n] = to_elem<T>(v[0] * v[1] * dv[2]);
-            }
+        for (int n = 0; n < nns; ++n) {
+          double v[3], dv[3];
+          for (int d = 0; d < 3; ++d) {
+            if (order[d] == 4) hermite1d(par[n][d], par[n][3 + d], t[d], &v[d], &dv[d]);
+            else lagrange1d(order[d], par[n][d], t[d], &v[d], &dv[d]);
+          }
+          dphi[((size_t)g * 3 + 0) * nns + n] = to_elem<T>(dv[0] * v[1] * v[2]);
+          dphi[((size_t)g * 3 + 1) * nns + n] = to_elem<T>(v[0] * dv[1] * v[2]);
+          dphi[((size_t)g * 3 + 2) * nns + n] = to_elem<T>(v[0] * v[1] * dv[2]);
+        }
       }
   std::vector<int32_t> pairs;
   for (int m = 0; m < nns; ++m)
@@ -183,21 +209,26 @@ __device__ __forceinline__ float tp_rsqrt<float>(float a) {
 template <typename T>
 __global__ void __launch_bounds__(kTPThreads)
 laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, const int32_t* __restrict__ en,
-                  const double* __restrict__ coords, const double* __restrict__ kappa, const T* __restrict__ dphi,
+                  const double* __restrict__ coords, const double* __restrict__ scale,
+                  const double* __restrict__ kappa, const T* __restrict__ dphi,
                   const T* __restrict__ wg, const int32_t* __restrict__ pairs, TPConfig cfg,
                   const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, double* __restrict__ values,
                   unsigned* err) {
   __shared__ T sx[3][kMaxNns];
   __shared__ T sM[kMaxNg][6];
   __shared__ int32_t snode[kMaxNns];
+  __shared__ double ssf[kMaxNns];
   const int nns = cfg.nns, ng = cfg.ng;
   for (int item = blockIdx.x; item < cnt; item += gridDim.x) {
     const int e = ce[item];
     for (int n = threadIdx.x; n < nns; n += blockDim.x) {
       const int node = en[(size_t)e * nns + n];
       snode[n] = node;
+      // scaled geometric parameters, as FIELD_INTERPOLATION_PARAMETERS_ELEMENT_GET forms them
+      const double sf = scale ? scale[(size_t)e * nns + n] : 1.0;
+      if (scale) ssf[n] = sf;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) sx[c][n] = from_double<T>(coords[(size_t)c * n_nodes + node]);
+      for (int c = 0; c < 3; ++c) sx[c][n] = from_double<T>(coords[(size_t)c * n_nodes + node] * sf);
     }
     const T kap = from_double<T>(kappa ? kappa[e] : 1.0);
     __syncthreads();
@@ -245,7 +276,8 @@ laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, 
         else accum(acc, t);
       }
       finish(acc);
-      const double v = to_double(acc);
+      double v = to_double(acc);
+      if (scale) v = v * ssf[m] * ssf[n];  // K(ms, ns) * SF(ms) * SF(ns)
       const int rm = snode[m], rn = snode[n];
       const long long pmn = csr_find(rp, ci, rm, rn + 1);
       if (pmn < 0) gfe_raise(err, GFE_DEVERR_SLOT);
@@ -267,7 +299,7 @@ __global__ void values_to_fp32(const double* __restrict__ v, float* __restrict__
 
 template <typename T>
 int launch_tp(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, const int32_t* en, const double* coords,
-              const double* kappa, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
+              const double* scale, const double* kappa, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
               const int32_t* rp, const int32_t* ci, double* values, cudaStream_t s, int* launches) {
   const TPTables<T>* t = nullptr;
   if (int rc = tp_tables<T>(order, ngauss, &t)) return rc;
@@ -276,7 +308,7 @@ int launch_tp(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, cons
     const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
     if (cnt <= 0) continue;
     const int grid = std::min(cnt, 8 * gfe::sm_count());
-    laplace_tp_kernel<T><<<grid, kTPThreads, 0, s>>>(color_elems + c0, cnt, n_nodes, en, coords, kappa, t->dphi,
+    laplace_tp_kernel<T><<<grid, kTPThreads, 0, s>>>(color_elems + c0, cnt, n_nodes, en, coords, scale, kappa, t->dphi,
                                                      t->w, t->pairs, t->cfg, rp, ci, values, err);
     ++*launches;
   }
@@ -286,15 +318,17 @@ int launch_tp(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, cons
 }  // namespace
 
 extern "C" int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_gauss, int32_t n_elem, int32_t n_nodes,
-                                       const int32_t* elem_nodes, const double* coords, const double* kappa,
+                                       const int32_t* elem_nodes, const double* coords, const double* scale,
+                                       const double* kappa,
                                        const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
                                        const int32_t* row_ptr, const int32_t* col_idx, int64_t nnz, double* values,
                                        float* values32, double* rhs, int32_t precision, void* stream) {
   const char* fn = "gfe_laplace_assemble_tp";
   if (!order || !n_gauss) return gfe::set_error(GFE_ERR_ARG, "%s: order and n_gauss are required", fn);
   for (int d = 0; d < 3; ++d) {
-    if (order[d] < 1 || order[d] > 3)
-      return gfe::set_error(GFE_ERR_ARG, "%s: Lagrange order %d in xi%d (1..3 supported)", fn, order[d], d + 1);
+    if (order[d] < 1 || order[d] > 4)
+      return gfe::set_error(GFE_ERR_ARG, "%s: interpolation %d in xi%d (1..3 Lagrange, 4 cubic Hermite supported)",
+                            fn, order[d], d + 1);
     if (n_gauss[d] < 1 || n_gauss[d] > 4)
       return gfe::set_error(GFE_ERR_ARG, "%s: %d Gauss points in xi%d (1..4 supported)", fn, n_gauss[d], d + 1);
   }
@@ -311,14 +345,14 @@ extern "C" int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_ga
   void* prof = gfe::stage_begin(GFE_STAGE_LAPLACE_ELEMENTS, s);
   int launches = 0, rc;
   if (precision == GFE_FP64)
-    rc = launch_tp<double>(order, n_gauss, n_nodes, elem_nodes, coords, kappa, color_elems, color_ptr_host, n_colors,
-                           row_ptr, col_idx, values, s, &launches);
+    rc = launch_tp<double>(order, n_gauss, n_nodes, elem_nodes, coords, scale, kappa, color_elems, color_ptr_host,
+                           n_colors, row_ptr, col_idx, values, s, &launches);
   else if (precision == GFE_MIXED)
-    rc = launch_tp<float>(order, n_gauss, n_nodes, elem_nodes, coords, kappa, color_elems, color_ptr_host, n_colors,
-                          row_ptr, col_idx, values, s, &launches);
+    rc = launch_tp<float>(order, n_gauss, n_nodes, elem_nodes, coords, scale, kappa, color_elems, color_ptr_host,
+                          n_colors, row_ptr, col_idx, values, s, &launches);
   else
-    rc = launch_tp<f2>(order, n_gauss, n_nodes, elem_nodes, coords, kappa, color_elems, color_ptr_host, n_colors,
-                       row_ptr, col_idx, values, s, &launches);
+    rc = launch_tp<f2>(order, n_gauss, n_nodes, elem_nodes, coords, scale, kappa, color_elems, color_ptr_host,
+                       n_colors, row_ptr, col_idx, values, s, &launches);
   gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, launches);
   if (rc) return rc;
   if (values32 && nnz > 0) values_to_fp32<<<4 * gfe::sm_count(), 256, 0, s>>>(values, values32, nnz);

@@ -51,21 +51,27 @@ class LaplaceAssembly:
     elem_nodes: [E][nns] int (0-based, Iron local node order, xi1 fastest); coords: [3][N] float64;
     kappa: [E] element conductivity or None (standard Laplace subtype);
     colour_elems / colour_ptr: an element colouring (elements of one colour share no node);
-    order: Lagrange order per direction (1..3, an int or three), nns = prod(order + 1);
-    n_gauss: Gauss points per direction (1..4; default order + 1).
+    order: Iron's interpolation per direction (an int or three): 1..3 = Lagrange of that order,
+    4 = cubic Hermite; an element has prod(order + 1) parameters for Lagrange directions and 4 per
+    Hermite direction (2 nodes x value and slope);
+    n_gauss: Gauss points per direction (1..4; default order + 1, 4 for Hermite);
+    scale: [E][nns] element parameter scale factors (Hermite arc-length scaling) or None.
+    For Hermite meshes elem_nodes holds element parameter DOFs and coords the geometric parameters
+    per DOF (positions and derivatives).
     Trilinear elements with 2x2x2 Gauss points use the sum-factorised kernels (and, on Iron's
     regular generated mesh, the row-owning one); every other basis uses gfe_laplace_assemble_tp.
     """
 
     def __init__(self, elem_nodes, coords, kappa=None, colour_elems=None, colour_ptr=None, device=None,
-                 structure=None, order=1, n_gauss=None):
+                 structure=None, order=1, n_gauss=None, scale=None):
         dev = device if device is not None else _lib.require_cuda()
         _lib.load()
         self.device = torch.device(dev)
         self.order = tuple(int(o) for o in (order if np.ndim(order) else (order,) * 3))
         self.n_gauss = tuple(int(g) for g in (n_gauss if n_gauss is not None and np.ndim(n_gauss) else
-                                              ((n_gauss,) * 3 if n_gauss is not None else [o + 1 for o in self.order])))
-        nns = int(np.prod([o + 1 for o in self.order]))
+                                              ((n_gauss,) * 3 if n_gauss is not None else
+                                               [min(o + 1, 4) for o in self.order])))
+        nns = int(np.prod([4 if o == 4 else o + 1 for o in self.order]))
         self.tensor_product = self.order != (1, 1, 1) or self.n_gauss != (2, 2, 2)
         en = np.ascontiguousarray(elem_nodes, dtype=np.int32)
         if en.ndim != 2 or en.shape[1] != nns:
@@ -84,6 +90,12 @@ class LaplaceAssembly:
         self.elem_nodes = torch.from_numpy(en).to(self.device)
         self.coords = torch.from_numpy(xyz).to(self.device)
         self.kappa = None if kappa is None else torch.as_tensor(np.asarray(kappa, np.float64)).to(self.device)
+        if scale is not None:
+            scale = np.ascontiguousarray(scale, dtype=np.float64)
+            if scale.shape != en.shape:
+                raise GfeError(-1, f"scale factors must be [E][{nns}] like the element parameters")
+            self.tensor_product = True
+        self.scale = None if scale is None else torch.from_numpy(scale).to(self.device)
         self.colour_elems = torch.from_numpy(np.ascontiguousarray(colour_elems, dtype=np.int32)).to(self.device)
         if structure is None:
             self.row_ptr, self.col_idx = csr_structure(self.elem_nodes, self.n_nodes)
@@ -95,6 +107,14 @@ class LaplaceAssembly:
         self.rhs = torch.empty(self.n_nodes, dtype=torch.float64, device=self.device)
         self.regular = None  # (nx, ny, nz) when the mesh is Iron's trilinear regular generated mesh
         self.grid = None     # (nelem, order) of a regular generated mesh of any order
+
+    @classmethod
+    def from_hermite_mesh(cls, mesh, kappa=None, device=None, n_gauss=4):
+        """Tricubic Hermite mesh (iron_gb300.mesh.HermiteMesh): parameters per DOF and, with
+        arc-length scaling, its scale factors."""
+        order, ptr = mesh.colouring()
+        return cls(mesh.elem_params, mesh.params, kappa=kappa, colour_elems=order, colour_ptr=ptr, device=device,
+                   order=4, n_gauss=n_gauss, scale=mesh.scale)
 
     @classmethod
     def from_regular_mesh(cls, mesh, kappa=None, device=None, n_gauss=None):
@@ -128,7 +148,8 @@ class LaplaceAssembly:
             cp = self.colour_ptr
             _lib.call("gfe_laplace_assemble_tp", (C.c_int32 * 3)(*self.order), (C.c_int32 * 3)(*self.n_gauss),
                       self.n_elements, self.n_nodes, _lib.ptr(self.elem_nodes), _lib.ptr(self.coords),
-                      _lib.ptr(self.kappa), _lib.ptr(self.colour_elems), cp.ctypes.data_as(C.c_void_p), len(cp) - 1,
+                      _lib.ptr(self.scale), _lib.ptr(self.kappa), _lib.ptr(self.colour_elems),
+                      cp.ctypes.data_as(C.c_void_p), len(cp) - 1,
                       _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx), self.nnz, _lib.ptr(self.values), _lib.ptr(v32),
                       _lib.ptr(self.rhs), prec, _lib.stream_handle(stream))
             if check:

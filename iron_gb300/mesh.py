@@ -159,3 +159,82 @@ class RegularMesh:
         idx = (I, J, K)[axis]
         lim = (tx, ty, tz)[axis] - 1
         return np.nonzero((idx == (0 if side == 0 else lim)).reshape(-1))[0].astype(np.int64)
+
+
+@dataclass
+class HermiteMesh:
+    """Iron's regular generated mesh of tricubic Hermite hexahedra on a box: 8 parameters per node
+    (value, d/ds1, d/ds2, d2/ds1ds2, d/ds3, d2/ds1ds3, d2/ds2ds3, d3/ds1ds2ds3), DOF = 8 node + k,
+    nodes and elements numbered xi1 fastest.
+
+    scaling "unit": derivative parameters are derivatives with respect to xi, no scale factors.
+    scaling "arc_length": derivative parameters are with respect to arc length, and each element
+    carries scale factors h1^d1 h2^d2 h3^d3 for the parameter with derivative bits (d1, d2, d3),
+    as Iron's arc-length scaling stores them.
+    elem_params [E][64], params [3][8N] (geometric parameters per DOF), scale [E][64] or None."""
+
+    nelem: tuple
+    extent: tuple = (1.0, 1.0, 1.0)
+    scaling: str = "unit"
+    elem_params: np.ndarray = field(init=False)
+    params: np.ndarray = field(init=False)
+    scale: np.ndarray | None = field(init=False)
+
+    def __post_init__(self):
+        nx, ny, nz = self.nelem
+        tx, ty, tz = nx + 1, ny + 1, nz + 1
+        h = np.array(self.extent, dtype=np.float64) / np.array(self.nelem, dtype=np.float64)
+        N = tx * ty * tz
+        K, J, I = np.meshgrid(np.arange(tz), np.arange(ty), np.arange(tx), indexing="ij")
+        pos = np.stack([I.reshape(-1) * h[0], J.reshape(-1) * h[1], K.reshape(-1) * h[2]])
+        p = np.zeros((3, 8 * N))
+        for c in range(3):
+            p[c, 0::8] = pos[c]
+            # d/ds_c of coordinate c: 1 per unit arc length, h_c per unit xi
+            p[c, (1 << c)::8] = 1.0 if self.scaling == "arc_length" else h[c]
+        self.params = p
+        lin = regular_elements(self.nelem, 1)  # [E][8] local nodes xi1 fastest
+        self.elem_params = (8 * lin[:, :, None] + np.arange(8)[None, None, :]).reshape(len(lin), 64).astype(np.int32)
+        if self.scaling == "arc_length":
+            k = np.arange(8)
+            sf = h[0] ** (k & 1) * h[1] ** ((k >> 1) & 1) * h[2] ** ((k >> 2) & 1)
+            self.scale = np.tile(np.tile(sf, 8), (len(lin), 1))
+        elif self.scaling == "unit":
+            self.scale = None
+        else:
+            raise ValueError(self.scaling)
+
+    @property
+    def n_nodes(self) -> int:
+        return int(np.prod([n + 1 for n in self.nelem]))
+
+    @property
+    def n_dofs(self) -> int:
+        return 8 * self.n_nodes
+
+    @property
+    def n_elements(self) -> int:
+        return int(np.prod(self.nelem))
+
+    def jitter_interior(self, seed: int, fraction: float = 0.05) -> None:
+        """Move interior nodes and perturb their first and cross derivatives (seeded), so that
+        elements are curved but keep a positive Jacobian."""
+        rng = np.random.default_rng(seed)
+        interior = ~boundary_node_mask(self.nelem, 1)
+        h = np.array(self.extent) / np.array(self.nelem)
+        for c in range(3):
+            for k in range(8):
+                d = self.params[c, k::8]
+                scale = h[c] if k == 0 else (self.params[c, (1 << c)::8].max() if k in (1, 2, 4) else 0.2 * h[c])
+                d[interior] += rng.uniform(-1, 1, interior.sum()) * fraction * scale
+
+    def colouring(self):
+        return parity_colouring(self.nelem)
+
+    def face_dofs(self, axis: int, side: int) -> np.ndarray:
+        """All parameter DOFs of the nodes on the face xi_axis = side (0 or 1)."""
+        tx, ty, tz = [n + 1 for n in self.nelem]
+        K, J, I = np.meshgrid(np.arange(tz), np.arange(ty), np.arange(tx), indexing="ij")
+        idx = (I, J, K)[axis].reshape(-1)
+        nodes = np.flatnonzero(idx == (0 if side == 0 else (tx, ty, tz)[axis] - 1))
+        return (8 * nodes[:, None] + np.arange(8)[None, :]).reshape(-1)

@@ -52,6 +52,8 @@ def lib():
         L.orc_laplace_element.argtypes = [C.c_int, i32p, i32p, C.c_int, f64p, C.c_double, f64p]
         L.orc_laplace_assemble.argtypes = [C.c_int, i32p, i32p, C.c_int, C.c_int, i32p, f64p, C.c_void_p,
                                            i32p, i32p, f64p, C.c_void_p, C.c_int]
+        L.orc_laplace_assemble_scaled.argtypes = [C.c_int, i32p, i32p, C.c_int, C.c_int, i32p, f64p, C.c_void_p,
+                                                  C.c_void_p, i32p, i32p, f64p, C.c_void_p, C.c_int]
         L.orc_csr_spmv.argtypes = [C.c_int, i32p, i32p, f64p, f64p, f64p]
         L.orc_solver_system.argtypes = [C.c_int, i32p, i32p, f64p, C.c_void_p, u8p, C.c_void_p, f64p, i32p, i32p,
                                         i32p, f64p, f64p, C.c_int64, C.POINTER(C.c_int32)]
@@ -176,6 +178,25 @@ def laplace_assemble(nxi, order, ngauss, elem_nodes, coords, kappa, rp, ci, n_th
     if rc != 0:
         raise RuntimeError(f"oracle assembly failed ({rc})")
     return vals, rhs
+
+
+def laplace_assemble_scaled(nxi, interp, ngauss, elem_params, params, scale, kappa, rp, ci):
+    """Laplace assembly on a mesh of any tensor-product basis (interp per direction: 1..3 Lagrange
+    order, 4 cubic Hermite), with element parameters elem_params [E][nns] (0-based DOFs), the
+    geometric parameters per DOF params [nxi][n_dofs] and optional scale factors [E][nns]."""
+    elem_params = _i32(elem_params)
+    params = _f64(params)
+    E = elem_params.shape[0]
+    N = params.shape[1]
+    vals = np.zeros(int(rp[-1]) - 1)
+    sc = None if scale is None else _f64(scale)
+    kap = None if kappa is None else _f64(kappa)
+    rc = lib().orc_laplace_assemble_scaled(nxi, _i32(interp), _i32(ngauss), E, N, elem_params, params,
+                                           None if sc is None else sc.ctypes.data,
+                                           None if kap is None else kap.ctypes.data, _i32(rp), _i32(ci), vals, None, 1)
+    if rc != 0:
+        raise RuntimeError(f"oracle assembly failed ({rc})")
+    return vals
 
 
 def spmv(rp, ci, vals, x):

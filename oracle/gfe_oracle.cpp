@@ -14,6 +14,7 @@
 // (src/types.F90:909-929, ROW_INDICES(M+1), COLUMN_INDICES(nnz)).
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -79,10 +80,26 @@ double lagrange1d(int order, int a, int deriv, double xi) {
   return 0.0;
 }
 
+// 1D cubic Hermite on [0,1], src/basis_routines.F90:7607-7701 (HERMITE_CUBIC_EVALUATE): node a
+// (0-based, 0 or 1), node derivative k (0 = value, 1 = first derivative), deriv 0 = value, 1 = d/dxi.
+double hermite1d(int a, int k, int deriv, double xi) {
+  if (deriv == 0) {
+    if (a == 0) return k == 0 ? (2.0 * xi - 3.0) * xi * xi + 1.0 : ((xi - 2.0) * xi + 1.0) * xi;
+    return k == 0 ? xi * xi * (3.0 - 2.0 * xi) : xi * xi * (xi - 1.0);
+  }
+  if (a == 0) return k == 0 ? 6.0 * xi * (xi - 1.0) : (3.0 * xi - 4.0) * xi + 1.0;
+  return k == 0 ? 6.0 * xi * (1.0 - xi) : xi * (3.0 * xi - 2.0);
+}
+
 // Tensor-product table in Iron's order: element parameter ns with xi1 fastest
 // (src/basis_routines.F90:3243-3370), Gauss point ng = i + (j-1 + (k-1) n2) n1 (:3820).
 // Layout of the returned table: tab[(ng * (nxi+1) + nu) * nns + ns], nu 0 = value,
 // nu = 1..nxi = d/dxi_nu (Iron's partial-derivative indices 2, 4, 7: src/constants.F90:180-185).
+// order[d]: Iron's interpolation specification per xi direction: 1..3 = Lagrange of that order,
+// 4 = cubic Hermite (BASIS_CUBIC_HERMITE_INTERPOLATION, src/basis_routines.F90:83-86).  Element
+// parameters run over the local nodes (xi1 fastest) and, within a node, over its derivatives in
+// Iron's order (the count doubles for every Hermite direction in xi order, :2633-2662), so with
+// three Hermite directions the derivative index is d1 + 2 d2 + 4 d3.
 struct TPBasis {
   int nxi = 0, nns = 0, ng = 0;
   int nnx[3] = {1, 1, 1}, ngx[3] = {1, 1, 1}, order[3] = {1, 1, 1};
@@ -92,22 +109,35 @@ struct TPBasis {
 bool make_tp_basis(int nxi, const int* order, const int* ngauss, TPBasis& b) {
   if (nxi < 1 || nxi > 3) return false;
   b.nxi = nxi;
-  b.nns = 1;
   b.ng = 1;
   double gx[3][4], gw[3][4];
   for (int d = 0; d < 3; ++d) {
     b.nnx[d] = 1; b.ngx[d] = 1; b.order[d] = 1;
     gx[d][0] = 0.5; gw[d][0] = 1.0;
   }
+  int nder = 1;  // derivatives per node
   for (int d = 0; d < nxi; ++d) {
-    if (order[d] < 1 || order[d] > 3) return false;
+    if (order[d] < 1 || order[d] > 4) return false;
     b.order[d] = order[d];
-    b.nnx[d] = order[d] + 1;
+    b.nnx[d] = order[d] == 4 ? 2 : order[d] + 1;
+    if (order[d] == 4) nder *= 2;
     b.ngx[d] = ngauss[d];
     if (!gauss_legendre(ngauss[d], gx[d], gw[d])) return false;
-    b.nns *= b.nnx[d];
     b.ng *= b.ngx[d];
   }
+  // element parameters: (node position, node derivative) per direction, in Iron's order
+  std::vector<std::array<int, 6>> par;
+  for (int a3 = 0; a3 < b.nnx[2]; ++a3)
+    for (int a2 = 0; a2 < b.nnx[1]; ++a2)
+      for (int a1 = 0; a1 < b.nnx[0]; ++a1)
+        for (int k = 0; k < nder; ++k) {
+          std::array<int, 6> q = {a1, a2, a3, 0, 0, 0};
+          int bit = 0;
+          for (int d = 0; d < nxi; ++d)
+            if (b.order[d] == 4) q[3 + d] = (k >> bit++) & 1;
+          par.push_back(q);
+        }
+  b.nns = (int)par.size();
   b.tab.assign((size_t)b.ng * (nxi + 1) * b.nns, 0.0);
   b.wts.assign(b.ng, 0.0);
   for (int g3 = 0; g3 < b.ngx[2]; ++g3)
@@ -118,17 +148,16 @@ bool make_tp_basis(int nxi, const int* order, const int* ngauss, TPBasis& b) {
         double w = 1.0;
         for (int d = 0; d < nxi; ++d) w *= gw[d][gi[d]];
         b.wts[g] = w;
-        for (int a3 = 0; a3 < b.nnx[2]; ++a3)
-          for (int a2 = 0; a2 < b.nnx[1]; ++a2)
-            for (int a1 = 0; a1 < b.nnx[0]; ++a1) {
-              int ns = a1 + b.nnx[0] * (a2 + b.nnx[1] * a3);
-              const int ai[3] = {a1, a2, a3};
-              for (int nu = 0; nu <= nxi; ++nu) {
-                double v = 1.0;
-                for (int d = 0; d < nxi; ++d) v *= lagrange1d(b.order[d], ai[d], (nu == d + 1) ? 1 : 0, gx[d][gi[d]]);
-                b.tab[((size_t)g * (nxi + 1) + nu) * b.nns + ns] = v;
-              }
+        for (int ns = 0; ns < b.nns; ++ns)
+          for (int nu = 0; nu <= nxi; ++nu) {
+            double v = 1.0;
+            for (int d = 0; d < nxi; ++d) {
+              const int der = (nu == d + 1) ? 1 : 0;
+              v *= b.order[d] == 4 ? hermite1d(par[ns][d], par[ns][3 + d], der, gx[d][gi[d]])
+                                   : lagrange1d(b.order[d], par[ns][d], der, gx[d][gi[d]]);
             }
+            b.tab[((size_t)g * (nxi + 1) + nu) * b.nns + ns] = v;
+          }
       }
   return true;
 }
@@ -417,10 +446,15 @@ int orc_laplace_element(int nxi, const int* order, const int* ngauss, int ncomp,
 // column DOFs = element node DOFs (one component, one domain).
 // n_threads > 1: element-partitioned threads with private value copies summed at the end
 // (used for the multi-core CPU baseline only).
-int orc_laplace_assemble(int nxi, const int* order, const int* ngauss, int n_elem, int n_nodes,
-                         const int32_t* elem_nodes, const double* coords /*[nxi][N]*/, const double* kappa,
-                         const int32_t* row_ptr, const int32_t* col_idx, double* values, double* rhs,
-                         int n_threads) {
+// scale (optional) [n_elem][nns]: element parameter scale factors.  The geometric parameters are
+// interpolated scaled (FIELD_INTERPOLATION_PARAMETERS_ELEMENT_GET multiplies them by the scale
+// factors), and the element matrix is scaled as K(ms, ns) * SF(ms) * SF(ns)
+// (src/Laplace_equations_routines.F90:555-579).  elem_nodes then holds element parameter DOFs
+// and coords the parameters per DOF.
+int orc_laplace_assemble_scaled(int nxi, const int* order, const int* ngauss, int n_elem, int n_nodes,
+                                const int32_t* elem_nodes, const double* coords /*[nxi][N]*/, const double* scale,
+                                const double* kappa, const int32_t* row_ptr, const int32_t* col_idx, double* values,
+                                double* rhs, int n_threads) {
   TPBasis b;
   if (!make_tp_basis(nxi, order, ngauss, b)) return -1;
   const int n = b.nns;
@@ -438,9 +472,14 @@ int orc_laplace_assemble(int nxi, const int* order, const int* ngauss, int n_ele
       for (int s = 0; s < n; ++s) {
         int node = elem_nodes[(size_t)e * n + s];
         dofs[s] = node + 1;
-        for (int c = 0; c < nxi; ++c) xe[(size_t)c * n + s] = coords[(size_t)c * n_nodes + node];
+        const double sf = scale ? scale[(size_t)e * n + s] : 1.0;
+        for (int c = 0; c < nxi; ++c) xe[(size_t)c * n + s] = coords[(size_t)c * n_nodes + node] * sf;
       }
       laplace_element(b, x, nxi, kappa ? kappa[e] : 1.0, K.data());
+      if (scale)
+        for (int ms = 0; ms < n; ++ms)
+          for (int ns = 0; ns < n; ++ns)
+            K[(size_t)ms * n + ns] = K[(size_t)ms * n + ns] * scale[(size_t)e * n + ms] * scale[(size_t)e * n + ns];
       if (csr_values_add(row_ptr, col_idx, out, n, dofs.data(), n, dofs.data(), K.data()) != 0) {
         status[t] = -2;
         return;
@@ -463,6 +502,14 @@ int orc_laplace_assemble(int nxi, const int* order, const int* ngauss, int n_ele
   for (int s : status)
     if (s) return s;
   return 0;
+}
+
+int orc_laplace_assemble(int nxi, const int* order, const int* ngauss, int n_elem, int n_nodes,
+                         const int32_t* elem_nodes, const double* coords, const double* kappa,
+                         const int32_t* row_ptr, const int32_t* col_idx, double* values, double* rhs,
+                         int n_threads) {
+  return orc_laplace_assemble_scaled(nxi, order, ngauss, n_elem, n_nodes, elem_nodes, coords, nullptr, kappa, row_ptr,
+                                     col_idx, values, rhs, n_threads);
 }
 
 // ---------------------------------------------------------------------------------------

@@ -68,3 +68,36 @@ def test_rejects_unsupported_bases(gfe_cuda):
     m = M.RegularMesh((1, 1, 1), order=2)
     with pytest.raises(Exception, match="Gauss"):
         LaplaceAssembly.from_regular_mesh(m, n_gauss=5).assemble("fp64")
+
+
+@pytest.mark.parametrize("scaling", ["unit", "arc_length"])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed_df", 1e-12), ("mixed", 2e-5)])
+def test_cubic_hermite_matches_oracle(gfe_cuda, scaling, precision, tol):
+    hm = M.HermiteMesh((2, 2, 2), extent=(1.0, 0.8, 1.2), scaling=scaling)
+    hm.jitter_interior(5)
+    kap = np.exp(np.random.default_rng(6).uniform(np.log(0.1), np.log(10.0), hm.n_elements))
+    A = LaplaceAssembly.from_hermite_mesh(hm, kappa=kap)
+    vals = A.assemble(precision).cpu().numpy()
+    rp, ci, _ = A.to_iron_csr()
+    orp, oci = oracle.csr_structure(hm.elem_params, hm.n_dofs)
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    ref = oracle.laplace_assemble_scaled(3, [4, 4, 4], [4, 4, 4], hm.elem_params, hm.params, hm.scale, kap, orp, oci)
+    assert np.abs(vals - ref).max() <= tol * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("scaling", ["unit", "arc_length"])
+def test_cubic_hermite_patch_test(gfe_cuda, scaling):
+    """u = x on a stretched box: every parameter of the x = 0 and x = 1 face nodes fixed to the
+    exact parameters (value x, d/ds1 of x, zero elsewhere); the reduced solve returns the exact
+    parameters at every other DOF."""
+    hm = M.HermiteMesh((3, 2, 2), extent=(1.0, 0.7, 1.4), scaling=scaling)
+    A = LaplaceAssembly.from_hermite_mesh(hm)
+    A.assemble("fp64")
+    exact = torch.from_numpy(hm.params[0].copy()).cuda()
+    fixed = torch.zeros(hm.n_dofs, dtype=torch.uint8, device="cuda")
+    for side in (0, 1):
+        fixed[torch.from_numpy(hm.face_dofs(0, side)).cuda()] = 1
+    x = torch.where(fixed.bool(), exact, torch.zeros_like(exact))
+    info = A.solve_reduced(fixed, x, rtol=1e-13, system=A.solver_system(fixed, col_listed=None))
+    assert info.relative_residual <= 1e-13
+    assert (x - exact).abs().max().item() <= 1e-10
