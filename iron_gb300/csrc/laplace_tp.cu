@@ -91,6 +91,38 @@ void lagrange1d(int p, int k, double t, double* val, double* der) {
   *der = d;
 }
 
+// Tetrahedral simplex bases (Iron's interpolation 7 = linear, 8 = quadratic): basis functions are
+// products over the four area coordinates of factors chosen by the node's position index (1 = 1,
+// 2 = L resp. 2L, 3 = L(2L-1)), the xi derivatives are d/dL4 - d/dL_i, and the Gauss points are
+// Gauss_Simplex's tetrahedral rules of orders 1..3 (1, 4, 5 points; weights sum to 1/6)
+// (src/basis_routines.F90:4813-5875, 6041-6270, 6898-7600, 8177-8313).
+double simplex_factor(int interp, int pos, bool deriv, double L) {
+  if (interp == 7) return pos == 1 ? (deriv ? 0.0 : 1.0) : (deriv ? 1.0 : L);
+  if (pos == 1) return deriv ? 0.0 : 1.0;
+  if (pos == 2) return deriv ? 2.0 : 2.0 * L;
+  return deriv ? 4.0 * L - 1.0 : L * (2.0 * L - 1.0);
+}
+
+void simplex_rule(int order, std::vector<std::array<double, 4>>& L, std::vector<double>& w) {
+  if (order == 1) {
+    L.push_back({0.25, 0.25, 0.25, 0.25});
+    w.push_back(1.0 / 6.0);
+    return;
+  }
+  const double a = order == 2 ? 1.0 / std::sqrt(5.0) : 1.0 / 3.0;
+  const double wa = order == 2 ? 0.25 : 9.0 / 20.0;
+  const double l1 = (1.0 + 3.0 * a) / 4.0, l2 = (1.0 - a) / 4.0, l3 = (1.0 - a) / 4.0, l4 = 1.0 - l1 - l2 - l3;
+  if (order == 3) {
+    L.push_back({0.25, 0.25, 0.25, 0.25});
+    w.push_back(-4.0 / 5.0 / 6.0);
+  }
+  L.push_back({l1, l2, l3, l4});
+  L.push_back({l4, l1, l2, l3});
+  L.push_back({l3, l4, l1, l2});
+  L.push_back({l2, l3, l4, l1});
+  for (int k = 0; k < 4; ++k) w.push_back(wa / 6.0);
+}
+
 template <typename T>
 T to_elem(double v);
 template <>
@@ -117,9 +149,30 @@ struct TPTables {
 
 std::mutex g_tp_mu;
 
+using TPKey = std::tuple<int, int, int, int, int, int, int>;
+
+// copy one configuration's tables to the device and cache them (caller holds g_tp_mu)
+template <typename T>
+int upload_tables(const TPKey& key, std::map<TPKey, TPTables<T>>& cache, int nns, int ng, const std::vector<T>& dphi,
+                  const std::vector<T>& w, const TPTables<T>** out) {
+  std::vector<int32_t> pairs;
+  for (int m = 0; m < nns; ++m)
+    for (int n = m; n < nns; ++n) pairs.push_back(m | (n << 16));
+  TPTables<T> t;
+  t.cfg = {nns, ng, (int)pairs.size()};
+  GFE_CUDA_TRY(cudaMalloc(&t.dphi, sizeof(T) * dphi.size()));
+  GFE_CUDA_TRY(cudaMalloc(&t.w, sizeof(T) * w.size()));
+  GFE_CUDA_TRY(cudaMalloc(&t.pairs, sizeof(int32_t) * pairs.size()));
+  GFE_CUDA_TRY(cudaMemcpy(t.dphi, dphi.data(), sizeof(T) * dphi.size(), cudaMemcpyHostToDevice));
+  GFE_CUDA_TRY(cudaMemcpy(t.w, w.data(), sizeof(T) * w.size(), cudaMemcpyHostToDevice));
+  GFE_CUDA_TRY(cudaMemcpy(t.pairs, pairs.data(), sizeof(int32_t) * pairs.size(), cudaMemcpyHostToDevice));
+  *out = &(cache[key] = t);
+  return GFE_OK;
+}
+
 template <typename T>
 int tp_tables(const int32_t* order, const int32_t* ngauss, const TPTables<T>** out) {
-  static std::map<std::tuple<int, int, int, int, int, int, int>, TPTables<T>> cache;
+  static std::map<TPKey, TPTables<T>> cache;
   int dev = 0;
   GFE_CUDA_TRY(cudaGetDevice(&dev));
   const auto key = std::make_tuple(dev, order[0], order[1], order[2], ngauss[0], ngauss[1], ngauss[2]);
@@ -128,6 +181,30 @@ int tp_tables(const int32_t* order, const int32_t* ngauss, const TPTables<T>** o
   if (it != cache.end()) {
     *out = &it->second;
     return GFE_OK;
+  }
+  if (order[0] == 7 || order[0] == 8) {
+    static const int lin[4][4] = {{2, 1, 1, 1}, {1, 2, 1, 1}, {1, 1, 2, 1}, {1, 1, 1, 2}};
+    static const int quad[10][4] = {{3, 1, 1, 1}, {1, 3, 1, 1}, {1, 1, 3, 1}, {1, 1, 1, 3}, {2, 2, 1, 1},
+                                    {2, 1, 2, 1}, {2, 1, 1, 2}, {1, 2, 2, 1}, {1, 1, 2, 2}, {1, 2, 1, 2}};
+    std::vector<std::array<double, 4>> gl;
+    std::vector<double> gw;
+    simplex_rule(ngauss[0], gl, gw);
+    const int nns = order[0] == 7 ? 4 : 10, ng = (int)gl.size();
+    std::vector<T> dphi((size_t)ng * 3 * nns), w(ng);
+    for (int g = 0; g < ng; ++g) {
+      w[g] = to_elem<T>(gw[g]);
+      for (int n = 0; n < nns; ++n) {
+        const int* pos = order[0] == 7 ? lin[n] : quad[n];
+        double dL[4];
+        for (int k = 0; k < 4; ++k) {
+          double d = 1.0;
+          for (int j = 0; j < 4; ++j) d *= simplex_factor(order[0], pos[j], j == k, gl[g][j]);
+          dL[k] = d;
+        }
+        for (int a = 0; a < 3; ++a) dphi[((size_t)g * 3 + a) * nns + n] = to_elem<T>(dL[3] - dL[a]);
+      }
+    }
+    return upload_tables<T>(key, cache, nns, ng, dphi, w, out);
   }
   // element parameters in Iron's order: local nodes xi1 fastest, then each node's derivatives,
   // whose count doubles for every Hermite direction in xi order (src/basis_routines.F90:2633-2662)
@@ -168,19 +245,7 @@ int tp_tables(const int32_t* order, const int32_t* ngauss, const TPTables<T>** o
           dphi[((size_t)g * 3 + 2) * nns + n] = to_elem<T>(v[0] * v[1] * dv[2]);
         }
       }
-  std::vector<int32_t> pairs;
-  for (int m = 0; m < nns; ++m)
-    for (int n = m; n < nns; ++n) pairs.push_back(m | (n << 16));
-  TPTables<T> t;
-  t.cfg = {nns, ng, (int)pairs.size()};
-  GFE_CUDA_TRY(cudaMalloc(&t.dphi, sizeof(T) * dphi.size()));
-  GFE_CUDA_TRY(cudaMalloc(&t.w, sizeof(T) * w.size()));
-  GFE_CUDA_TRY(cudaMalloc(&t.pairs, sizeof(int32_t) * pairs.size()));
-  GFE_CUDA_TRY(cudaMemcpy(t.dphi, dphi.data(), sizeof(T) * dphi.size(), cudaMemcpyHostToDevice));
-  GFE_CUDA_TRY(cudaMemcpy(t.w, w.data(), sizeof(T) * w.size(), cudaMemcpyHostToDevice));
-  GFE_CUDA_TRY(cudaMemcpy(t.pairs, pairs.data(), sizeof(int32_t) * pairs.size(), cudaMemcpyHostToDevice));
-  *out = &(cache[key] = t);
-  return GFE_OK;
+  return upload_tables<T>(key, cache, nns, ng, dphi, w, out);
 }
 
 // Iron's CSR search (MATRIX_VALUES_ADD_DP2): bisection until at most 10 candidates, then a
@@ -325,7 +390,11 @@ extern "C" int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_ga
                                        float* values32, double* rhs, int32_t precision, void* stream) {
   const char* fn = "gfe_laplace_assemble_tp";
   if (!order || !n_gauss) return gfe::set_error(GFE_ERR_ARG, "%s: order and n_gauss are required", fn);
-  for (int d = 0; d < 3; ++d) {
+  const bool simplex = order[0] == 7 || order[0] == 8;
+  if (simplex && (order[1] != order[0] || order[2] != order[0] || n_gauss[0] < 1 || n_gauss[0] > 3))
+    return gfe::set_error(GFE_ERR_ARG, "%s: tetrahedra need the same simplex interpolation in every xi and a "
+                          "Gauss_Simplex order of 1..3 in n_gauss[0]", fn);
+  for (int d = 0; d < 3 && !simplex; ++d) {
     if (order[d] < 1 || order[d] > 4)
       return gfe::set_error(GFE_ERR_ARG, "%s: interpolation %d in xi%d (1..3 Lagrange, 4 cubic Hermite supported)",
                             fn, order[d], d + 1);

@@ -53,7 +53,8 @@ class LaplaceAssembly:
     colour_elems / colour_ptr: an element colouring (elements of one colour share no node);
     order: Iron's interpolation per direction (an int or three): 1..3 = Lagrange of that order,
     4 = cubic Hermite; an element has prod(order + 1) parameters for Lagrange directions and 4 per
-    Hermite direction (2 nodes x value and slope);
+    Hermite direction (2 nodes x value and slope); 7 / 8 = linear / quadratic tetrahedra (4 / 10
+    nodes in Iron's order, n_gauss = the Gauss_Simplex order 1..3);
     n_gauss: Gauss points per direction (1..4; default order + 1, 4 for Hermite);
     scale: [E][nns] element parameter scale factors (Hermite arc-length scaling) or None.
     For Hermite meshes elem_nodes holds element parameter DOFs and coords the geometric parameters
@@ -68,10 +69,19 @@ class LaplaceAssembly:
         _lib.load()
         self.device = torch.device(dev)
         self.order = tuple(int(o) for o in (order if np.ndim(order) else (order,) * 3))
-        self.n_gauss = tuple(int(g) for g in (n_gauss if n_gauss is not None and np.ndim(n_gauss) else
-                                              ((n_gauss,) * 3 if n_gauss is not None else
-                                               [min(o + 1, 4) for o in self.order])))
-        nns = int(np.prod([4 if o == 4 else o + 1 for o in self.order]))
+        simplex = self.order[0] in (7, 8)
+        if simplex:
+            # tetrahedra: one simplex interpolation, n_gauss = Gauss_Simplex order (default: exact
+            # for straight-sided elements, 1 for linear and 2 for quadratic)
+            q = int(n_gauss if n_gauss is not None and not np.ndim(n_gauss) else
+                    (n_gauss[0] if n_gauss is not None else self.order[0] - 6))
+            self.n_gauss = (q, q, q)
+            nns = 4 if self.order[0] == 7 else 10
+        else:
+            self.n_gauss = tuple(int(g) for g in (n_gauss if n_gauss is not None and np.ndim(n_gauss) else
+                                                  ((n_gauss,) * 3 if n_gauss is not None else
+                                                   [min(o + 1, 4) for o in self.order])))
+            nns = int(np.prod([4 if o == 4 else o + 1 for o in self.order]))
         self.tensor_product = self.order != (1, 1, 1) or self.n_gauss != (2, 2, 2)
         en = np.ascontiguousarray(elem_nodes, dtype=np.int32)
         if en.ndim != 2 or en.shape[1] != nns:
@@ -107,6 +117,11 @@ class LaplaceAssembly:
         self.rhs = torch.empty(self.n_nodes, dtype=torch.float64, device=self.device)
         self.regular = None  # (nx, ny, nz) when the mesh is Iron's trilinear regular generated mesh
         self.grid = None     # (nelem, order) of a regular generated mesh of any order
+
+    @classmethod
+    def from_tet_mesh(cls, mesh, kappa=None, device=None, n_gauss=None):
+        """Tetrahedral mesh (iron_gb300.mesh.TetMesh), greedy element colouring."""
+        return cls(mesh.elem_nodes, mesh.coords, kappa=kappa, device=device, order=6 + mesh.order, n_gauss=n_gauss)
 
     @classmethod
     def from_hermite_mesh(cls, mesh, kappa=None, device=None, n_gauss=4):

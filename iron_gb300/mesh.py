@@ -238,3 +238,80 @@ class HermiteMesh:
         idx = (I, J, K)[axis].reshape(-1)
         nodes = np.flatnonzero(idx == (0 if side == 0 else (tx, ty, tz)[axis] - 1))
         return (8 * nodes[:, None] + np.arange(8)[None, :]).reshape(-1)
+
+
+@dataclass
+class TetMesh:
+    """Tetrahedral mesh of a box: every cell of a regular grid split into six tetrahedra along its
+    main diagonal (conforming across cells), order 1 (4 vertices) or 2 (plus 6 edge nodes in
+    Iron's quadratic-simplex order: edges 1-2, 1-3, 1-4, 2-3, 3-4, 2-4).  coords [3][N],
+    elem_nodes [E][4 or 10] (0-based)."""
+
+    nelem: tuple
+    order: int = 1
+    extent: tuple = (1.0, 1.0, 1.0)
+    elem_nodes: np.ndarray = field(init=False)
+    coords: np.ndarray = field(init=False)
+
+    def __post_init__(self):
+        nx, ny, nz = self.nelem
+        tx, ty, tz = nx + 1, ny + 1, nz + 1
+        vid = lambda i, j, k: i + tx * (j + ty * k)  # noqa: E731
+        tets = []
+        perms = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+        for k in range(nz):
+            for j in range(ny):
+                for i in range(nx):
+                    for p in perms:
+                        cur = [i, j, k]
+                        t = [vid(*cur)]
+                        for d in p:
+                            cur[d] += 1
+                            t.append(vid(*cur))
+                        tets.append(t)
+        tets = np.array(tets, dtype=np.int64)
+        K, J, I = np.meshgrid(np.arange(tz), np.arange(ty), np.arange(tx), indexing="ij")
+        h = np.array(self.extent) / np.array(self.nelem)
+        verts = np.stack([I.reshape(-1) * h[0], J.reshape(-1) * h[1], K.reshape(-1) * h[2]])
+        self.n_vertices = verts.shape[1]
+        if self.order == 1:
+            self.elem_nodes, self.coords = tets.astype(np.int32), verts
+        elif self.order == 2:
+            pairs = [(0, 1), (0, 2), (0, 3), (1, 2), (2, 3), (1, 3)]
+            e = np.stack([np.sort(tets[:, [a, b]], axis=1) for a, b in pairs], axis=1)  # [E][6][2]
+            uniq, inv = np.unique(e.reshape(-1, 2), axis=0, return_inverse=True)
+            mid = (verts[:, uniq[:, 0]] + verts[:, uniq[:, 1]]) / 2.0
+            self.coords = np.concatenate([verts, mid], axis=1)
+            self.elem_nodes = np.concatenate([tets, self.n_vertices + inv.reshape(-1, 6)], axis=1).astype(np.int32)
+            self.edges = uniq
+        else:
+            raise ValueError("tetrahedra of order 1 or 2")
+
+    @property
+    def n_nodes(self) -> int:
+        return self.coords.shape[1]
+
+    @property
+    def n_elements(self) -> int:
+        return self.elem_nodes.shape[0]
+
+    def boundary_mask(self) -> np.ndarray:
+        x = self.coords
+        ext = np.array(self.extent)[:, None]
+        return np.any(np.isclose(x, 0.0) | np.isclose(x, ext), axis=0)
+
+    def jitter_interior(self, seed: int, fraction: float = 0.1) -> None:
+        """Move interior vertices (seeded) and keep edge nodes at their edges' midpoints, so that
+        elements stay straight-sided."""
+        rng = np.random.default_rng(seed)
+        h = np.array(self.extent) / np.array(self.nelem)
+        interior = ~self.boundary_mask()[: self.n_vertices]
+        d = rng.uniform(-1, 1, (3, self.n_vertices)) * (fraction * h)[:, None]
+        d[:, ~interior] = 0.0
+        self.coords[:, : self.n_vertices] += d
+        if self.order == 2:
+            self.coords[:, self.n_vertices:] = (self.coords[:, self.edges[:, 0]] + self.coords[:, self.edges[:, 1]]) / 2
+
+    def face_nodes(self, axis: int, side: int) -> np.ndarray:
+        target = 0.0 if side == 0 else self.extent[axis]
+        return np.flatnonzero(np.isclose(self.coords[axis], target))

@@ -106,7 +106,70 @@ struct TPBasis {
   std::vector<double> tab, wts;
 };
 
+// Tetrahedral simplex basis, src/basis_routines.F90: Basis_SimplexBasisCreate :4813-5875 (node
+// positions per area coordinate: 1 absent, 2 on an edge (L for linear, 2L for quadratic),
+// 3 vertex L(2L-1); SIMPLEX_LINEAR/QUADRATIC_EVALUATE :8177-8313), BASIS_SIMPLEX_BASIS_EVALUATE
+// :6041-6270 (d/dxi_i = d/dL4 - d/dL_i), Gauss_Simplex :6898-7600 (tetrahedra, orders 1..3:
+// 1, 4, 5 points in area coordinates, weights summing to 1/6).  interp 7 = linear (4 nodes),
+// 8 = quadratic (10 nodes); quad_order = Gauss_Simplex order.
+double simplex_factor(int interp, int pos, int deriv, double L) {
+  if (interp == 7) return pos == 1 ? (deriv ? 0.0 : 1.0) : (deriv ? 1.0 : L);
+  if (pos == 1) return deriv ? 0.0 : 1.0;
+  if (pos == 2) return deriv ? 2.0 : 2.0 * L;
+  return deriv ? 4.0 * L - 1.0 : L * (2.0 * L - 1.0);
+}
+
+bool make_simplex_basis(int interp, int quad_order, TPBasis& b) {
+  static const int lin[4][4] = {{2, 1, 1, 1}, {1, 2, 1, 1}, {1, 1, 2, 1}, {1, 1, 1, 2}};
+  static const int quad[10][4] = {{3, 1, 1, 1}, {1, 3, 1, 1}, {1, 1, 3, 1}, {1, 1, 1, 3}, {2, 2, 1, 1},
+                                  {2, 1, 2, 1}, {2, 1, 1, 2}, {1, 2, 2, 1}, {1, 1, 2, 2}, {1, 2, 1, 2}};
+  std::vector<std::array<double, 4>> gl;
+  std::vector<double> gw;
+  if (quad_order == 1) {
+    gl.push_back({0.25, 0.25, 0.25, 0.25});
+    gw.push_back(1.0 / 6.0);
+  } else if (quad_order == 2 || quad_order == 3) {
+    const double a = quad_order == 2 ? 1.0 / std::sqrt(5.0) : 1.0 / 3.0;
+    const double wa = quad_order == 2 ? 0.25 : 9.0 / 20.0;
+    const double l1 = (1.0 + 3.0 * a) / 4.0, l2 = (1.0 - a) / 4.0, l3 = (1.0 - a) / 4.0, l4 = 1.0 - l1 - l2 - l3;
+    if (quad_order == 3) {
+      gl.push_back({0.25, 0.25, 0.25, 0.25});
+      gw.push_back(-4.0 / 5.0 / 6.0);
+    }
+    gl.push_back({l1, l2, l3, l4});
+    gl.push_back({l4, l1, l2, l3});
+    gl.push_back({l3, l4, l1, l2});
+    gl.push_back({l2, l3, l4, l1});
+    for (int k = 0; k < 4; ++k) gw.push_back(wa / 6.0);
+  } else {
+    return false;
+  }
+  if (interp != 7 && interp != 8) return false;
+  const int nns = interp == 7 ? 4 : 10;
+  b.nxi = 3;
+  b.nns = nns;
+  b.ng = (int)gl.size();
+  b.tab.assign((size_t)b.ng * 4 * nns, 0.0);
+  b.wts = gw;
+  for (int g = 0; g < b.ng; ++g)
+    for (int ns = 0; ns < nns; ++ns) {
+      const int* pos = interp == 7 ? lin[ns] : quad[ns];
+      double dL[4];  // d phi / d L_k
+      double v = 1.0;
+      for (int k = 0; k < 4; ++k) v *= simplex_factor(interp, pos[k], 0, gl[g][k]);
+      for (int k = 0; k < 4; ++k) {
+        double d = 1.0;
+        for (int j = 0; j < 4; ++j) d *= simplex_factor(interp, pos[j], j == k, gl[g][j]);
+        dL[k] = d;
+      }
+      b.tab[((size_t)g * 4 + 0) * nns + ns] = v;
+      for (int i = 0; i < 3; ++i) b.tab[((size_t)g * 4 + i + 1) * nns + ns] = dL[3] - dL[i];
+    }
+  return true;
+}
+
 bool make_tp_basis(int nxi, const int* order, const int* ngauss, TPBasis& b) {
+  if (nxi == 3 && (order[0] == 7 || order[0] == 8)) return make_simplex_basis(order[0], ngauss[0], b);
   if (nxi < 1 || nxi > 3) return false;
   b.nxi = nxi;
   b.ng = 1;

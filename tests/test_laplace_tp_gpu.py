@@ -101,3 +101,35 @@ def test_cubic_hermite_patch_test(gfe_cuda, scaling):
     info = A.solve_reduced(fixed, x, rtol=1e-13, system=A.solver_system(fixed, col_listed=None))
     assert info.relative_residual <= 1e-13
     assert (x - exact).abs().max().item() <= 1e-10
+
+
+@pytest.mark.parametrize("order,quad", [(1, 1), (1, 2), (2, 2), (2, 3)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed_df", 1e-12), ("mixed", 2e-5)])
+def test_tetrahedra_match_oracle(gfe_cuda, order, quad, precision, tol):
+    tm = M.TetMesh((3, 2, 2), order=order, extent=(1.0, 0.8, 1.2))
+    tm.jitter_interior(7)
+    kap = np.exp(np.random.default_rng(8).uniform(np.log(0.1), np.log(10.0), tm.n_elements))
+    A = LaplaceAssembly.from_tet_mesh(tm, kappa=kap, n_gauss=quad)
+    vals = A.assemble(precision).cpu().numpy()
+    rp, ci, _ = A.to_iron_csr()
+    orp, oci = oracle.csr_structure(tm.elem_nodes, tm.n_nodes)
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    ref = oracle.laplace_assemble_scaled(3, [6 + order] * 3, [quad] * 3, tm.elem_nodes, tm.coords, None, kap, orp, oci)
+    assert np.abs(vals - ref).max() <= tol * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_tetrahedra_patch_test(gfe_cuda, order):
+    tm = M.TetMesh((3, 3, 2), order=order)
+    tm.jitter_interior(9)
+    A = LaplaceAssembly.from_tet_mesh(tm)
+    A.assemble("fp64")
+    fixed = torch.zeros(tm.n_nodes, dtype=torch.uint8, device="cuda")
+    x = torch.zeros(tm.n_nodes, dtype=torch.float64, device="cuda")
+    right = torch.from_numpy(tm.face_nodes(0, 1)).cuda()
+    fixed[torch.from_numpy(tm.face_nodes(0, 0)).cuda()] = 1
+    fixed[right] = 1
+    x[right] = 1.0
+    info = A.solve_reduced(fixed, x, rtol=1e-13, system=A.solver_system(fixed, col_listed=None))
+    assert info.relative_residual <= 1e-13
+    assert (x - torch.from_numpy(tm.coords[0]).cuda()).abs().max().item() <= 1e-10
