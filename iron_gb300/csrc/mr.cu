@@ -458,16 +458,62 @@ __device__ __forceinline__ void tinv3(const T A[3][3], T B[3][3]) {
   B[2][2] = (A[0][0] * A[1][1] - A[1][0] * A[0][1]) / det;
 }
 
-// P = w Jz Z^-1 sigma(Z, p) of the residual; also returns Jz.
+// The same forward-mode arithmetic in FP32 for the FP32 paths of the consistent tangent.
+struct DualF {
+  float v, d;
+};
+__device__ __forceinline__ DualF operator+(DualF a, DualF b) { return {a.v + b.v, a.d + b.d}; }
+__device__ __forceinline__ DualF operator-(DualF a, DualF b) { return {a.v - b.v, a.d - b.d}; }
+__device__ __forceinline__ DualF operator-(DualF a) { return {-a.v, -a.d}; }
+__device__ __forceinline__ DualF operator*(DualF a, DualF b) { return {a.v * b.v, a.v * b.d + a.d * b.v}; }
+__device__ __forceinline__ DualF operator*(float a, DualF b) { return {a * b.v, a * b.d}; }
+__device__ __forceinline__ DualF operator*(DualF a, float b) { return {a.v * b, a.d * b}; }
+__device__ __forceinline__ DualF operator/(DualF a, DualF b) {
+  const float r = 1.0f / b.v;
+  return {a.v * r, (a.d - a.v * r * b.d) * r};
+}
+__device__ __forceinline__ DualF operator/(DualF a, float b) { return {a.v / b, a.d / b}; }
+__device__ __forceinline__ DualF operator+(DualF a, float b) { return {a.v + b, a.d}; }
+__device__ __forceinline__ DualF dpowm13(DualF a) {
+  const float v = 1.0f / cbrtf(a.v);
+  return {v, -v / (3.0f * a.v) * a.d};
+}
+
+template <typename S>
+struct DualOf {
+  using type = Dual;
+};
+template <>
+struct DualOf<float> {
+  using type = DualF;
+};
+
+// J_z = sqrt|det(Z^T Z)| as Iron forms it (COORDINATE_METRICS_CALCULATE); the FP32 dual path takes
+// |det Z| (the same value for a square Z) in FP64 dual arithmetic on the exactly widened entries.
 template <typename T>
-__device__ __forceinline__ void point_P(const T Z[3][3], const double A[3][3], double Jx, double w, T p, double c1,
-                                        double c2, T P[3][3], T& Jz) {
+__device__ __forceinline__ T point_jz(const T (&)[3][3], const T (&G)[3][3]) {
+  return dsqrt(dabs(tdet3(G)));
+}
+__device__ __forceinline__ DualF point_jz(const DualF (&Z)[3][3], const DualF (&)[3][3]) {
+  Dual D[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) D[i][j] = {f32_to_f64_exact(Z[i][j].v), f32_to_f64_exact(Z[i][j].d)};
+  const Dual j = dabs(tdet3(D));
+  return {(float)j.v, (float)j.d};
+}
+
+// P = w Jz Z^-1 sigma(Z, p) of the residual; also returns Jz.  R: type of the constants.
+template <typename T, typename R = double>
+__device__ __forceinline__ void point_P(const T (&Z)[3][3], const R A[3][3], R Jx, R w, T p, R c1, R c2, T P[3][3],
+                                        T& Jz) {
   T G[3][3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) G[i][j] = Z[0][i] * Z[0][j] + Z[1][i] * Z[1][j] + Z[2][i] * Z[2][j];
-  Jz = dsqrt(dabs(tdet3(G)));
+  Jz = point_jz(Z, G);
   T Zi[3][3];
   tinv3(Z, Zi);
   const T J = Jz / Jx;
@@ -483,8 +529,8 @@ __device__ __forceinline__ void point_P(const T Z[3][3], const double A[3][3], d
 #pragma unroll
     for (int j = 0; j < 3; ++j) C[i][j] = Fb[0][i] * Fb[0][j] + Fb[1][i] * Fb[1][j] + Fb[2][i] * Fb[2][j];
   const T I1 = C[0][0] + C[1][1] + C[2][2];
-  const double t1 = -2.0 * c2;
-  const T t2 = 2.0 * (I1 * c2 + c1);
+  const R t1 = R(-2.0) * c2;
+  const T t2 = R(2.0) * (I1 * c2 + c1);
   T Sv[6] = {t1 * C[0][0] + t2, t1 * C[1][1] + t2, t1 * C[2][2] + t2, t1 * C[1][0], t1 * C[2][0], t1 * C[2][1]};
   // sigma_bar = Fb S Fb^T / J (full tensor form of the Voigt push-forward)
   T Sm[3][3] = {{Sv[0], Sv[3], Sv[4]}, {Sv[3], Sv[1], Sv[5]}, {Sv[4], Sv[5], Sv[2]}};
@@ -497,7 +543,7 @@ __device__ __forceinline__ void point_P(const T Z[3][3], const double A[3][3], d
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j < 3; ++j) sg[i][j] = (FS[i][0] * Fb[j][0] + FS[i][1] * Fb[j][1] + FS[i][2] * Fb[j][2]) / J;
-  const T tr3 = (sg[0][0] + sg[1][1] + sg[2][2]) / 3.0;
+  const T tr3 = (sg[0][0] + sg[1][1] + sg[2][2]) / R(3.0);
 #pragma unroll
   for (int i = 0; i < 3; ++i) sg[i][i] = sg[i][i] - tr3 + p;
   const T wj = Jz * w;
@@ -508,20 +554,23 @@ __device__ __forceinline__ void point_P(const T Z[3][3], const double A[3][3], d
 }
 
 // Gauss-point inputs of the tangent: Z (3x3), the material-frame matrix A, J_x, w, p
-struct GPIn {
-  double Z[3][3], A[3][3], Jx, w, p;
+template <typename S>
+struct GPInT {
+  S Z[3][3], A[3][3], Jx, w, p;
 };
+using GPIn = GPInT<double>;
 
-__device__ __forceinline__ void gauss_inputs(const Tables& T, int g, const double* sz, const double* sx,
-                                             const double* sp, GPIn& o) {
-  double X[3][3];
+template <typename S>
+__device__ __forceinline__ void gauss_inputs(const TablesT<S>& T, int g, const S* sz, const S* sx, const S* sp,
+                                             GPInT<S>& o) {
+  S X[3][3];
 #pragma unroll
   for (int c = 0; c < 3; ++c)
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      double a = 0.0, b = 0.0;
+      S a = S(0), b = S(0);
       for (int ns = 0; ns < NQ; ++ns) {
-        const double d = T.dphi[g][k][ns];
+        const S d = T.dphi[g][k][ns];
         a += d * sz[c * NQ + ns];
         b += d * sx[c * NQ + ns];
       }
@@ -529,10 +578,10 @@ __device__ __forceinline__ void gauss_inputs(const Tables& T, int g, const doubl
       X[c][k] = b;
     }
   o.Jx = vol_jacobian(X);
-  double N[3][3], NX[3][3];
+  S N[3][3], NX[3][3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const double n = sqrt(X[0][k] * X[0][k] + X[1][k] * X[1][k] + X[2][k] * X[2][k]);
+    const S n = sqrt(X[0][k] * X[0][k] + X[1][k] * X[1][k] + X[2][k] * X[2][k]);
 #pragma unroll
     for (int c = 0; c < 3; ++c) N[c][k] = X[c][k] / n;
   }
@@ -541,22 +590,24 @@ __device__ __forceinline__ void gauss_inputs(const Tables& T, int g, const doubl
 #pragma unroll
     for (int j = 0; j < 3; ++j) NX[i][j] = N[0][i] * X[0][j] + N[1][i] * X[1][j] + N[2][i] * X[2][j];
   inv3(NX, o.A);
-  double p = 0.0;
+  S p = S(0);
   for (int m = 0; m < NL; ++m) p += T.psi[g][m] * sp[m];
   o.p = p;
   o.w = T.w[g];
 }
 
 // dP/d(seed) for seed 0..8 = Z[seed/3][seed%3], seed 9 = p.  out[9] = dP[xi][mh] row-major.
-__device__ __forceinline__ void point_dP(const GPIn& in, int seed, double c1, double c2, double out[9], double* Jz_v) {
-  Dual Z[3][3];
+template <typename S>
+__device__ __forceinline__ void point_dP(const GPInT<S>& in, int seed, S c1, S c2, S out[9], S* Jz_v) {
+  using D = typename DualOf<S>::type;
+  D Z[3][3];
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) Z[i][j] = {in.Z[i][j], (i * 3 + j == seed) ? 1.0 : 0.0};
-  const Dual p = {in.p, seed == 9 ? 1.0 : 0.0};
-  Dual P[3][3], Jz;
-  point_P<Dual>(Z, in.A, in.Jx, in.w, p, c1, c2, P, Jz);
+    for (int j = 0; j < 3; ++j) Z[i][j] = {in.Z[i][j], (i * 3 + j == seed) ? S(1) : S(0)};
+  const D p = {in.p, seed == 9 ? S(1) : S(0)};
+  D P[3][3], Jz;
+  point_P<D, S>(Z, in.A, in.Jx, in.w, p, c1, c2, P, Jz);
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -580,7 +631,7 @@ __device__ void tangent_points(const Tables& T, TanShared& S, double c1, double 
   for (int task = threadIdx.x; task < NG * 10; task += blockDim.x) {
     const int g = task / 10, seed = task % 10;
     double o[9];
-    point_dP(S.in[g], seed, c1, c2, o, nullptr);
+    point_dP<double>(S.in[g], seed, c1, c2, o, nullptr);
 #pragma unroll
     for (int k = 0; k < 9; ++k) S.dPdZ[g][seed][k] = o[k];
   }
@@ -841,16 +892,16 @@ struct GPShared {
 
 // One thread per (element, Gauss point).  out[item][g][kGPOut] in the contraction type TO:
 // D[(mh*3+nh)*9 + xi*3+zeta], Hv[81 + xi*3+mh], Pv[90 + xi*3+nh].  KS is the kinematics type:
-// double, or float for Iron's analytic tangent on the FP32 paths (element data rounded once per
-// node when staged, the volume Jacobians det(Z), det(X) still evaluated in FP64 from the exactly
-// widened gradients).  The consistent tangent (EXACT) always runs its dual numbers in FP64.
+// double, or float on the FP32 paths (element data rounded once per node when staged, the volume
+// Jacobians det(Z), det(X) still evaluated in FP64 from the exactly widened gradients; for the
+// consistent tangent (EXACT) the forward-mode passes run in FP32 dual numbers, with J_z and its
+// derivative in FP64 dual arithmetic).
 template <typename TO, bool EXACT, typename KS = double>
 __global__ void __launch_bounds__(kGPThreads)
 mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
              const int32_t* __restrict__ elin, int32_t nq2, const double* __restrict__ xg,
              const double* __restrict__ dep, const double* __restrict__ cpar, const TablesT<KS>* __restrict__ Tg,
              TO* __restrict__ out, unsigned* err) {
-  static_assert(!EXACT || std::is_same<KS, double>::value, "the consistent tangent runs in FP64");
   extern __shared__ double smem_d[];
   KS* smem = reinterpret_cast<KS*>(smem_d);
   constexpr int kTabWords = (int)(sizeof(TablesT<KS>) / sizeof(KS));
@@ -920,11 +971,11 @@ mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __
         o[90 + xi * 3 + m] = (TO)(jgw * q.Zi[xi][m]);
       }
   } else {
-    const double c1 = cpar[0], c2 = cpar[1];
-    GPIn in;
+    const KS c1 = (KS)cpar[0], c2 = (KS)cpar[1];
+    GPInT<KS> in;
     gauss_inputs(T, g, S.z[le], S.x[le], S.p[le], in);
     for (int seed = 0; seed < 10; ++seed) {
-      double d[9], Jz;
+      KS d[9], Jz;
       point_dP(in, seed, c1, c2, d, &Jz);
       if (seed < 9) {
         const int nh = seed / 3, z = seed % 3;
@@ -935,9 +986,9 @@ mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __
       } else {
 #pragma unroll
         for (int k = 0; k < 9; ++k) o[81 + k] = (TO)d[k];
-        double Zi[3][3];
-        const double dz = inv3(in.Z, Zi);
-        if (!(dz > 0.0) || !isfinite(dz)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+        KS Zi[3][3];
+        const KS dz = inv3(in.Z, Zi);
+        if (!(dz > KS(0)) || !isfinite(dz)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
 #pragma unroll
         for (int xi = 0; xi < 3; ++xi)
 #pragma unroll
@@ -1332,8 +1383,8 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
   const size_t gsm = sizeof(Tables) + sizeof(GPShared<double>);
   const size_t gsm_k = sizeof(TablesT<KF>) + sizeof(GPShared<KF>);
   const size_t csm = sizeof(ContractShared<TS>);
-  const void* gk = mode == 0 ? (const void*)mr_gp_kernel<TS, false, KF> : (const void*)mr_gp_kernel<TS, true>;
-  if ((rc = set_smem(gk, mode == 0 ? gsm_k : gsm))) return rc;
+  const void* gk = mode == 0 ? (const void*)mr_gp_kernel<TS, false, KF> : (const void*)mr_gp_kernel<TS, true, KF>;
+  if ((rc = set_smem(gk, gsm_k))) return rc;
   int max_cnt = 0;
   for (int c = 0; c < n_colors; ++c) max_cnt = std::max(max_cnt, color_ptr_host[c + 1] - color_ptr_host[c]);
   if (values) GFE_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)nnz, s));
@@ -1376,8 +1427,8 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
         else
           launch_contract_tc<false, false>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
       } else {
-        mr_gp_kernel<TS, true><<<ggrid, kGPThreads, gsm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar,
-                                                              T, gpbuf, err);
+        mr_gp_kernel<TS, true, KF><<<ggrid, kGPThreads, gsm_k, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg,
+                                                                    dep, cpar, TK, gpbuf, err);
         if (tc_mode == GFE_TC_TF32X3)
           launch_contract_tc<true, true>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
         else
@@ -1389,8 +1440,8 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
       mr_contract_kernel<TS, false><<<cgrid, kCThreads, csm, s>>>(color_elems + c0, cnt, T, gpbuf, sl, values,
                                                                   K_out, err);
     } else {
-      mr_gp_kernel<TS, true><<<ggrid, kGPThreads, gsm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar, T,
-                                                            gpbuf, err);
+      mr_gp_kernel<TS, true, KF><<<ggrid, kGPThreads, gsm_k, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep,
+                                                                  cpar, TK, gpbuf, err);
       mr_contract_kernel<TS, true><<<cgrid, kCThreads, csm, s>>>(color_elems + c0, cnt, T, gpbuf, sl, values, K_out,
                                                                  err);
     }
