@@ -138,6 +138,16 @@ int gfe_solver_rhs(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, co
  * (the update of the dependent field from the solver variables, coupling coefficient 1). */
 int gfe_solver_update_dependent(int32_t n, const int32_t* solver_of_dof, const double* x, double* u, void* stream);
 
+/* The same structure for the Jacobian of Iron's regular generated mesh of nx x ny x nz triquadratic
+ * displacement / trilinear pressure elements (DOFs: the three displacement components on the
+ * (2n+1)^3 node grid, then the pressure on the (n+1)^3 vertex grid, nodes xi1 fastest), in closed
+ * form: every row is the clipped boxes of displacement and pressure nodes of the elements around
+ * its node, in ascending order.  Bit-identical to gfe_csr_structure of that mesh's element DOFs
+ * (JacobianMatrix_StructureCalculate, src/equations_matrices_routines.F90:4609-4948), without the
+ * per-row sort.  Arguments as for gfe_csr_structure.  Synchronises `stream`. */
+int gfe_mr_regular_structure(int32_t nx, int32_t ny, int32_t nz, int32_t* row_ptr, int32_t* col_idx,
+                             int64_t col_capacity, int64_t* nnz_host, void* stream);
+
 /* ---- Laplace / diffusion assembly (K1 + K2) -------------------------------------------- */
 
 /* Assemble the global stiffness matrix of the Laplace equation on trilinear-Lagrange hexahedra

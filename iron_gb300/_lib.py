@@ -67,6 +67,7 @@ SIGNATURES = {
     "gfe_laplace_assemble_tp": (C.c_int, [vp, vp, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp, vp, C.c_int64, vp, vp,
                                           vp, i32, vp]),
     "gfe_laplace_regular_check": (C.c_int, [i32, i32, i32, vp, vp, C.POINTER(C.c_int64), vp]),
+    "gfe_mr_regular_structure": (C.c_int, [i32, i32, i32, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
     "gfe_csr_spmv": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),
     "gfe_solver_structure": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, C.c_int64, C.POINTER(C.c_int32),
                                        C.POINTER(C.c_int64), vp]),

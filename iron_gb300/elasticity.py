@@ -12,6 +12,7 @@ then the hydrostatic pressure over the linear nodes (separated component order).
 from __future__ import annotations
 
 import ctypes as C
+import functools
 
 import numpy as np
 import torch
@@ -23,6 +24,16 @@ from .mesh import RegularMesh, linear_component
 
 # tensor-core contraction of the Jacobian (tcgen05 kind::tf32): three-pass split / one pass
 GFE_TC_TF32X3, GFE_TC_TF32 = 3, 4
+
+
+@functools.lru_cache(maxsize=64)
+def _regular_q2_mesh(nelem: tuple, extent: tuple):
+    """Host arrays of Iron's regular Q2/Q1 mesh (kept across device-state evictions of a serving
+    engine: generating the 64^3 mesh on the host takes about 0.1 s)."""
+    m = RegularMesh(nelem, order=2, extent=extent)
+    elin, lin2g = linear_component(m.elem_nodes, 2)
+    order, ptr = m.colouring()
+    return m, elin, lin2g, order, ptr
 
 
 class MooneyRivlinAssembly:
@@ -48,21 +59,36 @@ class MooneyRivlinAssembly:
         dofs = np.concatenate([eq2, eq2 + nq, eq2 + 2 * nq, elin + 3 * nq], axis=1)
         self.elem_dofs = torch.from_numpy(np.ascontiguousarray(dofs, np.int32)).to(self.device)
         self.row_ptr = self.col_idx = self.slots = self.values = None
+        self.regular = None  # (nx, ny, nz) on Iron's regular generated mesh: closed-form structure
         if build_jacobian:
             self.build_structure()
 
     @classmethod
     def from_regular_mesh(cls, nelem, extent=(1.0, 1.0, 1.0), device=None, build_jacobian=True):
-        m = RegularMesh(nelem, order=2, extent=extent)
-        elin, lin2g = linear_component(m.elem_nodes, 2)
-        order, ptr = m.colouring()
-        obj = cls(m.elem_nodes, elin, m.coords, order, ptr, len(lin2g), device=device, build_jacobian=build_jacobian)
+        m, elin, lin2g, order, ptr = _regular_q2_mesh(tuple(int(v) for v in nelem), tuple(float(v) for v in extent))
+        obj = cls(m.elem_nodes, elin, m.coords, order, ptr, len(lin2g), device=device, build_jacobian=False)
         obj.mesh = m
         obj.lin_to_global = lin2g
+        obj.regular = tuple(int(v) for v in nelem)
+        if build_jacobian:
+            obj.build_structure()
         return obj
 
     def build_structure(self, stream=None):
-        self.row_ptr, self.col_idx = csr_structure(self.elem_dofs, self.ndof, stream)
+        """CSR structure (closed form on Iron's regular generated mesh, else sorted from the element
+        DOF lists) and the per-element slot map."""
+        if getattr(self, "regular", None) is not None:
+            nx, ny, nz = self.regular
+            rp = torch.empty(self.ndof + 1, dtype=torch.int32, device=self.device)
+            nnz = C.c_int64(0)
+            st = _lib.stream_handle(stream)
+            _lib.call("gfe_mr_regular_structure", nx, ny, nz, _lib.ptr(rp), None, 0, C.byref(nnz), st)
+            ci = torch.empty(max(int(nnz.value), 1), dtype=torch.int32, device=self.device)
+            _lib.call("gfe_mr_regular_structure", nx, ny, nz, _lib.ptr(rp), _lib.ptr(ci), int(ci.numel()),
+                      C.byref(nnz), st)
+            self.row_ptr, self.col_idx = rp, ci[: int(nnz.value)]
+        else:
+            self.row_ptr, self.col_idx = csr_structure(self.elem_dofs, self.ndof, stream)
         self.nnz = int(self.col_idx.numel())
         self.slots = torch.empty((self.n_elements, 89, 89), dtype=torch.int32, device=self.device)
         _lib.call("gfe_mr_slot_map", self.n_elements, _lib.ptr(self.eq2), _lib.ptr(self.elin), self.n_q2,

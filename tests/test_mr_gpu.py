@@ -124,3 +124,14 @@ def test_tensor_core_assembly_matches_fp64(gfe_cuda, precision, tol):
         ref = getattr(A, fn)(dep, [C1, C2], precision="fp64").clone()
         got = getattr(A, fn)(dep, [C1, C2], precision=precision)
         assert (got - ref).abs().max().item() <= tol * ref.abs().max().item(), fn
+
+
+@pytest.mark.parametrize("ne", [(1, 1, 1), (2, 3, 1), (3, 2, 4), (5, 1, 2)])
+def test_closed_form_structure_equals_sorted_structure(gfe_cuda, ne):
+    """gfe_mr_regular_structure (boxes of the regular Q2/Q1 mesh) is bit-identical to the structure
+    sorted and deduplicated from the element DOF lists (gfe_csr_structure)."""
+    from iron_gb300.laplace import csr_structure
+    A = MooneyRivlinAssembly.from_regular_mesh(ne)
+    assert A.regular == ne
+    rp, ci = csr_structure(A.elem_dofs, A.ndof)
+    assert torch.equal(A.row_ptr, rp) and torch.equal(A.col_idx, ci)
