@@ -89,6 +89,8 @@ SIGNATURES = {
     "gfe_cg_status": (C.c_int, [i32, vp, vp, vp]),
     "gfe_minres_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(C.c_int32),
                                    C.POINTER(C.c_double), vp]),
+    "gfe_minres_solve_nodal": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, f64, i32, i32,
+                                         C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_int32), vp]),
     "gfe_gmres_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, vp, f64, i32, i32, i32, C.POINTER(C.c_int32),
                                   C.POINTER(C.c_double), vp]),
     "gfe_saddle_preconditioner": (C.c_int, [i32, i32, vp, vp, vp, vp, vp, vp]),

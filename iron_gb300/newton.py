@@ -38,6 +38,7 @@ from ._lib import GfeError
 class LinearSolveInfo:
     iterations: int
     relative_residual: float
+    nodal: bool = False  # MINRES ran the node-grouped sparse product
 
 
 def saddle_preconditioner(row_ptr, col_idx, values, n_u: int, fixed=None, out=None, stream=None) -> torch.Tensor:
@@ -50,18 +51,29 @@ def saddle_preconditioner(row_ptr, col_idx, values, n_u: int, fixed=None, out=No
 
 
 def minres_solve(row_ptr, col_idx, values, f, fixed, x, minv=None, values32=None, rtol: float = 1e-5,
-                 max_iters: int = 20000, precision: str = "fp64", stream=None) -> LinearSolveInfo:
+                 max_iters: int = 20000, precision: str = "fp64", stream=None, n_node: int = 0,
+                 n_comp: int = 3) -> LinearSolveInfo:
     """Solve K x = f (K symmetric, possibly indefinite) with x fixed where fixed != 0 by
-    preconditioned MINRES (gfe_minres_solve).  x: Dirichlet values on entry, solution on exit."""
+    preconditioned MINRES (gfe_minres_solve).  x: Dirichlet values on entry, solution on exit.
+    n_node > 0: the first n_comp * n_node rows are a vector field's components in separated
+    component order (the u rows of the u-p system, n_node = n_q2); the sparse products then group
+    each node's rows (gfe_minres_solve_nodal) where they share a column list."""
     n = row_ptr.numel() - 1
     prec = _lib.GFE_FP64 if precision == "fp64" else _lib.GFE_MIXED
     if prec == _lib.GFE_MIXED and values32 is None:
         raise GfeError(-1, "mixed-precision MINRES needs the FP32 copy of the matrix")
     it = C.c_int32(0)
     rel = C.c_double(0.0)
-    _lib.call("gfe_minres_solve", n, _lib.ptr(row_ptr), _lib.ptr(col_idx), _lib.ptr(values),
-              _lib.ptr(values32 if prec == _lib.GFE_MIXED else None), _lib.ptr(minv), _lib.ptr(f), _lib.ptr(fixed),
-              _lib.ptr(x), float(rtol), int(max_iters), prec, C.byref(it), C.byref(rel), _lib.stream_handle(stream))
+    v32 = _lib.ptr(values32 if prec == _lib.GFE_MIXED else None)
+    if n_node > 0:
+        used = C.c_int32(0)
+        _lib.call("gfe_minres_solve_nodal", n, int(n_node), int(n_comp), _lib.ptr(row_ptr), _lib.ptr(col_idx),
+                  _lib.ptr(values), v32, _lib.ptr(minv), _lib.ptr(f), _lib.ptr(fixed), _lib.ptr(x), float(rtol),
+                  int(max_iters), prec, C.byref(it), C.byref(rel), C.byref(used), _lib.stream_handle(stream))
+        return LinearSolveInfo(int(it.value), float(rel.value), bool(used.value))
+    _lib.call("gfe_minres_solve", n, _lib.ptr(row_ptr), _lib.ptr(col_idx), _lib.ptr(values), v32, _lib.ptr(minv),
+              _lib.ptr(f), _lib.ptr(fixed), _lib.ptr(x), float(rtol), int(max_iters), prec, C.byref(it),
+              C.byref(rel), _lib.stream_handle(stream))
     return LinearSolveInfo(int(it.value), float(rel.value))
 
 
@@ -182,7 +194,7 @@ class NewtonSolver:
         if self.linear_solver == "minres":
             li = minres_solve(asm.row_ptr, asm.col_idx, vals, self._Rt, fixed_u8, self._du, minv=self._minv,
                               values32=v32, rtol=self.lin_rtol, max_iters=self.lin_max, precision=self.precision,
-                              stream=self.stream)
+                              stream=self.stream, n_node=asm.n_q2)
         else:
             li = gmres_solve(asm.row_ptr, asm.col_idx, vals, self._Rt, fixed_u8, self._du, minv=self._minv,
                              values32=v32, rtol=self.lin_rtol, max_iters=self.lin_max, restart=self.restart,

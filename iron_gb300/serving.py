@@ -315,7 +315,7 @@ def _mr_newton_step(a, dep, c, fixed_u8, fixed_b, R, du, minv, values32, precisi
     du.zero_()
     R.neg_()
     li = minres_solve(a.row_ptr, a.col_idx, vals, R, fixed_u8, du, minv=minv, values32=v32, rtol=MR_LINEAR_RTOL,
-                      max_iters=100000, precision=precision, stream=stream)
+                      max_iters=100000, precision=precision, stream=stream, n_node=a.n_q2)
     dep.add_(du)
     a.residual(dep, c, out=R, stream=stream)
     R.masked_fill_(fixed_b, 0.0)

@@ -37,8 +37,9 @@ def _stretched(A, lam, seed):
     return torch.from_numpy(dep).cuda()
 
 
+@pytest.mark.parametrize("nodal", [False, True])
 @pytest.mark.parametrize("precision,rtol", [("fp64", 1e-11), ("mixed", 1e-9)])
-def test_minres_matches_dense_solve(gfe_cuda, precision, rtol):
+def test_minres_matches_dense_solve(gfe_cuda, precision, rtol, nodal):
     A = MooneyRivlinAssembly.from_regular_mesh((2, 2, 1))
     dep = _stretched(A, 1.05, 0)
     fixed, _ = uniaxial_roller_conditions(A, 1.05)
@@ -49,8 +50,9 @@ def test_minres_matches_dense_solve(gfe_cuda, precision, rtol):
     x = torch.zeros(A.ndof, dtype=torch.float64, device="cuda")
     v32 = vals.float() if precision == "mixed" else None
     info = minres_solve(A.row_ptr, A.col_idx, vals, f, fixed, x, minv=minv, values32=v32, rtol=rtol,
-                        precision=precision)
+                        precision=precision, n_node=A.n_q2 if nodal else 0)
     assert info.relative_residual <= rtol
+    assert info.nodal == (nodal and precision == "mixed")  # FP64 keeps the per-row product
     # dense reference on the free DOFs
     rp, ci, v = A.row_ptr.cpu().numpy(), A.col_idx.cpu().numpy(), vals.cpu().numpy()
     K = _dense(rp, ci, v, A.ndof)
@@ -80,6 +82,49 @@ def test_minres_on_spd_system_matches_cg(gfe_cuda):
     info = minres_solve(L.row_ptr, L.col_idx, L.values, None, fixed_t, x2, rtol=1e-13)
     assert info.relative_residual <= 1e-13
     assert (x1 - x2).abs().max().item() <= 1e-10
+
+
+def test_minres_nodal_product_matches_per_row_product(gfe_cuda):
+    """The node-grouped product (u rows of a node share one column list) sums each row in the same
+    order as the per-row product; only the inner products add rows in another order, so the two
+    solves agree to rounding and take (nearly) the same iterations."""
+    A = MooneyRivlinAssembly.from_regular_mesh((4, 3, 3))
+    dep = _stretched(A, 1.08, 5)
+    fixed, _ = uniaxial_roller_conditions(A, 1.08)
+    vals = A.tangent(dep, [C1, C2]).clone()
+    f = torch.from_numpy(np.random.default_rng(6).normal(0, 1, A.ndof)).cuda()
+    minv = saddle_preconditioner(A.row_ptr, A.col_idx, vals, 3 * A.n_q2, fixed)
+    v32 = vals.float()
+    rtol = 1e-8
+    out = []
+    for n_node in (0, A.n_q2):
+        x = torch.zeros(A.ndof, dtype=torch.float64, device="cuda")
+        info = minres_solve(A.row_ptr, A.col_idx, vals, f, fixed, x, minv=minv, values32=v32, rtol=rtol,
+                            precision="mixed", n_node=n_node)
+        assert info.relative_residual <= rtol and info.nodal == (n_node > 0)
+        out.append((x, info.iterations))
+    (x0, i0), (x1, i1) = out
+    assert abs(i0 - i1) <= max(2, i0 // 20)
+    assert (x0 - x1).abs().max().item() <= 1e3 * rtol * x0.abs().max().item()
+
+
+def test_minres_nodal_falls_back_when_rows_differ(gfe_cuda):
+    """A Laplace matrix read as two components of n/2 nodes: rows i and i + n/2 belong to different
+    nodes and hold different column lists, so the solver keeps the per-row product."""
+    m = RegularMesh((5, 4, 3))
+    L = LaplaceAssembly.from_regular_mesh(m)
+    L.assemble("fp64")
+    fixed = np.zeros(m.n_nodes, np.uint8)
+    fixed[m.face_nodes(0, 0)] = 1
+    fixed[m.face_nodes(0, 1)] = 1
+    x0 = np.where(fixed == 1, m.coords[0], 0.0)
+    fixed_t = torch.from_numpy(fixed).cuda()
+    x = torch.from_numpy(x0).cuda()
+    v32 = L.values.float()
+    info = minres_solve(L.row_ptr, L.col_idx, L.values, None, fixed_t, x, values32=v32, rtol=1e-12,
+                        precision="mixed", n_node=m.n_nodes // 2, n_comp=2)
+    assert not info.nodal and info.relative_residual <= 1e-12
+    assert (x - torch.from_numpy(m.coords[0]).cuda()).abs().max().item() <= 1e-9
 
 
 def test_saddle_preconditioner_matches_definition(gfe_cuda):
