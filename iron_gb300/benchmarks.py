@@ -159,6 +159,16 @@ def bench_mr_newton(args, log, clock_sampler):
     A = MooneyRivlinAssembly.from_regular_mesh((n, n, n), device=dev)
     fixed, full = uniaxial_roller_conditions(A, lam)
     exact = uniaxial_exact_state(A, lam, 2.0, 6.0)
+    # untimed warm-up of both arms' code paths on a 4^3 mesh: the first use of a library kernel in a
+    # process can take seconds (its code is paged in), which would otherwise land in the first arm
+    log("warm-up (4^3, both precisions)")
+    Aw = MooneyRivlinAssembly.from_regular_mesh((4, 4, 4), device=dev)
+    fw, fullw = uniaxial_roller_conditions(Aw, lam)
+    for prec in ("fp64", "mixed"):
+        NewtonSolver(Aw, [2.0, 6.0], precision=prec, linear_relative_tolerance=1e-6).solve(
+            Aw.initial_state(0.0), fw, fullw, load_increments=1)
+    torch.cuda.synchronize()
+    del Aw
     res, states = {}, {}
     with clock_sampler(dev.index) as clk:
         for prec in ("fp64", "mixed"):

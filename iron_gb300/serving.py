@@ -46,6 +46,21 @@ LAPLACE_RTOL = 1e-10
 MR_LINEAR_RTOL = 1e-3
 MR_STRETCH = (1.0, 1.1)
 CG_CHUNK = 25
+# share of the device torch's caching allocator may hold while an engine runs (the rest stays
+# free for the library's stream-ordered scratch)
+TORCH_MEMORY_FRACTION = 0.85
+# times a request that ran out of device memory is retried (after the engine has drained and
+# released the allocator's cache)
+OOM_RETRIES = 2
+
+
+# engines alive in the process: the allocator cap is lifted when the last one closes
+_ENGINES = {"live": 0}
+_ENGINES_LOCK = threading.Lock()
+
+
+def _is_out_of_memory(e: BaseException) -> bool:
+    return isinstance(e, torch.cuda.OutOfMemoryError) or (isinstance(e, GfeError) and e.status == -7)
 
 
 # torch registers every captured graph with the process-wide CUDA generator state, which is not
@@ -425,6 +440,13 @@ class ServingEngine:
         _lib.load()
         free, _total = torch.cuda.mem_get_info(self.dev)
         self.ledger = HbmLedger(hbm_budget if hbm_budget is not None else 0.6 * free)
+        # torch's caching allocator keeps the blocks of evicted state and finished requests reserved;
+        # capped below the device size it releases them before growing further, so the library's
+        # stream-ordered scratch (MINRES / CG vectors, outside the ledger) always finds room
+        with _ENGINES_LOCK:
+            _ENGINES["live"] += 1
+            self._closed = False
+            torch.cuda.set_per_process_memory_fraction(TORCH_MEMORY_FRACTION, self.dev)
         self.workers = workers
         self.use_graphs = use_graphs
         self.mr_precision = mr_precision
@@ -435,7 +457,7 @@ class ServingEngine:
         self.slots: dict = {}  # (worker, "laplace", n) -> slot
         self.lock = threading.Lock()
         self.cv = threading.Condition(self.lock)
-        self.stats = {"evictions": 0, "graphs_captured": 0, "max_concurrent": 0}
+        self.stats = {"evictions": 0, "graphs_captured": 0, "max_concurrent": 0, "oom_retries": 0}
         self._graveyard: list = []
 
     @property
@@ -455,7 +477,7 @@ class ServingEngine:
             slot = self.slots.pop(sk, None)
             if slot is not None:
                 self._graveyard.append(slot)
-        self.stats["evictions"] = self.ledger.evictions
+        self.stats["evictions"] += len(evicted)
 
     def _prepare(self, req: Request, worker: int):
         """Resident mesh and, for Laplace, the worker's slot (built on first use, one build at a
@@ -491,12 +513,20 @@ class ServingEngine:
         """Serve `requests` (arrival times in seconds from the start).  With realtime, a request
         is not admitted before its arrival time.  Returns summary statistics; per-request results
         and times are stored on the requests.  Raises GfeError after the running requests have
-        finished if a request failed or cannot fit the budget at all."""
+        finished if a request failed or cannot fit the budget at all.
+
+        A request that runs out of device memory (the ledger's estimates do not see the caching
+        allocator's fragmentation) goes back to the head of the queue: the engine admits nothing
+        until the running requests have finished, drops its resident state, returns the
+        allocator's cached blocks and admits again; a request that fails that way OOM_RETRIES
+        times is an error."""
         order = sorted(requests, key=lambda r: r.arrival)
         pending: deque = deque()
         free_workers = list(range(self.workers))
         running = 0
         errors = []
+        retries: dict = {}
+        compact = [False]
         t0 = time.perf_counter()
         clock = (lambda: time.perf_counter() - t0) if realtime else (lambda: math.inf)
         nxt = 0
@@ -516,14 +546,24 @@ class ServingEngine:
                     slot.run(req, stream, self.mr_precision)
                     del slot  # per-request working memory
             except Exception as e:  # reported after the loop
-                errors.append((req.rid, repr(e)))
+                oom = _is_out_of_memory(e) and retries.get(req.rid, 0) < OOM_RETRIES
+                if not oom:
+                    errors.append((req.rid, repr(e)))
+            else:
+                oom = False
             finally:
                 req.t_done = time.perf_counter() - t0
                 with self.cv:
                     running -= 1
-                    done_count += 1
                     self.ledger.finish(req.rid, req.kind, req.n)
                     free_workers.append(worker)
+                    if oom:
+                        retries[req.rid] = retries.get(req.rid, 0) + 1
+                        pending.appendleft(req)
+                        compact[0] = True
+                        self.stats["oom_retries"] += 1
+                    else:
+                        done_count += 1
                     self.cv.notify_all()
 
         threads = []
@@ -533,6 +573,19 @@ class ServingEngine:
                 while nxt < len(order) and order[nxt].arrival <= now:
                     pending.append(order[nxt])
                     nxt += 1
+                if compact[0]:
+                    if running > 0:
+                        self.cv.wait(timeout=0.5)
+                        continue
+                    # nothing in flight: drop the resident state too (its blocks pin the fragmented
+                    # segments) and return every cached block before admitting again.  The engine
+                    # lock is released meanwhile (the reset takes the capture lock first).
+                    self.cv.release()
+                    try:
+                        self._reset_resident()
+                    finally:
+                        self.cv.acquire()
+                    compact[0] = False
                 # admit in arrival order; a request that does not fit may be overtaken
                 i = 0
                 while i < len(pending) and free_workers:
@@ -572,7 +625,20 @@ class ServingEngine:
         return summarize(order)
 
     def close(self):
-        """Drop every resident mesh and slot (graphs are destroyed under the capture lock)."""
+        """Drop every resident mesh and slot, return the cached blocks to the device and lift the
+        engine's cap on torch's allocator once no other engine is alive."""
+        if getattr(self, "_closed", True):
+            return
+        self._reset_resident()
+        with _ENGINES_LOCK:
+            self._closed = True
+            _ENGINES["live"] -= 1
+            if _ENGINES["live"] == 0:
+                torch.cuda.set_per_process_memory_fraction(1.0, self.dev)
+
+    def _reset_resident(self):
+        """Drop every resident mesh and slot (graphs are destroyed under the capture lock) and
+        return the allocator's cached blocks to the device.  No request may be running."""
         with _GRAPH_LOCK:
             with self.lock:
                 dead = list(self.slots.values()) + self._graveyard
@@ -583,6 +649,9 @@ class ServingEngine:
             for slot in dead:
                 if hasattr(slot, "release"):
                     slot.release()
+            del dead
+        torch.cuda.synchronize(self.dev)
+        torch.cuda.empty_cache()
 
     def __del__(self):
         try:
@@ -672,17 +741,23 @@ def bench(args, log, clock_sampler):
         make_inputs(r)
     dev = torch.device("cuda", 0)
     eng = ServingEngine(dev, workers=getattr(args, "serve_workers", 8))
-    # warm-up: one small request of each kind (library load, kernel attributes)
-    warm = request_stream(n_requests=4, seed=99, n_lo=4, n_hi=5)
+    # warm-up of both arms: small requests of each kind (library load and page-in, kernel attributes)
+    warm = request_stream(n_requests=4, laplace_fraction=0.5, seed=99, n_lo=4, n_hi=5)
+    assert {r.kind for r in warm} == {"laplace", "mr"}
     for r in warm:
         make_inputs(r)
     eng.serve(warm, realtime=False)
+    for r in warm:
+        r.result = None
+    plain_fp64(warm, realtime=False)
     log("serve: engine")
     with clock_sampler(dev.index) as clk:
         s_eng = eng.serve(reqs, realtime=True)
     res_engine = {r.rid: r.result for r in reqs}
     info_engine = {r.rid: dict(r.info) for r in reqs}
     log(f"serve: engine p50 {s_eng['p50_ms']:.1f} ms p99 {s_eng['p99_ms']:.1f} ms; plain FP64 baseline")
+    engine_stats = dict(eng.stats)
+    eng.close()  # the plain path runs on an empty device, as a process of its own would
     for r in reqs:
         r.result = None
     with clock_sampler(dev.index) as clk2:
@@ -708,7 +783,7 @@ def bench(args, log, clock_sampler):
         "throughput_speedup_vs_plain": s_eng["requests_per_s"] / s_plain["requests_per_s"],
         "laplace_max_abs_diff_vs_plain": lap_err,
         "mr_residual_after_ratio_vs_plain": [float(np.min(mr_ratio)), float(np.max(mr_ratio))] if mr_ratio else None,
-        "engine_stats": eng.stats, "clocks": clk.summary(), "clocks_plain": clk2.summary(),
+        "engine_stats": engine_stats, "clocks": clk.summary(), "clocks_plain": clk2.summary(),
     }
     print(json.dumps(line), flush=True)
     return 0

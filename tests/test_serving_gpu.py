@@ -1,7 +1,8 @@
 """The serving loop on the GPU: every request's result is the same alone and in the mix
 (bit-identical: the kernels are deterministic and requests share no mutable state), matches the
 plain FP64 path (Laplace solutions within 1e-8 of the unit boundary data; both solves stop at a
-relative residual of 1e-10), and a budget that holds one request at a time still serves the stream.
+relative residual of 1e-10), a budget that holds one request at a time still serves the stream,
+and a request that runs out of device memory is retried after the engine drains.
 """
 import numpy as np
 import pytest
@@ -78,3 +79,58 @@ def test_larger_meshes_many_workers(gfe_cuda):
     for r in reqs:
         assert np.array_equal(r.result, mixed[r.rid]), (r.rid, r.kind, r.n)
     eng1.close()
+
+
+@pytest.mark.parametrize("error", ["torch", "library"])
+def test_out_of_memory_request_is_retried_after_drain(gfe_cuda, monkeypatch, error):
+    """A request whose first attempt runs out of device memory (raised here on the host by a fake
+    of the failing allocation, before any of its work is queued) goes back to the head of the
+    queue; the engine drains, releases the allocator's cache, and the retry gives the request's
+    usual result."""
+    import torch
+
+    from iron_gb300 import serving as S
+    from iron_gb300._lib import GfeError
+
+    reqs = _stream(8, 21)
+    eng = ServingEngine(gfe_cuda, workers=3)
+    eng.serve(reqs, realtime=False)
+    ref = {r.rid: r.result.copy() for r in reqs}
+    victims = {reqs[2].rid, reqs[5].rid}
+    failed = set()
+    real_prepare = S.ServingEngine._prepare
+
+    def flaky_prepare(self, req, worker):
+        if req.rid in victims and req.rid not in failed:
+            failed.add(req.rid)
+            if error == "torch":
+                raise torch.cuda.OutOfMemoryError("fake out of memory")
+            raise GfeError(-7, "fake device scratch allocation failure")
+        return real_prepare(self, req, worker)
+
+    monkeypatch.setattr(S.ServingEngine, "_prepare", flaky_prepare)
+    for r in reqs:
+        r.result = None
+    eng.serve(reqs, realtime=False)
+    assert failed == victims and eng.stats["oom_retries"] == 2
+    for r in reqs:
+        assert np.array_equal(r.result, ref[r.rid]), (r.rid, r.kind, r.n)
+
+
+def test_repeated_out_of_memory_is_an_error(gfe_cuda, monkeypatch):
+    from iron_gb300 import serving as S
+    from iron_gb300._lib import GfeError
+
+    reqs = _stream(4, 22)
+    eng = ServingEngine(gfe_cuda, workers=2)
+    real_prepare = S.ServingEngine._prepare
+
+    def always_oom(self, req, worker):
+        if req.rid == reqs[1].rid:
+            raise GfeError(-7, "fake device scratch allocation failure")
+        return real_prepare(self, req, worker)
+
+    monkeypatch.setattr(S.ServingEngine, "_prepare", always_oom)
+    with pytest.raises(GfeError, match="1 request"):
+        eng.serve(reqs, realtime=False)
+    assert eng.stats["oom_retries"] == S.OOM_RETRIES
