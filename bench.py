@@ -41,8 +41,10 @@ def parse():
     ap.add_argument("--impl", default="gfe", choices=["gfe", "reference"])
     ap.add_argument("--n", type=int, default=128, help="elements per side")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed_df", "mixed"])
-    ap.add_argument("--workload", default="laplace", choices=["laplace", "mr", "mr_newton", "mr_adjoint", "serve"],
-                    help="laplace: the headline assembly workload; mr: Mooney-Rivlin Q2/Q1 residual + Jacobian "
+    ap.add_argument("--workload", default="laplace",
+                    choices=["laplace", "laplace_bases", "mr", "mr_newton", "mr_adjoint", "serve"],
+                    help="laplace: the headline assembly workload; laplace_bases: higher-order Lagrange, "
+                         "Hermite and simplex Laplace assembly; mr: Mooney-Rivlin Q2/Q1 residual + Jacobian "
                          "assembly (32^3); mr_newton: load-stepped Newton solve of the uniaxial stretch (32^3); "
                          "mr_adjoint: batched residual adjoint (16^3 x 64); serve: request stream")
     ap.add_argument("--path", default="auto", choices=["auto", "regular", "general"],
@@ -175,6 +177,23 @@ def cpu_baseline(n_sample: int, threads: int):
     dt = time.perf_counter() - t0
     oracle.use_build(prev)
     return m.n_elements / dt, dt, m.n_elements
+
+
+def cpu_baseline_bases(interp, ngauss, elem_params, params, scale, kappa):
+    """The oracle's basis-generic Laplace assembly timed on one sample mesh on all host cores."""
+    import oracle
+
+    threads = os.cpu_count() or 1
+    rp, ci = oracle.csr_structure(elem_params, params.shape[1])
+    prev = oracle.use_build("timing")
+    try:
+        t0 = time.perf_counter()
+        oracle.laplace_assemble_scaled(3, interp, ngauss, elem_params, params, scale, kappa, rp, ci, threads)
+        dt = time.perf_counter() - t0
+    finally:
+        oracle.use_build(prev)
+    E = elem_params.shape[0]
+    return E / dt, dt, E, threads
 
 
 def run_reference(args):
@@ -440,7 +459,9 @@ def main():
     if args.workload != "laplace":
         from iron_gb300 import benchmarks
 
-        return benchmarks.run(args, log=log, clock_sampler=ClockSampler)
+        args.hbm_peak = measured_peaks()
+        return benchmarks.run(args, log=log, clock_sampler=ClockSampler,
+                              cpu_bases=cpu_baseline_bases if args.workload == "laplace_bases" else None)
     if args.impl == "reference":
         return run_reference(args)
     return run_gfe(args)

@@ -5,6 +5,10 @@ mr:         Mooney-Rivlin mixed u-p (triquadratic u, trilinear p) residual, Iron
             uniaxial stretch state with a small seeded perturbation.
 mr_adjoint: residual and its hand-written adjoint for a batch of 64 parameter sets on a 16^3 mesh
             (c10, c01 log-uniform in [0.5, 10], displacement perturbation N(0, (0.01 h)^2), seeded).
+laplace_bases: the basis-generic Laplace assembly (triquadratic and tricubic Lagrange hexahedra,
+            tricubic Hermite with arc-length scale factors, linear and quadratic tetrahedra) on
+            jittered meshes with log-uniform conductivity, FP64 / float-float / FP32, against the
+            oracle on a sample of each mesh.
 serve:      the request stream of iron_gb300.serving.
 
 Each prints one JSON line.
@@ -146,6 +150,110 @@ def bench_mr_adjoint(args, log, clock_sampler):
     return 0
 
 
+# (name, mesh builder, bench size, CPU sample size, Gauss points per direction or simplex order)
+BASES = [
+    ("lagrange_q2_hex", "q2", 48, 16, 3),
+    ("lagrange_q3_hex", "q3", 24, 10, 4),
+    ("hermite_cubic_hex", "hermite", 32, 12, 4),
+    ("simplex_p1_tet", "tet1", 96, 48, 1),
+    ("simplex_p2_tet", "tet2", 40, 24, 3),
+]
+SIMPLEX_POINTS = {1: 1, 2: 4, 3: 5}
+
+
+def _bases_problem(kind: str, n: int, ng: int, seed: int = 0, device=None):
+    """Jittered mesh of side n and its LaplaceAssembly (conductivity log-uniform in [0.1, 10]);
+    returns (assembly or None when device is None, interp codes, elem_params, params, scale, kappa)."""
+    from . import mesh as M
+    from .laplace import LaplaceAssembly
+
+    rng = np.random.default_rng(seed + 1)
+    if kind in ("q2", "q3"):
+        o = 2 if kind == "q2" else 3
+        m = M.RegularMesh((n, n, n), order=o)
+        m.jitter_interior(seed)
+        kap = np.exp(rng.uniform(np.log(0.1), np.log(10.0), m.n_elements))
+        A = LaplaceAssembly.from_regular_mesh(m, kappa=kap, n_gauss=ng, device=device) if device else None
+        return A, [o] * 3, m.elem_nodes, m.coords, None, kap
+    if kind == "hermite":
+        m = M.HermiteMesh((n, n, n), extent=(1.0, 1.0, 1.0), scaling="arc_length")
+        m.jitter_interior(seed)
+        kap = np.exp(rng.uniform(np.log(0.1), np.log(10.0), m.n_elements))
+        A = LaplaceAssembly.from_hermite_mesh(m, kappa=kap, n_gauss=ng, device=device) if device else None
+        return A, [4] * 3, m.elem_params, m.params, m.scale, kap
+    o = 1 if kind == "tet1" else 2
+    m = M.TetMesh((n, n, n), order=o)
+    m.jitter_interior(seed)
+    kap = np.exp(rng.uniform(np.log(0.1), np.log(10.0), m.n_elements))
+    A = LaplaceAssembly.from_tet_mesh(m, kappa=kap, n_gauss=ng, device=device) if device else None
+    return A, [6 + o] * 3, m.elem_nodes, m.coords, None, kap
+
+
+def bench_laplace_bases(args, log, clock_sampler, cpu_fn=None):
+    """Per basis: assembly time in each precision (CUDA events, inputs resident, values larger
+    than L2 except where noted), error against the FP64 assembly, algorithmic flops and bytes,
+    the fraction of the FP64-pipe and HBM peaks, and the oracle's rate on a sample of the same
+    mesh kind (cpu_fn, supplied by bench.py)."""
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    fp64_peak = _lib.probe_fma_rate(_lib.GFE_FP64)
+    hbm_peak, hbm_source = getattr(args, "hbm_peak", (6800.0, "fallback"))
+    cases = {}
+    with clock_sampler(dev.index) as clk:
+        for name, kind, n, n_cpu, ng in BASES:
+            log(f"{name}: {n}^3 mesh")
+            A, interp, ep, params, scale, kap = _bases_problem(kind, n, ng, device=dev)
+            E, nns = ep.shape
+            ndof, nnz = params.shape[1], A.nnz
+            pts = SIMPLEX_POINTS[ng] if kind.startswith("tet") else ng ** 3
+            flop = E * pts * (18 * nns + 45 + 18 * nns + 6 * nns * nns)
+            in_bytes = E * (nns * 4 + 8) + ndof * (3 * 8 + 8) + (E * nns * 8 if scale is not None else 0)
+            res = {}
+            v64 = None
+            for prec in ("fp64", "mixed_df", "mixed"):
+                ms = _events_time(lambda: A.assemble(prec, check=False), args.steps, args.warmup, stream)
+                A.assemble(prec)
+                if prec == "fp64":
+                    v64 = A.values.clone()
+                    err = 0.0
+                else:
+                    err = float((A.values - v64).abs().max() / v64.abs().max())
+                byts = in_bytes + nnz * (8 if prec == "fp64" else 12)
+                res[prec] = {"ms": ms, "elements_per_s": E / (ms * 1e-3), "dofs_per_s": ndof / (ms * 1e-3),
+                             "rel_err_vs_fp64": err, "algorithmic_bytes": byts,
+                             "hbm_frac": byts / (ms * 1e-3) / 1e9 / hbm_peak,
+                             "fp64_equiv_gflops": flop / (ms * 1e-3) / 1e9,
+                             "fp64_pipe_frac": flop / (ms * 1e-3) / 1e9 / fp64_peak}
+            del v64
+            cpu = None
+            if cpu_fn is not None:
+                _, interp_s, ep_s, params_s, scale_s, kap_s = _bases_problem(kind, n_cpu, ng)
+                rate, dt, E_s, threads = cpu_fn(interp_s, [ng] * 3, ep_s, params_s, scale_s, kap_s)
+                cpu = {"value": rate, "unit": "elements/s", "cores": threads, "kind": "port",
+                       "sample": f"{n_cpu}^3 {kind} mesh = {E_s} elements, one assembly ({dt:.2f} s)"}
+            cases[name] = {"elements_per_side": n, "elements": E, "dofs": ndof, "nnz": nnz,
+                           "element_dofs": nns, "gauss_points": pts, "flop_per_element": flop // E,
+                           "values_MB": nnz * 8 / 1e6, "precisions": res, "cpu_baseline": cpu}
+            del A
+            torch.cuda.empty_cache()
+    _lib.raise_device_errors("bench laplace bases")
+    head = cases["lagrange_q2_hex"]["precisions"]["mixed_df"]
+    line = {
+        "metric": "assembled_elements_per_s", "value": head["elements_per_s"], "unit": "elements/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "dtype": "f64 (float-float element arithmetic)", "data": "synthetic",
+        "config": {"workload": "laplace_bases", "headline_case": "lagrange_q2_hex, mixed_df",
+                   "conductivity": "log-uniform [0.1,10] seeded", "jitter": "interior nodes, seeded",
+                   "l2": "CSR values larger than L2 except simplex_p1_tet (110 MB)"},
+        "fp64_pipe_gflops": fp64_peak, "hbm_gbs": hbm_peak, "hbm_peak_source": hbm_source,
+        "flop_formula": "E*points*(18*nen + 45 + 18*nen + 6*nen^2)",
+        "byte_formula": "E*(nen*4 + 8) + N*(3*8 + 8) [+ E*nen*8 scale factors] + nnz*8 [+ nnz*4 FP32 copy]",
+        "cases": cases, "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def bench_mr_newton(args, log, clock_sampler):
     """Uniaxial stretch of the Mooney-Rivlin box to lambda = 1.1 in 5 load steps (Iron's increment
     rule), roller conditions, Newton with the consistent tangent and MINRES; FP64 plain against
@@ -211,8 +319,10 @@ def bench_mr_newton(args, log, clock_sampler):
     return 0
 
 
-def run(args, log, clock_sampler):
+def run(args, log, clock_sampler, cpu_bases=None):
     _lib.load()
+    if args.workload == "laplace_bases":
+        return bench_laplace_bases(args, log, clock_sampler, cpu_bases)
     if args.workload == "mr":
         return bench_mr(args, log, clock_sampler)
     if args.workload == "mr_newton":

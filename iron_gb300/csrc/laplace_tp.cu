@@ -271,7 +271,20 @@ __device__ __forceinline__ float tp_rsqrt<float>(float a) {
   return rsqrtf(a);
 }
 
-template <typename T>
+// Element group of GROUP threads: GROUP = kTPThreads gives one element a block (triquadratic,
+// tricubic and Hermite elements: up to 64 nodes, 2,080 entry pairs); GROUP = 32 gives one element
+// a warp, eight a block (elements of at most kSmallNns nodes and kSmallNg Gauss points: linear and
+// quadratic tetrahedra, trilinear hexahedra with other rules), whose few pairs would otherwise
+// leave most of a block idle at every barrier.
+constexpr int kSmallNns = 10, kSmallNg = 32;
+
+template <int GROUP>
+__device__ __forceinline__ void group_sync() {
+  if constexpr (GROUP == kTPThreads) __syncthreads();
+  else __syncwarp();
+}
+
+template <typename T, int GROUP, int MAXN, int MAXG>
 __global__ void __launch_bounds__(kTPThreads)
 laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, const int32_t* __restrict__ en,
                   const double* __restrict__ coords, const double* __restrict__ scale,
@@ -279,14 +292,22 @@ laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, 
                   const T* __restrict__ wg, const int32_t* __restrict__ pairs, TPConfig cfg,
                   const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, double* __restrict__ values,
                   unsigned* err) {
-  __shared__ T sx[3][kMaxNns];
-  __shared__ T sM[kMaxNg][6];
-  __shared__ int32_t snode[kMaxNns];
-  __shared__ double ssf[kMaxNns];
+  static_assert(GROUP == kTPThreads || GROUP == 32, "an element takes a block or a warp");
+  constexpr int EPB = kTPThreads / GROUP;
+  __shared__ T sx_all[EPB][3][MAXN];
+  __shared__ T sM_all[EPB][MAXG][6];
+  __shared__ int32_t snode_all[EPB][MAXN];
+  __shared__ double ssf_all[EPB][MAXN];
+  const int sub = threadIdx.x % GROUP, grp = threadIdx.x / GROUP;
+  T (*sx)[MAXN] = sx_all[grp];
+  T (*sM)[6] = sM_all[grp];
+  int32_t* snode = snode_all[grp];
+  double* ssf = ssf_all[grp];
   const int nns = cfg.nns, ng = cfg.ng;
-  for (int item = blockIdx.x; item < cnt; item += gridDim.x) {
+  // the item loop is uniform over a group (a block or a warp), so the group barriers below match
+  for (int item = blockIdx.x * EPB + grp; item < cnt; item += gridDim.x * EPB) {
     const int e = ce[item];
-    for (int n = threadIdx.x; n < nns; n += blockDim.x) {
+    for (int n = sub; n < nns; n += GROUP) {
       const int node = en[(size_t)e * nns + n];
       snode[n] = node;
       // scaled geometric parameters, as FIELD_INTERPOLATION_PARAMETERS_ELEMENT_GET forms them
@@ -296,8 +317,8 @@ laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, 
       for (int c = 0; c < 3; ++c) sx[c][n] = from_double<T>(coords[(size_t)c * n_nodes + node] * sf);
     }
     const T kap = from_double<T>(kappa ? kappa[e] : 1.0);
-    __syncthreads();
-    for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+    group_sync<GROUP>();
+    for (int g = sub; g < ng; g += GROUP) {
       T J[3][3];
 #pragma unroll
       for (int c = 0; c < 3; ++c)
@@ -322,9 +343,9 @@ laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, 
       sM[g][0] = A00 * sc; sM[g][1] = A11 * sc; sM[g][2] = A22 * sc;
       sM[g][3] = A01 * sc; sM[g][4] = A02 * sc; sM[g][5] = A12 * sc;
     }
-    __syncthreads();
+    group_sync<GROUP>();
     using Acc = typename std::conditional<std::is_same<T, double>::value, double, f2>::type;
-    for (int p = threadIdx.x; p < cfg.npairs; p += blockDim.x) {
+    for (int p = sub; p < cfg.npairs; p += GROUP) {
       const int32_t mn = pairs[p];
       const int m = mn & 0xffff, n = mn >> 16;
       Acc acc = from_double<Acc>(0.0);
@@ -353,7 +374,7 @@ laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, 
         else values[pnm] += v;
       }
     }
-    __syncthreads();
+    group_sync<GROUP>();
   }
 }
 
@@ -372,9 +393,18 @@ int launch_tp(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, cons
   for (int c = 0; c < n_colors; ++c) {
     const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
     if (cnt <= 0) continue;
-    const int grid = std::min(cnt, 8 * gfe::sm_count());
-    laplace_tp_kernel<T><<<grid, kTPThreads, 0, s>>>(color_elems + c0, cnt, n_nodes, en, coords, scale, kappa, t->dphi,
-                                                     t->w, t->pairs, t->cfg, rp, ci, values, err);
+    if (t->cfg.nns <= kSmallNns && t->cfg.ng <= kSmallNg) {
+      constexpr int EPB = kTPThreads / 32;
+      const int grid = std::min((cnt + EPB - 1) / EPB, 8 * gfe::sm_count());
+      laplace_tp_kernel<T, 32, kSmallNns, kSmallNg><<<grid, kTPThreads, 0, s>>>(
+          color_elems + c0, cnt, n_nodes, en, coords, scale, kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci, values,
+          err);
+    } else {
+      const int grid = std::min(cnt, 8 * gfe::sm_count());
+      laplace_tp_kernel<T, kTPThreads, kMaxNns, kMaxNg><<<grid, kTPThreads, 0, s>>>(
+          color_elems + c0, cnt, n_nodes, en, coords, scale, kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci, values,
+          err);
+    }
     ++*launches;
   }
   return GFE_OK;

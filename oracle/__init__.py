@@ -180,7 +180,7 @@ def laplace_assemble(nxi, order, ngauss, elem_nodes, coords, kappa, rp, ci, n_th
     return vals, rhs
 
 
-def laplace_assemble_scaled(nxi, interp, ngauss, elem_params, params, scale, kappa, rp, ci):
+def laplace_assemble_scaled(nxi, interp, ngauss, elem_params, params, scale, kappa, rp, ci, n_threads=1):
     """Laplace assembly on a mesh of any tensor-product basis (interp per direction: 1..3 Lagrange
     order, 4 cubic Hermite), with element parameters elem_params [E][nns] (0-based DOFs), the
     geometric parameters per DOF params [nxi][n_dofs] and optional scale factors [E][nns]."""
@@ -193,7 +193,8 @@ def laplace_assemble_scaled(nxi, interp, ngauss, elem_params, params, scale, kap
     kap = None if kappa is None else _f64(kappa)
     rc = lib().orc_laplace_assemble_scaled(nxi, _i32(interp), _i32(ngauss), E, N, elem_params, params,
                                            None if sc is None else sc.ctypes.data,
-                                           None if kap is None else kap.ctypes.data, _i32(rp), _i32(ci), vals, None, 1)
+                                           None if kap is None else kap.ctypes.data, _i32(rp), _i32(ci), vals, None,
+                                           int(n_threads))
     if rc != 0:
         raise RuntimeError(f"oracle assembly failed ({rc})")
     return vals
