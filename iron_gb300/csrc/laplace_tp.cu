@@ -378,6 +378,89 @@ laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, 
   }
 }
 
+// Linear tetrahedra, one element a thread.  GB300's FP64 pipe charges a warp instruction in full
+// however few lanes it has active, so the warp-per-element path, whose Gauss-point phase runs on
+// ng lanes and pair phase on 10, leaves the pipe mostly idle for a 4-node element; here every lane
+// computes a whole element.  Same arithmetic, in the same order, as laplace_tp_kernel.
+template <typename T>
+__global__ void __launch_bounds__(kTPThreads)
+laplace_tet4_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, const int32_t* __restrict__ en,
+                    const double* __restrict__ coords, const double* __restrict__ kappa,
+                    const T* __restrict__ dphi, const T* __restrict__ wg, int ng, const int32_t* __restrict__ rp,
+                    const int32_t* __restrict__ ci, double* __restrict__ values, unsigned* err) {
+  using Acc = typename std::conditional<std::is_same<T, double>::value, double, f2>::type;
+  for (int item = blockIdx.x * blockDim.x + threadIdx.x; item < cnt; item += gridDim.x * blockDim.x) {
+    const int e = ce[item];
+    int node[4];
+    T x[3][4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      node[n] = en[(size_t)e * 4 + n];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) x[c][n] = from_double<T>(coords[(size_t)c * n_nodes + node[n]]);
+    }
+    const T kap = from_double<T>(kappa ? kappa[e] : 1.0);
+    Acc K[10];
+#pragma unroll
+    for (int p = 0; p < 10; ++p) K[p] = from_double<Acc>(0.0);
+    for (int g = 0; g < ng; ++g) {
+      const T* dg = dphi + (size_t)g * 12;
+      T J[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          T s = from_double<T>(0.0);
+#pragma unroll
+          for (int n = 0; n < 4; ++n) s = s + x[c][n] * dg[a * 4 + n];
+          J[c][a] = s;
+        }
+      const T G00 = J[0][0] * J[0][0] + J[1][0] * J[1][0] + J[2][0] * J[2][0];
+      const T G11 = J[0][1] * J[0][1] + J[1][1] * J[1][1] + J[2][1] * J[2][1];
+      const T G22 = J[0][2] * J[0][2] + J[1][2] * J[1][2] + J[2][2] * J[2][2];
+      const T G01 = J[0][0] * J[0][1] + J[1][0] * J[1][1] + J[2][0] * J[2][1];
+      const T G02 = J[0][0] * J[0][2] + J[1][0] * J[1][2] + J[2][0] * J[2][2];
+      const T G12 = J[0][1] * J[0][2] + J[1][1] * J[1][2] + J[2][1] * J[2][2];
+      const T A00 = G11 * G22 - G12 * G12, A11 = G00 * G22 - G02 * G02, A22 = G00 * G11 - G01 * G01;
+      const T A01 = G02 * G12 - G01 * G22, A02 = G01 * G12 - G02 * G11, A12 = G01 * G02 - G00 * G12;
+      const T det = G00 * A00 + G01 * A01 + G02 * A02;
+      if (!(det > from_double<T>(0.0))) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+      const T sc = kap * wg[g] * tp_rsqrt(det);
+      const T M0 = A00 * sc, M1 = A11 * sc, M2 = A22 * sc, M3 = A01 * sc, M4 = A02 * sc, M5 = A12 * sc;
+      int p = 0;
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int n = m; n < 4; ++n, ++p) {
+          const T am0 = dg[m], am1 = dg[4 + m], am2 = dg[8 + m];
+          const T an0 = dg[n], an1 = dg[4 + n], an2 = dg[8 + n];
+          const T b0 = M0 * an0 + M3 * an1 + M4 * an2;
+          const T b1 = M3 * an0 + M1 * an1 + M5 * an2;
+          const T b2 = M4 * an0 + M5 * an1 + M2 * an2;
+          const T t = am0 * b0 + am1 * b1 + am2 * b2;
+          if constexpr (std::is_same<T, float>::value) accum(K[p], f2{t, 0.0f});
+          else accum(K[p], t);
+        }
+    }
+    int p = 0;
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+#pragma unroll
+      for (int n = m; n < 4; ++n, ++p) {
+        finish(K[p]);
+        const double v = to_double(K[p]);
+        const long long pmn = csr_find(rp, ci, node[m], node[n] + 1);
+        if (pmn < 0) gfe_raise(err, GFE_DEVERR_SLOT);
+        else values[pmn] += v;
+        if (m != n) {
+          const long long pnm = csr_find(rp, ci, node[n], node[m] + 1);
+          if (pnm < 0) gfe_raise(err, GFE_DEVERR_SLOT);
+          else values[pnm] += v;
+        }
+      }
+  }
+}
+
 __global__ void values_to_fp32(const double* __restrict__ v, float* __restrict__ v32, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     v32[i] = (float)v[i];
@@ -390,10 +473,16 @@ int launch_tp(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, cons
   const TPTables<T>* t = nullptr;
   if (int rc = tp_tables<T>(order, ngauss, &t)) return rc;
   unsigned* err = gfe::device_error_word();
+  // linear tetrahedra (no scale factors): one element a thread
+  const bool simplex_p1 = order[0] == 7 && t->cfg.nns == 4 && !scale;
   for (int c = 0; c < n_colors; ++c) {
     const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
     if (cnt <= 0) continue;
-    if (t->cfg.nns <= kSmallNns && t->cfg.ng <= kSmallNg) {
+    if (simplex_p1) {
+      const int grid = std::min((cnt + kTPThreads - 1) / kTPThreads, 16 * gfe::sm_count());
+      laplace_tet4_kernel<T><<<grid, kTPThreads, 0, s>>>(color_elems + c0, cnt, n_nodes, en, coords, kappa, t->dphi,
+                                                         t->w, t->cfg.ng, rp, ci, values, err);
+    } else if (t->cfg.nns <= kSmallNns && t->cfg.ng <= kSmallNg) {
       constexpr int EPB = kTPThreads / 32;
       const int grid = std::min((cnt + EPB - 1) / EPB, 8 * gfe::sm_count());
       laplace_tp_kernel<T, 32, kSmallNns, kSmallNg><<<grid, kTPThreads, 0, s>>>(
