@@ -298,7 +298,9 @@ laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, 
   __shared__ T sM_all[EPB][MAXG][6];
   __shared__ int32_t snode_all[EPB][MAXN];
   __shared__ double ssf_all[EPB][MAXN];
+  __shared__ T sJ_all[EPB][MAXG][9];
   const int sub = threadIdx.x % GROUP, grp = threadIdx.x / GROUP;
+  T (*sJ)[9] = sJ_all[grp];
   T (*sx)[MAXN] = sx_all[grp];
   T (*sM)[6] = sM_all[grp];
   int32_t* snode = snode_all[grp];
@@ -318,16 +320,22 @@ laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, 
     }
     const T kap = from_double<T>(kappa ? kappa[e] : 1.0);
     group_sync<GROUP>();
+    // the 9 ng Jacobian entries dx_c/dxi_a spread over the group's lanes, then one lane a Gauss
+    // point for the metric: a lane per Gauss point alone leaves most lanes idle through the
+    // longest part (ng of GROUP lanes active)
+    for (int q = sub; q < 9 * ng; q += GROUP) {
+      const int g = q / 9, c = (q % 9) / 3, a = q % 3;
+      T s = from_double<T>(0.0);
+      for (int n = 0; n < nns; ++n) s = s + sx[c][n] * dphi[((size_t)g * 3 + a) * nns + n];
+      sJ[g][q % 9] = s;
+    }
+    group_sync<GROUP>();
     for (int g = sub; g < ng; g += GROUP) {
       T J[3][3];
 #pragma unroll
       for (int c = 0; c < 3; ++c)
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-          T s = from_double<T>(0.0);
-          for (int n = 0; n < nns; ++n) s = s + sx[c][n] * dphi[((size_t)g * 3 + a) * nns + n];
-          J[c][a] = s;
-        }
+        for (int a = 0; a < 3; ++a) J[c][a] = sJ[g][c * 3 + a];
       const T G00 = J[0][0] * J[0][0] + J[1][0] * J[1][0] + J[2][0] * J[2][0];
       const T G11 = J[0][1] * J[0][1] + J[1][1] * J[1][1] + J[2][1] * J[2][1];
       const T G22 = J[0][2] * J[0][2] + J[1][2] * J[1][2] + J[2][2] * J[2][2];
