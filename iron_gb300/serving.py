@@ -432,7 +432,10 @@ class HbmLedger:
 class ServingEngine:
     """Persistent request loop over `workers` CUDA streams with an HBM budget (bytes; default 60 % of
     the free device memory, leaving room for allocator caching and the library's stream-ordered
-    scratch, which the estimates do not itemise)."""
+    scratch, which the estimates do not itemise).  While an engine is alive torch's caching
+    allocator is capped at TORCH_MEMORY_FRACTION of the device (lifted by close() of the last
+    engine), and a request that runs out of device memory is retried after the engine drains and
+    drops its resident state (see serve())."""
 
     def __init__(self, device=None, workers: int = 8, hbm_budget: int | None = None, use_graphs: bool = True,
                  mr_precision: str = "mixed"):
