@@ -228,15 +228,16 @@ int gfe_laplace_assemble_regular_host(int32_t nx, int32_t ny, int32_t nz, const 
                                       int32_t precision, void* workspace, int32_t slab_layers, void* stream);
 
 /* The Laplace assembly of gfe_laplace_assemble on hexahedra of any tensor-product basis of Lagrange
- * order 1..3 or cubic Hermite per direction, with 1..4 Gauss points per direction, and on linear or
- * quadratic tetrahedra (Iron's element routine is basis-generic: LaplaceEquation_FiniteElementCalculate,
+ * order 1..3 or cubic Hermite per direction, with 1..4 Gauss points per direction, and on linear,
+ * quadratic or cubic tetrahedra (Iron's element routine is basis-generic: LaplaceEquation_FiniteElementCalculate,
  * src/Laplace_equations_routines.F90:433-747, with the quadrature of BASIS_QUADRATURE_CREATE,
  * src/basis_routines.F90:3720-4090, and Gauss_Simplex, :6898-7600).
  *  order[3]   host array of Iron's interpolation specification per xi (INTERPOLATION_XI):
- *             1, 2, 3 = linear / quadratic / cubic Lagrange, 4 = cubic Hermite; 7 / 8 in all three
- *             = linear / quadratic simplex (tetrahedra of 4 / 10 nodes in Iron's node order)
+ *             1, 2, 3 = linear / quadratic / cubic Lagrange, 4 = cubic Hermite; 7 / 8 / 9 in all
+ *             three = linear / quadratic / cubic simplex (tetrahedra of 4 / 10 / 20 nodes in
+ *             Iron's node order)
  *  n_gauss[3] host array of Gauss points per xi; for tetrahedra n_gauss[0] is the Gauss_Simplex
- *             order 1..3 (1, 4 or 5 points)
+ *             order 1..5 (1, 4, 5, 11 or 14 points)
  *  elem_nodes [n_elem][nns] 0-based element parameter DOFs in Iron's order (local nodes xi1 fastest,
  *             then each node's derivatives: value, d/ds1, d/ds2, d2/ds1ds2, d/ds3, ... over the
  *             Hermite directions); n_nodes = number of DOFs; coords [3][n_nodes] geometric

@@ -91,19 +91,74 @@ void lagrange1d(int p, int k, double t, double* val, double* der) {
   *der = d;
 }
 
-// Tetrahedral simplex bases (Iron's interpolation 7 = linear, 8 = quadratic): basis functions are
-// products over the four area coordinates of factors chosen by the node's position index (1 = 1,
-// 2 = L resp. 2L, 3 = L(2L-1)), the xi derivatives are d/dL4 - d/dL_i, and the Gauss points are
-// Gauss_Simplex's tetrahedral rules of orders 1..3 (1, 4, 5 points; weights sum to 1/6)
-// (src/basis_routines.F90:4813-5875, 6041-6270, 6898-7600, 8177-8313).
+// Tetrahedral simplex bases (Iron's interpolation 7 = linear, 8 = quadratic, 9 = cubic): basis
+// functions are products over the four area coordinates of factors chosen by the node's position
+// index (linear: 1, L; quadratic: 1, 2L, L(2L-1); cubic: 1, 3L, 3/2 L(3L-1), 1/2 L(3L-1)(3L-2)),
+// the xi derivatives are d/dL4 - d/dL_i, and the Gauss points are Gauss_Simplex's tetrahedral
+// rules of orders 1..5 (1, 4, 5, 11, 14 points; weights sum to 1/6)
+// (src/basis_routines.F90:4813-5875, 6041-6270, 6898-7600, 8092-8313).
 double simplex_factor(int interp, int pos, bool deriv, double L) {
   if (interp == 7) return pos == 1 ? (deriv ? 0.0 : 1.0) : (deriv ? 1.0 : L);
+  if (interp == 9) {
+    if (pos == 1) return deriv ? 0.0 : 1.0;
+    if (pos == 2) return deriv ? 3.0 : 3.0 * L;
+    if (pos == 3) return deriv ? 1.5 * (6.0 * L - 1.0) : 1.5 * L * (3.0 * L - 1.0);
+    return deriv ? (13.5 * L - 9.0) * L + 1.0 : 0.5 * L * (3.0 * L - 1.0) * (3.0 * L - 2.0);
+  }
   if (pos == 1) return deriv ? 0.0 : 1.0;
   if (pos == 2) return deriv ? 2.0 : 2.0 * L;
   return deriv ? 4.0 * L - 1.0 : L * (2.0 * L - 1.0);
 }
 
+// Symmetric point sets of the tetrahedral rules, in Gauss_Simplex's order: `four` = one area
+// coordinate (1 + 3a)/4, the others (1 - a)/4, cycled; `six` = two coordinates (1 + 2b)/4 and two
+// (1 - 2b)/4 over the six placements.
+void simplex_four(double a, double wt, std::vector<std::array<double, 4>>& L, std::vector<double>& w) {
+  const double h = (1.0 + 3.0 * a) / 4.0, o = (1.0 - a) / 4.0, r = 1.0 - h - o - o;
+  const std::array<double, 4> base = {h, o, o, r};
+  for (int s = 0; s < 4; ++s) {
+    std::array<double, 4> p;
+    for (int k = 0; k < 4; ++k) p[k] = base[(k - s + 4) % 4];
+    L.push_back(p);
+    w.push_back(wt / 6.0);
+  }
+}
+
+void simplex_six(double b, double wt, std::vector<std::array<double, 4>>& L, std::vector<double>& w) {
+  const double hi = (1.0 + 2.0 * b) / 4.0, lo = (1.0 - 2.0 * b) / 4.0, r = 1.0 - hi - hi - lo;
+  // positions of the two large coordinates, in the rule's order
+  static const int at[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+  for (int s = 0; s < 6; ++s) {
+    std::array<double, 4> p;
+    int small = 0;
+    for (int k = 0; k < 4; ++k) {
+      if (k == at[s][0] || k == at[s][1]) p[k] = hi;
+      else p[k] = small++ == 0 ? lo : r;
+    }
+    L.push_back(p);
+    w.push_back(wt / 6.0);
+  }
+}
+
 void simplex_rule(int order, std::vector<std::array<double, 4>>& L, std::vector<double>& w) {
+  if (order == 4) {
+    L.push_back({0.25, 0.25, 0.25, 0.25});
+    w.push_back(-148.0 / 1875.0 / 6.0);
+    simplex_four(5.0 / 7.0, 343.0 / 7500.0, L, w);
+    simplex_six(std::sqrt(70.0) / 28.0, 56.0 / 375.0, L, w);
+    return;
+  }
+  if (order == 5) {
+    const double two_pi = 6.283185307179586;
+    const double lam =
+        4.0 / 27.0 * (4.0 * std::sqrt(79.0) * std::cos((std::acos(67.0 * std::sqrt(79.0) / 24964.0) + two_pi) / 3.0) + 71.0);
+    const double disc = std::sqrt(9.0 * lam * lam - 248.0 * lam + 1680.0), den = 112.0 - 10.0 * lam;
+    const double a1 = (disc + 28.0 - 3.0 * lam) / den, a2 = (28.0 - 3.0 * lam - disc) / den;
+    simplex_four(a1, ((21.0 - lam) * a2 - 7.0) / (420.0 * a1 * a1 * (a2 - a1)), L, w);
+    simplex_four(a2, ((21.0 - lam) * a1 - 7.0) / (420.0 * a2 * a2 * (a1 - a2)), L, w);
+    simplex_six(1.0 / std::sqrt(lam), lam * lam / 840.0, L, w);
+    return;
+  }
   if (order == 1) {
     L.push_back({0.25, 0.25, 0.25, 0.25});
     w.push_back(1.0 / 6.0);
@@ -182,19 +237,24 @@ int tp_tables(const int32_t* order, const int32_t* ngauss, const TPTables<T>** o
     *out = &it->second;
     return GFE_OK;
   }
-  if (order[0] == 7 || order[0] == 8) {
+  if (order[0] == 7 || order[0] == 8 || order[0] == 9) {
     static const int lin[4][4] = {{2, 1, 1, 1}, {1, 2, 1, 1}, {1, 1, 2, 1}, {1, 1, 1, 2}};
     static const int quad[10][4] = {{3, 1, 1, 1}, {1, 3, 1, 1}, {1, 1, 3, 1}, {1, 1, 1, 3}, {2, 2, 1, 1},
                                     {2, 1, 2, 1}, {2, 1, 1, 2}, {1, 2, 2, 1}, {1, 1, 2, 2}, {1, 2, 1, 2}};
+    // cubic: vertices, the two nodes of each edge (nearer the first vertex first), the face nodes
+    static const int cub[20][4] = {{4, 1, 1, 1}, {1, 4, 1, 1}, {1, 1, 4, 1}, {1, 1, 1, 4}, {3, 2, 1, 1},
+                                   {2, 3, 1, 1}, {3, 1, 2, 1}, {2, 1, 3, 1}, {3, 1, 1, 2}, {2, 1, 1, 3},
+                                   {1, 3, 2, 1}, {1, 2, 3, 1}, {1, 1, 3, 2}, {1, 1, 2, 3}, {1, 3, 1, 2},
+                                   {1, 2, 1, 3}, {2, 2, 2, 1}, {2, 2, 1, 2}, {2, 1, 2, 2}, {1, 2, 2, 2}};
     std::vector<std::array<double, 4>> gl;
     std::vector<double> gw;
     simplex_rule(ngauss[0], gl, gw);
-    const int nns = order[0] == 7 ? 4 : 10, ng = (int)gl.size();
+    const int nns = order[0] == 7 ? 4 : (order[0] == 8 ? 10 : 20), ng = (int)gl.size();
     std::vector<T> dphi((size_t)ng * 3 * nns), w(ng);
     for (int g = 0; g < ng; ++g) {
       w[g] = to_elem<T>(gw[g]);
       for (int n = 0; n < nns; ++n) {
-        const int* pos = order[0] == 7 ? lin[n] : quad[n];
+        const int* pos = order[0] == 7 ? lin[n] : (order[0] == 8 ? quad[n] : cub[n]);
         double dL[4];
         for (int k = 0; k < 4; ++k) {
           double d = 1.0;
@@ -517,10 +577,10 @@ extern "C" int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_ga
                                        float* values32, double* rhs, int32_t precision, void* stream) {
   const char* fn = "gfe_laplace_assemble_tp";
   if (!order || !n_gauss) return gfe::set_error(GFE_ERR_ARG, "%s: order and n_gauss are required", fn);
-  const bool simplex = order[0] == 7 || order[0] == 8;
-  if (simplex && (order[1] != order[0] || order[2] != order[0] || n_gauss[0] < 1 || n_gauss[0] > 3))
+  const bool simplex = order[0] == 7 || order[0] == 8 || order[0] == 9;
+  if (simplex && (order[1] != order[0] || order[2] != order[0] || n_gauss[0] < 1 || n_gauss[0] > 5))
     return gfe::set_error(GFE_ERR_ARG, "%s: tetrahedra need the same simplex interpolation in every xi and a "
-                          "Gauss_Simplex order of 1..3 in n_gauss[0]", fn);
+                          "Gauss_Simplex order of 1..5 in n_gauss[0]", fn);
   for (int d = 0; d < 3 && !simplex; ++d) {
     if (order[d] < 1 || order[d] > 4)
       return gfe::set_error(GFE_ERR_ARG, "%s: interpolation %d in xi%d (1..3 Lagrange, 4 cubic Hermite supported)",

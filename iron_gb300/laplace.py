@@ -69,14 +69,14 @@ class LaplaceAssembly:
         _lib.load()
         self.device = torch.device(dev)
         self.order = tuple(int(o) for o in (order if np.ndim(order) else (order,) * 3))
-        simplex = self.order[0] in (7, 8)
+        simplex = self.order[0] in (7, 8, 9)
         if simplex:
             # tetrahedra: one simplex interpolation, n_gauss = Gauss_Simplex order (default: exact
-            # for straight-sided elements, 1 for linear and 2 for quadratic)
+            # for straight-sided elements, 1 for linear, 2 for quadratic, 4 for cubic)
             q = int(n_gauss if n_gauss is not None and not np.ndim(n_gauss) else
-                    (n_gauss[0] if n_gauss is not None else self.order[0] - 6))
+                    (n_gauss[0] if n_gauss is not None else {7: 1, 8: 2, 9: 4}[self.order[0]]))
             self.n_gauss = (q, q, q)
-            nns = 4 if self.order[0] == 7 else 10
+            nns = {7: 4, 8: 10, 9: 20}[self.order[0]]
         else:
             self.n_gauss = tuple(int(g) for g in (n_gauss if n_gauss is not None and np.ndim(n_gauss) else
                                                   ((n_gauss,) * 3 if n_gauss is not None else

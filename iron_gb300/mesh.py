@@ -240,12 +240,21 @@ class HermiteMesh:
         return (8 * nodes[:, None] + np.arange(8)[None, :]).reshape(-1)
 
 
+# Iron's cubic-simplex node position indices per area coordinate (1..4), local nodes 1..20
+CUBIC_TET_POSITIONS = [(4, 1, 1, 1), (1, 4, 1, 1), (1, 1, 4, 1), (1, 1, 1, 4), (3, 2, 1, 1), (2, 3, 1, 1),
+                       (3, 1, 2, 1), (2, 1, 3, 1), (3, 1, 1, 2), (2, 1, 1, 3), (1, 3, 2, 1), (1, 2, 3, 1),
+                       (1, 1, 3, 2), (1, 1, 2, 3), (1, 3, 1, 2), (1, 2, 1, 3), (2, 2, 2, 1), (2, 2, 1, 2),
+                       (2, 1, 2, 2), (1, 2, 2, 2)]
+
+
 @dataclass
 class TetMesh:
     """Tetrahedral mesh of a box: every cell of a regular grid split into six tetrahedra along its
-    main diagonal (conforming across cells), order 1 (4 vertices) or 2 (plus 6 edge nodes in
-    Iron's quadratic-simplex order: edges 1-2, 1-3, 1-4, 2-3, 3-4, 2-4).  coords [3][N],
-    elem_nodes [E][4 or 10] (0-based)."""
+    main diagonal (conforming across cells), order 1 (4 vertices), 2 (plus 6 edge nodes in
+    Iron's quadratic-simplex order: edges 1-2, 1-3, 1-4, 2-3, 3-4, 2-4) or 3 (Iron's 20-node cubic
+    simplex: vertices, two nodes on each edge, one on each face, in the order of the node
+    position indices of src/basis_routines.F90:5236-5353).  coords [3][N], elem_nodes
+    [E][4, 10 or 20] (0-based); vertices are nodes 0..n_vertices-1."""
 
     nelem: tuple
     order: int = 1
@@ -284,8 +293,38 @@ class TetMesh:
             self.coords = np.concatenate([verts, mid], axis=1)
             self.elem_nodes = np.concatenate([tets, self.n_vertices + inv.reshape(-1, 6)], axis=1).astype(np.int32)
             self.edges = uniq
+        elif self.order == 3:
+            # a node is the point sum_i (p_i - 1)/3 V_i of its position indices p_i: keyed by the
+            # (vertex, weight) pairs with non-zero weight, so neighbouring elements share it
+            pos = np.array(CUBIC_TET_POSITIONS) - 1  # [20][4] weights in thirds
+            E = tets.shape[0]
+            vid4 = np.broadcast_to(tets[:, None, :], (E, 20, 4))
+            wt = np.broadcast_to(pos[None, :, :], (E, 20, 4))
+            key_v = np.where(wt > 0, vid4, -1)
+            order = np.argsort(key_v, axis=2, kind="stable")
+            kv = np.take_along_axis(key_v, order, axis=2)
+            kw = np.take_along_axis(np.where(wt > 0, wt, 0), order, axis=2)
+            keys = np.concatenate([kv, kw], axis=2).reshape(-1, 8)
+            higher = (pos.max(axis=1) < 3)[None, :].repeat(E, axis=0).reshape(-1)
+            uniq, inv = np.unique(keys[higher], axis=0, return_inverse=True)
+            nodes = np.empty(E * 20, dtype=np.int64)
+            nodes[~higher] = tets[:, pos.argmax(axis=1)[pos.max(axis=1) == 3]].reshape(-1)
+            nodes[higher] = self.n_vertices + inv.reshape(-1)
+            self.elem_nodes = nodes.reshape(E, 20).astype(np.int32)
+            self.node_vertices = uniq[:, :4]
+            self.node_weights = uniq[:, 4:] / 3.0
+            self.coords = np.concatenate([verts, self._higher_coords(verts)], axis=1)
         else:
-            raise ValueError("tetrahedra of order 1 or 2")
+            raise ValueError("tetrahedra of order 1, 2 or 3")
+
+    def _higher_coords(self, verts):
+        """Coordinates of the cubic edge and face nodes from their vertices and weights."""
+        out = np.zeros((3, self.node_vertices.shape[0]))
+        for k in range(4):
+            v = self.node_vertices[:, k]
+            on = v >= 0
+            out[:, on] += self.node_weights[on, k] * verts[:, v[on]]
+        return out
 
     @property
     def n_nodes(self) -> int:
@@ -311,6 +350,8 @@ class TetMesh:
         self.coords[:, : self.n_vertices] += d
         if self.order == 2:
             self.coords[:, self.n_vertices:] = (self.coords[:, self.edges[:, 0]] + self.coords[:, self.edges[:, 1]]) / 2
+        elif self.order == 3:
+            self.coords[:, self.n_vertices:] = self._higher_coords(self.coords[:, : self.n_vertices])
 
     def face_nodes(self, axis: int, side: int) -> np.ndarray:
         target = 0.0 if side == 0 else self.extent[axis]

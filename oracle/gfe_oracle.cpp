@@ -109,20 +109,57 @@ struct TPBasis {
 // Tetrahedral simplex basis, src/basis_routines.F90: Basis_SimplexBasisCreate :4813-5875 (node
 // positions per area coordinate: 1 absent, 2 on an edge (L for linear, 2L for quadratic),
 // 3 vertex L(2L-1); SIMPLEX_LINEAR/QUADRATIC_EVALUATE :8177-8313), BASIS_SIMPLEX_BASIS_EVALUATE
-// :6041-6270 (d/dxi_i = d/dL4 - d/dL_i), Gauss_Simplex :6898-7600 (tetrahedra, orders 1..3:
-// 1, 4, 5 points in area coordinates, weights summing to 1/6).  interp 7 = linear (4 nodes),
-// 8 = quadratic (10 nodes); quad_order = Gauss_Simplex order.
+// :6041-6270 (d/dxi_i = d/dL4 - d/dL_i), Gauss_Simplex :6898-7600 (tetrahedra, orders 1..5:
+// 1, 4, 5, 11, 14 points in area coordinates, weights summing to 1/6).  interp 7 = linear
+// (4 nodes), 8 = quadratic (10 nodes), 9 = cubic (20 nodes: vertices, two nodes on each edge,
+// one on each face; positions :5236-5353, SIMPLEX_CUBIC_EVALUATE :8092-8169 with factors 1, 3L,
+// 3/2 L(3L-1), 1/2 L(3L-1)(3L-2) for positions 1..4); quad_order = Gauss_Simplex order.
 double simplex_factor(int interp, int pos, int deriv, double L) {
   if (interp == 7) return pos == 1 ? (deriv ? 0.0 : 1.0) : (deriv ? 1.0 : L);
+  if (interp == 9) {
+    switch (pos) {
+      case 1: return deriv ? 0.0 : 1.0;
+      case 2: return deriv ? 3.0 : 3.0 * L;
+      case 3: return deriv ? 1.5 * (6.0 * L - 1.0) : 1.5 * L * (3.0 * L - 1.0);
+      default: return deriv ? 13.5 * L * L - 9.0 * L + 1.0 : 0.5 * L * (3.0 * L - 1.0) * (3.0 * L - 2.0);
+    }
+  }
   if (pos == 1) return deriv ? 0.0 : 1.0;
   if (pos == 2) return deriv ? 2.0 : 2.0 * L;
   return deriv ? 4.0 * L - 1.0 : L * (2.0 * L - 1.0);
+}
+
+// The symmetric orbits of the tetrahedral rules, in Gauss_Simplex's point order: a = the four
+// points with one area coordinate (1 + 3a)/4 and three (1 - a)/4, cycled; b = the six points with
+// two coordinates (1 + 2b)/4 and two (1 - 2b)/4.
+void simplex_orbit_a(double a, double wt, std::vector<std::array<double, 4>>& L, std::vector<double>& w) {
+  const double l1 = (1.0 + 3.0 * a) / 4.0, l2 = (1.0 - a) / 4.0, l3 = (1.0 - a) / 4.0, l4 = 1.0 - l1 - l2 - l3;
+  L.push_back({l1, l2, l3, l4});
+  L.push_back({l4, l1, l2, l3});
+  L.push_back({l3, l4, l1, l2});
+  L.push_back({l2, l3, l4, l1});
+  for (int k = 0; k < 4; ++k) w.push_back(wt / 6.0);
+}
+
+void simplex_orbit_b(double b, double wt, std::vector<std::array<double, 4>>& L, std::vector<double>& w) {
+  const double p = (1.0 + 2.0 * b) / 4.0, q = (1.0 - 2.0 * b) / 4.0, r = 1.0 - p - p - q;
+  L.push_back({p, p, q, r});
+  L.push_back({p, q, p, r});
+  L.push_back({p, q, r, p});
+  L.push_back({q, p, p, r});
+  L.push_back({q, p, r, p});
+  L.push_back({q, r, p, p});
+  for (int k = 0; k < 6; ++k) w.push_back(wt / 6.0);
 }
 
 bool make_simplex_basis(int interp, int quad_order, TPBasis& b) {
   static const int lin[4][4] = {{2, 1, 1, 1}, {1, 2, 1, 1}, {1, 1, 2, 1}, {1, 1, 1, 2}};
   static const int quad[10][4] = {{3, 1, 1, 1}, {1, 3, 1, 1}, {1, 1, 3, 1}, {1, 1, 1, 3}, {2, 2, 1, 1},
                                   {2, 1, 2, 1}, {2, 1, 1, 2}, {1, 2, 2, 1}, {1, 1, 2, 2}, {1, 2, 1, 2}};
+  static const int cub[20][4] = {{4, 1, 1, 1}, {1, 4, 1, 1}, {1, 1, 4, 1}, {1, 1, 1, 4}, {3, 2, 1, 1},
+                                 {2, 3, 1, 1}, {3, 1, 2, 1}, {2, 1, 3, 1}, {3, 1, 1, 2}, {2, 1, 1, 3},
+                                 {1, 3, 2, 1}, {1, 2, 3, 1}, {1, 1, 3, 2}, {1, 1, 2, 3}, {1, 3, 1, 2},
+                                 {1, 2, 1, 3}, {2, 2, 2, 1}, {2, 2, 1, 2}, {2, 1, 2, 2}, {1, 2, 2, 2}};
   std::vector<std::array<double, 4>> gl;
   std::vector<double> gw;
   if (quad_order == 1) {
@@ -141,11 +178,29 @@ bool make_simplex_basis(int interp, int quad_order, TPBasis& b) {
     gl.push_back({l3, l4, l1, l2});
     gl.push_back({l2, l3, l4, l1});
     for (int k = 0; k < 4; ++k) gw.push_back(wa / 6.0);
+  } else if (quad_order == 4) {
+    gl.push_back({0.25, 0.25, 0.25, 0.25});
+    gw.push_back(-148.0 / 1875.0 / 6.0);
+    simplex_orbit_a(5.0 / 7.0, 343.0 / 7500.0, gl, gw);
+    simplex_orbit_b(std::sqrt(70.0) / 28.0, 56.0 / 375.0, gl, gw);
+  } else if (quad_order == 5) {
+    // lambda: the root of Keast's cubic that the rule's two a orbits and one b orbit are built on
+    const double pi2 = 2.0 * 3.14159265358979323846;
+    const double lam = 4.0 / 27.0 *
+                       (4.0 * std::sqrt(79.0) * std::cos((std::acos(67.0 * std::sqrt(79.0) / 24964.0) + pi2) / 3.0) + 71.0);
+    const double root = std::sqrt(9.0 * lam * lam - 248.0 * lam + 1680.0);
+    const double a1 = (root + 28.0 - 3.0 * lam) / (112.0 - 10.0 * lam);
+    const double a2 = (-root + 28.0 - 3.0 * lam) / (112.0 - 10.0 * lam);
+    const double wa1 = ((21.0 - lam) * a2 - 7.0) / (420.0 * a1 * a1 * (a2 - a1));
+    const double wa2 = ((21.0 - lam) * a1 - 7.0) / (420.0 * a2 * a2 * (a1 - a2));
+    simplex_orbit_a(a1, wa1, gl, gw);
+    simplex_orbit_a(a2, wa2, gl, gw);
+    simplex_orbit_b(1.0 / std::sqrt(lam), lam * lam / 840.0, gl, gw);
   } else {
     return false;
   }
-  if (interp != 7 && interp != 8) return false;
-  const int nns = interp == 7 ? 4 : 10;
+  if (interp != 7 && interp != 8 && interp != 9) return false;
+  const int nns = interp == 7 ? 4 : (interp == 8 ? 10 : 20);
   b.nxi = 3;
   b.nns = nns;
   b.ng = (int)gl.size();
@@ -153,7 +208,7 @@ bool make_simplex_basis(int interp, int quad_order, TPBasis& b) {
   b.wts = gw;
   for (int g = 0; g < b.ng; ++g)
     for (int ns = 0; ns < nns; ++ns) {
-      const int* pos = interp == 7 ? lin[ns] : quad[ns];
+      const int* pos = interp == 7 ? lin[ns] : (interp == 8 ? quad[ns] : cub[ns]);
       double dL[4];  // d phi / d L_k
       double v = 1.0;
       for (int k = 0; k < 4; ++k) v *= simplex_factor(interp, pos[k], 0, gl[g][k]);
@@ -169,7 +224,7 @@ bool make_simplex_basis(int interp, int quad_order, TPBasis& b) {
 }
 
 bool make_tp_basis(int nxi, const int* order, const int* ngauss, TPBasis& b) {
-  if (nxi == 3 && (order[0] == 7 || order[0] == 8)) return make_simplex_basis(order[0], ngauss[0], b);
+  if (nxi == 3 && (order[0] == 7 || order[0] == 8 || order[0] == 9)) return make_simplex_basis(order[0], ngauss[0], b);
   if (nxi < 1 || nxi > 3) return false;
   b.nxi = nxi;
   b.ng = 1;

@@ -1,4 +1,5 @@
 """Laplace assembly on higher-order tensor-product Lagrange hexahedra (gfe_laplace_assemble_tp)
+and on linear, quadratic and cubic tetrahedra with Gauss_Simplex orders 1..5
 against the oracle's restatement of Iron's basis-generic element routine: triquadratic and
 tricubic elements, anisotropic Gauss rules, trilinear elements with a non-default rule, FP64 /
 float-float / FP32 element arithmetic; the patch test u = x on curved (jittered) quadratic and
@@ -103,7 +104,7 @@ def test_cubic_hermite_patch_test(gfe_cuda, scaling):
     assert (x - exact).abs().max().item() <= 1e-10
 
 
-@pytest.mark.parametrize("order,quad", [(1, 1), (1, 2), (2, 2), (2, 3)])
+@pytest.mark.parametrize("order,quad", [(1, 1), (1, 2), (1, 5), (2, 2), (2, 3), (2, 4), (3, 3), (3, 4), (3, 5)])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed_df", 1e-12), ("mixed", 2e-5)])
 def test_tetrahedra_match_oracle(gfe_cuda, order, quad, precision, tol):
     tm = M.TetMesh((3, 2, 2), order=order, extent=(1.0, 0.8, 1.2))
@@ -118,7 +119,7 @@ def test_tetrahedra_match_oracle(gfe_cuda, order, quad, precision, tol):
     assert np.abs(vals - ref).max() <= tol * np.abs(ref).max()
 
 
-@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("order", [1, 2, 3])
 def test_tetrahedra_patch_test(gfe_cuda, order):
     tm = M.TetMesh((3, 3, 2), order=order)
     tm.jitter_interior(9)
