@@ -6,7 +6,7 @@ mr:         Mooney-Rivlin mixed u-p (triquadratic u, trilinear p) residual, Iron
 mr_adjoint: residual and its hand-written adjoint for a batch of 64 parameter sets on a 16^3 mesh
             (c10, c01 log-uniform in [0.5, 10], displacement perturbation N(0, (0.01 h)^2), seeded).
 laplace_bases: the basis-generic Laplace assembly (triquadratic and tricubic Lagrange hexahedra,
-            tricubic Hermite with arc-length scale factors, linear and quadratic tetrahedra) on
+            tricubic Hermite with arc-length scale factors, linear, quadratic and cubic tetrahedra) on
             jittered meshes with log-uniform conductivity, FP64 / float-float / FP32, against the
             oracle on a sample of each mesh.
 serve:      the request stream of iron_gb300.serving.
@@ -157,8 +157,9 @@ BASES = [
     ("hermite_cubic_hex", "hermite", 32, 12, 4),
     ("simplex_p1_tet", "tet1", 96, 48, 1),
     ("simplex_p2_tet", "tet2", 40, 24, 3),
+    ("simplex_p3_tet", "tet3", 24, 8, 4),
 ]
-SIMPLEX_POINTS = {1: 1, 2: 4, 3: 5}
+SIMPLEX_POINTS = {1: 1, 2: 4, 3: 5, 4: 11, 5: 14}
 
 
 def _bases_problem(kind: str, n: int, ng: int, seed: int = 0, device=None):
@@ -181,7 +182,7 @@ def _bases_problem(kind: str, n: int, ng: int, seed: int = 0, device=None):
         kap = np.exp(rng.uniform(np.log(0.1), np.log(10.0), m.n_elements))
         A = LaplaceAssembly.from_hermite_mesh(m, kappa=kap, n_gauss=ng, device=device) if device else None
         return A, [4] * 3, m.elem_params, m.params, m.scale, kap
-    o = 1 if kind == "tet1" else 2
+    o = int(kind[-1])
     m = M.TetMesh((n, n, n), order=o)
     m.jitter_interior(seed)
     kap = np.exp(rng.uniform(np.log(0.1), np.log(10.0), m.n_elements))
