@@ -1244,8 +1244,12 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
       }
       // the A tile is rewritten by the next half: wait for this half's products
       if (!tc::mbar_wait(&S.mbar, parity, kTWaitPolls)) {
+        // the MMAs of this half may still be writing tensor memory: wait once more (bounded) for
+        // their commit before anything releases it; if that wait also ends without the commit,
+        // the tensor memory stays allocated (abort = 2) rather than being freed under the MMAs
         gfe_raise(err, GFE_DEVERR_TIMEOUT);
-        S.abort = 1;
+        const bool drained = tc::mbar_wait(&S.mbar, parity, kTWaitPolls);
+        atomicMax(&S.abort, drained ? 1 : 2);
       }
       parity ^= 1u;
       tc::fence_after_sync();
@@ -1282,7 +1286,7 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, 64);
+  if (warp == 0 && S.abort < 2) tc::tmem_dealloc(tmem, 64);
 }
 
 size_t vjp_smem() { return sizeof(Tables) + sizeof(TanShared) + sizeof(double) * (ND + NG * 9 + NG + NG * 2); }

@@ -1429,8 +1429,7 @@ extern "C" int gfe_saddle_preconditioner(int32_t n, int32_t n_u, const int32_t* 
 // ---------------------------------------------------------------------------------------------
 // Some callers of this library may not allocate device memory at all: host codes that run the
 // solve from inside a memory pool they do not own (a framework's caching allocator, a
-// statically partitioned serving process) or from places where a cudaMalloc would synchronise the
-// device or be forbidden.  gfe_cg_solve_noalloc serves them: its working vectors live in one
+// statically partitioned serving process), where a cudaMalloc is forbidden.  gfe_cg_solve_noalloc serves them: its working vectors live in one
 // fixed array in the library's own device memory, sized for GFE_NOALLOC_MAX_ROWS rows, which every
 // GPU that loads the library keeps for the lifetime of the process.
 namespace {
@@ -1507,8 +1506,16 @@ extern "C" int gfe_cg_solve_noalloc(int32_t n, const int32_t* row_ptr, const int
   set_dirichlet<<<grid, kThreads, 0, s>>>(n, x, fixed, true);
   cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
   norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, sc, red2 + grid - 1);
+  unsigned dev_err = 0;
   GFE_CUDA_TRY(cudaMemcpyAsync(&b2, red2 + grid - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GFE_CUDA_TRY(cudaMemcpyAsync(&dev_err, err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   GFE_CUDA_TRY(cudaStreamSynchronize(s));
+  // this entry point holds no library error word (that word is allocated on first use), so a
+  // zero or non-finite diagonal on a free row, which gfe_cg_solve raises as GFE_DEVERR_NONFINITE on
+  // the device error word, is returned here as the call's status
+  if (dev_err)
+    return set_error(GFE_ERR_NUMERIC, "%s: zero or non-finite diagonal entry on a free row (device error bits 0x%x)",
+                     fn, dev_err);
   if (b2 == 0.0) {
     if (iters_host) *iters_host = 0;
     if (rel_host) *rel_host = 0.0;
