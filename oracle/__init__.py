@@ -129,6 +129,24 @@ def regular_coords(nelem, order: int, origin, extent):
     return out
 
 
+def regular_triangle_mesh(nelem):
+    """Linear triangles of Iron's regular generated mesh in two dimensions
+    (src/generated_mesh_routines.F90:1641-1660): grid squares stepped xi1 fastest, each split into
+    the triangles (np, np+1, np+1+NX) and (np, np+1+NX, np+NX), NX = nodes per row.  0-based node
+    numbers [2*E][3]; the nodes are those of regular_mesh(nelem, 1)."""
+    n1, n2 = int(nelem[0]), int(nelem[1])
+    NX = n1 + 1
+    out = np.zeros((2 * n1 * n2, 3), np.int32)
+    e = 0
+    for j in range(n2):
+        for i in range(n1):
+            p = i + j * NX
+            out[e] = (p, p + 1, p + 1 + NX)
+            out[e + 1] = (p, p + 1 + NX, p + NX)
+            e += 2
+    return out
+
+
 def linear_component(elem_first, nnx_first):
     elem_first = _i32(elem_first)
     nnx = _i32(list(nnx_first) + [1] * (3 - len(nnx_first)))

@@ -223,8 +223,72 @@ bool make_simplex_basis(int interp, int quad_order, TPBasis& b) {
   return true;
 }
 
+// Linear triangles (interp 7 with two xi directions): area coordinates L1..L3, node n at vertex n
+// (BASIS_SIMPLEX_BASIS_EVALUATE :6041-6270 with d/dxi_i = d/dL3 - d/dL_i in two dimensions), and
+// Gauss_Simplex's triangle rules of orders 1..5 (:6898-7600, numberOfVertices = 3) in its point
+// order: the centroid, and orbits of the three points with one coordinate (1 + 2a)/3 and two
+// (1 - a)/3, cycled as (l1, l2, l3), (l3, l1, l2), (l2, l3, l1); weights sum to 1/2.
+void triangle_orbit(double a, double wt, std::vector<std::array<double, 4>>& L, std::vector<double>& w) {
+  const double l1 = (1.0 + 2.0 * a) / 3.0, l2 = (1.0 - a) / 3.0, l3 = 1.0 - l1 - l2;
+  L.push_back({l1, l2, l3, 0.0});
+  L.push_back({l3, l1, l2, 0.0});
+  L.push_back({l2, l3, l1, 0.0});
+  for (int k = 0; k < 3; ++k) w.push_back(wt / 2.0);
+}
+
+bool make_triangle_basis(int interp, int quad_order, TPBasis& b) {
+  if (interp != 7) return false;
+  std::vector<std::array<double, 4>> gl;
+  std::vector<double> gw;
+  const double third = 1.0 / 3.0;
+  switch (quad_order) {
+    case 1:
+      gl.push_back({third, third, third, 0.0});
+      gw.push_back(0.5);
+      break;
+    case 2:
+      triangle_orbit(-0.5, third, gl, gw);
+      break;
+    case 3:
+      gl.push_back({third, third, third, 0.0});
+      gw.push_back(-0.75 / 2.0);
+      triangle_orbit(0.4, 25.0 / 48.0, gl, gw);
+      break;
+    case 4: {
+      const double r = std::sqrt(950.0 - 220.0 * std::sqrt(10.0));
+      const double a1 = (-10.0 + 5.0 * std::sqrt(10.0) + r) / 30.0, a2 = (-10.0 + 5.0 * std::sqrt(10.0) - r) / 30.0;
+      triangle_orbit(a1, (5.0 * a2 - 2.0) / (60.0 * a1 * a1 * (a2 - a1)), gl, gw);
+      triangle_orbit(a2, (5.0 * a1 - 2.0) / (60.0 * a2 * a2 * (a1 - a2)), gl, gw);
+      break;
+    }
+    case 5: {
+      const double q = std::sqrt(15.0);
+      gl.push_back({third, third, third, 0.0});
+      gw.push_back(9.0 / 40.0 / 2.0);
+      triangle_orbit((1.0 + q) / 7.0, (155.0 - q) / 1200.0, gl, gw);
+      triangle_orbit((1.0 - q) / 7.0, (155.0 + q) / 1200.0, gl, gw);
+      break;
+    }
+    default:
+      return false;
+  }
+  b.nxi = 2;
+  b.nns = 3;
+  b.ng = (int)gl.size();
+  b.tab.assign((size_t)b.ng * 3 * 3, 0.0);
+  b.wts = gw;
+  for (int g = 0; g < b.ng; ++g)
+    for (int ns = 0; ns < 3; ++ns) {
+      b.tab[((size_t)g * 3 + 0) * 3 + ns] = gl[g][ns];
+      // d L_ns / d xi_i = d/dL3 - d/dL_i
+      for (int i = 0; i < 2; ++i) b.tab[((size_t)g * 3 + i + 1) * 3 + ns] = (ns == 2 ? 1.0 : 0.0) - (ns == i ? 1.0 : 0.0);
+    }
+  return true;
+}
+
 bool make_tp_basis(int nxi, const int* order, const int* ngauss, TPBasis& b) {
   if (nxi == 3 && (order[0] == 7 || order[0] == 8 || order[0] == 9)) return make_simplex_basis(order[0], ngauss[0], b);
+  if (nxi == 2 && (order[0] == 7 || order[0] == 8 || order[0] == 9)) return make_triangle_basis(order[0], ngauss[0], b);
   if (nxi < 1 || nxi > 3) return false;
   b.nxi = nxi;
   b.ng = 1;
