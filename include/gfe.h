@@ -314,6 +314,19 @@ int gfe_mr_tangent(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int3
                    const double* dep, const double* cpar, const int32_t* slots, double* values, int64_t nnz,
                    double* K_out, int32_t precision, void* stream);
 
+/* Iron's finite-difference Jacobian, its default for finite elasticity, in FP64: per element the
+ * residual R0 and, for each of the 89 element parameters j, the residual with parameter j raised by
+ * delta = (1 + ||dep||_2) step, column j = (R_j - R0) / delta, where ||dep||_2 is the L2 norm of the
+ * whole dependent vector.  Replaces EquationsSet_FiniteElementJacobianEvaluateFD
+ * (src/equations_set_routines.F90:2839-2962) inside EquationsSet_JacobianEvaluateStaticFEM;
+ * `step` is Iron's jacobianFiniteDifferenceStepSize (default 1e-6, set by
+ * cmfe_Equations_JacobianFiniteDifferenceStepSizeSet, src/opencmiss_iron.F90:25271-25348).  Outputs
+ * as gfe_mr_jacobian.  Allocates and frees a small norm scratch on `stream`. */
+int gfe_mr_jacobian_fd(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, int32_t n_lin,
+                       const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
+                       const double* dep, const double* cpar, double step, const int32_t* slots, double* values,
+                       int64_t nnz, double* K_out, void* stream);
+
 /* Adjoint of the residual (K6): for `batch` problems, du[b] = v[b]^T dR/d(dep) ([batch][ndof]) and
  * dc[b] = v[b]^T dR/d(c10, c01) ([batch][2]).  No counterpart routine in Iron (its gradients come
  * from finite differences); checked against central differences and Iron-style one-sided FD.

@@ -78,6 +78,7 @@ SIGNATURES = {
     "gfe_mr_slot_map": (C.c_int, [i32, vp, vp, i32, vp, vp, vp, vp, vp]),
     "gfe_mr_jacobian": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, vp, vp, vp, vp, i64, vp, i32, vp]),
     "gfe_mr_tangent": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, vp, vp, vp, vp, i64, vp, i32, vp]),
+    "gfe_mr_jacobian_fd": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, vp, vp, f64, vp, vp, i64, vp, vp]),
     "gfe_mr_residual_vjp": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]),
     "gfe_cg_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(C.c_int32),
                                C.POINTER(C.c_double), vp]),

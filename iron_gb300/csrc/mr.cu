@@ -288,6 +288,46 @@ __device__ __forceinline__ void residual_stress(const GP& q, double c1, double c
 // ----------------------------------------------------------------------------------------------
 constexpr int kResWarps = 4;
 
+// One warp: the 89 residual entries of one element from its staged geometry sx[81], deformed
+// positions sz[81] and pressures sp[8] (shared memory), with Gauss-point scratch sP[27*9] and
+// stp[27].  Lane g < 27 evaluates Gauss point g (metrics, deformation gradient, stress) and leaves
+// P_g = J_z w_g Z^-1 sigma (3x3) and J_x w_g (J_z/J_x - 1); then lane i forms entries i, i + 32,
+// i + 64 as sums over the Gauss points in a fixed order and hands each to emit(i, value).
+template <typename Emit>
+__device__ __forceinline__ void warp_element_residual(const Tables& T, int lane, const double* sx, const double* sz,
+                                                      const double* sp, double c1, double c2, double* sP, double* stp,
+                                                      unsigned* err, Emit emit) {
+  if (lane < NG) {
+    GP q;
+    if (!gauss_point(T, lane, sz, sx, sp, q)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+    double sig[6];
+    residual_stress(q, c1, c2, sig);
+    const double jgw = q.Jz * q.w;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int mh = 0; mh < 3; ++mh)
+        sP[lane * 9 + k * 3 + mh] = jgw * (q.Zi[k][0] * sig[t2v(0, mh)] + q.Zi[k][1] * sig[t2v(1, mh)] +
+                                           q.Zi[k][2] * sig[t2v(2, mh)]);
+    stp[lane] = q.Jx * q.w * (q.Jz / q.Jx - 1.0);
+  }
+  __syncwarp();
+  for (int i = lane; i < ND; i += 32) {
+    double s = 0.0;
+    if (i < 81) {
+      const int ms = i % NQ, mh = i / NQ;
+      for (int g = 0; g < NG; ++g)
+        s += T.dphi[g][0][ms] * sP[g * 9 + 0 + mh] + T.dphi[g][1][ms] * sP[g * 9 + 3 + mh] +
+             T.dphi[g][2][ms] * sP[g * 9 + 6 + mh];
+    } else {
+      const int ms = i - 81;
+      for (int g = 0; g < NG; ++g) s += stp[g] * T.psi[g][ms];
+    }
+    emit(i, s);
+  }
+  __syncwarp();
+}
+
 __global__ void __launch_bounds__(kResWarps * 32)
 mr_residual_kernel(const int32_t* __restrict__ elems, int32_t count, int32_t batch, const int32_t* __restrict__ eq2,
                    const int32_t* __restrict__ elin, int32_t nq2, int32_t nlin, const double* __restrict__ xg,
@@ -312,7 +352,6 @@ mr_residual_kernel(const int32_t* __restrict__ elems, int32_t count, int32_t bat
   double* stp = sP + NG * 9;
   int* sd = reinterpret_cast<int*>(stp + NG);
   const long long total = (long long)count * batch;
-  const int64_t ndof = 3ll * nq2 + nlin;
   for (long long item = (long long)blockIdx.x * kResWarps + w; item < total; item += (long long)gridDim.x * kResWarps) {
     const int b = (int)(item / count);
     const int e = __ldg(elems + (item % count));
@@ -333,39 +372,116 @@ mr_residual_kernel(const int32_t* __restrict__ elems, int32_t count, int32_t bat
     }
     const double c1 = cpar[2 * b], c2 = cpar[2 * b + 1];
     __syncwarp();
-    if (lane < NG) {
-      GP q;
-      if (!gauss_point(T, lane, sz, sx, sp, q)) gfe_raise(err, GFE_DEVERR_JACOBIAN);
-      double sig[6];
-      residual_stress(q, c1, c2, sig);
-      const double jgw = q.Jz * q.w;
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int mh = 0; mh < 3; ++mh)
-          sP[lane * 9 + k * 3 + mh] = jgw * (q.Zi[k][0] * sig[t2v(0, mh)] + q.Zi[k][1] * sig[t2v(1, mh)] +
-                                             q.Zi[k][2] * sig[t2v(2, mh)]);
-      stp[lane] = q.Jx * q.w * (q.Jz / q.Jx - 1.0);
-    }
-    __syncwarp();
     double* Rb = R + b * dep_stride;
-    for (int i = lane; i < ND; i += 32) {
-      double s = 0.0;
-      if (i < 81) {
-        const int ms = i % NQ, mh = i / NQ;
-        for (int g = 0; g < NG; ++g)
-          s += T.dphi[g][0][ms] * sP[g * 9 + 0 + mh] + T.dphi[g][1][ms] * sP[g * 9 + 3 + mh] +
-               T.dphi[g][2][ms] * sP[g * 9 + 6 + mh];
-      } else {
-        const int ms = i - 81;
-        for (int g = 0; g < NG; ++g) s += stp[g] * T.psi[g][ms];
-      }
+    warp_element_residual(T, lane, sx, sz, sp, c1, c2, sP, stp, err, [&](int i, double s) {
       if (!isfinite(s)) gfe_raise(err, GFE_DEVERR_NONFINITE);
       Rb[sd[i]] += s;
-    }
-    __syncwarp();
+    });
   }
-  (void)ndof;
+}
+
+// ----------------------------------------------------------------------------------------------
+// Finite-difference Jacobian (Iron's default for finite elasticity)
+// ----------------------------------------------------------------------------------------------
+// EquationsSet_FiniteElementJacobianEvaluateFD (src/equations_set_routines.F90:2839-2962): the
+// element residual R0 at the current parameters, then for every element parameter j (27 nodes of
+// each displacement component, then the 8 pressure nodes) the residual with that parameter raised
+// by delta = (1 + ||dep||_2) * step, and column j = (R_j - R0) / delta.  ||dep||_2 is the L2 norm
+// of the whole dependent parameter vector (DistributedVector_L2Norm).  One CTA per element of a
+// colour: warp 0 forms R0, then the warps take the 89 perturbed residuals in turn, each on its
+// own copy of the element parameters, and add their column into the CSR values through the slot
+// map (elements of one colour share no DOF).
+constexpr int kFDWarps = 4;
+constexpr int kNormParts = 512;
+
+struct FDShared {
+  double x[81], z0[81], p0[8], R0[ND];
+  double z[kFDWarps][81], p[kFDWarps][8], P[kFDWarps][NG * 9], tp[kFDWarps][NG], col[kFDWarps][ND];
+  double delta;
+};
+
+// partial sums of squares of the dependent vector in a fixed order (kNormParts contiguous chunks)
+__global__ void sumsq_parts(const double* __restrict__ v, int64_t n, double* __restrict__ parts) {
+  __shared__ double red[256];
+  const int64_t chunk = (n + kNormParts - 1) / kNormParts;
+  const int64_t a = blockIdx.x * chunk, b = a + chunk < n ? a + chunk : n;
+  double s = 0.0;
+  for (int64_t i = a + threadIdx.x; i < b; i += blockDim.x) s += v[i] * v[i];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) parts[blockIdx.x] = red[0];
+}
+
+__global__ void __launch_bounds__(kFDWarps * 32)
+mr_jacobian_fd_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
+                      const int32_t* __restrict__ elin, int32_t nq2, const double* __restrict__ xg,
+                      const double* __restrict__ dep, const double* __restrict__ cpar, const Tables* __restrict__ Tg,
+                      const double* __restrict__ norm_parts, double step, const int32_t* __restrict__ slots,
+                      double* __restrict__ values, double* __restrict__ Kout, unsigned* err) {
+  extern __shared__ double smem[];
+  Tables& T = *reinterpret_cast<Tables*>(smem);
+  FDShared& S = *reinterpret_cast<FDShared*>(smem + sizeof(Tables) / sizeof(double));
+  {
+    const double* src = reinterpret_cast<const double*>(Tg);
+    for (int i = threadIdx.x; i < (int)(sizeof(Tables) / sizeof(double)); i += blockDim.x) smem[i] = src[i];
+  }
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < kNormParts; ++i) s += norm_parts[i];
+    S.delta = (1.0 + sqrt(s)) * step;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const double c1 = cpar[0], c2 = cpar[1];
+  const double delta = S.delta;
+  for (int item = blockIdx.x; item < count; item += gridDim.x) {
+    const int e = __ldg(elems + item);
+    for (int i = threadIdx.x; i < NQ; i += blockDim.x) {
+      const int n = __ldg(eq2 + (size_t)e * NQ + i);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        S.x[c * NQ + i] = __ldg(xg + (size_t)c * nq2 + n);
+        S.z0[c * NQ + i] = dep[(size_t)c * nq2 + n];
+      }
+    }
+    if (threadIdx.x < NL) S.p0[threadIdx.x] = dep[(size_t)3 * nq2 + __ldg(elin + (size_t)e * NL + threadIdx.x)];
+    __syncthreads();
+    if (w == 0)
+      warp_element_residual(T, lane, S.x, S.z0, S.p0, c1, c2, S.P[0], S.tp[0], err,
+                            [&](int i, double s) { S.R0[i] = s; });
+    __syncthreads();
+    const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
+    double* Ke = Kout ? Kout + (size_t)e * ND * ND : nullptr;
+    for (int j = w; j < ND; j += kFDWarps) {
+      for (int i = lane; i < 81; i += 32) S.z[w][i] = S.z0[i];
+      if (lane < NL) S.p[w][lane] = S.p0[lane];
+      __syncwarp();
+      if (lane == 0) {
+        if (j < 81) S.z[w][j] = S.z0[j] + delta;
+        else S.p[w][j - 81] = S.p0[j - 81] + delta;
+      }
+      __syncwarp();
+      warp_element_residual(T, lane, S.x, S.z[w], S.p[w], c1, c2, S.P[w], S.tp[w], err,
+                            [&](int i, double s) { S.col[w][i] = (s - S.R0[i]) / delta; });
+      // column j: rows r = lane, lane + 32, lane + 64
+      for (int r = lane; r < ND; r += 32) {
+        const double v = S.col[w][r];
+        if (!isfinite(v)) gfe_raise(err, GFE_DEVERR_NONFINITE);
+        if (Ke) Ke[(size_t)r * ND + j] = v;
+        if (sl && !(r >= 81 && j >= 81)) {
+          const int pos = __ldg(sl + (size_t)r * ND + j);
+          if (pos >= 0) values[pos] += v;
+          else gfe_raise(err, GFE_DEVERR_SLOT);
+        }
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  }
 }
 
 // slot map: for each element (in colour order) and each (r, c), the 0-based CSR position of
@@ -1495,6 +1611,53 @@ extern "C" int gfe_mr_tangent(int32_t n_elem, const int32_t* eq2, const int32_t*
                               double* values, int64_t nnz, double* K_out, int32_t precision, void* stream) {
   return jacobian_entry_point(1, n_elem, eq2, elin, nq2, nlin, xg, color_elems, color_ptr_host, n_colors, dep, cpar,
                               slots, values, nnz, K_out, precision, stream, "gfe_mr_tangent");
+}
+
+extern "C" int gfe_mr_jacobian_fd(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2,
+                                  int32_t nlin, const double* xg, const int32_t* color_elems,
+                                  const int32_t* color_ptr_host, int32_t n_colors, const double* dep,
+                                  const double* cpar, double step, const int32_t* slots, double* values, int64_t nnz,
+                                  double* K_out, void* stream) {
+  const char* fn = "gfe_mr_jacobian_fd";
+  int rc = check_mesh(n_elem, eq2, elin, nq2, nlin, xg, fn);
+  if (rc) return rc;
+  if (!dep || !cpar || !(step > 0.0) || (n_elem > 0 && (!color_elems || !color_ptr_host || n_colors <= 0)))
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (!K_out && (!slots || !values)) return gfe::set_error(GFE_ERR_ARG, "%s: need CSR values + slots or K_out", fn);
+  if (color_ptr_host[0] != 0 || color_ptr_host[n_colors] != n_elem)
+    return gfe::set_error(GFE_ERR_ARG, "%s: colour offsets must run from 0 to n_elem", fn);
+  const Tables* T = nullptr;
+  if ((rc = device_tables(&T))) return rc;
+  cudaStream_t s = gfe::as_stream(stream);
+  const int64_t ndof = 3ll * nq2 + nlin;
+  const size_t sm = sizeof(Tables) + sizeof(FDShared);
+  if ((rc = set_smem((const void*)mr_jacobian_fd_kernel, sm))) return rc;
+  double* parts = nullptr;
+  if ((rc = gfe::scratch_alloc((void**)&parts, sizeof(double) * kNormParts, s, "FD step norm"))) return rc;
+  if (values) {
+    cudaError_t e = cudaMemsetAsync(values, 0, sizeof(double) * (size_t)nnz, s);
+    if (e != cudaSuccess) {
+      gfe::scratch_free(parts, s);
+      return gfe::set_error(GFE_ERR_CUDA, "%s: %s", fn, cudaGetErrorString(e));
+    }
+  }
+  unsigned* err = gfe::device_error_word();
+  void* prof = gfe::stage_begin(GFE_STAGE_MR_JACOBIAN, s);
+  sumsq_parts<<<kNormParts, 256, 0, s>>>(dep, ndof, parts);
+  int launches = 1;
+  for (int c = 0; c < n_colors; ++c) {
+    const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
+    if (cnt <= 0) continue;
+    const int grid = std::min(cnt, 8 * gfe::sm_count());
+    const int32_t* sl = slots ? slots + (size_t)c0 * ND * ND : nullptr;
+    mr_jacobian_fd_kernel<<<grid, kFDWarps * 32, sm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar, T,
+                                                          parts, step, sl, values, K_out, err);
+    ++launches;
+  }
+  gfe::stage_end(GFE_STAGE_MR_JACOBIAN, prof, s, launches);
+  gfe::scratch_free(parts, s);
+  GFE_LAUNCH_CHECK(fn);
+  return GFE_OK;
 }
 
 extern "C" int gfe_mr_residual_vjp(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2,

@@ -25,6 +25,13 @@ from .mesh import RegularMesh, linear_component
 # tensor-core contraction of the Jacobian (tcgen05 kind::tf32): three-pass split / one pass
 GFE_TC_TF32X3, GFE_TC_TF32 = 3, 4
 
+# Jacobian calculation types, mirroring Iron's CMFE_EQUATIONS_JACOBIAN_*_CALCULATED selectors of
+# cmfe_Equations_JacobianCalculationTypeSet (src/opencmiss_iron.F90:25188-25264): "fd" is Iron's
+# default for finite elasticity (one-sided differences of the residual), "analytic" Iron's analytic
+# Jacobian, "consistent" the exact derivative of the residual (this package's default).
+JACOBIAN_TYPES = ("fd", "analytic", "consistent")
+FD_STEP_DEFAULT = 1e-6  # Iron's jacobianFiniteDifferenceStepSize default
+
 
 @functools.lru_cache(maxsize=64)
 def _regular_q2_mesh(nelem: tuple, extent: tuple):
@@ -159,6 +166,65 @@ class MooneyRivlinAssembly:
 
     def element_tangents(self, dep: torch.Tensor, c, precision: str = "fp64", stream=None) -> torch.Tensor:
         return self._element_jacobians("gfe_mr_tangent", dep, c, precision, True, stream, True)
+
+    def jacobian_fd(self, dep: torch.Tensor, c, step: float = FD_STEP_DEFAULT, stream=None, check=True,
+                    dense: bool = False) -> torch.Tensor:
+        """Iron's finite-difference Jacobian (its default for finite elasticity) assembled into
+        self.values, or dense element matrices [E][89][89] with dense=True: column j of every element
+        matrix is (R(dep + delta e_j) - R(dep)) / delta with delta = (1 + ||dep||_2) * step
+        (src/equations_set_routines.F90:2839-2962).  FP64."""
+        if not dense and self.slots is None:
+            self.build_structure(stream)
+        dep = dep.to(self.device, torch.float64).contiguous()
+        cp = self._cpar(c, 1)
+        cptr = self.colour_ptr
+        K = torch.empty((self.n_elements, 89, 89), dtype=torch.float64, device=self.device) if dense else None
+        _lib.call("gfe_mr_jacobian_fd", self.n_elements, _lib.ptr(self.eq2), _lib.ptr(self.elin), self.n_q2,
+                  self.n_lin, _lib.ptr(self.xg), _lib.ptr(self.colour_elems), cptr.ctypes.data_as(C.c_void_p),
+                  len(cptr) - 1, _lib.ptr(dep), _lib.ptr(cp), float(step), None if dense else _lib.ptr(self.slots),
+                  None if dense else _lib.ptr(self.values), 0 if dense else self.nnz, _lib.ptr(K),
+                  _lib.stream_handle(stream))
+        if check:
+            _lib.raise_device_errors("gfe_mr_jacobian_fd", stream)
+        return K if dense else self.values
+
+    # -- Iron's Jacobian calculation type selector ---------------------------------------------
+    @property
+    def jacobian_calculation_type(self) -> str:
+        """'fd' | 'analytic' | 'consistent': which Jacobian evaluate_jacobian() assembles
+        (cmfe_Equations_JacobianCalculationTypeSet, src/opencmiss_iron.F90:25188-25264)."""
+        return getattr(self, "_jac_type", "consistent")
+
+    @jacobian_calculation_type.setter
+    def jacobian_calculation_type(self, kind: str) -> None:
+        if kind not in JACOBIAN_TYPES:
+            raise GfeError(-1, f"Jacobian calculation type must be one of {JACOBIAN_TYPES}, not {kind!r}")
+        self._jac_type = kind
+
+    @property
+    def jacobian_finite_difference_step_size(self) -> float:
+        """Step of the FD Jacobian (cmfe_Equations_JacobianFiniteDifferenceStepSizeSet,
+        src/opencmiss_iron.F90:25271-25348); Iron's default 1e-6."""
+        return getattr(self, "_fd_step", FD_STEP_DEFAULT)
+
+    @jacobian_finite_difference_step_size.setter
+    def jacobian_finite_difference_step_size(self, step: float) -> None:
+        if not step > 0.0:
+            raise GfeError(-1, "the finite-difference step must be positive")
+        self._fd_step = float(step)
+
+    def evaluate_jacobian(self, dep: torch.Tensor, c, precision: str = "fp64", stream=None, check=True,
+                          kind: str | None = None) -> torch.Tensor:
+        """Assemble the Jacobian of the selected calculation type into self.values.  The FD
+        Jacobian is FP64 (differences of FP64 residuals); `precision` applies to the other two."""
+        kind = kind or self.jacobian_calculation_type
+        if kind == "fd":
+            return self.jacobian_fd(dep, c, self.jacobian_finite_difference_step_size, stream, check)
+        if kind == "analytic":
+            return self.jacobian(dep, c, precision, stream, check)
+        if kind == "consistent":
+            return self.tangent(dep, c, precision, stream, check)
+        raise GfeError(-1, f"Jacobian calculation type must be one of {JACOBIAN_TYPES}, not {kind!r}")
 
     def residual_vjp(self, dep: torch.Tensor, c, v: torch.Tensor, stream=None):
         """(v^T dR/d dep, v^T dR/d(c10, c01)) for one or a batch of problems."""

@@ -9,12 +9,13 @@ incremented Dirichlet conditions before each load step
 Defaults mirror Iron's Newton solver (src/solver_routines.F90:17960-18032, 18942-18991):
 absolute tolerance 1e-10 and relative tolerance 1e-5 on the residual norm, solution tolerance
 1e-5 on the step, 50 iterations, backtracking line search with cubic interpolation and
-alpha = 1e-4.  Iron's default Jacobian is its one-sided finite-difference Jacobian; here the
-default is the consistent tangent (the exact derivative of the residual, which the FD Jacobian
-approximates), and Iron's analytic Jacobian is selectable.  The linear solve of each Newton step
+alpha = 1e-4.  Iron's default Jacobian is its one-sided finite-difference Jacobian
+(jacobian="fd", gfe_mr_jacobian_fd, step 1e-6 as Iron's); here the default is the consistent
+tangent (the exact derivative of the residual, which the FD Jacobian approximates), and Iron's
+analytic Jacobian is selectable (jacobian="analytic").  The linear solve of each Newton step
 replaces PETSc KSP: preconditioned MINRES for the consistent tangent (symmetric indefinite) and
-restarted GMRES (Iron's default Krylov method) for Iron's analytic Jacobian, which is not
-symmetric; both are preconditioned by the diagonal of gfe_saddle_preconditioner.
+restarted GMRES (Iron's default Krylov method) for the FD and analytic Jacobians, which are not
+symmetric; all are preconditioned by the diagonal of gfe_saddle_preconditioner.
 
 Precision 'mixed': FP32 basis-gradient contraction for the Jacobian and FP32 Krylov iterations
 (FP32 matrix copy and vectors) inside FP64 refinement residuals; the nonlinear residual, its norm, the line search and the
@@ -120,19 +121,19 @@ class NewtonSolver:
     """Newton's method with a backtracking (cubic) line search on R(dep) = 0 for a
     MooneyRivlinAssembly, with Dirichlet DOFs eliminated."""
 
-    def __init__(self, asm, c, *, jacobian: str = "consistent", precision: str = "fp64",
+    def __init__(self, asm, c, *, jacobian: str = "consistent", precision: str = "fp64", fd_step: float = 1e-6,
                  absolute_tolerance: float = 1e-10, relative_tolerance: float = 1e-5,
                  solution_tolerance: float = 1e-5, maximum_iterations: int = 50, linesearch_alpha: float = 1e-4,
                  linear_relative_tolerance: float = 1e-5, linear_maximum_iterations: int = 50000,
                  linear_solver: str | None = None, gmres_restart: int = 30, stream=None):
-        if jacobian not in ("consistent", "analytic"):
-            raise GfeError(-1, f"unknown Jacobian type {jacobian!r} (consistent | analytic)")
+        if jacobian not in ("consistent", "analytic", "fd"):
+            raise GfeError(-1, f"unknown Jacobian type {jacobian!r} (consistent | analytic | fd)")
         if linear_solver is None:
             linear_solver = "minres" if jacobian == "consistent" else "gmres"
         if linear_solver not in ("minres", "gmres"):
             raise GfeError(-1, f"unknown linear solver {linear_solver!r} (minres | gmres)")
-        if linear_solver == "minres" and jacobian == "analytic":
-            raise GfeError(-1, "Iron's analytic Jacobian is not symmetric: use linear_solver='gmres'")
+        if linear_solver == "minres" and jacobian != "consistent":
+            raise GfeError(-1, f"the {jacobian} Jacobian is not symmetric: use linear_solver='gmres'")
         if precision not in ("fp64", "mixed"):
             raise GfeError(-1, f"unknown precision {precision!r} (fp64 | mixed)")
         if asm.row_ptr is None:
@@ -140,6 +141,7 @@ class NewtonSolver:
         self.asm = asm
         self.c = torch.as_tensor(c, dtype=torch.float64, device=asm.device).reshape(2)
         self.jacobian = jacobian
+        self.fd_step = float(fd_step)
         self.precision = precision
         self.atol = float(absolute_tolerance)
         self.rtol = float(relative_tolerance)
@@ -177,6 +179,8 @@ class NewtonSolver:
         asm = self.asm
         if self.jacobian == "consistent":
             vals = asm.tangent(dep, self.c, precision=self.precision, stream=self.stream)
+        elif self.jacobian == "fd":
+            vals = asm.jacobian_fd(dep, self.c, step=self.fd_step, stream=self.stream)
         else:
             vals = asm.jacobian(dep, self.c, precision=self.precision, stream=self.stream)
         info.jacobian_evaluations += 1
