@@ -89,6 +89,56 @@ int gfe_profile_read(int stage, double* ms_host, int64_t* launches_host, int res
  * (FP32).  Used as the FP64 / FP32 pipe roof of the element kernels. */
 int gfe_probe_fma_rate(int32_t precision, double* gflops_host, void* stream);
 
+/* ---- context and mesh handles ------------------------------------------------------------ */
+
+/* A context owns what Iron keeps per rank around its element loops: the CUDA stream the work is
+ * ordered on (borrowed; NULL = legacy default stream), a device error word of its own (kernels
+ * launched through the context report there, read with gfe_ctx_device_errors), and a cache of
+ * mesh structures keyed by a hash of the connectivity.  Use one context per host thread.  The
+ * context is created on, and must be used with, the current device.  Iron's counterparts are the
+ * equations set's matrices and their structure (EquationsMatrices_CreateFinish ->
+ * EquationsMatrix_StructureCalculate, src/equations_matrices_routines.F90:4316-4602), built once and
+ * reused by every assembly, and the per-rank error state of src/base_routines.F90. */
+typedef struct gfe_ctx gfe_ctx;
+typedef struct gfe_mesh gfe_mesh;
+int gfe_ctx_create(void* stream, gfe_ctx** ctx);
+/* Frees the context and its error word; structures still used by live mesh handles are freed with
+ * the last of them.  Synchronises the context's stream. */
+int gfe_ctx_destroy(gfe_ctx* ctx);
+/* Read and clear the context's device error word (GFE_DEVERR_* bits).  Synchronises the stream. */
+int gfe_ctx_device_errors(gfe_ctx* ctx, uint32_t* bits_host);
+/* Number of distinct mesh structures in the context's cache. */
+int gfe_ctx_cached_meshes(gfe_ctx* ctx, int32_t* count_host);
+
+/* Mesh handle of a general mesh: elem_nodes_host [n_elem][nodes_per_elem] 0-based node numbers in
+ * host memory.  The CSR structure (as gfe_csr_structure: Iron's, 1-based) and a greedy element
+ * colouring are built on the first handle of a connectivity and shared by later handles of the
+ * same connectivity (looked up by hash, confirmed by comparison).  Synchronises the stream. */
+int gfe_mesh_create(gfe_ctx* ctx, int32_t n_elem, int32_t nodes_per_elem, const int32_t* elem_nodes_host,
+                    int32_t n_nodes, gfe_mesh** mesh);
+/* Mesh handle of Iron's regular generated mesh of nx x ny x nz trilinear hexahedra
+ * (GENERATED_MESH_REGULAR_TYPE, src/generated_mesh_routines.F90:1568-1640): the connectivity is
+ * generated, the structure verified as the clipped 27-point stencil, and the assembly may take the
+ * row-owning regular-mesh kernel. */
+int gfe_mesh_create_regular(gfe_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, gfe_mesh** mesh);
+int gfe_mesh_destroy(gfe_mesh* mesh);
+/* The mesh's CSR structure (device pointers owned by the context's cache, valid while the handle
+ * lives): row_ptr [n_rows + 1], col_idx [nnz], both 1-based as Iron stores them; any output may be
+ * NULL.  The analogue of cmfe_DistributedMatrix_StorageLocationsGet (src/opencmiss_iron.F90:45823). */
+int gfe_mesh_csr(const gfe_mesh* mesh, const int32_t** row_ptr, const int32_t** col_idx, int64_t* nnz,
+                 int32_t* n_rows);
+/* Laplace assembly on a trilinear mesh handle (gfe_laplace_assemble, or on a regular mesh with an
+ * FP32-pipe precision gfe_laplace_assemble_regular), on the context's stream and error word:
+ * coords [3][n_nodes], kappa_e [n_elem] or NULL, values [nnz] (FP64) out, values32 / rhs optional.
+ * Replaces EquationsSet_AssembleStaticLinearFEM (src/equations_set_routines.F90:1203-1364) for the
+ * Laplace equations set. */
+int gfe_assemble_laplace(gfe_ctx* ctx, const gfe_mesh* mesh, const double* coords, const double* kappa_e,
+                         double* values, float* values32, double* rhs, int32_t precision);
+/* Jacobi-CG on the mesh's matrix (gfe_cg_solve on the context's stream and error word). */
+int gfe_solve_laplace(gfe_ctx* ctx, const gfe_mesh* mesh, const double* values, const float* values32,
+                      const double* f, const uint8_t* fixed, double* x, double rtol, int32_t max_iters,
+                      int32_t precision, int32_t* iters_host, double* rel_host);
+
 /* ---- CSR structure (K3) ------------------------------------------------------------------ */
 
 /* Compressed-row sparsity of an FEM matrix whose rows and columns are the DOFs of one field

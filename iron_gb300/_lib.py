@@ -54,6 +54,17 @@ SIGNATURES = {
     "gfe_profile_enable": (C.c_int, [C.c_int]),
     "gfe_profile_read": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int64), C.c_int]),
     "gfe_probe_fma_rate": (C.c_int, [i32, C.POINTER(C.c_double), vp]),
+    "gfe_ctx_create": (C.c_int, [vp, C.POINTER(vp)]),
+    "gfe_ctx_destroy": (C.c_int, [vp]),
+    "gfe_ctx_device_errors": (C.c_int, [vp, C.POINTER(C.c_uint32)]),
+    "gfe_ctx_cached_meshes": (C.c_int, [vp, C.POINTER(C.c_int32)]),
+    "gfe_mesh_create": (C.c_int, [vp, i32, i32, vp, i32, C.POINTER(vp)]),
+    "gfe_mesh_create_regular": (C.c_int, [vp, i32, i32, i32, C.POINTER(vp)]),
+    "gfe_mesh_destroy": (C.c_int, [vp]),
+    "gfe_mesh_csr": (C.c_int, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
+    "gfe_assemble_laplace": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, i32]),
+    "gfe_solve_laplace": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_double)]),
     "gfe_csr_structure": (C.c_int, [i32, i32, vp, i32, vp, vp, i64, C.POINTER(C.c_int64), vp]),
     "gfe_laplace_assemble": (C.c_int, [i32, i32, vp, vp, vp, vp, vp, i32, vp, vp, i64, vp, vp, vp, i32, vp]),
     "gfe_laplace_element_matrices": (C.c_int, [i32, i32, vp, vp, vp, vp, i32, vp]),

@@ -38,6 +38,9 @@ unsigned* device_error_word() {
   return g_err_word[dev];
 }
 
+unsigned* thread_error_word() { return t_err_word; }
+void set_thread_error_word(unsigned* w) { t_err_word = w; }
+
 int scratch_alloc(void** p, size_t bytes, cudaStream_t s, const char* what) {
   *p = nullptr;
   if (bytes == 0) bytes = 16;

@@ -14,8 +14,12 @@ namespace gfe {
 // Record the message of a failure for gfe_last_error() on this host thread and return `code`.
 int set_error(int code, const char* fmt, ...);
 
-// Device-resident error word of the current device (lazily allocated once per device).
+// Device-resident error word of the current device (lazily allocated once per device), or the
+// word this host thread routed its kernels to (gfe_set_thread_error_word).
 unsigned* device_error_word();
+// The calling thread's override of the error word (nullptr: the per-device word), and its reset.
+unsigned* thread_error_word();
+void set_thread_error_word(unsigned* w);
 
 // Stream-ordered scratch allocation; returns GFE_ERR_NOMEM with a message on failure.
 int scratch_alloc(void** p, size_t bytes, cudaStream_t s, const char* what);
