@@ -239,7 +239,9 @@ laplace_assemble_color(const int32_t* __restrict__ elems, int32_t count, int32_t
   int nd[8];
   T x[3][8];
   load_element<T>(e, elem_nodes, coords, n_nodes, nd, x);
-  const T kap = from_double<T>(kappa ? __ldg(kappa + e) : 1.0);
+  const double kd = kappa ? __ldg(kappa + e) : 1.0;
+  if (!isfinite(kd)) gfe_raise(err, GFE_DEVERR_NONFINITE);
+  const T kap = from_double<T>(kd);
   T p, q;
   gauss_pq(p, q);
   T K[36];
@@ -277,7 +279,9 @@ laplace_element_kernel(int32_t n_elem, int32_t n_nodes, const int32_t* __restric
   int nd[8];
   T x[3][8];
   load_element<T>(e, elem_nodes, coords, n_nodes, nd, x);
-  const T kap = from_double<T>(kappa ? kappa[e] : 1.0);
+  const double kd = kappa ? kappa[e] : 1.0;
+  if (!isfinite(kd)) gfe_raise(err, GFE_DEVERR_NONFINITE);
+  const T kap = from_double<T>(kd);
   T p, q;
   gauss_pq(p, q);
   T K[36];
@@ -397,7 +401,7 @@ laplace_regular_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__
   const long long e_share = W * (blockIdx.x + 1) / gridDim.x;
   T p, q;
   gauss_pq(p, q);
-  bool bad = false;
+  bool bad = false, nonfinite = false;
   while (s < e_share) {  // uniform across the CTA
     const long long col = s / nl;
     const int off = (int)(s - col * nl);
@@ -422,7 +426,9 @@ laplace_regular_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__
           for (int c = 0; c < 3; ++c) x[c][m] = load_coord(coords + c * NXY * NZ + n);
         }
         const long long e = (long long)ex + (long long)ey * nx + (long long)ez * nx * ny;
-        const T kap = from_double<T>(kappa ? __ldg(kappa + e) : 1.0);
+        const double kd = kappa ? __ldg(kappa + e) : 1.0;
+        if (!isfinite(kd)) nonfinite = true;
+        const T kap = from_double<T>(kd);
         T K[36];
         if (!laplace_hex8<T>(x, kap, p, q, K)) bad = true;
 #pragma unroll
@@ -510,6 +516,7 @@ laplace_regular_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__
     }
   }
   if (bad) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+  if (nonfinite) gfe_raise(err, GFE_DEVERR_NONFINITE);
 }
 
 // Persistent grid of the regular-mesh kernel: the resident CTAs, but no more than one CTA per

@@ -378,7 +378,9 @@ laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, 
 #pragma unroll
       for (int c = 0; c < 3; ++c) sx[c][n] = from_double<T>(coords[(size_t)c * n_nodes + node] * sf);
     }
-    const T kap = from_double<T>(kappa ? kappa[e] : 1.0);
+    const double kd = kappa ? kappa[e] : 1.0;
+    if (!isfinite(kd)) gfe_raise(err, GFE_DEVERR_NONFINITE);
+    const T kap = from_double<T>(kd);
     group_sync<GROUP>();
     // the 9 ng Jacobian entries dx_c/dxi_a spread over the group's lanes, then one lane a Gauss
     // point for the metric: a lane per Gauss point alone leaves most lanes idle through the
@@ -467,7 +469,9 @@ laplace_tet4_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes
 #pragma unroll
       for (int c = 0; c < 3; ++c) x[c][n] = from_double<T>(coords[(size_t)c * n_nodes + node[n]]);
     }
-    const T kap = from_double<T>(kappa ? kappa[e] : 1.0);
+    const double kd = kappa ? kappa[e] : 1.0;
+    if (!isfinite(kd)) gfe_raise(err, GFE_DEVERR_NONFINITE);
+    const T kap = from_double<T>(kd);
     Acc K[10];
 #pragma unroll
     for (int p = 0; p < 10; ++p) K[p] = from_double<Acc>(0.0);

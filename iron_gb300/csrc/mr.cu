@@ -537,22 +537,16 @@ __device__ __forceinline__ Dual operator/(Dual a, Dual b) {
 }
 __device__ __forceinline__ Dual operator/(Dual a, double b) { return {a.v / b, a.d / b}; }
 __device__ __forceinline__ Dual operator+(Dual a, double b) { return {a.v + b, a.d}; }
-__device__ __forceinline__ double val(double a) { return a; }
-__device__ __forceinline__ double val(Dual a) { return a.v; }
-__device__ __forceinline__ double dsqrt(double a) { return sqrt(a); }
 __device__ __forceinline__ Dual dsqrt(Dual a) {
   const double s = sqrt(a.v);
   return {s, a.d / (2.0 * s)};
 }
-__device__ __forceinline__ double dabs(double a) { return fabs(a); }
 __device__ __forceinline__ Dual dabs(Dual a) { return a.v < 0.0 ? -a : a; }
 // x^(-1/3)
-__device__ __forceinline__ double dpowm13(double a) { return pow(a, -1.0 / 3.0); }
 __device__ __forceinline__ Dual dpowm13(Dual a) {
   const double v = pow(a.v, -1.0 / 3.0);
   return {v, -v / (3.0 * a.v) * a.d};
 }
-__device__ __forceinline__ double cst(double a) { return a; }
 
 template <typename T>
 __device__ __forceinline__ T tdet3(const T A[3][3]) {
@@ -580,7 +574,6 @@ struct DualF {
 };
 __device__ __forceinline__ DualF operator+(DualF a, DualF b) { return {a.v + b.v, a.d + b.d}; }
 __device__ __forceinline__ DualF operator-(DualF a, DualF b) { return {a.v - b.v, a.d - b.d}; }
-__device__ __forceinline__ DualF operator-(DualF a) { return {-a.v, -a.d}; }
 __device__ __forceinline__ DualF operator*(DualF a, DualF b) { return {a.v * b.v, a.v * b.d + a.d * b.v}; }
 __device__ __forceinline__ DualF operator*(float a, DualF b) { return {a * b.v, a * b.d}; }
 __device__ __forceinline__ DualF operator*(DualF a, float b) { return {a.v * b, a.d * b}; }
@@ -731,156 +724,259 @@ __device__ __forceinline__ void point_dP(const GPInT<S>& in, int seed, S c1, S c
   if (Jz_v) *Jz_v = Jz.v;
 }
 
-constexpr int kTanThreads = 128;
+// ----------------------------------------------------------------------------------------------
+// Reverse-mode adjoint of the residual (one reverse sweep per Gauss point)
+// ----------------------------------------------------------------------------------------------
+// For a cotangent v of the element residual, the u-rows give the cotangent of P_g,
+// V_g[xi][mh] = sum_ms v(mh, ms) g_ms[xi], and the p-rows that of w (J_z - J_x), Vp_g = sum_ms
+// v_p(ms) psi_ms.  One reverse sweep through the formulas of point_P, in the opposite order,
+// yields Zbar = dL/dZ (3x3), pbar = dL/dp and the material cotangents (c1bar, c2bar) at the cost
+// of a few forward evaluations, instead of the 10 forward-mode passes of the tangent.  The
+// element's du is then sum_g Zbar_g[c][k] g_ms[k] (u) and sum_g pbar_g psi_ms (p).
+//   Q = Z^-1 sgd,  P = w J_z Q                      Qbar = w J_z V,  Jzbar += w V:Q
+//   sgd = sg - tr(sg)/3 I + p I                    sgbar = dev(sgdbar), pbar = tr(sgdbar)
+//   sg = Fb S Fb^T / J                             Hbar = sgbar / J, FSbar = Hbar Fb, Fbbar = Hbar^T FS
+//   S = t1 C + t2 I, C = Fb^T Fb, t1 = -2 c2, t2 = 2 (I1 c2 + c1), I1 = tr C
+//   Fb = s Z A, s = J^(-1/3), J = J_z / J_x, J_z = |det Z| (dJ_z/dZ = J_z Z^-T)
+__device__ __forceinline__ void mm3(const double A[3][3], const double B[3][3], double C[3][3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[i][j] = A[i][0] * B[0][j] + A[i][1] * B[1][j] + A[i][2] * B[2][j];
+}
+// C = A^T B
+__device__ __forceinline__ void mtm3(const double A[3][3], const double B[3][3], double C[3][3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[i][j] = A[0][i] * B[0][j] + A[1][i] * B[1][j] + A[2][i] * B[2][j];
+}
+// C = A B^T
+__device__ __forceinline__ void mmt3(const double A[3][3], const double B[3][3], double C[3][3]) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[i][j] = A[i][0] * B[j][0] + A[i][1] * B[j][1] + A[i][2] * B[j][2];
+}
+__device__ __forceinline__ double dot9(const double A[3][3], const double B[3][3]) {
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) s += A[i][j] * B[i][j];
+  return s;
+}
 
-struct TanShared {
-  double x[81], z[81], p[8];
-  GPIn in[NG];
-  double dPdZ[NG][10][9];  // [g][seed][xi*3+mh]
-  double wJZi[NG][9];      // w J_z Z^-1[zeta][nh] (p-row coefficients)
+__device__ __forceinline__ void point_P_vjp(const GPIn& in, double c1, double c2, const double V[3][3], double Vp,
+                                            double Zb[3][3], double& pb, double& c1b, double& c2b) {
+  // forward
+  double G[3][3];
+  mtm3(in.Z, in.Z, G);
+  const double Jz = sqrt(fabs(det3(G)));
+  double Zi[3][3];
+  inv3(in.Z, Zi);
+  const double J = Jz / in.Jx;
+  const double s = pow(J, -1.0 / 3.0);
+  double M[3][3], Fb[3][3];
+  mm3(in.Z, in.A, M);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Fb[i][j] = M[i][j] * s;
+  double C[3][3];
+  mtm3(Fb, Fb, C);
+  const double I1 = C[0][0] + C[1][1] + C[2][2];
+  const double t1 = -2.0 * c2, t2 = 2.0 * (I1 * c2 + c1);
+  double S[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) S[i][j] = t1 * C[i][j] + (i == j ? t2 : 0.0);
+  double FS[3][3], sg[3][3];
+  mm3(Fb, S, FS);
+  mmt3(FS, Fb, sg);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) sg[i][j] /= J;
+  const double tr3 = (sg[0][0] + sg[1][1] + sg[2][2]) / 3.0;
+  double sgd[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) sgd[i][j] = sg[i][j] - (i == j ? tr3 - in.p : 0.0);
+  double Q[3][3];
+  mm3(Zi, sgd, Q);
+  const double wj = Jz * in.w;
+  // reverse
+  double Jzb = in.w * (dot9(V, Q) + Vp);  // P = wj Q and the p-row term w (J_z - J_x)
+  double Qb[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Qb[i][j] = wj * V[i][j];
+  double Zib[3][3], sgdb[3][3];
+  mmt3(Qb, sgd, Zib);  // Q = Zi sgd: Zibar = Qbar sgd^T, sgdbar = Zi^T Qbar
+  mtm3(Zi, Qb, sgdb);
+  const double trb = sgdb[0][0] + sgdb[1][1] + sgdb[2][2];
+  pb = trb;
+  double sgb[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) sgb[i][j] = sgdb[i][j] - (i == j ? trb / 3.0 : 0.0);
+  // sg = H / J with H = FS Fb^T
+  double Jb = -dot9(sgb, sg) / J;
+  double Hb[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Hb[i][j] = sgb[i][j] / J;
+  double FSb[3][3], Fbb[3][3], T1[3][3];
+  mm3(Hb, Fb, FSb);   // H = FS Fb^T: FSbar = Hbar Fb
+  mtm3(Hb, FS, Fbb);  // Fbbar += Hbar^T FS
+  // FS = Fb S: Fbbar += FSbar S^T (S symmetric), Sbar = Fb^T FSbar
+  mm3(FSb, S, T1);
+  double Sb[3][3];
+  mtm3(Fb, FSb, Sb);
+  const double t2b = Sb[0][0] + Sb[1][1] + Sb[2][2];
+  const double t1b = dot9(Sb, C);
+  const double I1b = 2.0 * c2 * t2b;
+  c1b = 2.0 * t2b;
+  c2b = 2.0 * I1 * t2b - 2.0 * t1b;
+  double Cb[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Cb[i][j] = t1 * Sb[i][j] + (i == j ? I1b : 0.0);
+  // C = Fb^T Fb: Fbbar += Fb (Cbar + Cbar^T)
+  double Cs[3][3], T2[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Cs[i][j] = Cb[i][j] + Cb[j][i];
+  mm3(Fb, Cs, T2);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Fbb[i][j] += T1[i][j] + T2[i][j];
+  // Fb = s M: sbar = Fbbar : M, Mbar = s Fbbar; M = Z A: Zbar += Mbar A^T
+  const double sb = dot9(Fbb, M);
+  double Mb[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Mb[i][j] = s * Fbb[i][j];
+  mmt3(Mb, in.A, Zb);
+  // s = J^(-1/3), J = J_z / J_x
+  Jb += sb * (-s / (3.0 * J));
+  Jzb += Jb / in.Jx;
+  // Zi = Z^-1: Zbar -= Zi^T Zibar Zi^T;  J_z = |det Z|: Zbar += Jzbar J_z Zi^T
+  double T3[3][3], T4[3][3];
+  mtm3(Zi, Zib, T3);   // Zi^T Zibar
+  mmt3(T3, Zi, T4);    // (Zi^T Zibar) Zi^T
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Zb[i][j] += -T4[i][j] + Jzb * Jz * Zi[j][i];
+}
+
+constexpr int kAdjWarps = 4;
+
+struct AdjWarpShared {
+  double x[81], z[81], p[8], v[ND];
+  double Zb[NG][9], pb[NG], cb[NG][2];
   int dofs[ND];
 };
 
-__device__ void tangent_points(const Tables& T, TanShared& S, double c1, double c2) {
-  if (threadIdx.x < NG) gauss_inputs(T, threadIdx.x, S.z, S.x, S.p, S.in[threadIdx.x]);
-  __syncthreads();
-  for (int task = threadIdx.x; task < NG * 10; task += blockDim.x) {
-    const int g = task / 10, seed = task % 10;
-    double o[9];
-    point_dP<double>(S.in[g], seed, c1, c2, o, nullptr);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) S.dPdZ[g][seed][k] = o[k];
-  }
-  if (threadIdx.x < NG) {
-    const GPIn& in = S.in[threadIdx.x];
-    double Zi[3][3];
-    const double dz = inv3(in.Z, Zi);
-    double G[3][3];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) G[i][j] = in.Z[0][i] * in.Z[0][j] + in.Z[1][i] * in.Z[1][j] + in.Z[2][i] * in.Z[2][j];
-    const double Jz = sqrt(fabs(det3(G)));
-    (void)dz;
-    for (int z = 0; z < 3; ++z)
-      for (int nh = 0; nh < 3; ++nh) S.wJZi[threadIdx.x][z * 3 + nh] = in.w * Jz * Zi[z][nh];
-  }
-  __syncthreads();
-}
-
-__device__ __forceinline__ void load_element_state(int e, const int32_t* eq2, const int32_t* elin, int nq2,
-                                                   const double* xg, const double* dep, double* sx, double* sz,
-                                                   double* sp, int* dofs) {
-  for (int i = threadIdx.x; i < NQ; i += blockDim.x) {
-    const int n = __ldg(eq2 + (size_t)e * NQ + i);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      sx[c * NQ + i] = __ldg(xg + (size_t)c * nq2 + n);
-      sz[c * NQ + i] = dep[(size_t)c * nq2 + n];
-      if (dofs) dofs[c * NQ + i] = c * nq2 + n;
-    }
-  }
-  if (threadIdx.x < NL) {
-    const int n = __ldg(elin + (size_t)e * NL + threadIdx.x);
-    sp[threadIdx.x] = dep[(size_t)3 * nq2 + n];
-    if (dofs) dofs[81 + threadIdx.x] = 3 * nq2 + n;
-  }
-}
-
-// Vector-Jacobian products of `batch` problems: du[b] = v[b]^T dR/d(dep), dc[b] = v[b]^T dR/d(c10, c01).
-// Elements colour by colour (du scatter without conflicts); dc accumulated per element into
-// dc_elem[b][E][2] and summed afterwards in fixed order.
-__global__ void __launch_bounds__(kTanThreads)
-mr_vjp_kernel(const int32_t* __restrict__ elems, int32_t count, int32_t batch, const int32_t* __restrict__ eq2,
-              const int32_t* __restrict__ elin, int32_t nq2, int32_t nlin, const double* __restrict__ xg,
-              const double* __restrict__ dep, const double* __restrict__ cpar, const double* __restrict__ v,
-              const Tables* __restrict__ Tg, double* __restrict__ du, double* __restrict__ dc_elem, int32_t n_elem) {
+// Reverse-mode vector-Jacobian products: one warp per (element, parameter set) of a colour.
+__global__ void __launch_bounds__(kAdjWarps * 32)
+mr_vjp_reverse_kernel(const int32_t* __restrict__ elems, int32_t count, int32_t batch,
+                      const int32_t* __restrict__ eq2, const int32_t* __restrict__ elin, int32_t nq2, int32_t nlin,
+                      const double* __restrict__ xg, const double* __restrict__ dep, const double* __restrict__ cpar,
+                      const double* __restrict__ v, const Tables* __restrict__ Tg, double* __restrict__ du,
+                      double* __restrict__ dc_elem, int32_t n_elem, unsigned* err) {
   extern __shared__ double smem[];
   Tables& T = *reinterpret_cast<Tables*>(smem);
-  TanShared& S = *reinterpret_cast<TanShared*>(smem + sizeof(Tables) / sizeof(double));
-  double* vv = reinterpret_cast<double*>(&S + 1);  // [89] element adjoint
-  double* Vg = vv + ND;                            // [27][9] V_g[xi][mh] ; [27] Vp_g
-  double* Vp = Vg + NG * 9;
-  double* dcs = Vp + NG;                           // [27][2]
+  AdjWarpShared* W = reinterpret_cast<AdjWarpShared*>(smem + sizeof(Tables) / sizeof(double));
   for (int i = threadIdx.x; i < (int)(sizeof(Tables) / sizeof(double)); i += blockDim.x)
     smem[i] = reinterpret_cast<const double*>(Tg)[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  AdjWarpShared& S = W[w];
   const int64_t ndof = 3ll * nq2 + nlin;
-  for (long long item = blockIdx.x; item < (long long)count * batch; item += gridDim.x) {
+  const long long total = (long long)count * batch;
+  for (long long item = (long long)blockIdx.x * kAdjWarps + w; item < total; item += (long long)gridDim.x * kAdjWarps) {
     const int b = (int)(item / count);
-    const int li = (int)(item % count);
-    const int e = __ldg(elems + li);
+    const int e = __ldg(elems + (item % count));
     const double* d = dep + b * ndof;
+    const double* vb = v + b * ndof;
+    for (int i = lane; i < NQ; i += 32) {
+      const int n = __ldg(eq2 + (size_t)e * NQ + i);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        S.x[c * NQ + i] = __ldg(xg + (size_t)c * nq2 + n);
+        S.z[c * NQ + i] = d[(size_t)c * nq2 + n];
+        S.dofs[c * NQ + i] = c * nq2 + n;
+        S.v[c * NQ + i] = vb[(size_t)c * nq2 + n];
+      }
+    }
+    if (lane < NL) {
+      const int n = __ldg(elin + (size_t)e * NL + lane);
+      S.p[lane] = d[(size_t)3 * nq2 + n];
+      S.dofs[81 + lane] = 3 * nq2 + n;
+      S.v[81 + lane] = vb[(size_t)3 * nq2 + n];
+    }
     const double c1 = cpar[2 * b], c2 = cpar[2 * b + 1];
-    __syncthreads();
-    load_element_state(e, eq2, elin, nq2, xg, d, S.x, S.z, S.p, S.dofs);
-    __syncthreads();
-    for (int i = threadIdx.x; i < ND; i += blockDim.x) vv[i] = v[b * ndof + S.dofs[i]];
-    tangent_points(T, S, c1, c2);  // contains __syncthreads
-    // V_g[xi][mh] = sum_ms v(mh,ms) g_ms[xi];  Vp_g = sum_ms v_p(ms) psi_ms
-    for (int t = threadIdx.x; t < NG * 10; t += blockDim.x) {
-      const int g = t / 10, k = t % 10;
-      if (k < 9) {
-        const int xi = k / 3, mh = k % 3;
-        double s = 0.0;
-        for (int ms = 0; ms < NQ; ++ms) s += vv[mh * NQ + ms] * T.dphi[g][xi][ms];
-        Vg[g * 9 + k] = s;
-      } else {
-        double s = 0.0;
-        for (int ms = 0; ms < NL; ++ms) s += vv[81 + ms] * T.psi[g][ms];
-        Vp[g] = s;
-      }
-    }
-    __syncthreads();
-    // dc: P is affine in (c1, c2) with the pressure term independent of c: dP/dc1 = P(1,0,p=0)
-    if (threadIdx.x < NG) {
-      const int g = threadIdx.x;
-      const GPIn& in = S.in[g];
-      double acc[2];
-      for (int q = 0; q < 2; ++q) {
-        double Pm[3][3], Jz;
-        point_P<double>(in.Z, in.A, in.Jx, in.w, 0.0, q == 0 ? 1.0 : 0.0, q == 0 ? 0.0 : 1.0, Pm, Jz);
-        double s = 0.0;
-        for (int xi = 0; xi < 3; ++xi)
-          for (int mh = 0; mh < 3; ++mh) s += Vg[g * 9 + xi * 3 + mh] * Pm[xi][mh];
-        acc[q] = s;
-      }
-      dcs[g * 2] = acc[0];
-      dcs[g * 2 + 1] = acc[1];
-    }
-    __syncthreads();
-    if (threadIdx.x < 2) {
-      double s = 0.0;
-      for (int g = 0; g < NG; ++g) s += dcs[g * 2 + threadIdx.x];
-      dc_elem[((size_t)b * n_elem + e) * 2 + threadIdx.x] = s;
-    }
-    // du entries: u columns (nh, ns) and p columns
-    double* dub = du + b * ndof;
-    for (int cidx = threadIdx.x; cidx < ND; cidx += blockDim.x) {
-      double s = 0.0;
-      if (cidx < 81) {
-        const int nh = cidx / NQ, ns = cidx % NQ;
-        for (int g = 0; g < NG; ++g) {
+    __syncwarp();
+    if (lane < NG) {
+      const int g = lane;
+      GPIn in;
+      gauss_inputs(T, g, S.z, S.x, S.p, in);
+      double V[3][3];
+#pragma unroll
+      for (int xi = 0; xi < 3; ++xi)
+#pragma unroll
+        for (int mh = 0; mh < 3; ++mh) {
           double t = 0.0;
-#pragma unroll
-          for (int zeta = 0; zeta < 3; ++zeta) {
-            const double* dp = S.dPdZ[g][nh * 3 + zeta];
-            double vz = 0.0;
-#pragma unroll
-            for (int k = 0; k < 9; ++k) vz += Vg[g * 9 + k] * dp[k];
-            vz += Vp[g] * S.wJZi[g][zeta * 3 + nh];
-            t += vz * T.dphi[g][zeta][ns];
-          }
-          s += t;
+          for (int ms = 0; ms < NQ; ++ms) t += S.v[mh * NQ + ms] * T.dphi[g][xi][ms];
+          V[xi][mh] = t;
         }
-      } else {
-        const int ns = cidx - 81;
-        for (int g = 0; g < NG; ++g) {
-          double vz = 0.0;
+      double Vp = 0.0;
 #pragma unroll
-          for (int k = 0; k < 9; ++k) vz += Vg[g * 9 + k] * S.dPdZ[g][9][k];
-          s += vz * T.psi[g][ns];
-        }
-      }
-      dub[S.dofs[cidx]] += s;
+      for (int ms = 0; ms < NL; ++ms) Vp += S.v[81 + ms] * T.psi[g][ms];
+      double Zb[3][3], pb, c1b, c2b;
+      point_P_vjp(in, c1, c2, V, Vp, Zb, pb, c1b, c2b);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) S.Zb[g][i * 3 + k] = Zb[i][k];
+      S.pb[g] = pb;
+      S.cb[g][0] = c1b;
+      S.cb[g][1] = c2b;
     }
+    __syncwarp();
+    if (lane < 2) {
+      double t = 0.0;
+      for (int g = 0; g < NG; ++g) t += S.cb[g][lane];
+      dc_elem[((size_t)b * n_elem + e) * 2 + lane] = t;
+    }
+    double* dub = du + b * ndof;
+    for (int i = lane; i < ND; i += 32) {
+      double t = 0.0;
+      if (i < 81) {
+        const int c = i / NQ, ns = i % NQ;
+        for (int g = 0; g < NG; ++g)
+          t += S.Zb[g][c * 3 + 0] * T.dphi[g][0][ns] + S.Zb[g][c * 3 + 1] * T.dphi[g][1][ns] +
+               S.Zb[g][c * 3 + 2] * T.dphi[g][2][ns];
+      } else {
+        const int ns = i - 81;
+        for (int g = 0; g < NG; ++g) t += S.pb[g] * T.psi[g][ns];
+      }
+      if (!isfinite(t)) gfe_raise(err, GFE_DEVERR_NONFINITE);
+      dub[S.dofs[i]] += t;
+    }
+    __syncwarp();
   }
 }
 
@@ -912,7 +1008,7 @@ __global__ void sum_dc(const double* __restrict__ dc_elem, int32_t n_elem, int32
 // space with Z^-1 = dxi/dz (dphi/dz = Z^-T g), only the lower u-u triangle evaluated and mirrored
 // to the upper (:1269-1274), p-u = J_z w dphi_ns/dz_nh psi_ms, u-p = J_z w (push(C^-1) dphi_ms)_mh
 // psi_ns.  Consistent tangent: D_g^(mh,nh)[xi][zeta] = dP[xi][mh]/dZ[nh][zeta] from the forward-mode
-// passes of tangent_points, Hv = dP/dp, Pv = w J_z Z^-1.
+// passes of point_dP, Hv = dP/dp, Pv = w J_z Z^-1.
 
 // Iron's per-Gauss-point tangent blocks in spatial coordinates (src/finite_elasticity_routines.F90:
 // 649-795 and 1072-1192): sub[0..2] = J_z w (c_sub + sigma) for the diagonal component blocks,
@@ -1405,8 +1501,6 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
   if (warp == 0 && S.abort < 2) tc::tmem_dealloc(tmem, 64);
 }
 
-size_t vjp_smem() { return sizeof(Tables) + sizeof(TanShared) + sizeof(double) * (ND + NG * 9 + NG + NG * 2); }
-
 size_t residual_smem() { return sizeof(Tables) + kResWarps * sizeof(double) * (81 + 81 + 8 + NG * 9 + NG + 48); }
 
 int check_mesh(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin, const double* xg,
@@ -1500,7 +1594,6 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
   } else {
     TK = T;
   }
-  const size_t gsm = sizeof(Tables) + sizeof(GPShared<double>);
   const size_t gsm_k = sizeof(TablesT<KF>) + sizeof(GPShared<KF>);
   const size_t csm = sizeof(ContractShared<TS>);
   const void* gk = mode == 0 ? (const void*)mr_gp_kernel<TS, false, KF> : (const void*)mr_gp_kernel<TS, true, KF>;
@@ -1679,15 +1772,16 @@ extern "C" int gfe_mr_residual_vjp(int32_t n_elem, const int32_t* eq2, const int
   double* dc_elem = nullptr;
   if ((rc = gfe::scratch_alloc((void**)&dc_elem, sizeof(double) * 2 * (size_t)n_elem * batch, s, "vjp partials")))
     return rc;
-  const size_t sm = vjp_smem();
-  if ((rc = set_smem((const void*)mr_vjp_kernel, sm))) { gfe::scratch_free(dc_elem, s); return rc; }
+  const size_t sm = sizeof(Tables) + kAdjWarps * sizeof(AdjWarpShared);
+  if ((rc = set_smem((const void*)mr_vjp_reverse_kernel, sm))) { gfe::scratch_free(dc_elem, s); return rc; }
+  unsigned* err = gfe::device_error_word();
   for (int c = 0; c < n_colors; ++c) {
     const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
     if (cnt <= 0) continue;
     const long long items = (long long)cnt * batch;
-    const int grid = (int)std::min<long long>(items, 8ll * gfe::sm_count());
-    mr_vjp_kernel<<<grid, kTanThreads, sm, s>>>(color_elems + c0, cnt, batch, eq2, elin, nq2, nlin, xg, dep, cpar, v,
-                                                T, du, dc_elem, n_elem);
+    const int grid = (int)std::min<long long>((items + kAdjWarps - 1) / kAdjWarps, 16ll * gfe::sm_count());
+    mr_vjp_reverse_kernel<<<grid, kAdjWarps * 32, sm, s>>>(color_elems + c0, cnt, batch, eq2, elin, nq2, nlin, xg,
+                                                           dep, cpar, v, T, du, dc_elem, n_elem, err);
   }
   sum_dc<<<batch, 32, 0, s>>>(dc_elem, n_elem, batch, dc);
   gfe::scratch_free(dc_elem, s);

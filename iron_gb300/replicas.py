@@ -12,6 +12,11 @@ from __future__ import annotations
 import torch
 
 
+class ReplicaLost(RuntimeError):
+    """A collective of the replica bookkeeping failed: another rank left the job (exited, was
+    killed, or stopped answering within the process group's timeout)."""
+
+
 def _active() -> bool:
     return torch.distributed.is_available() and torch.distributed.is_initialized()
 
@@ -22,7 +27,10 @@ def world_size() -> int:
 
 def barrier() -> None:
     if _active():
-        torch.distributed.barrier()
+        try:
+            torch.distributed.barrier()
+        except Exception as e:  # gloo / NCCL report a lost peer as various RuntimeErrors
+            raise ReplicaLost(f"barrier failed: {e}") from e
 
 
 def max_over_replicas(value: float, device: torch.device | None = None) -> float:
@@ -31,7 +39,10 @@ def max_over_replicas(value: float, device: torch.device | None = None) -> float
     if not _active():
         return float(value)
     t = torch.tensor([float(value)], dtype=torch.float64, device=device)
-    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    try:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    except Exception as e:
+        raise ReplicaLost(f"maximum over replicas failed: {e}") from e
     return float(t.item())
 
 

@@ -91,6 +91,12 @@ class Request:
     t_done: float = math.nan
     result: np.ndarray | None = field(default=None, repr=False)
     info: dict = field(default_factory=dict)
+    cancelled: bool = False
+
+    def cancel(self) -> None:
+        """Withdraw the request.  A request still queued (not yet admitted) is dropped by the
+        engine and never runs; one already admitted runs to completion."""
+        self.cancelled = True
 
     @property
     def elements(self) -> int:
@@ -589,6 +595,10 @@ class ServingEngine:
                     finally:
                         self.cv.acquire()
                     compact[0] = False
+                # requests withdrawn while queued are dropped without running
+                for req in [r for r in pending if r.cancelled]:
+                    pending.remove(req)
+                    done_count += 1
                 # admit in arrival order; a request that does not fit may be overtaken
                 i = 0
                 while i < len(pending) and free_workers:
@@ -664,12 +674,17 @@ class ServingEngine:
 
 
 def summarize(reqs: list[Request]) -> dict:
+    cancelled = sum(1 for r in reqs if r.cancelled and math.isnan(r.t_admit))
+    reqs = [r for r in reqs if not (r.cancelled and math.isnan(r.t_admit))]
+    if not reqs:
+        return {"requests": 0, "cancelled": cancelled}
     lat = np.array([r.latency for r in reqs]) * 1e3
     t_end = max(r.t_done for r in reqs)
     t_first = min(r.arrival for r in reqs)
     span = t_end - t_first
     E = sum(r.elements for r in reqs)
-    out = {"requests": len(reqs), "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+    out = {"requests": len(reqs), "cancelled": cancelled,
+           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
            "mean_ms": float(lat.mean()), "max_ms": float(lat.max()), "span_s": span,
            "requests_per_s": len(reqs) / span, "elements_per_s": E / span}
     for kind in ("laplace", "mr"):
