@@ -52,7 +52,7 @@ def parse():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=2000, help="serve workload: requests in the stream")
     ap.add_argument("--serve-workers", type=int, default=8, help="serve workload: concurrent request slots")
-    ap.add_argument("--cpu-sample-n", type=int, default=96, help="side of the CPU-baseline sample mesh")
+    ap.add_argument("--cpu-sample-n", type=int, default=48, help="side of the single-core CPU-baseline sample mesh")
     return ap.parse_args()
 
 
@@ -163,20 +163,23 @@ def profile_traffic_per_unit(kernel: str):
     return None
 
 
-def cpu_baseline(n_sample: int, threads: int):
-    """The oracle (Iron's algorithm restated in C++) timed on a bounded sample on the host cores."""
+def cpu_baseline(n_sample: int, threads: int, structure=None):
+    """The oracle (Iron's algorithm restated in C++) timed on an n_sample^3 mesh of the workload on
+    `threads` host cores.  Returns (elements/s, seconds, elements, oracle values, (row_ptr, col_idx))."""
     import oracle
 
     m, kappa = make_problem(n_sample, seed=0)
-    rp, ci = oracle.csr_structure(m.elem_nodes, m.n_nodes)
+    rp, ci = structure if structure is not None else oracle.csr_structure(m.elem_nodes, m.n_nodes)
     # the timing build: the compiler's default FMA contraction, as a normal build of Iron would have
     prev = oracle.use_build("timing")
-    oracle.laplace_assemble(3, [1, 1, 1], [2, 2, 2], m.elem_nodes[:64], m.coords, kappa[:64], rp, ci, 1)
-    t0 = time.perf_counter()
-    oracle.laplace_assemble(3, [1, 1, 1], [2, 2, 2], m.elem_nodes, m.coords, kappa, rp, ci, threads)
-    dt = time.perf_counter() - t0
-    oracle.use_build(prev)
-    return m.n_elements / dt, dt, m.n_elements
+    try:
+        oracle.laplace_assemble(3, [1, 1, 1], [2, 2, 2], m.elem_nodes[:64], m.coords, kappa[:64], rp, ci, 1)
+        t0 = time.perf_counter()
+        vals, _ = oracle.laplace_assemble(3, [1, 1, 1], [2, 2, 2], m.elem_nodes, m.coords, kappa, rp, ci, threads)
+        dt = time.perf_counter() - t0
+    finally:
+        oracle.use_build(prev)
+    return m.n_elements / dt, dt, m.n_elements, vals, (rp, ci)
 
 
 def cpu_baseline_bases(interp, ngauss, elem_params, params, scale, kappa):
@@ -200,11 +203,17 @@ def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
+    import oracle
+
     threads = os.cpu_count() or 1
-    n = args.cpu_sample_n
+    n = args.n
+    m, _ = make_problem(n, seed=0)
+    structure = oracle.csr_structure(m.elem_nodes, m.n_nodes)
+    del m
     vals = []
+    E = n ** 3
     for i in range(args.warmup + args.steps):
-        v, dt, E = cpu_baseline(n, threads)
+        v, dt, E, _, _ = cpu_baseline(n, threads, structure)
         if i >= args.warmup:
             vals.append(v)
     value = float(np.median(vals))
@@ -212,12 +221,11 @@ def run_reference(args):
         "impl": "reference", "metric": "assembled_elements_per_s", "value": value, "unit": "elements/s",
         "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "elements_per_side": args.n, "sample_elements_per_side": n,
-                   "gauss": "2x2x2", "conductivity": "log-uniform [0.1,10]", "jitter": "+-0.1h"},
+        "config": {"workload": WORKLOAD, "elements_per_side": n, "elements": E, "gauss": "2x2x2",
+                   "conductivity": "log-uniform [0.1,10] seeded", "jitter": "+-0.1h seeded"},
         "cpu_baseline": {"value": value, "unit": "elements/s", "cores": threads, "kind": "port",
-                         "sample": f"{n}^3 = {n**3} elements per step (same element density as the {args.n}^3 "
-                                   f"workload); Iron's algorithm restated in C++ (oracle/), Iron itself cannot be "
-                                   f"built here (Fortran+MPI+PETSc)"},
+                         "sample": f"the whole {n}^3 = {E} element workload per step; Iron's algorithm restated in "
+                                   f"C++ (oracle/), Iron itself cannot be built here (Fortran+MPI+PETSc)"},
         "e2e": {"value": value, "unit": "elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -436,14 +444,66 @@ def run_gfe(args):
         line["solve"] = solve
     if rank == 0:
         threads = os.cpu_count() or 1
-        log("cpu baseline")
-        v, dt, Es = cpu_baseline(args.cpu_sample_n, threads)
+        log("cpu baseline: the oracle on the whole workload")
+        v, dt, Es, ovals, _ = cpu_baseline(args.n, threads)
         line["cpu_baseline"] = {"value": v, "unit": "elements/s", "cores": threads, "kind": "port",
-                                "sample": f"{args.cpu_sample_n}^3 = {Es} elements, one assembly ({dt:.2f} s)"}
+                                "sample": f"the whole {args.n}^3 = {Es} element workload, one assembly ({dt:.2f} s)"}
+        # the assembled values of the GPU kernels against the oracle's at full size
+        scale = float(np.abs(ovals).max())
+        acc = {}
+        for prec in precisions:
+            pth = "general" if prec == "fp64" else path
+            g = A.assemble(prec, path=pth).cpu().numpy()
+            acc[prec] = float(np.abs(g - ovals).max() / scale)
+        line["assembly_rel_err_vs_oracle"] = acc
+        del ovals
+        n1 = args.cpu_sample_n
+        log(f"cpu baseline: one core on a {n1}^3 sample")
+        v1, dt1, E1, _, _ = cpu_baseline(n1, 1)
+        line["cpu_baseline_single_core"] = {"value": v1, "unit": "elements/s", "cores": 1, "kind": "port",
+                                            "sample": f"{n1}^3 = {E1} elements, one assembly ({dt1:.2f} s); one "
+                                                      "core matches one Iron MPI rank"}
+        if solve is not None:
+            log("solution against the oracle's FP64 solve (48^3)")
+            line["solve_vs_oracle_48"] = solution_vs_oracle(48, dev)
+        log("Mooney-Rivlin 32^3 Jacobians and 16^3 x 64 adjoint")
+        from iron_gb300 import benchmarks
+
+        line["mooney_rivlin_32"] = benchmarks.mr_measure(32, 5, 3, ClockSampler, log)
+        line["mooney_rivlin_adjoint_16x64"] = benchmarks.mr_adjoint_measure(16, 64, 5, 3, ClockSampler, log)
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def solution_vs_oracle(n: int, dev) -> dict:
+    """The benchmark's problem at n^3 (u = 0 at x = 0, u = 1 at x = 1) solved on the GPU (FP64 and
+    float-float assembly with FP32-refined CG, rtol 1e-12) against the oracle's FP64 assembly and CG
+    (rtol 1e-13): max |u - u_oracle| / max |u_oracle| per precision."""
+    import torch
+
+    import oracle
+    from iron_gb300.laplace import LaplaceAssembly
+
+    m, kappa = make_problem(n, seed=2)
+    A = LaplaceAssembly.from_regular_mesh(m, kappa=kappa, device=dev)
+    rp, ci = oracle.csr_structure(m.elem_nodes, m.n_nodes)
+    ov, _ = oracle.laplace_assemble(3, [1, 1, 1], [2, 2, 2], m.elem_nodes, m.coords, kappa, rp, ci,
+                                    os.cpu_count() or 1)
+    fixed = np.zeros(m.n_nodes, np.uint8)
+    x0 = np.zeros(m.n_nodes)
+    fixed[m.face_nodes(0, 0)] = 1
+    fixed[m.face_nodes(0, 1)] = 1
+    x0[m.face_nodes(0, 1)] = 1.0
+    uo, _, _ = oracle.cg_dirichlet(rp, ci, ov, None, fixed, x0, rtol=1e-13)
+    out = {}
+    for prec in ("fp64", "mixed_df"):
+        A.assemble(prec, fp32_copy=prec != "fp64")
+        x = torch.from_numpy(x0).to(dev)
+        A.solve(torch.from_numpy(fixed).to(dev), x, rtol=1e-12, precision=prec)
+        out[prec] = float(np.abs(x.cpu().numpy() - uo).max() / np.abs(uo).max())
+    return out
 
 
 def log(msg: str) -> None:
