@@ -236,9 +236,12 @@ int gfe_laplace_assemble_regular(int32_t nx, int32_t ny, int32_t nz, const doubl
                                  int32_t precision, void* stream);
 
 /* The same assembly with a caller-owned device workspace (16-byte aligned) of
- * gfe_laplace_regular_workspace_bytes(nx, ny, nz, precision) bytes for the converted coordinates,
- * so that nothing is allocated: the form to capture into a CUDA graph.  workspace may be NULL
- * (then it is allocated on `stream`, as gfe_laplace_assemble_regular does). */
+ * gfe_laplace_regular_workspace_bytes(nx, ny, nz, precision) bytes, so that nothing is allocated:
+ * the form to capture into a CUDA graph.  The workspace holds the converted coordinates and, for
+ * GFE_MIXED_DF, every element's Gauss-point metrics and element matrix (float-float, 672 bytes an
+ * element): the float-float element work runs as a metric kernel and a contraction kernel, each
+ * element once, and the rows are then gathered from the element matrices.  workspace may be NULL
+ * (then it is allocated and freed on `stream`, as gfe_laplace_assemble_regular does). */
 int64_t gfe_laplace_regular_workspace_bytes(int32_t nx, int32_t ny, int32_t nz, int32_t precision);
 int gfe_laplace_assemble_regular_ws(int32_t nx, int32_t ny, int32_t nz, const double* coords, const double* kappa,
                                     const int32_t* row_ptr, double* values, float* values32, double* rhs,

@@ -54,11 +54,11 @@ __device__ __forceinline__ T wwv(int k, int g, T p, T q) {
   return (k == 0) == (g == 0) ? p * p : q * q;
 }
 
-// Element stiffness of one trilinear hexahedron.  x[c][m]: coordinates of local node m
-// (m = m1 + 2 m2 + 4 m3, Iron's local node order).  Returns the 36 unique entries of the
-// symmetric 8x8 matrix (packed upper triangle, tri(m,n)).  Returns false if det(GL) <= 0.
+// Metrics of one trilinear hexahedron at its 8 Gauss points: M[g] = GU Jacobian w kappa as the six
+// entries 00 11 22 01 02 12 of the symmetric 3x3 matrix.  x[c][m]: coordinates of local node m
+// (m = m1 + 2 m2 + 4 m3, Iron's local node order).  Returns false if det(GL) <= 0.
 template <typename T>
-__device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T q, T (&K)[36]) {
+__device__ __forceinline__ bool hex8_metrics(const T (&x)[3][8], T kappa, T p, T q, T (&M)[8][6]) {
   const T zero = from_double<T>(0.0);
   // Jacobian columns: Jt[c][a][gd1][gd2]
   T Jt[3][3][2][2];
@@ -85,7 +85,6 @@ __device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T
     }
   }
   // M_g[ab] for the 8 Gauss points, symmetric: 00 11 22 01 02 12
-  T M[8][6];
   bool ok = true;
   const T eighth = kappa * from_double<T>(0.125);
 #pragma unroll
@@ -118,6 +117,15 @@ __device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T
     M[g][0] = A00 * sc; M[g][1] = A11 * sc; M[g][2] = A22 * sc;
     M[g][3] = A01 * sc; M[g][4] = A02 * sc; M[g][5] = A12 * sc;
   }
+  return ok;
+}
+
+// The element matrix from the Gauss-point metrics: the 36 unique entries of the symmetric 8x8
+// matrix (packed upper triangle, tri(m,n)), contracted one xi direction at a time.
+// Mg(g, k): entry k (00 11 22 01 02 12) of the metric at Gauss point g, read where it is needed.
+template <typename T, typename MetricAt>
+__device__ __forceinline__ void hex8_contract_at(MetricAt Mg, T p, T q, T (&K)[36]) {
+  const T zero = from_double<T>(0.0);
 #pragma unroll
   for (int k = 0; k < 36; ++k) K[k] = zero;
 
@@ -131,7 +139,7 @@ __device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int g0 = (i << d1) | (j << d2);
-        S[i][j] = M[g0][a] + M[g0 | (1 << a)][a];
+        S[i][j] = Mg(g0, a) + Mg(g0 | (1 << a), a);
       }
     T Tt[3][2];
 #pragma unroll
@@ -163,7 +171,7 @@ __device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T
 #pragma unroll
       for (int gcc = 0; gcc < 2; ++gcc) {
         const int g0 = (gbb << b) | (gcc << c);
-        const T m0 = M[g0][mi], m1 = M[g0 | (1 << a)][mi];
+        const T m0 = Mg(g0, mi), m1 = Mg(g0 | (1 << a), mi);
 #pragma unroll
         for (int i = 0; i < 2; ++i) U[i][gbb][gcc] = m0 * wv(i, 0, p, q) + m1 * wv(i, 1, p, q);
       }
@@ -198,6 +206,20 @@ __device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T
   }
 #pragma unroll
   for (int k = 0; k < 36; ++k) finish(K[k]);
+}
+
+template <typename T>
+__device__ __forceinline__ void hex8_contract(const T (&M)[8][6], T p, T q, T (&K)[36]) {
+  hex8_contract_at<T>([&](int g, int k) { return M[g][k]; }, p, q, K);
+}
+
+// Element stiffness of one trilinear hexahedron (metrics, then contraction).  Returns the 36
+// unique entries of the symmetric 8x8 matrix; false if det(GL) <= 0.
+template <typename T>
+__device__ __forceinline__ bool laplace_hex8(const T (&x)[3][8], T kappa, T p, T q, T (&K)[36]) {
+  T M[8][6];
+  const bool ok = hex8_metrics<T>(x, kappa, p, q, M);
+  hex8_contract<T>(M, p, q, K);
   return ok;
 }
 
@@ -519,6 +541,165 @@ laplace_regular_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__
   if (nonfinite) gfe_raise(err, GFE_DEVERR_NONFINITE);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Float-float on Iron's regular mesh: element work in two kernels, then a row gather
+// ---------------------------------------------------------------------------------------------
+// The float-float element routine is ~13.6 k instructions of straight-line code per element; inside
+// the row-owning kernel its instruction stream does not fit the SM's instruction cache and warps
+// stall on instruction fetch.  Split, each kernel's code fits: the metric kernel forms the 8
+// Gauss-point metrics of every element once, the contraction kernel turns them into the 36 element
+// matrix entries, and the gather kernel sums each CSR row from the matrices of the elements around
+// its node, in the fixed order of the row-owning kernel (the values are bit-identical to it).
+
+// Gauss-point metrics of element layers [ez0, ez1) into metrics, tiled by 32 elements (entry k of
+// Gauss point g of element e at (48 (e / 32) + 8 k + g) 32 + e % 32).
+template <typename T>
+__global__ void __launch_bounds__(256)
+laplace_metric_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ coords,
+                      const double* __restrict__ kappa, T* __restrict__ metrics, int32_t ez0, int32_t ez1,
+                      unsigned* err) {
+  const long long EXY = (long long)nx * ny;
+  const long long NX = nx + 1, NXY = NX * (ny + 1), N = NXY * (nz + 1);
+  T p, q;
+  gauss_pq(p, q);
+  bool bad = false, nonfinite = false;
+  for (long long e = ez0 * EXY + blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ez1 * EXY;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long ex = e % nx, ey = (e / nx) % ny, ez = e / EXY;
+    T x[3][8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const long long n = (ex + (m & 1)) + (ey + ((m >> 1) & 1)) * NX + (ez + (m >> 2)) * NXY;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) x[c][m] = load_coord(coords + c * N + n);
+    }
+    const double kd = kappa ? __ldg(kappa + e) : 1.0;
+    if (!isfinite(kd)) nonfinite = true;
+    T M[8][6];
+    if (!hex8_metrics<T>(x, from_double<T>(kd), p, q, M)) bad = true;
+    // tiles of 32 elements: entry j = 8 k + g of element e at (48 (e / 32) + j) 32 + e % 32, so a
+    // warp's 32 consecutive elements write (and the contraction reads) each entry as 256
+    // contiguous bytes, and a thread's 48 entries sit at immediate offsets from one address
+    T* dst = metrics + (e >> 5) * (48 * 32) + (e & 31);
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+      for (int g = 0; g < 8; ++g) dst[(k * 8 + g) * 32] = M[g][k];
+  }
+  if (bad) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+  if (nonfinite) gfe_raise(err, GFE_DEVERR_NONFINITE);
+}
+
+// Element matrices of element layers [ez0, ez1) from their metrics into Kel[36][E] (entry
+// tri(m, n) of element e at tri(m, n) E + e).
+template <typename T>
+__global__ void __launch_bounds__(256)
+laplace_contract_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ metrics, T* __restrict__ Kel,
+                        int32_t ez0, int32_t ez1) {
+  const long long EXY = (long long)nx * ny, E = EXY * nz;
+  T p, q;
+  gauss_pq(p, q);
+  for (long long e = ez0 * EXY + blockIdx.x * (long long)blockDim.x + threadIdx.x; e < ez1 * EXY;
+       e += (long long)gridDim.x * blockDim.x) {
+    // a direction's component is loaded where the contraction uses it, not all 48 entries up front
+    const T* src = metrics + (e >> 5) * (48 * 32) + (e & 31);
+    T K[36];
+    hex8_contract_at<T>([&](int g, int k) { return load_coord(src + (k * 8 + g) * 32); }, p, q, K);
+#pragma unroll
+    for (int k = 0; k < 36; ++k) Kel[k * E + e] = K[k];
+  }
+}
+
+// Rows of node layers [l0, l1) gathered from the element matrices Kel of the (up to 8) elements
+// around each node: a lane per row sums its 27-entry row in the order of the row-owning kernel
+// (surrounding elements c, b, a; local column lj).  A warp takes 32 consecutive rows, whose entries
+// are one contiguous range of the CSR values: the lanes stage their rows in shared memory and the
+// warp writes the range with coalesced stores.  No CTA barrier; each element matrix is read by its 8
+// nodes, mostly from L1/L2.
+constexpr int kGatherWarps = 8;
+constexpr int kGatherStage = 32 * 27;  // entries of 32 rows at most
+
+template <typename T>
+__global__ void __launch_bounds__(kGatherWarps * 32)
+laplace_gather_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ Kel, const int32_t* __restrict__ rp,
+                      double* __restrict__ values, float* __restrict__ values32, double* __restrict__ rhs,
+                      int32_t l0, int32_t l1) {
+  using A = typename AccOf<T>::type;
+  extern __shared__ __align__(16) unsigned char gsm[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double* st64 = reinterpret_cast<double*>(gsm) + w * kGatherStage;
+  float* st32 = reinterpret_cast<float*>(reinterpret_cast<double*>(gsm) + kGatherWarps * kGatherStage) +
+                w * kGatherStage;
+  const long long NX = nx + 1, NY = ny + 1, NZ = nz + 1, NXY = NX * NY;
+  const long long EXY = (long long)nx * ny, E = EXY * nz;
+  const long long r_end = l1 * NXY;
+  for (long long base = l0 * NXY + ((long long)blockIdx.x * kGatherWarps + w) * 32; base < r_end;
+       base += (long long)gridDim.x * kGatherWarps * 32) {
+    const long long r = base + lane;
+    const bool active = r < r_end;
+    const long long pos0 = (long long)__ldg(rp + base) - 1;
+    const long long pos_end = (long long)__ldg(rp + (base + 32 < r_end ? base + 32 : r_end)) - 1;
+    if (active) {
+      const int ni = (int)(r % NX), nj = (int)((r / NX) % NY), k = (int)(r / NXY);
+      A acc[27];
+#pragma unroll
+      for (int t = 0; t < 27; ++t) acc[t] = from_double<A>(0.0);
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int ez = k - 1 + c;
+        if (ez < 0 || ez >= nz) continue;
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+          const int ey2 = nj - 1 + b;
+          if (ey2 < 0 || ey2 >= ny) continue;
+#pragma unroll
+          for (int a = 0; a < 2; ++a) {
+            const int ex2 = ni - 1 + a;
+            if (ex2 < 0 || ex2 >= nx) continue;
+            const long long e = ex2 + ey2 * (long long)nx + ez * EXY;
+            const int li = (1 - a) + 2 * (1 - b) + 4 * (1 - c);
+#pragma unroll
+            for (int lj = 0; lj < 8; ++lj) {
+              const int di = a - 1 + (lj & 1), dj = b - 1 + ((lj >> 1) & 1), dk = c - 1 + (lj >> 2);
+              const int m = li < lj ? li : lj, n = li < lj ? lj : li;
+              const int t = (dk + 1) * 9 + (dj + 1) * 3 + (di + 1);
+              acc[t] = acc_add(acc[t], load_coord(Kel + tri(m, n) * E + e));
+            }
+          }
+        }
+      }
+      // the row, clipped to the mesh, in ascending column order, staged at its offset in the range
+      int o = (int)((long long)__ldg(rp + r) - 1 - pos0);
+#pragma unroll
+      for (int dk = -1; dk <= 1; ++dk) {
+        if (k + dk < 0 || k + dk >= NZ) continue;
+#pragma unroll
+        for (int dj = -1; dj <= 1; ++dj) {
+          if (nj + dj < 0 || nj + dj >= NY) continue;
+#pragma unroll
+          for (int di = -1; di <= 1; ++di) {
+            if (ni + di < 0 || ni + di >= NX) continue;
+            double v;
+            float v32;
+            entry_out(acc[(dk + 1) * 9 + (dj + 1) * 3 + (di + 1)], !std::is_same<T, float>::value, v, v32);
+            st64[o] = v;
+            st32[o] = v32;
+            ++o;
+          }
+        }
+      }
+      if (rhs) rhs[r] = 0.0;
+    }
+    __syncwarp();
+    const int total = (int)(pos_end - pos0);  // <= 32 x 27: the rows of a regular mesh
+    for (int i = lane; i < total; i += 32) {
+      values[pos0 + i] = st64[i];
+      if (values32) values32[pos0 + i] = st32[i];
+    }
+    __syncwarp();
+  }
+}
+
 // Persistent grid of the regular-mesh kernel: the resident CTAs, but no more than one CTA per
 // kRMinRun layers of one tile column.
 template <typename T>
@@ -595,33 +776,84 @@ int check_device_errors(cudaStream_t s, const char* fn, bool sync) {
   return GFE_OK;
 }
 
-// bytes of the converted-coordinate array the FP32-pipe precisions read (0 for FP64)
-size_t regular_workspace_bytes(int32_t nx, int32_t ny, int32_t nz, int precision) {
+// Workspace of the FP32-pipe precisions: the converted coordinates and, for float-float, behind
+// them at a 256-byte boundary the Gauss-point metrics (48 float-float numbers an element) and the
+// element matrices (36) of every element.  0 for FP64.
+size_t regular_coords_bytes(int32_t nx, int32_t ny, int32_t nz, int precision) {
   const size_t n3 = 3ull * (nx + 1) * (ny + 1) * (nz + 1);
   if (precision == GFE_FP64) return 0;
-  return n3 * (precision == GFE_MIXED ? sizeof(float) : sizeof(f2));
+  return (n3 * (precision == GFE_MIXED ? sizeof(float) : sizeof(f2)) + 255) & ~size_t(255);
+}
+size_t regular_metric_entries(int32_t nx, int32_t ny, int32_t nz) {  // 48 per element, tiles of 32
+  return 48ull * (((size_t)nx * ny * nz + 31) & ~size_t(31));
+}
+size_t regular_workspace_bytes(int32_t nx, int32_t ny, int32_t nz, int precision) {
+  const size_t cb = regular_coords_bytes(nx, ny, nz, precision);
+  if (precision != GFE_MIXED_DF) return cb;
+  return cb + (regular_metric_entries(nx, ny, nz) + 36ull * nx * ny * nz) * sizeof(f2);
+}
+
+constexpr int kSplitThreads = 256;
+
+// Float-float element work of element layers [ez0, ez1): metric kernel, then contraction kernel,
+// each element once, into the workspace's element-matrix array.
+void launch_elements_f2(cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const f2* ct, const double* kappa,
+                        void* ws, int32_t ez0, int32_t ez1, unsigned* err) {
+  if (ez1 <= ez0) return;
+  const long long cnt = (long long)(ez1 - ez0) * nx * ny;
+  const int grid = (int)std::min<long long>((cnt + kSplitThreads - 1) / kSplitThreads, 40ll * gfe::sm_count());
+  f2* metrics = reinterpret_cast<f2*>(static_cast<char*>(ws) + regular_coords_bytes(nx, ny, nz, GFE_MIXED_DF));
+  f2* Kel = metrics + regular_metric_entries(nx, ny, nz);
+  laplace_metric_kernel<f2><<<grid, kSplitThreads, 0, s>>>(nx, ny, nz, ct, kappa, metrics, ez0, ez1, err);
+  laplace_contract_kernel<f2><<<grid, kSplitThreads, 0, s>>>(nx, ny, nz, metrics, Kel, ez0, ez1);
+}
+
+void launch_gather_f2(cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const void* ws, const int32_t* rp,
+                      double* values, float* values32, double* rhs, int32_t l0, int32_t l1) {
+  if (l1 <= l0) return;
+  const long long rows = (long long)(l1 - l0) * (nx + 1) * (ny + 1);
+  const int grid = (int)std::min<long long>((rows + kGatherWarps * 32 - 1) / (kGatherWarps * 32),
+                                            8ll * gfe::sm_count());
+  const f2* Kel = reinterpret_cast<const f2*>(static_cast<const char*>(ws) +
+                                              regular_coords_bytes(nx, ny, nz, GFE_MIXED_DF)) +
+                  regular_metric_entries(nx, ny, nz);
+  const size_t smem = (size_t)kGatherWarps * kGatherStage * (sizeof(double) + sizeof(float));
+  cudaFuncSetAttribute((const void*)laplace_gather_kernel<f2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  laplace_gather_kernel<f2><<<grid, kGatherWarps * 32, smem, s>>>(nx, ny, nz, Kel, rp, values, values32, rhs, l0, l1);
 }
 
 // Node layers [l0, l1) (l0 a multiple of kRZ).  ws: caller workspace of regular_workspace_bytes(),
 // or NULL to allocate it on the stream; split: convert the coordinates into it first (the later
-// layer calls of one assembly reuse the converted array).
+// layer calls of one assembly reuse the converted array).  FP32: the row-owning tiled kernel.
+// Float-float: the element work of the element layers the rows read ([l0 - 1, l1) within the mesh;
+// a neighbouring slab on another stream may write the matrices of the layer between them at the
+// same time, with identical values), then the row gather.
 template <typename T>
 int launch_regular(cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const double* coords,
                    const double* kappa, const int32_t* rp, double* values, float* values32, double* rhs,
                    unsigned* err, void* ws, int32_t l0, int32_t l1, bool split) {
-  const size_t smem = 2 * 36 * kRThreads * sizeof(typename StoreOf<T>::type);
-  GFE_CUDA_TRY(cudaFuncSetAttribute((const void*)laplace_regular_kernel<T>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int grid = 0;
-  if (int rc = regular_grid<T>(nx, ny, l0, l1, smem, &grid)) return rc;
+  constexpr bool DF = std::is_same<T, f2>::value;
+  const int prec = DF ? GFE_MIXED_DF : GFE_MIXED;
   const long long n3 = 3ll * (nx + 1) * (ny + 1) * (nz + 1);
-  T* ct = static_cast<T*>(ws);
-  if (!ct)
-    if (int rc = gfe::scratch_alloc((void**)&ct, sizeof(T) * n3, s, "split coordinates")) return rc;
+  char* base = static_cast<char*>(ws);
+  if (!base)
+    if (int rc = gfe::scratch_alloc((void**)&base, regular_workspace_bytes(nx, ny, nz, prec), s, "split coordinates"))
+      return rc;
+  T* ct = reinterpret_cast<T*>(base);
   if (split || !ws) split_coords<T><<<4 * gfe::sm_count(), 256, 0, s>>>(n3, coords, ct);
-  laplace_regular_kernel<T><<<grid, kRThreads, smem, s>>>(nx, ny, nz, ct, kappa, rp, values, values32, rhs, err, l0,
-                                                           l1);
-  if (!ws) gfe::scratch_free(ct, s);
+  if constexpr (DF) {
+    launch_elements_f2(s, nx, ny, nz, ct, kappa, base, std::max(l0 - 1, 0), std::min(l1, nz), err);
+    launch_gather_f2(s, nx, ny, nz, base, rp, values, values32, rhs, l0, l1);
+  } else {
+    const size_t smem = 2 * 36 * kRThreads * sizeof(typename StoreOf<T>::type);
+    GFE_CUDA_TRY(cudaFuncSetAttribute((const void*)laplace_regular_kernel<T>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int grid = 0;
+    if (int rc = regular_grid<T>(nx, ny, l0, l1, smem, &grid)) return rc;
+    laplace_regular_kernel<T><<<grid, kRThreads, smem, s>>>(nx, ny, nz, ct, kappa, rp, values, values32, rhs, err,
+                                                             l0, l1);
+  }
+  if (!ws) gfe::scratch_free(base, s);
   return GFE_OK;
 }
 
@@ -750,7 +982,7 @@ extern "C" int gfe_laplace_assemble_regular_layers(int32_t nx, int32_t ny, int32
   else
     rc = launch_regular<f2>(s, nx, ny, nz, coords, kappa, row_ptr, values, values32, rhs, err, workspace, l0,
                             l1, cv);
-  gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, 1);
+  gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, precision == GFE_MIXED_DF ? 3 : 1);
   if (rc) return rc;
   GFE_LAUNCH_CHECK(fn);
   return GFE_OK;
@@ -873,6 +1105,11 @@ extern "C" int gfe_laplace_assemble_regular_host(int32_t nx, int32_t ny, int32_t
                                    sizeof(double) * (eh - elem_hi) * EXY, cudaMemcpyHostToDevice, hp->in));
       elem_hi = eh;
     }
+    // float-float: the element work of the slab's own element layers on the input stream, in slab
+    // order, so the next slab's rows find the matrices of the element layer below them written
+    if (precision == GFE_MIXED_DF)
+      launch_elements_f2(hp->in, nx, ny, nz, static_cast<const f2*>(workspace), kappa, workspace, l0,
+                         std::min<int32_t>(l1, nz), err);
     GFE_CUDA_TRY(cudaEventRecord(ev_in, hp->in));
     // the slab on alternating compute streams: one slab's last wave overlaps the next one's first
     cudaStream_t cs = hp->comp[i & 1];
@@ -884,9 +1121,10 @@ extern "C" int gfe_laplace_assemble_regular_host(int32_t nx, int32_t ny, int32_t
     else if (precision == GFE_MIXED)
       rc = launch_regular<float>(cs, nx, ny, nz, coords, kappa, row_ptr, values, nullptr, rhs, err, workspace,
                                  l0, l1, false);
-    else
-      rc = launch_regular<f2>(cs, nx, ny, nz, coords, kappa, row_ptr, values, nullptr, rhs, err, workspace,
-                              l0, l1, false);
+    else {
+      launch_gather_f2(cs, nx, ny, nz, workspace, row_ptr, values, nullptr, rhs, l0, l1);
+      rc = GFE_OK;
+    }
     if (rc) return rc;
     GFE_CUDA_TRY(cudaEventRecord(ev_c, cs));
     // the slab's rows are one contiguous range of the CSR values

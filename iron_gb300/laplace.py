@@ -179,9 +179,10 @@ class LaplaceAssembly:
             path = "general" if (prec == GFE_FP64 or self.regular is None) else "regular"
         if path == "regular":
             nx, ny, nz = self.regular
-            _lib.call("gfe_laplace_assemble_regular", nx, ny, nz, _lib.ptr(self.coords), _lib.ptr(self.kappa),
+            ws = self._regular_workspace(prec) if prec != GFE_FP64 else None
+            _lib.call("gfe_laplace_assemble_regular_ws", nx, ny, nz, _lib.ptr(self.coords), _lib.ptr(self.kappa),
                       _lib.ptr(self.row_ptr), _lib.ptr(self.values), _lib.ptr(v32), _lib.ptr(self.rhs), prec,
-                      _lib.stream_handle(stream))
+                      _lib.ptr(ws), _lib.stream_handle(stream))
         else:
             cp = self.colour_ptr
             _lib.call("gfe_laplace_assemble", self.n_elements, self.n_nodes, _lib.ptr(self.elem_nodes),
@@ -216,15 +217,23 @@ class LaplaceAssembly:
         L = _lib.load()
         nx, ny, nz = self.regular
         prec = PRECISIONS[precision]
-        if getattr(self, "_asm_ws_prec", None) != prec:
-            wb = int(L.gfe_laplace_regular_workspace_bytes(nx, ny, nz, prec))
-            self._asm_ws = torch.empty(max(wb, 16), dtype=torch.uint8, device=self.device)
-            self._asm_ws_prec = prec
+        ws = self._regular_workspace(prec)
         _lib.call("gfe_laplace_assemble_regular_host", nx, ny, nz, _lib.host_ptr(coords_host),
                   _lib.host_ptr(kappa_host), _lib.ptr(self.coords), _lib.ptr(self.kappa), _lib.ptr(self.row_ptr),
-                  _lib.ptr(self.values), _lib.host_ptr(values_host), _lib.ptr(self.rhs), prec, _lib.ptr(self._asm_ws), int(slab_layers),
-                  _lib.stream_handle(st))
+                  _lib.ptr(self.values), _lib.host_ptr(values_host), _lib.ptr(self.rhs), prec, _lib.ptr(ws),
+                  int(slab_layers), _lib.stream_handle(st))
         return values_host
+
+    def _regular_workspace(self, prec: int) -> torch.Tensor:
+        """Device workspace of the regular-mesh kernels for precision code `prec`, allocated once per
+        precision and kept (the float-float one also holds every element's Gauss-point metrics and
+        element matrix: 672 bytes an element)."""
+        cache = self.__dict__.setdefault("_ws_cache", {})
+        if prec not in cache:
+            nx, ny, nz = self.regular
+            wb = int(_lib.load().gfe_laplace_regular_workspace_bytes(nx, ny, nz, prec))
+            cache[prec] = torch.empty(max(wb, 16), dtype=torch.uint8, device=self.device)
+        return cache[prec]
 
     def element_matrices(self, precision: str = "fp64", stream=None) -> torch.Tensor:
         if self.tensor_product:

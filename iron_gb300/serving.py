@@ -177,6 +177,7 @@ class _LaplaceSlot:
         b = lm.base
         self.lm = lm
         self.asm = copy.copy(b)
+        self.asm.__dict__.pop("_ws_cache", None)  # a worker's assembly workspaces are its own
         # valid data for the warm-up run before capture: the undeformed mesh, unit conductivity
         self.asm.coords = b.coords.clone()
         self.asm.kappa = torch.ones(b.n_elements, dtype=torch.float64, device=dev)
@@ -286,6 +287,7 @@ class _MRSlot:
         b = mm.base
         self.mm = mm
         self.asm = copy.copy(b)
+        self.asm.__dict__.pop("_ws_cache", None)  # a worker's assembly workspaces are its own
         self.asm.xg = torch.empty_like(b.xg)
         self.asm.values = torch.empty(b.nnz, dtype=torch.float64, device=dev)
         self.values32 = torch.empty(b.nnz, dtype=torch.float32, device=dev)
@@ -355,7 +357,8 @@ def estimate_bytes(kind: str, n: int) -> tuple[int, int]:
         N = (n + 1) ** 3
         nnz = (3 * n + 1) ** 3  # exact for the regular trilinear mesh
         resident = 4 * (N + 1) + 4 * nnz + 36 * E + 41 * N
-        work = 12 * nnz + 56 * N + 8 * E + 40 * N + 24 * N + 16 * 2048 + 4096
+        # + the float-float workspace: coordinates and every element's metrics and matrix
+        work = 12 * nnz + 56 * N + 8 * E + 40 * N + 24 * N + 672 * E + 16 * 2048 + 4096
     else:
         Nq, Np = (2 * n + 1) ** 3, (n + 1) ** 3
         ndof = 3 * Nq + Np
