@@ -554,7 +554,7 @@ laplace_regular_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__
 // Gauss-point metrics of element layers [ez0, ez1) into metrics, tiled by 32 elements (entry k of
 // Gauss point g of element e at (48 (e / 32) + 8 k + g) 32 + e % 32).
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(128)
 laplace_metric_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ coords,
                       const double* __restrict__ kappa, T* __restrict__ metrics, int32_t ez0, int32_t ez1,
                       unsigned* err) {
@@ -593,7 +593,7 @@ laplace_metric_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ 
 // Element matrices of element layers [ez0, ez1) from their metrics into Kel[36][E] (entry
 // tri(m, n) of element e at tri(m, n) E + e).
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(128)
 laplace_contract_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ metrics, T* __restrict__ Kel,
                         int32_t ez0, int32_t ez1) {
   const long long EXY = (long long)nx * ny, E = EXY * nz;
@@ -793,7 +793,8 @@ size_t regular_workspace_bytes(int32_t nx, int32_t ny, int32_t nz, int precision
   return cb + (regular_metric_entries(nx, ny, nz) + 36ull * nx * ny * nz) * sizeof(f2);
 }
 
-constexpr int kSplitThreads = 256;
+constexpr int kSplitThreads = 128;
+constexpr int kContractThreads = 128;
 
 // Float-float element work of element layers [ez0, ez1): metric kernel, then contraction kernel,
 // each element once, into the workspace's element-matrix array.
@@ -802,10 +803,13 @@ void launch_elements_f2(cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, cons
   if (ez1 <= ez0) return;
   const long long cnt = (long long)(ez1 - ez0) * nx * ny;
   const int grid = (int)std::min<long long>((cnt + kSplitThreads - 1) / kSplitThreads, 40ll * gfe::sm_count());
+  // 128-thread blocks: with ~170 (metric) and ~130 (contraction) registers a thread, three and four
+  // blocks share an SM (12 and 16 warps), where 256-thread blocks left room for one
+  const int cgrid = (int)std::min<long long>((cnt + kContractThreads - 1) / kContractThreads, 60ll * gfe::sm_count());
   f2* metrics = reinterpret_cast<f2*>(static_cast<char*>(ws) + regular_coords_bytes(nx, ny, nz, GFE_MIXED_DF));
   f2* Kel = metrics + regular_metric_entries(nx, ny, nz);
   laplace_metric_kernel<f2><<<grid, kSplitThreads, 0, s>>>(nx, ny, nz, ct, kappa, metrics, ez0, ez1, err);
-  laplace_contract_kernel<f2><<<grid, kSplitThreads, 0, s>>>(nx, ny, nz, metrics, Kel, ez0, ez1);
+  laplace_contract_kernel<f2><<<cgrid, kContractThreads, 0, s>>>(nx, ny, nz, metrics, Kel, ez0, ez1);
 }
 
 void launch_gather_f2(cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const void* ws, const int32_t* rp,
