@@ -627,9 +627,7 @@ laplace_gather_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ 
   using A = typename AccOf<T>::type;
   extern __shared__ __align__(16) unsigned char gsm[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  double* st64 = reinterpret_cast<double*>(gsm) + w * kGatherStage;
-  float* st32 = reinterpret_cast<float*>(reinterpret_cast<double*>(gsm) + kGatherWarps * kGatherStage) +
-                w * kGatherStage;
+  A* stage = reinterpret_cast<A*>(gsm) + w * kGatherStage;  // the rows' sums, converted on the way out
   const long long NX = nx + 1, NY = ny + 1, NZ = nz + 1, NXY = NX * NY;
   const long long EXY = (long long)nx * ny, E = EXY * nz;
   const long long r_end = l1 * NXY;
@@ -679,12 +677,7 @@ laplace_gather_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ 
 #pragma unroll
           for (int di = -1; di <= 1; ++di) {
             if (ni + di < 0 || ni + di >= NX) continue;
-            double v;
-            float v32;
-            entry_out(acc[(dk + 1) * 9 + (dj + 1) * 3 + (di + 1)], !std::is_same<T, float>::value, v, v32);
-            st64[o] = v;
-            st32[o] = v32;
-            ++o;
+            stage[o++] = acc[(dk + 1) * 9 + (dj + 1) * 3 + (di + 1)];
           }
         }
       }
@@ -693,8 +686,11 @@ laplace_gather_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ 
     __syncwarp();
     const int total = (int)(pos_end - pos0);  // <= 32 x 27: the rows of a regular mesh
     for (int i = lane; i < total; i += 32) {
-      values[pos0 + i] = st64[i];
-      if (values32) values32[pos0 + i] = st32[i];
+      double v;
+      float v32;
+      entry_out(stage[i], !std::is_same<T, float>::value, v, v32);
+      values[pos0 + i] = v;
+      if (values32) values32[pos0 + i] = v32;
     }
     __syncwarp();
   }
@@ -821,7 +817,7 @@ void launch_gather_f2(cudaStream_t s, int32_t nx, int32_t ny, int32_t nz, const 
   const f2* Kel = reinterpret_cast<const f2*>(static_cast<const char*>(ws) +
                                               regular_coords_bytes(nx, ny, nz, GFE_MIXED_DF)) +
                   regular_metric_entries(nx, ny, nz);
-  const size_t smem = (size_t)kGatherWarps * kGatherStage * (sizeof(double) + sizeof(float));
+  const size_t smem = (size_t)kGatherWarps * kGatherStage * sizeof(f2);
   cudaFuncSetAttribute((const void*)laplace_gather_kernel<f2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   laplace_gather_kernel<f2><<<grid, kGatherWarps * 32, smem, s>>>(nx, ny, nz, Kel, rp, values, values32, rhs, l0, l1);
 }
