@@ -50,8 +50,15 @@ def parse():
     ap.add_argument("--path", default="auto", choices=["auto", "regular", "general"],
                     help="assembly kernel: regular-mesh tiled kernel (auto for generated meshes) or colour scatter")
     ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the Mooney-Rivlin keys of the headline line (for profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=2000, help="serve workload: requests in the stream")
     ap.add_argument("--serve-workers", type=int, default=8, help="serve workload: concurrent request slots")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="serve workload: Poisson arrival rate (1/s)")
+    ap.add_argument("--headline-serve-requests", type=int, default=200,
+                    help="requests of the below-capacity stream in the headline line (0: none)")
+    ap.add_argument("--headline-serve-rate", type=float, default=20.0,
+                    help="arrival rate (1/s) of the below-capacity stream in the headline line")
     ap.add_argument("--cpu-sample-n", type=int, default=48, help="side of the single-core CPU-baseline sample mesh")
     return ap.parse_args()
 
@@ -384,15 +391,23 @@ def run_gfe(args):
     else:
         used_path = path
     value = replicas.job_throughput(E, T["ms_per_step"], ws)
-    per_launch_ms = T["kernel_ms_total"] / max(T["launches"], 1)
-    n_launch_step = max(T["launches"] // max(args.steps, 1), 1)
-    units_per_launch = E / n_launch_step
     bytes_per_elem = algorithmic_bytes(E, N, nnz) / E
-    achieved = bytes_per_elem * units_per_launch / (per_launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
-    kname = ("laplace_regular_kernel" if used_path == "regular" else "laplace_assemble_color") + \
-        "<%s>" % {"fp64": "double", "mixed_df": "f2", "mixed": "float"}[head]
-    tpu = profile_traffic_per_unit(kname)
+    if used_path == "regular" and head == "mixed_df":
+        # float-float on the regular mesh: three kernels per assembly (Gauss-point metrics,
+        # contraction, row gather); the roofline is that of the whole assembly
+        knames = ["laplace_metric_kernel<f2>", "laplace_contract_kernel<f2>", "laplace_gather_kernel<f2>"]
+        per_launch_ms = T["kernel_ms_total"] / max(args.steps, 1)
+        units_per_launch = E
+    else:
+        knames = [("laplace_regular_kernel" if used_path == "regular" else "laplace_assemble_color") +
+                  "<%s>" % {"fp64": "double", "mixed_df": "f2", "mixed": "float"}[head]]
+        per_launch_ms = T["kernel_ms_total"] / max(T["launches"], 1)
+        units_per_launch = E / max(T["launches"] // max(args.steps, 1), 1)
+    achieved = bytes_per_elem * units_per_launch / (per_launch_ms * 1e-3) / 1e9
+    kname = " + ".join(knames)
+    parts = [profile_traffic_per_unit(k) for k in knames]
+    tpu = None if any(t is None for t in parts) else sum(parts)
     line = {
         "metric": "assembled_elements_per_s", "value": value, "unit": "elements/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": T["ms_per_step"], "higher_is_better": True,
@@ -466,11 +481,24 @@ def run_gfe(args):
         if solve is not None:
             log("solution against the oracle's FP64 solve (48^3)")
             line["solve_vs_oracle_48"] = solution_vs_oracle(48, dev)
-        log("Mooney-Rivlin 32^3 Jacobians and 16^3 x 64 adjoint")
-        from iron_gb300 import benchmarks
+        if not args.headline_only:
+            log("Mooney-Rivlin 32^3 Jacobians and 16^3 x 64 adjoint")
+            from iron_gb300 import benchmarks
 
-        line["mooney_rivlin_32"] = benchmarks.mr_measure(32, 5, 3, ClockSampler, log)
-        line["mooney_rivlin_adjoint_16x64"] = benchmarks.mr_adjoint_measure(16, 64, 5, 3, ClockSampler, log)
+            line["mooney_rivlin_32"] = benchmarks.mr_measure(32, 5, 3, ClockSampler, log)
+            line["mooney_rivlin_adjoint_16x64"] = benchmarks.mr_adjoint_measure(16, 64, 5, 3, ClockSampler, log)
+            if args.headline_serve_requests > 0:
+                from iron_gb300 import serving
+
+                rate = args.headline_serve_rate
+                log(f"serving: {args.headline_serve_requests} requests at {rate:g}/s")
+                reqs = serving.request_stream(n_requests=args.headline_serve_requests, rate=rate, seed=1,
+                                              mr_n_hi=serving.MR_SERVE_N_HI)
+                for r in reqs:
+                    serving.make_inputs(r)
+                m = serving.measure_stream(reqs, args.serve_workers, ClockSampler, log)
+                line["serve_stream_below_capacity"] = {
+                    "config": serving.stream_config(reqs, rate, 64, serving.MR_SERVE_N_HI, args.serve_workers), **m}
         print(json.dumps(line), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()

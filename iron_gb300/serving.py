@@ -2,9 +2,11 @@
 
 Requests are Laplace/diffusion problems (trilinear hexahedra, per-element conductivity, u = 0 at
 x = 0 and u = 1 at x = 1, solved to a relative residual of 1e-10) or Mooney-Rivlin problems
-(triquadratic u / trilinear p, per-request c10 and c01 and stretch lambda: the first Newton step
-of a uniaxial load step from the affine predictor -- residual, consistent tangent, MINRES
-correction to 1e-3, updated residual) on jittered regular meshes of different sizes.  The engine
+(triquadratic u / trilinear p, per-request c10 and c01 and stretch lambda: one uniaxial load step
+solved by Newton's method from the affine predictor to Iron's default tolerances -- absolute
+1e-10 and relative 1e-5 on the residual norm, 1e-5 on the step, linear solves to 1e-5 --
+with the consistent tangent and a cubic backtracking line search) on jittered regular meshes of
+different sizes.  The engine
 
 * admits requests in arrival order as soon as a worker slot is free and the request's device
   memory fits the HBM budget (a request that does not fit yet may be overtaken by later ones that
@@ -15,8 +17,14 @@ correction to 1e-3, updated residual) on jittered regular meshes of different si
   overlap with them (continuous batching);
 * replays CUDA graphs for the launch-bound Laplace requests: per (worker, mesh size) one graph for
   "assemble + CG start" and one for "25 CG iterations + status copy", replayed until the device
-  says the solve has converged.  Mooney-Rivlin requests (milliseconds-long kernels and host-side
-  Krylov control) run eagerly on their worker's stream.
+  says the solve has converged;
+* batches small Laplace requests: up to LAPLACE_BATCH queued requests of the same side
+  (side <= BATCH_MAX_N) run together through one pair of graphs holding every request's launch
+  sequence, so a single graph launch advances all of them and one status check per chunk serves
+  the batch.  Each request's sequence is its single-request sequence on its own buffers, so its
+  result is the one it has alone.
+  Mooney-Rivlin requests (milliseconds-long kernels and host-side Newton control) run eagerly
+  on their worker's stream.
 
 Kernels are deterministic (coloured scatters, fixed-order reductions), so a request's result does
 not depend on what runs beside it.  `plain_fp64` is the baseline: the FP64 drop-in path run one
@@ -40,12 +48,14 @@ from ._lib import GfeError
 from .elasticity import MooneyRivlinAssembly
 from .laplace import LaplaceAssembly
 from .mesh import RegularMesh, linear_component
-from .newton import minres_solve, saddle_preconditioner, uniaxial_roller_conditions
+from .newton import NewtonSolver, uniaxial_roller_conditions
 
 LAPLACE_RTOL = 1e-10
-MR_LINEAR_RTOL = 1e-3
 MR_STRETCH = (1.0, 1.1)
 CG_CHUNK = 25
+# small Laplace requests of one side are served in batches of up to LAPLACE_BATCH
+LAPLACE_BATCH = 8
+BATCH_MAX_N = 16
 # share of the device torch's caching allocator may hold while an engine runs (the rest stays
 # free for the library's stream-ordered scratch)
 TORCH_MEMORY_FRACTION = 0.85
@@ -108,13 +118,17 @@ class Request:
 
 
 def request_stream(n_requests: int = 2000, rate: float = 200.0, laplace_fraction: float = 0.7, n_lo: int = 4,
-                   n_hi: int = 64, seed: int = 0) -> list[Request]:
+                   n_hi: int = 64, seed: int = 0, mr_n_hi: int | None = None) -> list[Request]:
     """Poisson arrivals (exponential inter-arrival times at `rate` per second), kind Laplace with
-    probability laplace_fraction else Mooney-Rivlin, side n = round(exp(U(ln n_lo, ln n_hi)))."""
+    probability laplace_fraction else Mooney-Rivlin, side n = round(exp(U(ln n_lo, ln n_hi))).
+    mr_n_hi: a smaller upper side for the Mooney-Rivlin requests (the same uniform draw, mapped
+    onto [ln n_lo, ln mr_n_hi]); None keeps n_hi."""
     rng = np.random.default_rng(seed)
     t = np.cumsum(rng.exponential(1.0 / rate, n_requests))
     kinds = np.where(rng.random(n_requests) < laplace_fraction, "laplace", "mr")
-    ns = np.rint(np.exp(rng.uniform(math.log(n_lo), math.log(n_hi), n_requests))).astype(int)
+    u = rng.uniform(0.0, 1.0, n_requests)
+    hi = np.where(kinds == "mr", mr_n_hi if mr_n_hi is not None else n_hi, n_hi).astype(float)
+    ns = np.rint(np.exp(math.log(n_lo) + u * (np.log(hi) - math.log(n_lo)))).astype(int)
     seeds = rng.integers(0, 2 ** 31 - 1, n_requests)
     return [Request(i, str(kinds[i]), int(ns[i]), int(seeds[i]), float(t[i] - t[0])) for i in range(n_requests)]
 
@@ -170,10 +184,16 @@ class _LaplaceMesh:
         base.values = None  # the base object holds structure only
 
 
-class _LaplaceSlot:
-    """A worker's buffers and captured graphs for one Laplace mesh size."""
+def laplace_batch_capacity(n: int) -> int:
+    """Requests one Laplace slot of side n serves at once."""
+    return LAPLACE_BATCH if n <= BATCH_MAX_N else 1
 
-    def __init__(self, lm: _LaplaceMesh, dev, use_graphs: bool):
+
+class _LaplaceEntry:
+    """One request's buffers in a Laplace slot, and its two launch sequences (which the slot's
+    graphs capture)."""
+
+    def __init__(self, lm: _LaplaceMesh, dev):
         b = lm.base
         self.lm = lm
         self.asm = copy.copy(b)
@@ -192,11 +212,8 @@ class _LaplaceSlot:
         awb = int(L.gfe_laplace_regular_workspace_bytes(nx, ny, nz, 2))
         self.asm_ws = torch.empty(max(awb, 16), dtype=torch.uint8, device=dev)
         self.state = torch.zeros(C.sizeof(_CgState), dtype=torch.uint8).pin_memory()
-        self.use_graphs = use_graphs
-        self.g_begin = self.g_chunk = None
 
-    # the two launch sequences (also what the graphs capture)
-    def _begin(self, stream):
+    def begin(self, stream):
         a = self.asm
         nx, ny, nz = a.regular
         st = _lib.stream_handle(stream)
@@ -207,66 +224,122 @@ class _LaplaceSlot:
         _lib.call("gfe_cg_begin", a.n_nodes, _lib.ptr(a.row_ptr), _lib.ptr(a.col_idx), _lib.ptr(a.values), None,
                   _lib.ptr(self.lm.fixed), _lib.ptr(self.x), LAPLACE_RTOL, _lib.ptr(self.ws), st)
 
-    def _chunk(self, stream):
+    def chunk(self, stream):
         a = self.asm
         st = _lib.stream_handle(stream)
         _lib.call("gfe_cg_steps", a.n_nodes, _lib.ptr(a.row_ptr), _lib.ptr(a.col_idx), _lib.ptr(a.values),
                   _lib.ptr(self.lm.fixed), _lib.ptr(self.x), CG_CHUNK, _lib.ptr(self.ws), st)
         _lib.call("gfe_cg_status", a.n_nodes, _lib.ptr(self.ws), C.c_void_p(self.state.data_ptr()), st)
 
-    def capture(self, stream):
-        """Warm up once eagerly, then capture both sequences on `stream`.  Capture is thread-local
-        (other workers keep launching and allocating meanwhile) and, unlike torch.cuda.graph,
-        does not synchronise the whole device first."""
+    def load(self, req: Request) -> None:
+        """Queue the copies of a request's inputs (pinned host memory) on the current stream."""
+        self.asm.coords.copy_(req.inputs["coords"], non_blocking=True)
+        self.asm.kappa.copy_(req.inputs["kappa"], non_blocking=True)
+
+
+class _LaplaceSlot:
+    """A worker's buffers and captured graphs for one Laplace mesh size: laplace_batch_capacity(n)
+    entries.  A batch of k requests runs on the first w entries, w the width of the batch (the
+    next power of two, at most the capacity); entries past k repeat the last request's inputs and
+    their results are dropped.  All entries run on the worker's stream, one after the other, so a
+    graph is captured from that one stream only."""
+
+    def __init__(self, lm: _LaplaceMesh, dev, use_graphs: bool):
+        self.lm = lm
+        cap = laplace_batch_capacity(lm.mesh.nelem[0])
+        self.entries = [_LaplaceEntry(lm, dev) for _ in range(cap)]
+        self.use_graphs = use_graphs
+        self.graphs: dict = {}  # width -> (begin graph, chunk graph)
+        self.warm: set = set()
+
+    @property
+    def capacity(self) -> int:
+        return len(self.entries)
+
+    def width(self, k: int) -> int:
+        w = 1
+        while w < k:
+            w *= 2
+        return min(w, self.capacity)
+
+    def _fork(self, stream, w: int, step: str) -> None:
+        """Queue entries[0:w]'s `step` ("begin" | "chunk") on `stream`."""
+        for e in self.entries[:w]:
+            getattr(e, step)(stream)
+
+    def capture(self, stream, w: int = 1):
+        """Warm up the width-w launch sequences once eagerly, then (with graphs on) capture both
+        on `stream`.  Capture is thread-local (other workers keep launching and allocating
+        meanwhile) and, unlike torch.cuda.graph, does not synchronise the whole device first."""
         with torch.cuda.stream(stream):
-            self._begin(stream)
-            self._chunk(stream)
-            stream.synchronize()
+            if w not in self.warm:
+                self._fork(stream, w, "begin")
+                self._fork(stream, w, "chunk")
+                stream.synchronize()
+                self.warm.add(w)
+            if not self.use_graphs:
+                return
             graphs = []
             with _GRAPH_LOCK:
-                for fn in (self._begin, self._chunk):
+                for step in ("begin", "chunk"):
                     g = torch.cuda.CUDAGraph()
                     g.capture_begin(capture_error_mode="thread_local")
                     try:
-                        fn(stream)
+                        self._fork(stream, w, step)
                     finally:
                         g.capture_end()
                     graphs.append(g)
-            self.g_begin, self.g_chunk = graphs
+            self.graphs[w] = tuple(graphs)
         stream.synchronize()
 
     def release(self):
         with _GRAPH_LOCK:
-            self.g_begin = self.g_chunk = None
+            self.graphs = {}
 
-    def run(self, req: Request, stream) -> None:
-        a = self.asm
+    @property
+    def n_graphs(self) -> int:
+        return 2 * len(self.graphs)
+
+    def run(self, reqs: list[Request], stream) -> None:
+        """Solve `reqs` (1 to capacity requests of this slot's side) together."""
+        if not 1 <= len(reqs) <= self.capacity:
+            raise GfeError(-1, f"a Laplace slot of capacity {self.capacity} got {len(reqs)} requests")
+        w = self.width(len(reqs))
+        if w not in (self.graphs if self.use_graphs else self.warm):
+            with _GRAPH_LOCK:
+                self.capture(stream, w)
         with torch.cuda.stream(stream):
-            a.coords.copy_(req.inputs["coords"], non_blocking=True)
-            a.kappa.copy_(req.inputs["kappa"], non_blocking=True)
+            for i, e in enumerate(self.entries[:w]):
+                e.load(reqs[min(i, len(reqs) - 1)])
             if self.use_graphs:
-                self.g_begin.replay()
+                self.graphs[w][0].replay()
             else:
-                self._begin(stream)
-            st = _CgState.from_address(self.state.data_ptr())
+                self._fork(stream, w, "begin")
+            states = [_CgState.from_address(e.state.data_ptr()) for e in self.entries[:w]]
             chunks = 0
             while True:
                 if self.use_graphs:
-                    self.g_chunk.replay()
+                    self.graphs[w][1].replay()
                 else:
-                    self._chunk(stream)
+                    self._fork(stream, w, "chunk")
                 chunks += 1
                 stream.synchronize()
-                if st.done or chunks * CG_CHUNK > 200000:
+                if all(st.done for st in states) or chunks * CG_CHUNK > 200000:
                     break
-            out = torch.empty(a.n_nodes, dtype=torch.float64, pin_memory=True)
-            out.copy_(self.x, non_blocking=True)
+            outs = []
+            for e in self.entries[: len(reqs)]:
+                out = torch.empty(e.x.numel(), dtype=torch.float64, pin_memory=True)
+                out.copy_(e.x, non_blocking=True)
+                outs.append(out)
             stream.synchronize()
         bits = _lib.device_errors(stream)
-        if bits or st.done != 2:
-            raise GfeError(-5, f"request {req.rid}: Laplace solve ended with state {st.done}, device bits {bits:#x}")
-        req.result = out.numpy()
-        req.info = {"iterations": int(st.iterations), "rel_residual": math.sqrt(st.rr / st.rr0) if st.rr0 else 0.0}
+        for req, st, out in zip(reqs, states, outs):
+            if bits or st.done != 2:
+                raise GfeError(-5, f"request {req.rid}: Laplace solve ended with state {st.done}, "
+                                   f"device bits {bits:#x}")
+            req.result = out.numpy()
+            req.info = {"iterations": int(st.iterations), "rel_residual": math.sqrt(st.rr / st.rr0) if st.rr0 else 0.0,
+                        "batch": len(reqs)}
 
 
 class _MRMesh:
@@ -279,10 +352,11 @@ class _MRMesh:
         # the Dirichlet DOFs (rollers and the pulled face): boundary nodes are never jittered, so
         # the mask holds for every request of this size
         self.fixed, _ = uniaxial_roller_conditions(b, 1.0)
-        self.fixed_b = self.fixed.bool()
 
 
 class _MRSlot:
+    """One Mooney-Rivlin request's working state: its coordinates, values and solution."""
+
     def __init__(self, mm: _MRMesh, dev):
         b = mm.base
         self.mm = mm
@@ -290,27 +364,19 @@ class _MRSlot:
         self.asm.__dict__.pop("_ws_cache", None)  # a worker's assembly workspaces are its own
         self.asm.xg = torch.empty_like(b.xg)
         self.asm.values = torch.empty(b.nnz, dtype=torch.float64, device=dev)
-        self.values32 = torch.empty(b.nnz, dtype=torch.float32, device=dev)
-        n = b.ndof
-        self.dep = torch.empty(n, dtype=torch.float64, device=dev)
-        self.R = torch.empty(n, dtype=torch.float64, device=dev)
-        self.du = torch.empty(n, dtype=torch.float64, device=dev)
-        self.minv = torch.empty(n, dtype=torch.float64, device=dev)
+        self.dep = torch.empty(b.ndof, dtype=torch.float64, device=dev)
 
     def run(self, req: Request, stream, precision: str = "mixed") -> None:
         a = self.asm
         with torch.cuda.stream(stream):
             a.xg.copy_(req.inputs["coords"], non_blocking=True)
             c = req.inputs["c"].to(a.device, non_blocking=True)
-            mm = self.mm
             _mr_start_state(a.xg, req.inputs["lam"], self.dep)
-            info = _mr_newton_step(a, self.dep, c, mm.fixed, mm.fixed_b, self.R, self.du, self.minv, self.values32,
-                                   precision, stream)
+            req.info = _mr_load_step(a, self.dep, c, self.mm.fixed, precision, stream)
             out = torch.empty(a.ndof, dtype=torch.float64, pin_memory=True)
             out.copy_(self.dep, non_blocking=True)
             stream.synchronize()
         req.result = out.numpy()
-        req.info = info
 
 
 def _mr_start_state(xg: torch.Tensor, lam: float, dep: torch.Tensor) -> None:
@@ -323,35 +389,23 @@ def _mr_start_state(xg: torch.Tensor, lam: float, dep: torch.Tensor) -> None:
     dep[3 * nq:] = 0.0
 
 
-def _mr_newton_step(a, dep, c, fixed_u8, fixed_b, R, du, minv, values32, precision, stream) -> dict:
-    """One Newton correction of the MR problem: R, consistent tangent, MINRES to MR_LINEAR_RTOL,
-    dep += du, the new residual norm."""
-    a.residual(dep, c, out=R, stream=stream)
-    R.masked_fill_(fixed_b, 0.0)
-    r0 = float(torch.linalg.vector_norm(R))
-    vals = a.tangent(dep, c, precision=precision, stream=stream)
-    saddle_preconditioner(a.row_ptr, a.col_idx, vals, 3 * a.n_q2, fixed_u8, out=minv, stream=stream)
-    v32 = None
-    if precision == "mixed":
-        values32.copy_(vals)
-        v32 = values32
-    du.zero_()
-    R.neg_()
-    li = minres_solve(a.row_ptr, a.col_idx, vals, R, fixed_u8, du, minv=minv, values32=v32, rtol=MR_LINEAR_RTOL,
-                      max_iters=100000, precision=precision, stream=stream, n_node=a.n_q2)
-    dep.add_(du)
-    a.residual(dep, c, out=R, stream=stream)
-    R.masked_fill_(fixed_b, 0.0)
-    r1 = float(torch.linalg.vector_norm(R))
-    return {"linear_iterations": li.iterations, "residual_before": r0, "residual_after": r1}
+def _mr_load_step(a, dep, c, fixed_u8, precision, stream) -> dict:
+    """The request's load step: Newton from `dep` (the predictor, which holds the final Dirichlet
+    values) to Iron's default tolerances, consistent tangent, MINRES linear solves."""
+    solver = NewtonSolver(a, c, precision=precision, stream=stream)
+    info = solver.solve(dep, fixed_u8)[0]
+    return {"newton_iterations": info.iterations, "linear_iterations": int(sum(info.linear_iterations)),
+            "residual_norm": info.residual_norms[-1], "initial_residual_norm": info.residual_norms[0],
+            "reason": info.reason}
 
 
 # ---- the engine ------------------------------------------------------------------------------------
 
 def estimate_bytes(kind: str, n: int) -> tuple[int, int]:
-    """(resident bytes per mesh size, working bytes per slot) used for admission: upper estimates
-    of the device memory the engine allocates (torch tensors plus the library's stream-ordered
-    scratch), so the accounted total never falls below what is in use."""
+    """(resident bytes per mesh size, working bytes per request) used for admission: upper
+    estimates of the device memory the engine allocates (torch tensors plus the library's
+    stream-ordered scratch), so the accounted total never falls below what is in use.  A Laplace
+    slot holds laplace_batch_capacity(n) requests' working memory (slot_bytes)."""
     E = n ** 3
     if kind == "laplace":
         N = (n + 1) ** 3
@@ -366,8 +420,16 @@ def estimate_bytes(kind: str, n: int) -> tuple[int, int]:
         # with 125 u nodes and 27 p nodes; boundary rows have fewer
         nnz = 3 * Nq * 208 + Np * 402
         resident = 4 * (ndof + 1) + 4 * nnz + 4 * 89 * 89 * E + 4 * (27 + 8 + 89 + 1) * E + 24 * Nq + 10 * ndof
-        work = 12 * nnz + 24 * Nq + 32 * ndof + 84 * ndof + 27 * 99 * 8 * ((E + 7) // 8)
+        # values (FP64 + FP32 copy), coordinates, the solution and the Newton vectors, MINRES
+        # scratch, the element tangents of a colour batch
+        work = 12 * nnz + 24 * Nq + 48 * ndof + 84 * ndof + 27 * 99 * 8 * ((E + 7) // 8)
     return int(1.05 * resident) + (1 << 20), int(1.05 * work) + (1 << 20)
+
+
+def slot_bytes(kind: str, n: int) -> int:
+    """Working bytes charged per Laplace (worker, size) slot or per Mooney-Rivlin request."""
+    work = estimate_bytes(kind, n)[1]
+    return work * laplace_batch_capacity(n) if kind == "laplace" else work
 
 
 class HbmLedger:
@@ -375,9 +437,9 @@ class HbmLedger:
 
     Charges, against `budget` bytes: resident per-size state (charged when a request for a new size
     is admitted, kept until evicted), Laplace per-(worker, size) slots (kept with their size's
-    resident state), and Mooney-Rivlin per-request working memory (released when the request
-    ends).  Eviction frees least-recently-used sizes that no admitted request holds, together with
-    their slots."""
+    resident state; a slot serves a batch of up to laplace_batch_capacity(n) requests), and
+    Mooney-Rivlin per-request working memory (released when the request ends).  Eviction frees
+    least-recently-used sizes that no admitted request holds, together with their slots."""
 
     def __init__(self, budget: int):
         self.budget = int(budget)
@@ -406,7 +468,8 @@ class HbmLedger:
     def admit(self, rid: int, kind: str, n: int, worker: int):
         """Charge a request; returns (admitted, evicted size keys, dropped slot keys)."""
         key = (kind, n)
-        res_b, work_b = estimate_bytes(kind, n)
+        res_b = estimate_bytes(kind, n)[0]
+        work_b = slot_bytes(kind, n)
         need = 0 if key in self.resident else res_b
         if kind == "laplace":
             need += 0 if (worker,) + key in self.slots else work_b
@@ -469,7 +532,8 @@ class ServingEngine:
         self.slots: dict = {}  # (worker, "laplace", n) -> slot
         self.lock = threading.Lock()
         self.cv = threading.Condition(self.lock)
-        self.stats = {"evictions": 0, "graphs_captured": 0, "max_concurrent": 0, "oom_retries": 0}
+        self.stats = {"evictions": 0, "graphs_captured": 0, "max_concurrent": 0, "oom_retries": 0, "batches": 0,
+                      "batched_requests": 0}
         self._graveyard: list = []
 
     @property
@@ -513,10 +577,9 @@ class ServingEngine:
                 return _MRSlot(mesh, self.dev)
             if slot is None:
                 slot = _LaplaceSlot(mesh, self.dev, self.use_graphs)
-                if self.use_graphs:
-                    slot.capture(self.streams[worker])
-                    self.stats["graphs_captured"] += 2
+                slot.capture(self.streams[worker])
                 with self.lock:
+                    self.stats["graphs_captured"] += slot.n_graphs
                     self.slots[sk] = slot
         return slot
 
@@ -545,37 +608,47 @@ class ServingEngine:
         done_count = 0
         fatal = None
 
-        def work(req: Request, worker: int):
+        def work(group: list, worker: int):
             nonlocal running, done_count
             stream = self.streams[worker]
+            lead = group[0]
             try:
                 _lib.set_thread_error_word(self.err_words[worker])
                 with torch.cuda.stream(stream):
-                    slot = self._prepare(req, worker)
-                if req.kind == "laplace":
-                    slot.run(req, stream)
+                    slots = [self._prepare(r, worker) for r in group]
+                slot = slots[0]
+                del slots
+                if lead.kind == "laplace":
+                    before = slot.n_graphs
+                    slot.run(group, stream)
+                    with self.lock:
+                        self.stats["graphs_captured"] += slot.n_graphs - before
                 else:
-                    slot.run(req, stream, self.mr_precision)
+                    slot.run(lead, stream, self.mr_precision)
                     del slot  # per-request working memory
             except Exception as e:  # reported after the loop
-                oom = _is_out_of_memory(e) and retries.get(req.rid, 0) < OOM_RETRIES
+                oom = _is_out_of_memory(e) and all(retries.get(r.rid, 0) < OOM_RETRIES for r in group)
                 if not oom:
-                    errors.append((req.rid, repr(e)))
+                    errors.extend((r.rid, repr(e)) for r in group)
             else:
                 oom = False
             finally:
-                req.t_done = time.perf_counter() - t0
+                t_done = time.perf_counter() - t0
                 with self.cv:
                     running -= 1
-                    self.ledger.finish(req.rid, req.kind, req.n)
+                    for r in group:
+                        r.t_done = t_done
+                        self.ledger.finish(r.rid, r.kind, r.n)
                     free_workers.append(worker)
                     if oom:
-                        retries[req.rid] = retries.get(req.rid, 0) + 1
-                        pending.appendleft(req)
+                        # retried alone, at the head of the queue
+                        for r in reversed(group):
+                            retries[r.rid] = retries.get(r.rid, 0) + 1
+                            pending.appendleft(r)
                         compact[0] = True
                         self.stats["oom_retries"] += 1
                     else:
-                        done_count += 1
+                        done_count += len(group)
                     self.cv.notify_all()
 
         threads = []
@@ -602,7 +675,9 @@ class ServingEngine:
                 for req in [r for r in pending if r.cancelled]:
                     pending.remove(req)
                     done_count += 1
-                # admit in arrival order; a request that does not fit may be overtaken
+                # admit in arrival order; a request that does not fit may be overtaken.  A small
+                # Laplace request takes queued requests of its side along (up to the slot's
+                # capacity), except one that is being retried after running out of memory
                 i = 0
                 while i < len(pending) and free_workers:
                     req = pending[i]
@@ -612,10 +687,27 @@ class ServingEngine:
                     if ok:
                         free_workers.pop()
                         del pending[i]
-                        req.t_admit = clock() if realtime else time.perf_counter() - t0
+                        group = [req]
+                        if req.kind == "laplace" and req.rid not in retries:
+                            cap = laplace_batch_capacity(req.n)
+                            j = i
+                            while len(group) < cap and j < len(pending):
+                                r = pending[j]
+                                if (r.kind == "laplace" and r.n == req.n and r.rid not in retries
+                                        and self.ledger.admit(r.rid, r.kind, r.n, w)[0]):
+                                    group.append(r)
+                                    del pending[j]
+                                else:
+                                    j += 1
+                        now = clock() if realtime else time.perf_counter() - t0
+                        for r in group:
+                            r.t_admit = now
+                        if len(group) > 1:
+                            self.stats["batches"] += 1
+                            self.stats["batched_requests"] += len(group)
                         running += 1
                         self.stats["max_concurrent"] = max(self.stats["max_concurrent"], running)
-                        th = threading.Thread(target=work, args=(req, w), daemon=True)
+                        th = threading.Thread(target=work, args=(group, w), daemon=True)
                         threads.append(th)
                         th.start()
                     else:
@@ -703,6 +795,12 @@ def summarize(reqs: list[Request]) -> dict:
         its = [i for i in its if i is not None]
         if its:
             out[f"{kind}_solver_iterations_mean"] = float(np.mean(its))
+        nits = [r.info["newton_iterations"] for r in rk if "newton_iterations" in r.info]
+        if nits:
+            out[f"{kind}_newton_iterations_mean"] = float(np.mean(nits))
+        batch = [r.info["batch"] for r in rk if "batch" in r.info]
+        if batch:
+            out[f"{kind}_batch_mean"] = float(np.mean(batch))
     return out
 
 
@@ -738,12 +836,9 @@ def plain_fp64(requests: list[Request], realtime: bool = True) -> dict:
                                      device=dev)
             c = req.inputs["c"].to(dev)
             fixed, _full = uniaxial_roller_conditions(A, req.inputs["lam"])
-            fb = fixed.bool()
             dep = torch.empty(A.ndof, dtype=torch.float64, device=dev)
             _mr_start_state(A.xg, req.inputs["lam"], dep)
-            n = A.ndof
-            R, du, minv = (torch.empty(n, dtype=torch.float64, device=dev) for _ in range(3))
-            req.info = _mr_newton_step(A, dep, c, fixed, fb, R, du, minv, None, "fp64", None)
+            req.info = _mr_load_step(A, dep, c, fixed, "fp64", None)
             req.result = dep.cpu().numpy()
         torch.cuda.synchronize()
         req.t_done = time.perf_counter() - t0
@@ -752,16 +847,28 @@ def plain_fp64(requests: list[Request], realtime: bool = True) -> dict:
 
 # ---- bench entry -----------------------------------------------------------------------------------
 
-def bench(args, log, clock_sampler):
-    import json
-
-    n_req = getattr(args, "serve_requests", 2000)
-    reqs = request_stream(n_requests=n_req, seed=0)
-    log(f"serve: generating inputs for {len(reqs)} requests")
+def _agreement(reqs, res_engine) -> dict:
+    """Engine results against the plain FP64 path's (on the requests): Laplace solutions (both CG
+    to a relative residual of 1e-10); Mooney-Rivlin geometry and pressure (both Newton to Iron's
+    tolerances, FP32 contraction and Krylov in the engine, FP64 in the plain path)."""
+    lap, mr_x, mr_p = 0.0, 0.0, 0.0
     for r in reqs:
-        make_inputs(r)
+        a, b = res_engine[r.rid], r.result
+        if r.kind == "laplace":
+            lap = max(lap, float(np.abs(a - b).max()))
+        else:
+            nx = 3 * (2 * r.n + 1) ** 3
+            mr_x = max(mr_x, float(np.abs(a[:nx] - b[:nx]).max()))
+            mr_p = max(mr_p, float(np.abs(a[nx:] - b[nx:]).max() / max(np.abs(b[nx:]).max(), 1e-300)))
+    return {"laplace_max_abs_diff_vs_plain": lap, "mr_geometry_max_abs_diff_vs_plain": mr_x,
+            "mr_pressure_max_rel_diff_vs_plain": mr_p}
+
+
+def measure_stream(reqs: list[Request], workers: int, clock_sampler, log) -> dict:
+    """Serve `reqs` in real time through a fresh engine, then through plain_fp64 one at a time
+    (on an empty device), and compare.  Inputs must be made; a small warm-up stream runs first."""
     dev = torch.device("cuda", 0)
-    eng = ServingEngine(dev, workers=getattr(args, "serve_workers", 8))
+    eng = ServingEngine(dev, workers=workers)
     # warm-up of both arms: small requests of each kind (library load and page-in, kernel attributes)
     warm = request_stream(n_requests=4, laplace_fraction=0.5, seed=99, n_lo=4, n_hi=5)
     assert {r.kind for r in warm} == {"laplace", "mr"}
@@ -771,40 +878,62 @@ def bench(args, log, clock_sampler):
     for r in warm:
         r.result = None
     plain_fp64(warm, realtime=False)
-    log("serve: engine")
+    log(f"serve: engine, {len(reqs)} requests")
     with clock_sampler(dev.index) as clk:
         s_eng = eng.serve(reqs, realtime=True)
     res_engine = {r.rid: r.result for r in reqs}
-    info_engine = {r.rid: dict(r.info) for r in reqs}
     log(f"serve: engine p50 {s_eng['p50_ms']:.1f} ms p99 {s_eng['p99_ms']:.1f} ms; plain FP64 baseline")
     engine_stats = dict(eng.stats)
+    budget = eng.budget
     eng.close()  # the plain path runs on an empty device, as a process of its own would
     for r in reqs:
         r.result = None
     with clock_sampler(dev.index) as clk2:
         s_plain = plain_fp64(reqs, realtime=True)
-    # agreement with the plain FP64 path: Laplace solutions; MR post-step residual norms
-    lap_err, mr_ratio = 0.0, []
+    out = {"engine": s_eng, "plain_fp64_one_at_a_time": s_plain,
+           "p50_speedup_vs_plain": s_plain["p50_ms"] / s_eng["p50_ms"],
+           "p99_speedup_vs_plain": s_plain["p99_ms"] / s_eng["p99_ms"],
+           "throughput_speedup_vs_plain": s_eng["requests_per_s"] / s_plain["requests_per_s"]}
+    out.update(_agreement(reqs, res_engine))
+    out.update({"engine_stats": engine_stats, "hbm_budget_GB": budget / 1e9, "clocks": clk.summary(),
+                "clocks_plain": clk2.summary()})
+    if _lib.STALE_ERRORS:
+        out["stale_cuda_errors"] = {f"{k[0]}:{k[1]}": v for k, v in _lib.STALE_ERRORS.items()}
+    return out
+
+
+def stream_config(reqs: list[Request], rate: float, n_hi: int, mr_n_hi: int, workers: int) -> dict:
+    return {"workload": "serve_stream", "requests": len(reqs), "arrivals": f"Poisson {rate:g}/s", "laplace": 0.7,
+            "side": f"round(exp(U(ln 4, ln {n_hi})))", "mr_side": f"round(exp(U(ln 4, ln {mr_n_hi})))",
+            "laplace_solve": f"CG rtol {LAPLACE_RTOL}",
+            "mr_solve": "one load step: Newton to abs 1e-10 / rel 1e-5 (step 1e-5), MINRES rtol 1e-5",
+            "batching": f"up to {LAPLACE_BATCH} Laplace requests of one side <= {BATCH_MAX_N} per graph launch",
+            "workers": workers}
+
+
+# Mooney-Rivlin sides of the served streams: a Newton load step at side 64 (6.7 M unknowns) takes
+# the order of a minute on one GPU, so served Mooney-Rivlin requests stay at sides 4..MR_SERVE_N_HI
+MR_SERVE_N_HI = 16
+
+
+def bench(args, log, clock_sampler):
+    """The request-stream workload: Poisson arrivals at 200/s (sides 4..64, Mooney-Rivlin sides
+    4..MR_SERVE_N_HI), served by the engine and by the plain path."""
+    import json
+
+    n_req = getattr(args, "serve_requests", 2000)
+    rate = getattr(args, "serve_rate", 200.0)
+    workers = getattr(args, "serve_workers", 8)
+    reqs = request_stream(n_requests=n_req, rate=rate, seed=0, mr_n_hi=MR_SERVE_N_HI)
+    log(f"serve: generating inputs for {len(reqs)} requests")
     for r in reqs:
-        if r.kind == "laplace":
-            lap_err = max(lap_err, float(np.abs(res_engine[r.rid] - r.result).max()))
-        else:
-            a, b = info_engine[r.rid]["residual_after"], r.info["residual_after"]
-            mr_ratio.append(a / b if b > 0 else 1.0)
+        make_inputs(r)
+    m = measure_stream(reqs, workers, clock_sampler, log)
     line = {
-        "metric": "serve_p99_latency_ms", "value": s_eng["p99_ms"], "unit": "ms", "n_gpus": 1, "steps": 1,
+        "metric": "serve_p99_latency_ms", "value": m["engine"]["p99_ms"], "unit": "ms", "n_gpus": 1, "steps": 1,
         "warmup": 1, "higher_is_better": False, "dtype": "f64 (Laplace mixed_df assembly), f32/f64 (MR)",
-        "data": "synthetic",
-        "config": {"workload": "serve_stream", "requests": len(reqs), "arrivals": "Poisson 200/s", "laplace": 0.7,
-                   "side": "round(exp(U(ln 4, ln 64)))", "laplace_solve": f"CG rtol {LAPLACE_RTOL}",
-                   "mr_request": f"one Newton step, MINRES rtol {MR_LINEAR_RTOL}", "workers": eng.workers,
-                   "hbm_budget_GB": eng.budget / 1e9},
-        "engine": s_eng, "plain_fp64_one_at_a_time": s_plain,
-        "p99_speedup_vs_plain": s_plain["p99_ms"] / s_eng["p99_ms"],
-        "throughput_speedup_vs_plain": s_eng["requests_per_s"] / s_plain["requests_per_s"],
-        "laplace_max_abs_diff_vs_plain": lap_err,
-        "mr_residual_after_ratio_vs_plain": [float(np.min(mr_ratio)), float(np.max(mr_ratio))] if mr_ratio else None,
-        "engine_stats": engine_stats, "clocks": clk.summary(), "clocks_plain": clk2.summary(),
+        "data": "synthetic", "config": stream_config(reqs, rate, 64, MR_SERVE_N_HI, workers),
     }
+    line.update(m)
     print(json.dumps(line), flush=True)
     return 0

@@ -90,17 +90,49 @@ def test_ledger_charges_and_releases_exactly():
 
 
 def test_ledger_refuses_what_cannot_fit_and_keeps_held_sizes():
-    from iron_gb300.serving import HbmLedger
+    from iron_gb300.serving import BATCH_MAX_N, HbmLedger
 
-    L = HbmLedger(sum(estimate_bytes("laplace", 12)))
-    assert L.admit(1, "laplace", 10, 0)[0]
+    a, b = BATCH_MAX_N + 4, BATCH_MAX_N + 8  # sides with one request per slot
+    L = HbmLedger(sum(estimate_bytes("laplace", b)))
+    assert L.admit(1, "laplace", a, 0)[0]
     # a second size cannot evict the first while request 1 holds it
-    assert not L.admit(2, "laplace", 12, 1)[0]
-    L.finish(1, "laplace", 10)
-    ok, evicted, dropped = L.admit(2, "laplace", 12, 1)
-    assert ok and evicted == [("laplace", 10)] and dropped == [(0, "laplace", 10)]
+    assert not L.admit(2, "laplace", b, 1)[0]
+    L.finish(1, "laplace", a)
+    ok, evicted, dropped = L.admit(2, "laplace", b, 1)
+    assert ok and evicted == [("laplace", a)] and dropped == [(0, "laplace", a)]
     L.check()
     # the same worker and size again costs nothing more
     before = L.in_use
-    L.finish(2, "laplace", 12)
-    assert L.admit(3, "laplace", 12, 1)[0] and L.in_use == before
+    L.finish(2, "laplace", b)
+    assert L.admit(3, "laplace", b, 1)[0] and L.in_use == before
+
+
+def test_batched_slots_are_charged_for_their_capacity():
+    from iron_gb300.serving import BATCH_MAX_N, LAPLACE_BATCH, HbmLedger, laplace_batch_capacity, slot_bytes
+
+    assert laplace_batch_capacity(4) == laplace_batch_capacity(BATCH_MAX_N) == LAPLACE_BATCH
+    assert laplace_batch_capacity(BATCH_MAX_N + 1) == 1
+    n = 8
+    res, work = estimate_bytes("laplace", n)
+    assert slot_bytes("laplace", n) == LAPLACE_BATCH * work and slot_bytes("mr", n) == estimate_bytes("mr", n)[1]
+    L = HbmLedger(10 * (res + LAPLACE_BATCH * work))
+    # the first request of a batch charges the size and the whole slot, the others nothing
+    for rid in range(LAPLACE_BATCH):
+        assert L.admit(rid, "laplace", n, 0)[0]
+        assert L.in_use == res + LAPLACE_BATCH * work
+    for rid in range(LAPLACE_BATCH):
+        L.finish(rid, "laplace", n)
+    L.check()
+    assert L.users[("laplace", n)] == 0
+
+
+def test_mooney_rivlin_side_cap():
+    full = request_stream(2000, rate=200.0, seed=0)
+    capped = request_stream(2000, rate=200.0, seed=0, mr_n_hi=16)
+    assert [(r.kind, r.seed, r.arrival) for r in full] == [(r.kind, r.seed, r.arrival) for r in capped]
+    for a, b in zip(full, capped):
+        if a.kind == "laplace":
+            assert a.n == b.n
+        else:
+            assert 4 <= b.n <= 16 and b.n <= a.n
+    assert max(r.n for r in capped if r.kind == "laplace") > 16
