@@ -5,9 +5,14 @@ against `from iron_gb300 import iron` with the same object names, Create/Finish 
 properties and enumerations (bindings/python/tests/Laplace.py:99-187 and Cantilever.py are the
 models), and `problem.Solve()` runs the element loop, structure and solve on the GPU:
 
-- classical field, Laplace equation, standard or generalised (isotropic conductivity per element,
-  set as the materials field's element values) subtype, on Iron's regular generated mesh of
-  trilinear-Lagrange hexahedra with 2x2x2 Gauss points (GPU context / mesh-handle path);
+- classical field, Laplace equation, standard or generalised subtype on Iron's regular generated
+  mesh of trilinear-Lagrange hexahedra with 2x2x2 Gauss points.  The generalised materials field
+  has Iron's six components K11 K22 K33 K12 K23 K13 (constants or element values), and a fibre
+  field (FieldTypes.FIBRE, up to three node-based angles) passed to EquationsSet.CreateStart
+  as Iron's geometric-fibre field sets the material frame.  An isotropic tensor runs the standard
+  element loop with a per-element conductivity (GPU context / mesh-handle path, Jacobi-CG); any
+  other tensor runs the generalised element loop, whose matrix is not symmetric, and restarted
+  GMRES (Iron's default Krylov method);
 - elasticity, finite elasticity, Mooney-Rivlin subtype on a regular generated mesh of
   triquadratic-Lagrange displacement with a trilinear pressure basis (two mesh components,
   node-based pressure), 3x3x3 Gauss points, load-stepped Newton with the Jacobian type chosen by
@@ -389,15 +394,30 @@ class Field(CMFEType):
         pass
 
     def ComponentInterpolationSet(self, var, comp, interp):
-        if interp != FieldInterpolationTypes.NODE_BASED:
-            _fail("covered field components: node based (element-based pressure is not covered)")
+        self.interpolation = getattr(self, "interpolation", {})
+        self.interpolation[(var, int(comp))] = interp
 
     def DOFOrderTypeSet(self, var, order):
         if order != FieldDOFOrderTypes.SEPARATED:
             _fail("covered DOF order: separated (Iron's default for these fields)")
 
+    def NumberOfComponentsSet(self, var, n):
+        self.n_components = int(n)
+
     def CreateFinish(self):
-        pass
+        if getattr(self, "type", None) == FieldTypes.FIBRE:
+            # node-based fibre angles on the geometric mesh; Iron's default: one per dimension
+            gm = getattr(self.region, "generated_mesh", None)
+            if gm is None:
+                _fail("a fibre field needs the region's generated mesh")
+            nc = getattr(self, "n_components", 3)
+            if not 1 <= nc <= 3:
+                _fail("a fibre field has 1 to 3 angle components")
+            n = gm.number_of_nodes()
+            self.role = "fibre"
+            self.values = np.zeros(nc * n)
+            self.layout = lambda comp: ((comp - 1) * n, comp * n)
+            self.node_dof = lambda node, comp: (comp - 1) * n + node - 1
 
     # parameter access on the dependent / materials vectors, Iron's 1-based numbers
     def _layout(self):
@@ -444,6 +464,8 @@ class EquationsSet(CMFEType):
         self.user_number = user_number
         self.region = region
         self.geometric = getattr(geometric_field, "geometric", geometric_field)
+        # Iron's geometric-fibre argument: a fibre field carries the material frame's angles
+        self.fibre = geometric_field if getattr(geometric_field, "type", None) == FieldTypes.FIBRE else None
         spec = list(specification)
         if len(spec) != 3:
             _fail("an equations set specification is [class, type, subtype]")
@@ -496,7 +518,10 @@ class EquationsSet(CMFEType):
             field.node_dof = node_dof
 
     def DependentCreateFinish(self):
-        pass
+        interp = getattr(self.dependent, "interpolation", {})
+        for (var, comp), how in interp.items():
+            if how != FieldInterpolationTypes.NODE_BASED:
+                _fail("covered dependent field components: node based (element-based pressure is not covered)")
 
     def MaterialsCreateStart(self, user_number, field: Field):
         self.materials = field
@@ -721,12 +746,12 @@ class Problem(CMFEType):
         coords = torch.from_numpy(es.geometric.values.reshape(3, -1).copy()).to(dev)
         kappa = None
         if es.subtype == EquationsSetSubtypes.GENERALISED_LAPLACE:
-            E = nx * ny * nz
-            c = es.materials.constants.get(1, 1.0) if es.materials else 1.0
-            k = np.full(E, c)
-            for e, v in (es.materials.element_values.get(1, {}) if es.materials else {}).items():
-                k[e - 1] = v
-            kappa = torch.from_numpy(k).to(dev)
+            cond = self._conductivity(es, nx * ny * nz)
+            if np.all(cond[0] == cond[1]) and np.all(cond[0] == cond[2]) and not np.any(cond[3:]):
+                # kappa * I in any frame is kappa * I in xi space: the standard element loop
+                kappa = torch.from_numpy(cond[0].copy()).to(dev)
+            else:
+                return self._solve_laplace_generalised(es, bc, cond)
         values = torch.empty(mesh.nnz, dtype=torch.float64, device=dev)
         mesh.assemble_laplace(coords, kappa, values, "fp64")
         fixed, _, target = self._dirichlet(es, bc)
@@ -740,6 +765,52 @@ class Problem(CMFEType):
         dep.values[:] = x.cpu().numpy()
         rp, ci = mesh.csr()
         es.equations.matrix = (rp.cpu().numpy(), ci.cpu().numpy(), values.cpu().numpy())
+
+    @staticmethod
+    def _conductivity(es, E: int) -> np.ndarray:
+        """[6][E] materials components K11 K22 K33 K12 K23 K13: the component constants
+        (ComponentValuesInitialiseDP; 0 when unset, as Iron's new field) with element values over them."""
+        cond = np.zeros((6, E))
+        mat = es.materials
+        if mat is None:
+            _fail("the generalised Laplace equation needs its materials field")
+        if any(c > 6 for c in list(mat.constants) + list(mat.element_values)):
+            _fail("the generalised Laplace materials field has 6 components in 3D")
+        for c, v in mat.constants.items():
+            cond[c - 1] = v
+        for c, ev in mat.element_values.items():
+            for e, v in ev.items():
+                if not 1 <= e <= E:
+                    _fail(f"element {e} outside 1..{E}")
+                cond[c - 1, e - 1] = v
+        return cond
+
+    def _solve_laplace_generalised(self, es, bc, cond):
+        from .laplace import LaplaceAssembly
+        from .mesh import RegularMesh
+        from .newton import gmres_solve
+
+        gm = es.geometric.generated_mesh
+        dev = _lib.require_cuda()
+        m = RegularMesh(tuple(int(v) for v in gm.numberOfElements))
+        A = LaplaceAssembly.from_regular_mesh(m, device=dev)
+        A.coords = torch.from_numpy(es.geometric.values.reshape(3, -1).copy()).to(dev)
+        fib = None
+        if es.fibre is not None:
+            fib = es.fibre.values.reshape(-1, m.n_nodes)
+        A.assemble_generalised(cond, fib)
+        fixed, _, target = self._dirichlet(es, bc)
+        x = torch.from_numpy(np.where(fixed == 1, target, 0.0)).to(dev)
+        s = self.solver
+        rtol = 1e-13 if s.linearType == LinearSolverTypes.DIRECT else float(s.linearIterativeRelativeTolerance)
+        f = torch.zeros(A.n_nodes, dtype=torch.float64, device=dev)
+        info = gmres_solve(A.row_ptr, A.col_idx, A.values, f, torch.from_numpy(fixed).to(dev), x, rtol=rtol,
+                           max_iters=int(s.linearIterativeMaximumIterations))
+        if not info.relative_residual <= rtol:
+            _fail(f"GMRES stopped at relative residual {info.relative_residual:.3e} after {info.iterations} "
+                  "iterations")
+        es.dependent.values[:] = x.cpu().numpy()
+        es.equations.matrix = (A.row_ptr.cpu().numpy(), A.col_idx.cpu().numpy(), A.values.cpu().numpy())
 
     def _solve_mooney_rivlin(self, es, bc):
         from .elasticity import MooneyRivlinAssembly

@@ -194,6 +194,32 @@ class LaplaceAssembly:
             _lib.raise_device_errors("gfe_laplace_assemble", stream)
         return self.values
 
+    def assemble_generalised(self, conductivity, fibre=None, stream=None, check: bool = True) -> torch.Tensor:
+        """Generalised Laplace (gfe_laplace_assemble_generalised): assemble K into self.values (FP64)
+        with a full conductivity tensor per element in a material frame.  conductivity [6][n_elements]
+        (K11 K22 K33 K12 K23 K13 in material coordinates); fibre [n_angles][n_nodes] nodal fibre,
+        imbrication and sheet angles in radians (1 to 3 rows) or None for no fibre field.  Trilinear
+        hexahedra only; the matrix is not symmetric in general."""
+        if self.tensor_product:
+            raise GfeError(-1, "the generalised Laplace kernel is for trilinear hexahedra")
+        cond = torch.as_tensor(conductivity, dtype=torch.float64).to(self.device).contiguous()
+        if cond.shape != (6, self.n_elements):
+            raise GfeError(-1, f"conductivity must be [6][{self.n_elements}], got {tuple(cond.shape)}")
+        fib, n_ang = None, 0
+        if fibre is not None:
+            fib = torch.as_tensor(fibre, dtype=torch.float64).to(self.device).contiguous()
+            if fib.dim() != 2 or fib.shape[1] != self.n_nodes or not 1 <= fib.shape[0] <= 3:
+                raise GfeError(-1, f"fibre must be [1..3][{self.n_nodes}], got {tuple(fib.shape)}")
+            n_ang = fib.shape[0]
+        cp = self.colour_ptr
+        _lib.call("gfe_laplace_assemble_generalised", self.n_elements, self.n_nodes, _lib.ptr(self.elem_nodes),
+                  _lib.ptr(self.coords), _lib.ptr(cond), _lib.ptr(fib), n_ang, _lib.ptr(self.colour_elems),
+                  cp.ctypes.data_as(C.c_void_p), len(cp) - 1, _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx),
+                  self.nnz, _lib.ptr(self.values), _lib.ptr(self.rhs), _lib.stream_handle(stream))
+        if check:
+            _lib.raise_device_errors("gfe_laplace_assemble_generalised", stream)
+        return self.values
+
     def assemble_to_host(self, values_host: torch.Tensor, precision: str = "mixed_df", coords_host=None,
                          kappa_host=None, slab_layers: int = 16, stream=None) -> torch.Tensor:
         """End-to-end assembly with host buffers on Iron's regular generated mesh

@@ -54,6 +54,9 @@ def lib():
                                            i32p, i32p, f64p, C.c_void_p, C.c_int]
         L.orc_laplace_assemble_scaled.argtypes = [C.c_int, i32p, i32p, C.c_int, C.c_int, i32p, f64p, C.c_void_p,
                                                   C.c_void_p, i32p, i32p, f64p, C.c_void_p, C.c_int]
+        L.orc_laplace_generalised_element.argtypes = [C.c_int, i32p, i32p, f64p, f64p, C.c_void_p, C.c_int, f64p]
+        L.orc_laplace_generalised_assemble.argtypes = [C.c_int, i32p, i32p, C.c_int, C.c_int, i32p, f64p, f64p,
+                                                       C.c_void_p, C.c_int, i32p, i32p, f64p, C.c_void_p]
         L.orc_csr_spmv.argtypes = [C.c_int, i32p, i32p, f64p, f64p, f64p]
         L.orc_solver_system.argtypes = [C.c_int, i32p, i32p, f64p, C.c_void_p, u8p, C.c_void_p, f64p, i32p, i32p,
                                         i32p, f64p, f64p, C.c_int64, C.POINTER(C.c_int32)]
@@ -180,6 +183,41 @@ def laplace_element(nxi, order, ngauss, xe, kappa=1.0):
     if rc != 0:
         raise ValueError("bad element")
     return K
+
+
+def laplace_generalised_element(nxi, order, ngauss, xe, cond, fibre=None):
+    """Generalised Laplace element matrix: cond the element-constant conductivity components
+    (3D: K11 K22 K33 K12 K23 K13; 2D: K11 K22 K12), fibre [n_angles][nns] the element's fibre
+    angles (radians) or None for no fibre field."""
+    xe = _f64(xe)
+    nns = xe.shape[1]
+    K = np.zeros((nns, nns))
+    fe = None if fibre is None else _f64(fibre)
+    rc = lib().orc_laplace_generalised_element(nxi, _i32(order), _i32(ngauss), xe, _f64(cond),
+                                               None if fe is None else fe.ctypes.data,
+                                               0 if fe is None else fe.shape[0], K)
+    if rc != 0:
+        raise ValueError("bad element")
+    return K
+
+
+def laplace_generalised_assemble(nxi, order, ngauss, elem_nodes, coords, cond, rp, ci, fibre=None):
+    """Generalised Laplace assembly: cond [n_elem][3 or 6] element-constant conductivity, fibre
+    [n_angles][N] nodal fibre angles or None.  Returns (values, rhs)."""
+    elem_nodes = _i32(elem_nodes)
+    coords = _f64(coords)
+    E = elem_nodes.shape[0]
+    N = coords.shape[1]
+    vals = np.zeros(int(rp[-1]) - 1)
+    rhs = np.zeros(N)
+    fib = None if fibre is None else _f64(fibre)
+    rc = lib().orc_laplace_generalised_assemble(nxi, _i32(order), _i32(ngauss), E, N, elem_nodes, coords,
+                                                _f64(cond), None if fib is None else fib.ctypes.data,
+                                                0 if fib is None else fib.shape[0], _i32(rp), _i32(ci), vals,
+                                                rhs.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"oracle assembly failed ({rc})")
+    return vals, rhs
 
 
 def laplace_assemble(nxi, order, ngauss, elem_nodes, coords, kappa, rp, ci, n_threads=1):

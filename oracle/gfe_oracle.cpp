@@ -610,6 +610,204 @@ void laplace_element(const TPBasis& b, const double* const* x, int ncomp, double
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Generalised Laplace: a full conductivity tensor in a material frame.
+// src/Laplace_equations_routines.F90:585-707 (EQUATIONS_SET_GENERALISED_LAPLACE_SUBTYPE): per
+// Gauss point the materials field gives the conductivity in material coordinates (3D order
+// K11 K22 K33 K12 K23 K13, 2D K11 K22 K12, :640-656), Coordinates_MaterialSystemCalculate gives
+// dNudXi and dXidNu (src/coordinate_routines.F90:3841-3947), the conductivity in xi space is
+// dNudXi * K * dXidNu (:665-670), and
+//   K(ms,ns) += RWG * sum_{i,k,h} C(i,k) * dphi_ns/dxi_k * dphi_ms/dxi_h * GU(i,h)   (:680-693).
+// The RHS is zero.
+// ---------------------------------------------------------------------------------------
+void normalise3(int n, const double* a, double* out) {
+  double s = 0.0;
+  for (int i = 0; i < n; ++i) s += a[i] * a[i];
+  const double l = std::sqrt(s);
+  for (int i = 0; i < n; ++i) out[i] = a[i] / l;
+}
+
+void cross3(const double* a, const double* b, double* c) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+void matmul3(int n, const double A[3][3], const double B[3][3], double C[3][3]) {
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s += A[i][k] * B[k][j];
+      C[i][j] = s;
+    }
+}
+
+// dX/dNu of the material frame.  With fibre angles: the reference frame f = DX_DXI(:,1),
+// h = f x DX_DXI(:,2), g = h x f (normalised), rotated by the fibre angle about axis 3, the
+// imbrication angle about the new axis 2 and the sheet angle about the new axis 1
+// (Coordinates_MaterialSystemCalculatedXdNu3D, src/coordinate_routines.F90:4020-4127); in 2D
+// f = DX_DXI(:,1), g = (-f2, f1), R(angle) * [f g] with normalised columns (:3952-4000).
+// Without a fibre field: the normalised columns of DX_DXI (:3879-3884).
+void material_dxdnu(int nd, const Metrics& m, const double* angle, int n_angles, double dXdNu[3][3]) {
+  std::memset(dXdNu, 0, sizeof(double) * 9);
+  if (!angle) {
+    for (int xi = 0; xi < nd; ++xi) {
+      double c[3] = {m.dx_dxi[0][xi], m.dx_dxi[1][xi], m.dx_dxi[2][xi]}, o[3];
+      normalise3(nd, c, o);
+      for (int i = 0; i < nd; ++i) dXdNu[i][xi] = o[i];
+    }
+    return;
+  }
+  if (nd == 2) {
+    double f[2] = {m.dx_dxi[0][0], m.dx_dxi[1][0]}, g[2] = {-f[1], f[0]}, fn[2], gn[2];
+    normalise3(2, f, fn);
+    normalise3(2, g, gn);
+    const double R[3][3] = {{std::cos(angle[0]), std::sin(angle[0]), 0.0}, {-std::sin(angle[0]), std::cos(angle[0]), 0.0},
+                            {0.0, 0.0, 0.0}};
+    const double Rf[3][3] = {{fn[0], gn[0], 0.0}, {fn[1], gn[1], 0.0}, {0.0, 0.0, 0.0}};
+    double P[3][3];
+    matmul3(2, R, Rf, P);
+    for (int c = 0; c < 2; ++c) {
+      double col[2] = {P[0][c], P[1][c]}, o[2];
+      normalise3(2, col, o);
+      dXdNu[0][c] = o[0];
+      dXdNu[1][c] = o[1];
+    }
+    return;
+  }
+  double a[3] = {0.0, 0.0, 0.0};
+  for (int i = 0; i < n_angles && i < 3; ++i) a[i] = angle[i];
+  double f[3] = {m.dx_dxi[0][0], m.dx_dxi[1][0], m.dx_dxi[2][0]};
+  double d2[3] = {m.dx_dxi[0][1], m.dx_dxi[1][1], m.dx_dxi[2][1]};
+  double h[3], g[3], fn[3], gn[3], hn[3];
+  cross3(f, d2, h);
+  cross3(h, f, g);
+  normalise3(3, f, fn);
+  normalise3(3, g, gn);
+  normalise3(3, h, hn);
+  double R0[3][3];
+  for (int i = 0; i < 3; ++i) {
+    R0[i][0] = fn[i];
+    R0[i][1] = gn[i];
+    R0[i][2] = hn[i];
+  }
+  const double ca = std::cos(a[0]), sa = std::sin(a[0]), cb = std::cos(a[1]), sb = std::sin(a[1]),
+               cg = std::cos(a[2]), sg = std::sin(a[2]);
+  const double Rz[3][3] = {{ca, -sa, 0.0}, {sa, ca, 0.0}, {0.0, 0.0, 1.0}};
+  const double Ry[3][3] = {{cb, 0.0, sb}, {0.0, 1.0, 0.0}, {-sb, 0.0, cb}};
+  const double Rx[3][3] = {{1.0, 0.0, 0.0}, {0.0, cg, -sg}, {0.0, sg, cg}};
+  double T1[3][3], T2[3][3];
+  matmul3(3, R0, Rz, T1);
+  matmul3(3, T1, Ry, T2);
+  matmul3(3, T2, Rx, dXdNu);
+}
+
+// Iron's material conductivity tensor from the materials field components (:640-656).
+void conductivity_material(int nd, const double* k, double K[3][3]) {
+  std::memset(K, 0, sizeof(double) * 9);
+  if (nd == 2) {
+    K[0][0] = k[0]; K[1][1] = k[1]; K[0][1] = K[1][0] = k[2];
+  } else {
+    K[0][0] = k[0]; K[1][1] = k[1]; K[2][2] = k[2];
+    K[0][1] = K[1][0] = k[3];
+    K[1][2] = K[2][1] = k[4];
+    K[0][2] = K[2][0] = k[5];
+  }
+}
+
+// x: element geometric parameters x[comp][ns]; cond: the element's conductivity components
+// (element-constant materials field); fib: the element's fibre parameters fib[angle][ns]
+// (interpolated with the element basis) or nullptr for no fibre field.
+void laplace_element_generalised(const TPBasis& b, const double* const* x, const double* cond,
+                                 const double* const* fib, int n_angles, double* K) {
+  const int n = b.nns, nd = b.nxi;
+  std::fill(K, K + (size_t)n * n, 0.0);
+  Metrics m;
+  double Km[3][3];
+  conductivity_material(nd, cond, Km);
+  for (int g = 0; g < b.ng; ++g) {
+    metrics_at(b, g, x, nd, m);
+    const double rwg = m.jac * b.wts[g];
+    double ang[3] = {0.0, 0.0, 0.0};
+    if (fib) {
+      const double* phi = &b.tab[((size_t)g * (nd + 1)) * n];
+      for (int a = 0; a < n_angles; ++a) {
+        double s = 0.0;
+        for (int ns = 0; ns < n; ++ns) s += phi[ns] * fib[a][ns];
+        ang[a] = s;
+      }
+    }
+    double dXdNu[3][3], dNudX[3][3], dNudXi[3][3], dXidNu[3][3], T[3][3], C[3][3];
+    material_dxdnu(nd, m, fib ? ang : nullptr, n_angles, dXdNu);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) dNudX[i][j] = dXdNu[j][i];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) dNudXi[i][j] = i == j ? 1.0 : 0.0;
+    double P[3][3];
+    matmul3(nd, dNudX, m.dx_dxi, P);
+    for (int i = 0; i < nd; ++i)
+      for (int j = 0; j < nd; ++j) dNudXi[i][j] = P[i][j];
+    invert(nd, dNudXi, dXidNu);
+    matmul3(nd, dNudXi, Km, T);
+    matmul3(nd, T, dXidNu, C);
+    for (int ms = 0; ms < n; ++ms) {
+      double pgm[3];
+      for (int i = 0; i < nd; ++i) pgm[i] = b.tab[((size_t)g * (nd + 1) + i + 1) * n + ms];
+      for (int ns = 0; ns < n; ++ns) {
+        double pgn[3];
+        for (int i = 0; i < nd; ++i) pgn[i] = b.tab[((size_t)g * (nd + 1) + i + 1) * n + ns];
+        double sum = 0.0;
+        for (int i = 0; i < nd; ++i)
+          for (int k = 0; k < nd; ++k)
+            for (int h = 0; h < nd; ++h) sum += C[i][k] * pgn[k] * pgm[h] * m.gu[i][h];
+        K[(size_t)ms * n + ns] += sum * rwg;
+      }
+    }
+  }
+}
+
+int orc_laplace_generalised_element(int nxi, const int* order, const int* ngauss, const double* xe,
+                                    const double* cond, const double* fe /*[n_angles][nns] or null*/, int n_angles,
+                                    double* K) {
+  TPBasis b;
+  if (!make_tp_basis(nxi, order, ngauss, b)) return -1;
+  const double* x[3] = {xe, xe + b.nns, xe + 2 * b.nns};
+  const double* f[3] = {fe, fe ? fe + b.nns : nullptr, fe ? fe + 2 * b.nns : nullptr};
+  laplace_element_generalised(b, x, cond, fe ? f : nullptr, n_angles, K);
+  return 0;
+}
+
+// Whole-mesh generalised assembly (the loop of orc_laplace_assemble_scaled without scale
+// factors).  cond [n_elem][ncond] element-constant conductivity components; fibre [n_angles][N]
+// nodal fibre angles (radians) or nullptr.
+int orc_laplace_generalised_assemble(int nxi, const int* order, const int* ngauss, int n_elem, int n_nodes,
+                                     const int32_t* elem_nodes, const double* coords, const double* cond,
+                                     const double* fibre, int n_angles, const int32_t* row_ptr,
+                                     const int32_t* col_idx, double* values, double* rhs) {
+  TPBasis b;
+  if (!make_tp_basis(nxi, order, ngauss, b)) return -1;
+  const int n = b.nns, ncond = nxi == 2 ? 3 : 6;
+  const int64_t nnz = (int64_t)row_ptr[n_nodes] - 1;
+  std::fill(values, values + nnz, 0.0);
+  if (rhs) std::fill(rhs, rhs + n_nodes, 0.0);
+  std::vector<double> xe((size_t)nxi * n), fe((size_t)3 * n), K((size_t)n * n);
+  std::vector<int32_t> dofs(n);
+  const double* x[3] = {xe.data(), xe.data() + n, xe.data() + 2 * n};
+  const double* f[3] = {fe.data(), fe.data() + n, fe.data() + 2 * n};
+  for (int e = 0; e < n_elem; ++e) {
+    for (int s = 0; s < n; ++s) {
+      const int node = elem_nodes[(size_t)e * n + s];
+      dofs[s] = node + 1;
+      for (int c = 0; c < nxi; ++c) xe[(size_t)c * n + s] = coords[(size_t)c * n_nodes + node];
+      if (fibre)
+        for (int a = 0; a < n_angles; ++a) fe[(size_t)a * n + s] = fibre[(size_t)a * n_nodes + node];
+    }
+    laplace_element_generalised(b, x, cond + (size_t)e * ncond, fibre ? f : nullptr, n_angles, K.data());
+    if (csr_values_add(row_ptr, col_idx, values, n, dofs.data(), n, dofs.data(), K.data()) != 0) return -2;
+  }
+  return 0;
+}
+
 // Element matrix of one element of a (possibly 2D) Lagrange mesh.
 int orc_laplace_element(int nxi, const int* order, const int* ngauss, int ncomp, const double* xe /*[ncomp][nns]*/,
                         double kappa, double* K) {

@@ -5,8 +5,11 @@
   nodal solution matches the oracle's (Iron's element loop restated in C++, with its own CG) within
   1e-9 relative, and the equations matrix read back with LinearMatrixGet / StorageLocationsGet /
   DataGet has Iron's CSR structure (bit-identical) and the oracle's values within 1e-13 x max|K|;
-- the same sequence with the generalised Laplace subtype and element conductivities in the
-  materials field;
+- the same sequence with the generalised Laplace subtype: isotropic element conductivities in
+  the materials field's three diagonal components (the standard element loop), and a full
+  anisotropic tensor with a three-angle nodal fibre field as Iron's geometric-fibre field (the
+  generalised element loop and GMRES), matching the oracle's generalised assembly within
+  1e-13 x max|K| and a direct solve of the oracle's system within 1e-9;
 - the Mooney-Rivlin sequence of bindings/python/tests/Cantilever.py restricted to the covered
   elements (triquadratic displacement, trilinear node-based pressure basis, no body force): a
   homogeneous uniaxial stretch with roller conditions set by AddNode / SetNode, solved in load
@@ -25,7 +28,7 @@ from iron_gb300 import mesh as M
 pytestmark = pytest.mark.gpu
 
 
-def _laplace_sequence(subtype=iron.EquationsSetSubtypes.STANDARD_LAPLACE, kappa=None, n=5):
+def _laplace_sequence(subtype=iron.EquationsSetSubtypes.STANDARD_LAPLACE, cond=None, n=5, fibre=None):
     height, width, length = 1.0, 2.0, 3.0
     coordinateSystem = iron.CoordinateSystem()
     coordinateSystem.CreateStart(1)
@@ -63,10 +66,24 @@ def _laplace_sequence(subtype=iron.EquationsSetSubtypes.STANDARD_LAPLACE, kappa=
         geometricField.ComponentMeshComponentSet(iron.FieldVariableTypes.U, c, 1)
     geometricField.CreateFinish()
     generatedMesh.GeometricParametersCalculate(geometricField)
+    geometricFibreField = geometricField
+    if fibre is not None:
+        fibreField = iron.Field()
+        fibreField.CreateStart(13, region)
+        fibreField.TypeSet(iron.FieldTypes.FIBRE)
+        fibreField.MeshDecompositionSet(decomposition)
+        fibreField.GeometricFieldSet(geometricField)
+        fibreField.NumberOfComponentsSet(iron.FieldVariableTypes.U, fibre.shape[0])
+        fibreField.CreateFinish()
+        for c in range(fibre.shape[0]):
+            for k in range(fibre.shape[1]):
+                fibreField.ParameterSetUpdateNodeDP(iron.FieldVariableTypes.U, iron.FieldParameterSetTypes.VALUES,
+                                                    1, 1, k + 1, c + 1, float(fibre[c, k]))
+        geometricFibreField = fibreField
     equationsSetField = iron.Field()
     equationsSet = iron.EquationsSet()
     spec = [iron.EquationsSetClasses.CLASSICAL_FIELD, iron.EquationsSetTypes.LAPLACE_EQUATION, subtype]
-    equationsSet.CreateStart(10, region, geometricField, spec, 8, equationsSetField)
+    equationsSet.CreateStart(10, region, geometricFibreField, spec, 8, equationsSetField)
     equationsSet.CreateFinish()
     dependentField = iron.Field()
     equationsSet.DependentCreateStart(9, dependentField)
@@ -74,13 +91,14 @@ def _laplace_sequence(subtype=iron.EquationsSetSubtypes.STANDARD_LAPLACE, kappa=
     dependentField.DOFOrderTypeSet(iron.FieldVariableTypes.DELUDELN, iron.FieldDOFOrderTypes.SEPARATED)
     equationsSet.DependentCreateFinish()
     dependentField.ComponentValuesInitialiseDP(iron.FieldVariableTypes.U, iron.FieldParameterSetTypes.VALUES, 1, 0.5)
-    if kappa is not None:
+    if cond is not None:
         materialsField = iron.Field()
         equationsSet.MaterialsCreateStart(11, materialsField)
         equationsSet.MaterialsCreateFinish()
-        for e, k in enumerate(kappa):
-            materialsField.ParameterSetUpdateElementDP(iron.FieldVariableTypes.U, iron.FieldParameterSetTypes.VALUES,
-                                                       e + 1, 1, float(k))
+        for c in range(6):
+            for e, k in enumerate(cond[c]):
+                materialsField.ParameterSetUpdateElementDP(iron.FieldVariableTypes.U,
+                                                           iron.FieldParameterSetTypes.VALUES, e + 1, c + 1, float(k))
     equations = iron.Equations()
     equationsSet.EquationsCreateStart(equations)
     equations.sparsityType = iron.EquationsSparsityTypes.SPARSE
@@ -144,17 +162,48 @@ def _oracle_laplace(n, width, height, length, kappa):
 
 @pytest.mark.parametrize("generalised", [False, True])
 def test_laplace_example_sequence_matches_oracle(gfe_cuda, generalised):
-    kappa = None
+    kappa = cond = None
     subtype = iron.EquationsSetSubtypes.STANDARD_LAPLACE
     if generalised:
         kappa = np.exp(np.random.default_rng(4).uniform(np.log(0.1), np.log(10.0), 125))
+        cond = np.vstack([kappa, kappa, kappa, np.zeros((3, 125))])
         subtype = iron.EquationsSetSubtypes.GENERALISED_LAPLACE
-    u, (rp, ci, vals), dims, _ = _laplace_sequence(subtype, kappa)
+    u, (rp, ci, vals), dims, _ = _laplace_sequence(subtype, cond)
     uo, (orp, oci, ovals) = _oracle_laplace(*dims, kappa)
     assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
     assert np.abs(vals - ovals).max() <= 1e-13 * np.abs(ovals).max()
     assert u[0] == 0.0 and u[-1] == 1.0
     assert np.abs(u - uo).max() <= 1e-9 * np.abs(uo).max()
+
+
+def test_generalised_laplace_with_fibre_field_matches_oracle(gfe_cuda):
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+
+    n = 4
+    rng = np.random.default_rng(8)
+    L = rng.normal(size=(n ** 3, 3, 3))
+    T = L @ L.transpose(0, 2, 1) + 0.3 * np.eye(3)
+    cond = np.stack([T[:, 0, 0], T[:, 1, 1], T[:, 2, 2], T[:, 0, 1], T[:, 1, 2], T[:, 0, 2]])
+    fibre = rng.uniform(-0.8, 0.8, (3, (n + 1) ** 3))
+    u, (rp, ci, vals), (n, width, height, length), _ = _laplace_sequence(
+        iron.EquationsSetSubtypes.GENERALISED_LAPLACE, cond, n=n, fibre=fibre)
+    en = oracle.regular_mesh([n, n, n], 1)
+    xyz = oracle.regular_coords([n, n, n], 1, [0, 0, 0], [width, height, length])
+    N = xyz.shape[1]
+    orp, oci = oracle.csr_structure(en, N)
+    ovals, _ = oracle.laplace_generalised_assemble(3, [1, 1, 1], [2, 2, 2], en, xyz, cond.T.copy(), orp, oci, fibre)
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    assert np.abs(vals - ovals).max() <= 1e-13 * np.abs(ovals).max()
+    # the oracle's system solved directly: u = 0 at the first node, 1 at the last
+    K = sp.csr_matrix((ovals, oci - 1, orp - 1), shape=(N, N))
+    free = np.ones(N, bool)
+    free[[0, N - 1]] = False
+    x = np.zeros(N)
+    x[-1] = 1.0
+    x[free] = sla.spsolve(K[free][:, free].tocsc(), -K[free][:, ~free] @ x[~free])
+    assert u[0] == 0.0 and u[-1] == 1.0
+    assert np.abs(u - x).max() <= 1e-9 * np.abs(x).max()
 
 
 def test_context_mesh_cache_shares_structure(gfe_cuda):
