@@ -55,6 +55,13 @@ int gfe_version(void);
  * Returns the message length.  Replaces cmfe_ExtractErrorMessage (src/opencmiss_iron.F90:13159). */
 int gfe_last_error(char* buf, int len);
 
+/* Clear the CUDA runtime's error state of the calling host thread and return the cleared code
+ * (0: none).  Each entry point reports the launch errors of its own launches by that state, so a
+ * caller that mixes this library with other CUDA code calls it before an entry point; an error
+ * left there by other code is then not reported as the entry point's.  The library's own failures
+ * leave nothing behind.  No counterpart in the reference. */
+int gfe_clear_stale_error(void);
+
 /* Read and clear the device error word (bit set of GFE_DEVERR_* raised by kernels). */
 int gfe_device_errors(uint32_t* bits_host, void* stream);
 
@@ -225,6 +232,26 @@ int gfe_laplace_assemble(int32_t n_elem, int32_t n_nodes, const int32_t* elem_no
                          int32_t n_colors, const int32_t* row_ptr, const int32_t* col_idx, int64_t nnz,
                          double* values, float* values32, double* rhs, int32_t precision, void* stream);
 
+/* Generalised Laplace: the conductivity is a full symmetric tensor in a material frame.
+ * Replaces LaplaceEquation_FiniteElementCalculate's EQUATIONS_SET_GENERALISED_LAPLACE_SUBTYPE
+ * branch (src/Laplace_equations_routines.F90:585-707) with Coordinates_MaterialSystemCalculate
+ * (src/coordinate_routines.F90:3841-3947, 4020-4127) inside the same element loop and scatter as
+ * gfe_laplace_assemble.  FP64.
+ *  conductivity [6][n_elem] element-constant materials field, Iron's component order
+ *               K11 K22 K33 K12 K23 K13 in material coordinates
+ *  fibre        [n_angles][n_nodes] nodal fibre field (fibre, imbrication, sheet angles in radians,
+ *               interpolated trilinearly), or NULL: no fibre field (the material frame is then the
+ *               normalised columns of dX/dxi, as Iron's)
+ *  n_angles     1..3 with a fibre field, 0 without
+ * Other arguments as gfe_laplace_assemble; values are not symmetric in general (Iron rotates the
+ * tensor into xi space by a similarity transform).  Asynchronous, device errors as
+ * gfe_laplace_assemble (a non-finite conductivity raises GFE_DEVERR_NONFINITE). */
+int gfe_laplace_assemble_generalised(int32_t n_elem, int32_t n_nodes, const int32_t* elem_nodes, const double* coords,
+                                     const double* conductivity, const double* fibre, int32_t n_angles,
+                                     const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
+                                     const int32_t* row_ptr, const int32_t* col_idx, int64_t nnz, double* values,
+                                     double* rhs, void* stream);
+
 /* Same assembly for Iron's regular generated mesh of nx x ny x nz trilinear elements
  * (GENERATED_MESH_REGULAR_TYPE, src/generated_mesh_routines.F90:1568-1640: nodes and elements
  * numbered xi1 fastest), whose topology is implicit: no connectivity, colouring or column indices
@@ -337,20 +364,26 @@ int gfe_mr_residual(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int
                     const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
                     int32_t batch, const double* dep, const double* cpar, double* R, void* stream);
 
-/* Per-element CSR positions (0-based) of all 89x89 element entries, elements in colour order:
- * slots[n_elem][89][89] (-1 where absent).  Built once per mesh and structure. */
+/* Per-element CSR positions (0-based) of all 89x89 element entries, by element number:
+ * slots[e][r][c] (-1 where absent).  color_elems lists the elements to map (normally all, in any
+ * order).  Built once per mesh and structure. */
 int gfe_mr_slot_map(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, const int32_t* color_elems,
                     const int32_t* row_ptr, const int32_t* col_idx, int32_t* slots, void* stream);
 
-/* Iron's analytic Jacobian of one problem assembled into CSR values (zeroed first; needs `slots`)
- * and/or written as dense element matrices K_out[n_elem][89][89] (may be NULL).  Replaces the
- * element loop of EquationsSet_JacobianEvaluateStaticFEM (src/equations_set_routines.F90:4677-4798)
- * around FiniteElasticity_FiniteElementJacobianEvaluate (src/finite_elasticity_routines.F90:879-1296)
- * and EquationsMatrices_JacobianElementAdd (src/equations_matrices_routines.F90:2866-2909). */
+/* Iron's analytic Jacobian of one problem assembled into CSR values (needs `slots` and `row_ptr`;
+ * every value is written) and/or written as dense element matrices K_out[n_elem][89][89] (may be
+ * NULL).  Replaces the element loop of EquationsSet_JacobianEvaluateStaticFEM
+ * (src/equations_set_routines.F90:4677-4798) around FiniteElasticity_FiniteElementJacobianEvaluate
+ * (src/finite_elasticity_routines.F90:879-1296) and EquationsMatrices_JacobianElementAdd
+ * (src/equations_matrices_routines.F90:2866-2909).  The element matrices of the whole mesh are
+ * formed first (no colouring needed: color_elems is read as the list of all elements); each CSR
+ * row is then summed once from the rows of the elements around its node, in ascending element
+ * order, and written once.  Allocates and frees the element matrices (n_elem x 89 x 89 in the
+ * contraction type) and small scratch on `stream`. */
 int gfe_mr_jacobian(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, int32_t n_lin,
                     const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
-                    const double* dep, const double* cpar, const int32_t* slots, double* values, int64_t nnz,
-                    double* K_out, int32_t precision, void* stream);
+                    const double* dep, const double* cpar, const int32_t* slots, const int32_t* row_ptr,
+                    double* values, int64_t nnz, double* K_out, int32_t precision, void* stream);
 /* precision: GFE_FP64 (FP64 contraction), GFE_MIXED (FP32 CUDA-core contraction of the
  * basis-gradient x material blocks), GFE_TC_TF32X3 / GFE_TC_TF32 (the same contraction on the
  * tensor cores, tcgen05 kind::tf32 with FP32 accumulation in tensor memory, three-pass split or one
@@ -364,8 +397,8 @@ int gfe_mr_jacobian(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int
  * gfe_mr_jacobian.  Used by the Newton solver and checked against finite differences. */
 int gfe_mr_tangent(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, int32_t n_lin,
                    const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
-                   const double* dep, const double* cpar, const int32_t* slots, double* values, int64_t nnz,
-                   double* K_out, int32_t precision, void* stream);
+                   const double* dep, const double* cpar, const int32_t* slots, const int32_t* row_ptr,
+                   double* values, int64_t nnz, double* K_out, int32_t precision, void* stream);
 
 /* Iron's finite-difference Jacobian, its default for finite elasticity, in FP64: per element the
  * residual R0 and, for each of the 89 element parameters j, the residual with parameter j raised by
@@ -374,7 +407,8 @@ int gfe_mr_tangent(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int3
  * (src/equations_set_routines.F90:2839-2962) inside EquationsSet_JacobianEvaluateStaticFEM;
  * `step` is Iron's jacobianFiniteDifferenceStepSize (default 1e-6, set by
  * cmfe_Equations_JacobianFiniteDifferenceStepSizeSet, src/opencmiss_iron.F90:25271-25348).  Outputs
- * as gfe_mr_jacobian.  Allocates and frees a small norm scratch on `stream`. */
+ * as gfe_mr_jacobian, assembled colour by colour through the slot map (values zeroed first).
+ * Allocates and frees a small norm scratch on `stream`. */
 int gfe_mr_jacobian_fd(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t n_q2, int32_t n_lin,
                        const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
                        const double* dep, const double* cpar, double step, const int32_t* slots, double* values,

@@ -48,6 +48,7 @@ _lib = None
 vp, i32, i64, f64 = C.c_void_p, C.c_int32, C.c_int64, C.c_double
 SIGNATURES = {
     "gfe_version": (C.c_int, []),
+    "gfe_clear_stale_error": (C.c_int, []),
     "gfe_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "gfe_device_errors": (C.c_int, [C.POINTER(C.c_uint32), vp]),
     "gfe_set_thread_error_word": (C.c_int, [vp]),
@@ -67,6 +68,8 @@ SIGNATURES = {
                                     C.POINTER(C.c_double)]),
     "gfe_csr_structure": (C.c_int, [i32, i32, vp, i32, vp, vp, i64, C.POINTER(C.c_int64), vp]),
     "gfe_laplace_assemble": (C.c_int, [i32, i32, vp, vp, vp, vp, vp, i32, vp, vp, i64, vp, vp, vp, i32, vp]),
+    "gfe_laplace_assemble_generalised": (C.c_int, [i32, i32, vp, vp, vp, vp, i32, vp, vp, i32, vp, vp, i64, vp, vp,
+                                                   vp]),
     "gfe_laplace_element_matrices": (C.c_int, [i32, i32, vp, vp, vp, vp, i32, vp]),
     "gfe_laplace_assemble_regular": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp]),
     "gfe_laplace_regular_workspace_bytes": (C.c_int64, [i32, i32, i32, i32]),
@@ -87,8 +90,8 @@ SIGNATURES = {
     "gfe_solver_update_dependent": (C.c_int, [i32, vp, vp, vp, vp]),
     "gfe_mr_residual": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp]),
     "gfe_mr_slot_map": (C.c_int, [i32, vp, vp, i32, vp, vp, vp, vp, vp]),
-    "gfe_mr_jacobian": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, vp, vp, vp, vp, i64, vp, i32, vp]),
-    "gfe_mr_tangent": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, vp, vp, vp, vp, i64, vp, i32, vp]),
+    "gfe_mr_jacobian": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, vp, vp, vp, vp, vp, i64, vp, i32, vp]),
+    "gfe_mr_tangent": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, vp, vp, vp, vp, vp, i64, vp, i32, vp]),
     "gfe_mr_jacobian_fd": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, vp, vp, f64, vp, vp, i64, vp, vp]),
     "gfe_mr_residual_vjp": (C.c_int, [i32, vp, vp, i32, i32, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp, vp]),
     "gfe_cg_solve": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(C.c_int32),
@@ -141,9 +144,17 @@ def check(status: int) -> None:
         raise GfeError(status, last_error())
 
 
+# CUDA runtime errors that other code on a thread left behind before a library call, by
+# (entry point, error code): cleared so that the entry point's launch check reports only its own
+STALE_ERRORS: dict = {}
+
+
 def call(name: str, *args) -> None:
     L = load()
     fn = getattr(L, name)
+    stale = L.gfe_clear_stale_error()
+    if stale:
+        STALE_ERRORS[(name, stale)] = STALE_ERRORS.get((name, stale), 0) + 1
     check(fn(*args))
 
 

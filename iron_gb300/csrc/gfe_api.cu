@@ -21,6 +21,9 @@ int set_error(int code, const char* fmt, ...) {
   vsnprintf(buf, sizeof(buf), fmt, ap);
   va_end(ap);
   t_last_error = buf;
+  // the failure is reported by this return code: clear the CUDA runtime's per-thread error state,
+  // so a later launch check on this thread does not report it again as its own
+  cudaGetLastError();
   return code;
 }
 
@@ -71,6 +74,8 @@ int sm_count() {
 }  // namespace gfe
 
 extern "C" int gfe_version(void) { return 100; }
+
+extern "C" int gfe_clear_stale_error(void) { return (int)cudaGetLastError(); }
 
 extern "C" int gfe_last_error(char* buf, int len) {
   int n = (int)t_last_error.size();

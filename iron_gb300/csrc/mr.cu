@@ -454,7 +454,7 @@ mr_jacobian_fd_kernel(const int32_t* __restrict__ elems, int32_t count, const in
       warp_element_residual(T, lane, S.x, S.z0, S.p0, c1, c2, S.P[0], S.tp[0], err,
                             [&](int i, double s) { S.R0[i] = s; });
     __syncthreads();
-    const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
+    const int32_t* sl = slots ? slots + (size_t)e * ND * ND : nullptr;
     double* Ke = Kout ? Kout + (size_t)e * ND * ND : nullptr;
     for (int j = w; j < ND; j += kFDWarps) {
       for (int i = lane; i < 81; i += 32) S.z[w][i] = S.z0[i];
@@ -484,8 +484,8 @@ mr_jacobian_fd_kernel(const int32_t* __restrict__ elems, int32_t count, const in
   }
 }
 
-// slot map: for each element (in colour order) and each (r, c), the 0-based CSR position of
-// (dof_r, dof_c); -1 when absent.  One warp per (element, row).
+// slot map: for each element and each (r, c), the 0-based CSR position of (dof_r, dof_c); -1 when
+// absent, at slots[(e * 89 + r) * 89 + c] (element number e).  One warp per (element, row).
 __global__ void mr_slot_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
                                const int32_t* __restrict__ elin, int32_t nq2, const int32_t* __restrict__ rp,
                                const int32_t* __restrict__ ci, int32_t* __restrict__ slots) {
@@ -507,9 +507,115 @@ __global__ void mr_slot_kernel(const int32_t* __restrict__ elems, int32_t count,
         const int mid = lo + ((hi - lo) >> 1);  // no int32 overflow past 2^30 entries
         if (ci[mid] < col) lo = mid + 1; else hi = mid;
       }
-      slots[((size_t)item * ND + r) * ND + c] = (lo < hi0 && ci[lo] == col) ? lo : -1;
+      slots[((size_t)e * ND + r) * ND + c] = (lo < hi0 && ci[lo] == col) ? lo : -1;
     }
   }
+}
+
+// ----------------------------------------------------------------------------------------------
+// Row-owning assembly of element matrices (replaces EquationsMatrices_JacobianElementAdd,
+// src/equations_matrices_routines.F90:2866-2909, for a whole mesh at once)
+// ----------------------------------------------------------------------------------------------
+// The element matrices of all elements are first written to Kel[e][89][89]; then each CSR row is
+// summed once from the element rows of the elements around its node, in ascending element order,
+// in shared memory, and written out exactly once with coalesced stores.  Each element row and its
+// slot-map row are read once, contiguously.  Node incidence: for node k (quadratic nodes 0..nq2-1,
+// then linear nodes nq2 + l) up to kMaxInc entries (e * 64 + local index; local 0..26 quadratic,
+// 27..34 linear), sorted by element.
+constexpr int kMaxInc = 16;       // elements around one node (8 on a hexahedral grid)
+constexpr int kRowWarps = 8;      // warps (rows in flight) per CTA of mr_row_gather_kernel
+constexpr int kMaxRowLen = 512;   // entries of one Jacobian row (at most 402 on a regular Q2/Q1 grid)
+
+__global__ void mr_incidence_fill(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
+                                  const int32_t* __restrict__ elin, int32_t nq2, int32_t* __restrict__ cnt,
+                                  int32_t* __restrict__ list, unsigned* err) {
+  const long long n = (long long)count * (NQ + NL);
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int item = (int)(t / (NQ + NL)), loc = (int)(t % (NQ + NL));
+    const int e = __ldg(elems + item);
+    const int node = loc < NQ ? __ldg(eq2 + (size_t)e * NQ + loc) : nq2 + __ldg(elin + (size_t)e * NL + loc - NQ);
+    const int k = atomicAdd(cnt + node, 1);
+    if (k < kMaxInc) list[(size_t)node * kMaxInc + k] = e * 64 + loc;
+    else gfe_raise(err, GFE_DEVERR_SLOT);
+  }
+}
+
+// sort each node's incidence list by element (insertion sort of at most kMaxInc entries)
+__global__ void mr_incidence_sort(int32_t n_nodes, const int32_t* __restrict__ cnt, int32_t* __restrict__ list) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n_nodes; k += gridDim.x * blockDim.x) {
+    int32_t* L = list + (size_t)k * kMaxInc;
+    const int m = min(cnt[k], kMaxInc);
+    for (int i = 1; i < m; ++i) {
+      const int32_t v = L[i];
+      int j = i - 1;
+      while (j >= 0 && L[j] > v) {
+        L[j + 1] = L[j];
+        --j;
+      }
+      L[j + 1] = v;
+    }
+  }
+}
+
+// One warp per CSR row: values[row] = sum over the elements around the row's node of their element
+// rows, through the slot map (element number order).  Rows of displacement component mh take local
+// row mh * 27 + node index; pressure rows local row 81 + corner index.  The pressure-pressure block
+// is not assembled (zero in Iron's matrix).  Every entry of every row is written, so the values
+// need no zeroing first.
+template <typename TS>
+__global__ void __launch_bounds__(kRowWarps * 32)
+mr_row_gather_kernel(int32_t nq2, int32_t nlin, const int32_t* __restrict__ cnt, const int32_t* __restrict__ list,
+                     const TS* __restrict__ Kel, const int32_t* __restrict__ slots, const int32_t* __restrict__ rp,
+                     double* __restrict__ values, float* __restrict__ values32, unsigned* err) {
+  __shared__ double buf[kRowWarps][kMaxRowLen];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double* B = buf[w];
+  const long long n_rows = 3ll * nq2 + nlin;
+  for (long long row = (long long)blockIdx.x * kRowWarps + w; row < n_rows; row += (long long)gridDim.x * kRowWarps) {
+    int node, mh;
+    if (row < 3ll * nq2) {
+      mh = (int)(row / nq2);
+      node = (int)(row - (long long)mh * nq2);
+    } else {
+      mh = 0;
+      node = nq2 + (int)(row - 3ll * nq2);
+    }
+    const long long r0 = __ldg(rp + row) - 1;
+    const int len = (int)(__ldg(rp + row + 1) - 1 - r0);
+    if (len > kMaxRowLen) {
+      if (lane == 0) gfe_raise(err, GFE_DEVERR_SLOT);
+      continue;
+    }
+    for (int j = lane; j < len; j += 32) B[j] = 0.0;
+    __syncwarp();
+    const int m = min(__ldg(cnt + node), kMaxInc);
+    for (int i = 0; i < m; ++i) {
+      const int32_t packed = __ldg(list + (size_t)node * kMaxInc + i);
+      const int e = packed >> 6, loc = packed & 63;
+      const int lr = loc < NQ ? mh * NQ + loc : 81 + loc - NQ;
+      const size_t base = ((size_t)e * ND + lr) * ND;
+      const int cmax = lr >= 81 ? 81 : ND;
+      for (int c = lane; c < cmax; c += 32) {
+        const int pos = __ldg(slots + base + c);
+        const long long o = (long long)pos - r0;
+        if (pos >= 0 && o >= 0 && o < len) B[o] += (double)Kel[base + c];
+        else gfe_raise(err, GFE_DEVERR_SLOT);
+      }
+      __syncwarp();  // the next element may add to the same entries
+    }
+    for (int j = lane; j < len; j += 32) {
+      const double v = B[j];
+      values[r0 + j] = v;
+      if (values32) values32[r0 + j] = (float)v;
+    }
+    __syncwarp();
+  }
+}
+
+template <typename TS>
+__global__ void widen_element_matrices(const TS* __restrict__ src, size_t n, double* __restrict__ dst) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    dst[i] = (double)src[i];
 }
 
 // ----------------------------------------------------------------------------------------------
@@ -1212,37 +1318,11 @@ mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __
 
 constexpr int kCThreads = 256;
 
-// shared layout of mr_contract_kernel (in units of TS)
-// Adds one element's 89 x 89 matrix into the CSR values through its slot-map row block (and/or
-// writes it densely to Kout_e).  val(r, c) gives entry (r, c).  Positions within one element are
-// distinct, so each thread first reads kBatch slots and old values and then writes them all back:
-// kBatch independent read-modify-writes in flight instead of a chain of dependent ones.
-template <int kBatch, typename F>
-__device__ __forceinline__ void scatter_element(const int32_t* __restrict__ sl, double* __restrict__ values,
-                                                double* __restrict__ Kout_e, F val, unsigned* err) {
-  for (int k0 = threadIdx.x; k0 < ND * ND; k0 += kBatch * blockDim.x) {
-    int pos[kBatch];
-    double v[kBatch], old[kBatch];
-#pragma unroll
-    for (int j = 0; j < kBatch; ++j) {
-      const int k = k0 + j * blockDim.x;
-      pos[j] = -2;  // nothing to add
-      v[j] = 0.0;
-      if (k < ND * ND) {
-        const int r = k / ND, c = k % ND;
-        v[j] = (double)val(r, c);
-        if (Kout_e) Kout_e[k] = v[j];
-        if (sl && !(r >= 81 && c >= 81)) pos[j] = __ldg(sl + k);  // -1: absent from the structure
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < kBatch; ++j) old[j] = pos[j] >= 0 ? values[pos[j]] : 0.0;
-#pragma unroll
-    for (int j = 0; j < kBatch; ++j) {
-      if (pos[j] >= 0) values[pos[j]] = old[j] + v[j];
-      else if (pos[j] == -1) gfe_raise(err, GFE_DEVERR_SLOT);
-    }
-  }
+// Writes one element's 89 x 89 matrix, entry (r, c) = val(r, c), row-major at Ke: consecutive
+// threads write consecutive entries.
+template <typename KT, typename F>
+__device__ __forceinline__ void store_element(KT* __restrict__ Ke, F val) {
+  for (int k = threadIdx.x; k < ND * ND; k += blockDim.x) Ke[k] = (KT)val(k / ND, k % ND);
 }
 
 template <typename TS>
@@ -1256,11 +1336,11 @@ struct ContractShared {
   TS PvG[NG][81];      // sum_xi G[(g,xi)][ns] Pv[xi][nh]  -> [g][(nh,ns)]
 };
 
+// Element matrices of `count` elements into Kel[e][89][89] (element number e = elems[item]).
 template <typename TS, bool EXACT>
 __global__ void __launch_bounds__(kCThreads)
 mr_contract_kernel(const int32_t* __restrict__ elems, int32_t count, const Tables* __restrict__ Tg,
-                   const TS* __restrict__ gp, const int32_t* __restrict__ slots, double* __restrict__ values,
-                   double* __restrict__ Kout, unsigned* err) {
+                   const TS* __restrict__ gp, TS* __restrict__ Kel) {
   extern __shared__ __align__(16) unsigned char craw[];
   ContractShared<TS>& S = *reinterpret_cast<ContractShared<TS>*>(craw);
   const int tid = threadIdx.x;
@@ -1316,9 +1396,7 @@ mr_contract_kernel(const int32_t* __restrict__ elems, int32_t count, const Table
     }
     __syncthreads();
     TS(*Kuu)[81] = S.Kuu;
-    const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
-    double* Ke = Kout ? Kout + (size_t)__ldg(elems + item) * ND * ND : nullptr;
-    scatter_element<8>(sl, values, Ke, [&](int r, int c) -> TS {
+    store_element(Kel + (size_t)__ldg(elems + item) * ND * ND, [&](int r, int c) -> TS {
       if (r < 81 && c < 81) return (EXACT || r >= c) ? Kuu[r][c] : Kuu[c][r];  // Iron mirrors the lower u-u triangle
       TS s = TS(0);
       if (r < 81) {  // u rows, p columns
@@ -1327,7 +1405,7 @@ mr_contract_kernel(const int32_t* __restrict__ elems, int32_t count, const Table
         for (int g = 0; g < NG; ++g) s += S.psi[g][r - 81] * S.PvG[g][c];
       }
       return s;
-    }, err);
+    });
   }
 }
 
@@ -1342,8 +1420,8 @@ mr_contract_kernel(const int32_t* __restrict__ elems, int32_t count, const Table
 // tcgen05.mma kind::tf32 (N = 32, K = 88 in 11 steps of 8) accumulating in tensor memory.  With
 // SPLIT3 each operand is split into a TF32 head and a TF32 tail and the three products
 // hi*hi + lo*hi + hi*lo recover about FP32 accuracy; without it the contraction is plain TF32
-// (about 1e-3 relative).  u-p / p-u blocks, Iron's lower-triangle mirror and the scatter through the
-// slot map are as in mr_contract_kernel.
+// (about 1e-3 relative).  u-p / p-u blocks, Iron's lower-triangle mirror and the element-matrix
+// output are as in mr_contract_kernel.
 constexpr int kTCThreads = 256;
 constexpr int kTK = 88;                        // K = 27 Gauss points x 3, padded to 11 steps of 8
 constexpr int kTKC = kTK / 4;                  // core-matrix columns along K (4 TF32 = 16 bytes)
@@ -1375,8 +1453,7 @@ __device__ __forceinline__ uint32_t tc_offset(int row, int k) {
 template <bool EXACT, bool SPLIT3>
 __global__ void __launch_bounds__(kTCThreads, 1)
 mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Tables* __restrict__ Tg,
-                      const float* __restrict__ gp, const int32_t* __restrict__ slots, double* __restrict__ values,
-                      double* __restrict__ Kout, unsigned* err) {
+                      const float* __restrict__ gp, float* __restrict__ Kel, unsigned* err) {
   extern __shared__ __align__(1024) unsigned char traw[];
   TCShared& S = *reinterpret_cast<TCShared*>(traw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1480,9 +1557,7 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
     }
     tc::fence_before_sync();
     __syncthreads();
-    const int32_t* sl = slots ? slots + (size_t)item * ND * ND : nullptr;
-    double* Ke = Kout ? Kout + (size_t)__ldg(elems + item) * ND * ND : nullptr;
-    scatter_element<8>(sl, values, Ke, [&](int r, int c) -> float {
+    store_element(Kel + (size_t)__ldg(elems + item) * ND * ND, [&](int r, int c) -> float {
       if (r < 81 && c < 81) {
         const int rr = (EXACT || r >= c) ? r : c, cc = (EXACT || r >= c) ? c : r;  // Iron mirrors the lower triangle
         return S.K[(rr / 27 * 3 + cc / 27) * 27 + rr % 27][cc % 27];
@@ -1494,7 +1569,7 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
         for (int g = 0; g < NG; ++g) s += S.psi[g][r - 81] * S.PvG[g][c];
       }
       return s;
-    }, err);
+    });
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -1568,21 +1643,51 @@ extern "C" int gfe_mr_slot_map(int32_t n_elem, const int32_t* eq2, const int32_t
 namespace {
 
 // Element Jacobians of one problem (mode 0: Iron's analytic tangent, 1: consistent tangent), in the
-// contraction precision `precision`, assembled into CSR values through the slot map and/or written
-// as dense element matrices.  Per colour: the Gauss-point kernel fills a scratch array, the
-// contraction kernel consumes it.
+// contraction precision `precision`.  Elements in chunks of at most kElemChunk: the Gauss-point
+// kernel fills a scratch array, the contraction kernel turns it into element matrices Kel (all
+// elements; FP64 for GFE_FP64, else FP32); then the row gather assembles the CSR values (when
+// `values`), and K_out receives the element matrices in FP64 (when given).
+constexpr int kElemChunk = 1 << 16;
+
 template <bool EXACT, bool SPLIT3>
 void launch_contract_tc(int grid, cudaStream_t s, const int32_t* elems, int cnt, const Tables* T, const float* gp,
-                        const int32_t* sl, double* values, double* K_out, unsigned* err) {
-  mr_contract_tc_kernel<EXACT, SPLIT3><<<grid, kTCThreads, sizeof(TCShared), s>>>(elems, cnt, T, gp, sl, values,
-                                                                                 K_out, err);
+                        float* Kel, unsigned* err) {
+  mr_contract_tc_kernel<EXACT, SPLIT3><<<grid, kTCThreads, sizeof(TCShared), s>>>(elems, cnt, T, gp, Kel, err);
+}
+
+// Node incidence scratch (counts, then lists) and the row gather into `values`.
+template <typename TS>
+int gather_rows(int32_t n_elem, const int32_t* elems, const int32_t* eq2, const int32_t* elin, int32_t nq2,
+                int32_t nlin, const TS* Kel, const int32_t* slots, const int32_t* row_ptr, double* values,
+                cudaStream_t s, unsigned* err) {
+  const int32_t n_nodes = nq2 + nlin;
+  int32_t* inc = nullptr;
+  const size_t words = (size_t)n_nodes * (1 + kMaxInc);
+  int rc = gfe::scratch_alloc((void**)&inc, sizeof(int32_t) * words, s, "node incidence");
+  if (rc) return rc;
+  int32_t* cnt = inc;
+  int32_t* list = inc + n_nodes;
+  cudaError_t e = cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (size_t)n_nodes, s);
+  if (e != cudaSuccess) {
+    gfe::scratch_free(inc, s);
+    return gfe::set_error(GFE_ERR_CUDA, "node incidence: %s", cudaGetErrorString(e));
+  }
+  const int sms = gfe::sm_count();
+  mr_incidence_fill<<<8 * sms, 256, 0, s>>>(elems, n_elem, eq2, elin, nq2, cnt, list, err);
+  mr_incidence_sort<<<(n_nodes + 255) / 256, 256, 0, s>>>(n_nodes, cnt, list);
+  const long long rows = 3ll * nq2 + nlin;
+  const int grid = (int)std::min<long long>((rows + kRowWarps - 1) / kRowWarps, 16ll * sms);
+  mr_row_gather_kernel<TS><<<grid, kRowWarps * 32, 0, s>>>(nq2, nlin, cnt, list, Kel, slots, row_ptr, values,
+                                                          nullptr, err);
+  gfe::scratch_free(inc, s);
+  return GFE_OK;
 }
 
 template <typename TS>
-int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, const double* xg,
-                  const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors, const double* dep,
-                  const double* cpar, const int32_t* slots, double* values, int64_t nnz, double* K_out,
-                  cudaStream_t s, const char* fn, int tc_mode = 0) {
+int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
+                  const double* xg, const int32_t* elems, const double* dep, const double* cpar,
+                  const int32_t* slots, const int32_t* row_ptr, double* values, double* K_out, cudaStream_t s,
+                  const char* fn, int tc_mode = 0) {
   const Tables* T = nullptr;
   int rc = device_tables(&T);
   if (rc) return rc;
@@ -1594,74 +1699,81 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
   } else {
     TK = T;
   }
+  if (n_elem == 0) return GFE_OK;
   const size_t gsm_k = sizeof(TablesT<KF>) + sizeof(GPShared<KF>);
   const size_t csm = sizeof(ContractShared<TS>);
   const void* gk = mode == 0 ? (const void*)mr_gp_kernel<TS, false, KF> : (const void*)mr_gp_kernel<TS, true, KF>;
-  if ((rc = set_smem(gk, gsm_k))) return rc;
-  int max_cnt = 0;
-  for (int c = 0; c < n_colors; ++c) max_cnt = std::max(max_cnt, color_ptr_host[c + 1] - color_ptr_host[c]);
-  if (values) GFE_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)nnz, s));
-  TS* gpbuf = nullptr;
-  if ((rc = gfe::scratch_alloc((void**)&gpbuf, sizeof(TS) * (size_t)max_cnt * NG * kGPOut + 16, s,
-                               "Gauss-point tangent blocks")))
-    return rc;
   const void* ck = mode == 0 ? (const void*)mr_contract_kernel<TS, false> : (const void*)mr_contract_kernel<TS, true>;
-  if ((rc = set_smem(ck, csm))) {
-    gfe::scratch_free(gpbuf, s);
-    return rc;
-  }
+  if ((rc = set_smem(gk, gsm_k)) || (rc = set_smem(ck, csm))) return rc;
   if (tc_mode) {
     const void* tk[4] = {(const void*)mr_contract_tc_kernel<false, false>, (const void*)mr_contract_tc_kernel<false, true>,
                          (const void*)mr_contract_tc_kernel<true, false>, (const void*)mr_contract_tc_kernel<true, true>};
     for (const void* k : tk)
-      if ((rc = set_smem(k, sizeof(TCShared)))) {
-        gfe::scratch_free(gpbuf, s);
-        return rc;
-      }
+      if ((rc = set_smem(k, sizeof(TCShared)))) return rc;
+  }
+  const int chunk = std::min(n_elem, kElemChunk);
+  // element matrices: straight into K_out when it has the contraction's type
+  constexpr bool kDirect = std::is_same<TS, double>::value;
+  TS* Kel = nullptr;
+  bool own_kel = true;
+  if (kDirect && K_out) {
+    Kel = reinterpret_cast<TS*>(K_out);
+    own_kel = false;
+  } else if ((rc = gfe::scratch_alloc((void**)&Kel, sizeof(TS) * (size_t)n_elem * ND * ND, s, "element matrices"))) {
+    return rc;
+  }
+  TS* gpbuf = nullptr;
+  if ((rc = gfe::scratch_alloc((void**)&gpbuf, sizeof(TS) * (size_t)chunk * NG * kGPOut + 16, s,
+                               "Gauss-point tangent blocks"))) {
+    if (own_kel) gfe::scratch_free(Kel, s);
+    return rc;
   }
   unsigned* err = gfe::device_error_word();
   void* prof = gfe::stage_begin(GFE_STAGE_MR_JACOBIAN, s);
   int launches = 0;
-  for (int c = 0; c < n_colors; ++c) {
-    const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
-    if (cnt <= 0) continue;
+  const int sms = gfe::sm_count();
+  for (int c0 = 0; c0 < n_elem; c0 += chunk) {
+    const int cnt = std::min(chunk, n_elem - c0);
     const int ggrid = (cnt + kGPElems - 1) / kGPElems;
-    const int cgrid = std::min(cnt, 8 * gfe::sm_count());
-    const int32_t* sl = slots ? slots + (size_t)c0 * ND * ND : nullptr;
-    if (tc_mode) {
-      // TS is float here: the Gauss-point coefficients feed the tensor-core contraction
-      const float* gpf = reinterpret_cast<const float*>(gpbuf);
-      const int tgrid = std::min(cnt, gfe::sm_count());
-      if (mode == 0) {
-        mr_gp_kernel<TS, false, KF><<<ggrid, kGPThreads, gsm_k, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg,
-                                                                     dep, cpar, TK, gpbuf, err);
-        if (tc_mode == GFE_TC_TF32X3)
-          launch_contract_tc<false, true>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
-        else
-          launch_contract_tc<false, false>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
-      } else {
-        mr_gp_kernel<TS, true, KF><<<ggrid, kGPThreads, gsm_k, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg,
-                                                                    dep, cpar, TK, gpbuf, err);
-        if (tc_mode == GFE_TC_TF32X3)
-          launch_contract_tc<true, true>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
-        else
-          launch_contract_tc<true, false>(tgrid, s, color_elems + c0, cnt, T, gpf, sl, values, K_out, err);
+    if (mode == 0)
+      mr_gp_kernel<TS, false, KF><<<ggrid, kGPThreads, gsm_k, s>>>(elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar, TK,
+                                                                   gpbuf, err);
+    else
+      mr_gp_kernel<TS, true, KF><<<ggrid, kGPThreads, gsm_k, s>>>(elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar, TK,
+                                                                  gpbuf, err);
+    if constexpr (std::is_same<TS, float>::value) {
+      if (tc_mode) {
+        const int tgrid = std::min(cnt, sms);
+        if (mode == 0) {
+          if (tc_mode == GFE_TC_TF32X3) launch_contract_tc<false, true>(tgrid, s, elems + c0, cnt, T, gpbuf, Kel, err);
+          else launch_contract_tc<false, false>(tgrid, s, elems + c0, cnt, T, gpbuf, Kel, err);
+        } else {
+          if (tc_mode == GFE_TC_TF32X3) launch_contract_tc<true, true>(tgrid, s, elems + c0, cnt, T, gpbuf, Kel, err);
+          else launch_contract_tc<true, false>(tgrid, s, elems + c0, cnt, T, gpbuf, Kel, err);
+        }
+        launches += 2;
+        continue;
       }
-    } else if (mode == 0) {
-      mr_gp_kernel<TS, false, KF><<<ggrid, kGPThreads, gsm_k, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep,
-                                                                   cpar, TK, gpbuf, err);
-      mr_contract_kernel<TS, false><<<cgrid, kCThreads, csm, s>>>(color_elems + c0, cnt, T, gpbuf, sl, values,
-                                                                  K_out, err);
-    } else {
-      mr_gp_kernel<TS, true, KF><<<ggrid, kGPThreads, gsm_k, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep,
-                                                                  cpar, TK, gpbuf, err);
-      mr_contract_kernel<TS, true><<<cgrid, kCThreads, csm, s>>>(color_elems + c0, cnt, T, gpbuf, sl, values, K_out,
-                                                                 err);
     }
+    const int cgrid = std::min(cnt, 8 * sms);
+    if (mode == 0)
+      mr_contract_kernel<TS, false><<<cgrid, kCThreads, csm, s>>>(elems + c0, cnt, T, gpbuf, Kel);
+    else
+      mr_contract_kernel<TS, true><<<cgrid, kCThreads, csm, s>>>(elems + c0, cnt, T, gpbuf, Kel);
     launches += 2;
   }
-  gfe::stage_end(GFE_STAGE_MR_JACOBIAN, prof, s, launches);
   gfe::scratch_free(gpbuf, s);
+  if (values && (rc = gather_rows<TS>(n_elem, elems, eq2, elin, nq2, nlin, Kel, slots, row_ptr, values, s, err))) {
+    if (own_kel) gfe::scratch_free(Kel, s);
+    return rc;
+  }
+  if (K_out && own_kel) {
+    const size_t n = (size_t)n_elem * ND * ND;
+    widen_element_matrices<TS><<<8 * sms, 256, 0, s>>>(Kel, n, K_out);
+    ++launches;
+  }
+  gfe::stage_end(GFE_STAGE_MR_JACOBIAN, prof, s, launches + (values ? 3 : 0));
+  if (own_kel) gfe::scratch_free(Kel, s);
   GFE_LAUNCH_CHECK(fn);
   return GFE_OK;
 }
@@ -1669,23 +1781,25 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
 int jacobian_entry_point(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
                          const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host,
                          int32_t n_colors, const double* dep, const double* cpar, const int32_t* slots,
-                         double* values, int64_t nnz, double* K_out, int32_t precision, void* stream,
-                         const char* fn) {
+                         const int32_t* row_ptr, double* values, int64_t nnz, double* K_out, int32_t precision,
+                         void* stream, const char* fn) {
   int rc = check_mesh(n_elem, eq2, elin, nq2, nlin, xg, fn);
   if (rc) return rc;
   if (!dep || !cpar || (n_elem > 0 && (!color_elems || !color_ptr_host || n_colors <= 0)))
     return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
-  if (!K_out && (!slots || !values)) return gfe::set_error(GFE_ERR_ARG, "%s: need CSR values + slots or K_out", fn);
+  if (!K_out && !values) return gfe::set_error(GFE_ERR_ARG, "%s: need CSR values or K_out", fn);
+  if (values && (!slots || !row_ptr || nnz < 0))
+    return gfe::set_error(GFE_ERR_ARG, "%s: CSR values need the slot map and row_ptr", fn);
   if (color_ptr_host[0] != 0 || color_ptr_host[n_colors] != n_elem)
     return gfe::set_error(GFE_ERR_ARG, "%s: colour offsets must run from 0 to n_elem", fn);
   if (precision != GFE_FP64 && precision != GFE_MIXED && precision != GFE_TC_TF32X3 && precision != GFE_TC_TF32)
     return gfe::set_error(GFE_ERR_ARG, "%s: precision must be GFE_FP64, GFE_MIXED, GFE_TC_TF32X3 or GFE_TC_TF32", fn);
   cudaStream_t s = gfe::as_stream(stream);
   if (precision == GFE_FP64)
-    return jacobian_impl<double>(mode, n_elem, eq2, elin, nq2, xg, color_elems, color_ptr_host, n_colors, dep, cpar,
-                                 slots, values, nnz, K_out, s, fn);
-  return jacobian_impl<float>(mode, n_elem, eq2, elin, nq2, xg, color_elems, color_ptr_host, n_colors, dep, cpar,
-                              slots, values, nnz, K_out, s, fn, precision == GFE_MIXED ? 0 : precision);
+    return jacobian_impl<double>(mode, n_elem, eq2, elin, nq2, nlin, xg, color_elems, dep, cpar, slots, row_ptr,
+                                 values, K_out, s, fn);
+  return jacobian_impl<float>(mode, n_elem, eq2, elin, nq2, nlin, xg, color_elems, dep, cpar, slots, row_ptr, values,
+                              K_out, s, fn, precision == GFE_MIXED ? 0 : precision);
 }
 
 }  // namespace
@@ -1693,17 +1807,19 @@ int jacobian_entry_point(int mode, int32_t n_elem, const int32_t* eq2, const int
 extern "C" int gfe_mr_jacobian(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
                                const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host,
                                int32_t n_colors, const double* dep, const double* cpar, const int32_t* slots,
-                               double* values, int64_t nnz, double* K_out, int32_t precision, void* stream) {
+                               const int32_t* row_ptr, double* values, int64_t nnz, double* K_out, int32_t precision,
+                               void* stream) {
   return jacobian_entry_point(0, n_elem, eq2, elin, nq2, nlin, xg, color_elems, color_ptr_host, n_colors, dep, cpar,
-                              slots, values, nnz, K_out, precision, stream, "gfe_mr_jacobian");
+                              slots, row_ptr, values, nnz, K_out, precision, stream, "gfe_mr_jacobian");
 }
 
 extern "C" int gfe_mr_tangent(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2, int32_t nlin,
                               const double* xg, const int32_t* color_elems, const int32_t* color_ptr_host,
                               int32_t n_colors, const double* dep, const double* cpar, const int32_t* slots,
-                              double* values, int64_t nnz, double* K_out, int32_t precision, void* stream) {
+                              const int32_t* row_ptr, double* values, int64_t nnz, double* K_out, int32_t precision,
+                              void* stream) {
   return jacobian_entry_point(1, n_elem, eq2, elin, nq2, nlin, xg, color_elems, color_ptr_host, n_colors, dep, cpar,
-                              slots, values, nnz, K_out, precision, stream, "gfe_mr_tangent");
+                              slots, row_ptr, values, nnz, K_out, precision, stream, "gfe_mr_tangent");
 }
 
 extern "C" int gfe_mr_jacobian_fd(int32_t n_elem, const int32_t* eq2, const int32_t* elin, int32_t nq2,
@@ -1742,9 +1858,8 @@ extern "C" int gfe_mr_jacobian_fd(int32_t n_elem, const int32_t* eq2, const int3
     const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
     if (cnt <= 0) continue;
     const int grid = std::min(cnt, 8 * gfe::sm_count());
-    const int32_t* sl = slots ? slots + (size_t)c0 * ND * ND : nullptr;
     mr_jacobian_fd_kernel<<<grid, kFDWarps * 32, sm, s>>>(color_elems + c0, cnt, eq2, elin, nq2, xg, dep, cpar, T,
-                                                          parts, step, sl, values, K_out, err);
+                                                          parts, step, slots, values, K_out, err);
     ++launches;
   }
   gfe::stage_end(GFE_STAGE_MR_JACOBIAN, prof, s, launches);

@@ -143,8 +143,8 @@ class MooneyRivlinAssembly:
         _lib.call(fn, self.n_elements, _lib.ptr(self.eq2), _lib.ptr(self.elin), self.n_q2, self.n_lin,
                   _lib.ptr(self.xg), _lib.ptr(self.colour_elems), cptr.ctypes.data_as(C.c_void_p), len(cptr) - 1,
                   _lib.ptr(dep), _lib.ptr(cp), None if dense else _lib.ptr(self.slots),
-                  None if dense else _lib.ptr(self.values), 0 if dense else self.nnz, _lib.ptr(K), prec,
-                  _lib.stream_handle(stream))
+                  None if dense else _lib.ptr(self.row_ptr), None if dense else _lib.ptr(self.values),
+                  0 if dense else self.nnz, _lib.ptr(K), prec, _lib.stream_handle(stream))
         if check:
             _lib.raise_device_errors(fn, stream)
         return K if dense else self.values

@@ -91,7 +91,8 @@ def test_assembled_jacobian_matches_oracle(gfe_cuda, ne):
 def test_slot_map_beyond_2pow30_entries(gfe_cuda):
     """59^3 Q2/Q1 mesh: the Jacobian has more than 2^30 non-zeros, so the bisection midpoint of
     rows near the end would overflow int32 if computed as (lo + hi) / 2.  Sampled slot-map entries
-    of the last elements in colour order point at their (row, column) in the CSR."""
+    (indexed by element number) of the last elements in colour order point at their (row, column)
+    in the CSR."""
     A = MooneyRivlinAssembly.from_regular_mesh((59, 59, 59))
     assert A.nnz > 2 ** 30
     torch.cuda.synchronize()
@@ -101,7 +102,7 @@ def test_slot_map_beyond_2pow30_entries(gfe_cuda):
     for item in (A.n_elements - 1, A.n_elements - 2, A.colour_ptr[-2]):
         e = int(ce[item])
         d = dofs[e].cpu().numpy()
-        sl = A.slots[item].cpu().numpy()
+        sl = A.slots[e].cpu().numpy()
         for r in (0, 40, 80, 81, 88):
             lo, hi = int(rp[d[r]]) - 1, int(rp[d[r] + 1]) - 1
             cols = A.col_idx[lo:hi].cpu().numpy()
@@ -114,16 +115,26 @@ def test_slot_map_beyond_2pow30_entries(gfe_cuda):
     torch.cuda.empty_cache()
 
 
-@pytest.mark.parametrize("precision,tol", [("tf32x3", 2e-5), ("tf32", 4e-3)])
+@pytest.mark.parametrize("precision,tol", [("mixed", 2e-5), ("tf32x3", 2e-5), ("tf32", 4e-3)])
 def test_tensor_core_assembly_matches_fp64(gfe_cuda, precision, tol):
-    """CSR assembly (slot-map scatter) of the analytic Jacobian and the consistent tangent with the
-    tensor-core contraction against the FP64 contraction, on a mesh with several elements per colour."""
+    """CSR assembly (element matrices, then the row gather) of the analytic Jacobian and the
+    consistent tangent with the FP32 CUDA-core and the tensor-core contractions against the FP64
+    contraction; the FP64 element matrices widened from each path's give the same CSR values
+    through the oracle's scatter."""
     A = MooneyRivlinAssembly.from_regular_mesh((5, 4, 3))
     dep = torch.from_numpy(_state(A, 4)).cuda()
-    for fn in ("jacobian", "tangent"):
+    slots = A.slots.cpu().numpy().reshape(A.n_elements, -1)
+    for fn, dense in (("jacobian", "element_jacobians"), ("tangent", "element_tangents")):
         ref = getattr(A, fn)(dep, [C1, C2], precision="fp64").clone()
-        got = getattr(A, fn)(dep, [C1, C2], precision=precision)
-        assert (got - ref).abs().max().item() <= tol * ref.abs().max().item(), fn
+        got = getattr(A, fn)(dep, [C1, C2], precision=precision).cpu().numpy()
+        assert np.abs(got - ref.cpu().numpy()).max() <= tol * ref.abs().max().item(), fn
+        # the row gather sums exactly the element matrices of this precision
+        K = getattr(A, dense)(dep, [C1, C2], precision=precision).cpu().numpy().reshape(A.n_elements, -1)
+        keep = slots >= 0
+        keep &= ~((np.arange(89 * 89) // 89 >= 81) & (np.arange(89 * 89) % 89 >= 81))[None, :]
+        v = np.zeros(A.nnz)
+        np.add.at(v, slots[keep], K[keep])
+        assert np.abs(got - v).max() <= 1e-14 * np.abs(v).max(), fn
 
 
 @pytest.mark.parametrize("ne", [(1, 1, 1), (2, 3, 1), (3, 2, 4), (5, 1, 2)])
