@@ -525,6 +525,7 @@ __global__ void mr_slot_kernel(const int32_t* __restrict__ elems, int32_t count,
 constexpr int kMaxInc = 16;       // elements around one node (8 on a hexahedral grid)
 constexpr int kRowWarps = 8;      // warps (rows in flight) per CTA of mr_row_gather_kernel
 constexpr int kMaxRowLen = 512;   // entries of one Jacobian row (at most 402 on a regular Q2/Q1 grid)
+constexpr int kGatherGroup = 4;   // element rows whose loads are in flight together
 
 __global__ void mr_incidence_fill(const int32_t* __restrict__ elems, int32_t count, const int32_t* __restrict__ eq2,
                                   const int32_t* __restrict__ elin, int32_t nq2, int32_t* __restrict__ cnt,
@@ -589,19 +590,41 @@ mr_row_gather_kernel(int32_t nq2, int32_t nlin, const int32_t* __restrict__ cnt,
     for (int j = lane; j < len; j += 32) B[j] = 0.0;
     __syncwarp();
     const int m = min(__ldg(cnt + node), kMaxInc);
-    for (int i = 0; i < m; ++i) {
-      const int32_t packed = __ldg(list + (size_t)node * kMaxInc + i);
-      const int e = packed >> 6, loc = packed & 63;
-      const int lr = loc < NQ ? mh * NQ + loc : 81 + loc - NQ;
-      const size_t base = ((size_t)e * ND + lr) * ND;
-      const int cmax = lr >= 81 ? 81 : ND;
-      for (int c = lane; c < cmax; c += 32) {
-        const int pos = __ldg(slots + base + c);
-        const long long o = (long long)pos - r0;
-        if (pos >= 0 && o >= 0 && o < len) B[o] += (double)Kel[base + c];
-        else gfe_raise(err, GFE_DEVERR_SLOT);
+    const int32_t* L = list + (size_t)node * kMaxInc;
+    // groups of kGatherGroup element rows: every slot and value load of a group is issued before
+    // the group's additions, which then run in ascending element order
+    for (int i0 = 0; i0 < m; i0 += kGatherGroup) {
+      int pos[kGatherGroup][3];
+      TS val[kGatherGroup][3];
+#pragma unroll
+      for (int u = 0; u < kGatherGroup; ++u) {
+        const int i = i0 + u;
+        const int32_t packed = i < m ? __ldg(L + i) : -1;
+        const int e = packed >> 6, loc = packed & 63;
+        const int lr = loc < NQ ? mh * NQ + loc : 81 + loc - NQ;
+        const size_t base = ((size_t)(packed < 0 ? 0 : e) * ND + lr) * ND;
+        const int cmax = packed < 0 ? 0 : (lr >= 81 ? 81 : ND);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int c = lane + 32 * j;
+          pos[u][j] = -2;  // nothing to add
+          val[u][j] = TS(0);
+          if (c < cmax) {
+            pos[u][j] = __ldg(slots + base + c);
+            val[u][j] = __ldg(Kel + base + c);
+          }
+        }
       }
-      __syncwarp();  // the next element may add to the same entries
+#pragma unroll
+      for (int u = 0; u < kGatherGroup; ++u) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const long long o = (long long)pos[u][j] - r0;
+          if (pos[u][j] >= 0 && o >= 0 && o < len) B[o] += (double)val[u][j];
+          else if (pos[u][j] != -2) gfe_raise(err, GFE_DEVERR_SLOT);
+        }
+        __syncwarp();  // the next element may add to the same entries
+      }
     }
     for (int j = lane; j < len; j += 32) {
       const double v = B[j];
@@ -1318,23 +1341,102 @@ mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __
 
 constexpr int kCThreads = 256;
 
-// Writes one element's 89 x 89 matrix, entry (r, c) = val(r, c), row-major at Ke: consecutive
-// threads write consecutive entries.
-template <typename KT, typename F>
-__device__ __forceinline__ void store_element(KT* __restrict__ Ke, F val) {
-  for (int k = threadIdx.x; k < ND * ND; k += blockDim.x) Ke[k] = (KT)val(k / ND, k % ND);
+// u-p / p-u coefficients of one element: HvG[g][(mh,ms)] = sum_xi G[(g,xi)][ms] Hv_g[xi][mh] and
+// PvG[g][(nh,ns)] = sum_xi G[(g,xi)][ns] Pv_g[xi][nh] from the Gauss-point blocks Dg[g][99].
+template <typename TS, int GP>
+__device__ __forceinline__ void form_up_coefficients(const TS (*G)[GP], const TS (*Dg)[kGPOut], TS (*HvG)[81],
+                                                     TS (*PvG)[81]) {
+  for (int t = threadIdx.x; t < NG * 81; t += blockDim.x) {
+    const int g = t / 81, c = t % 81, h = c / 27, s = c % 27;
+    const TS g0 = G[g * 3 + 0][s], g1 = G[g * 3 + 1][s], g2 = G[g * 3 + 2][s];
+    HvG[g][c] = g0 * Dg[g][81 + h] + g1 * Dg[g][84 + h] + g2 * Dg[g][87 + h];
+    PvG[g][c] = g0 * Dg[g][90 + h] + g1 * Dg[g][93 + h] + g2 * Dg[g][96 + h];
+  }
 }
 
+// The u-u block of one element's 89 x 89 matrix (row-major at Ke) from the staged product
+// C[(mh*3+nh)*27+ms][ns]; Iron mirrors its lower triangle into the upper one unless EXACT.  One
+// warp writes each row (consecutive lanes, consecutive entries).
+template <bool EXACT, typename KT, typename CT, int P>
+__device__ __forceinline__ void write_uu_block(KT* __restrict__ Ke, const CT (*C)[P]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int cq[3], cr[3];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    cq[j] = (lane + 32 * j) / 27;
+    cr[j] = (lane + 32 * j) % 27;
+  }
+  for (int r = warp; r < 81; r += nw) {
+    const int rq = r / 27, rr = r % 27;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int c = lane + 32 * j;
+      if (c < 81) {
+        const CT v = (EXACT || r >= c) ? C[(rq * 3 + cq[j]) * 27 + rr][cr[j]] : C[(cq[j] * 3 + rq) * 27 + cr[j]][rr];
+        Ke[r * ND + c] = (KT)v;
+      }
+    }
+  }
+}
+
+// The u-p and p-u blocks of one element's matrix as 27-term sums of HvG / PvG with the pressure
+// basis psi, and the zero p-p block.
+template <typename KT, typename CT>
+__device__ __forceinline__ void write_up_blocks(KT* __restrict__ Ke, const CT (*HvG)[81], const CT (*PvG)[81],
+                                                const CT (*psi)[NL]) {
+  for (int t = threadIdx.x; t < 2 * 81 * NL + NL * NL; t += blockDim.x) {
+    if (t < 81 * NL) {  // u rows, p columns
+      const int r = t / NL, b = t % NL;
+      CT s = CT(0);
+      for (int g = 0; g < NG; ++g) s += HvG[g][r] * psi[g][b];
+      Ke[r * ND + 81 + b] = (KT)s;
+    } else if (t < 2 * 81 * NL) {  // p rows, u columns
+      const int b = (t - 81 * NL) / 81, c = (t - 81 * NL) % 81;
+      CT s = CT(0);
+      for (int g = 0; g < NG; ++g) s += psi[g][b] * PvG[g][c];
+      Ke[(81 + b) * ND + c] = (KT)s;
+    } else {
+      const int q = t - 2 * 81 * NL;
+      Ke[(81 + q / NL) * ND + 81 + q % NL] = KT(0);
+    }
+  }
+}
+
+// Per element the u-u block is one product, as in the tensor-core kernel below:
+//   C[(mh,nh,ms)][ns] = sum_{(g,zeta)} A[(mh,nh,ms)][(g,zeta)] G[(g,zeta)][ns],
+//   A[(mh,nh,ms)][(g,zeta)] = sum_xi G[(g,xi)][ms] D_g[(mh,nh)][xi][zeta],
+// 243 x 81 by 81 x 27.  A is formed in two passes of kCRows rows ([k][row] in shared memory, so a
+// thread's four rows are one vector load), and each thread of the product accumulates a 4 x 4 tile
+// of C in registers: two vector loads per 16 FMAs.  u-p / p-u blocks and Iron's lower-triangle
+// mirror are formed from C, HvG and PvG while the element matrix is written.
+constexpr int kCRows = 128;                   // rows of A per pass
+constexpr int kCTileRows = kCRows / 4;        // 32 row groups of 4
+constexpr int kCTileCols = 7;                 // 7 column groups of 4 (27 columns, padded to 28)
+
+// The arrays read with vector loads (A, G) come first: their rows are multiples of 16 bytes.
 template <typename TS>
 struct ContractShared {
-  TS G[81][28];        // G[(g,xi)][ms] (padded row)
-  TS psi[NG][NL];      // pressure basis at the Gauss points
-  TS Dg[NG][kGPOut];   // this element's Gauss-point blocks
-  TS H[81][81];        // H_mh[(g,xi)][(ns,nh)] of the current displacement component mh
-  TS Kuu[81][81];      // K_uu[(ms,mh)][(ns,nh)]
-  TS HvG[NG][81];      // sum_xi G[(g,xi)][ms] Hv[xi][mh]  -> [g][(mh,ms)]
-  TS PvG[NG][81];      // sum_xi G[(g,xi)][ns] Pv[xi][nh]  -> [g][(nh,ns)]
+  TS A[81][kCRows];     // A[(g,zeta)][row] of the current pass
+  TS G[81][28];         // G[(g,xi)][ms]; column 27 zero
+  TS C[2 * kCRows][28]; // C[(mh,nh,ms)][ns]
+  TS HvG[NG][81];       // sum_xi G[(g,xi)][ms] Hv[xi][mh]  -> [g][(mh,ms)]
+  TS PvG[NG][81];       // sum_xi G[(g,xi)][ns] Pv[xi][nh]  -> [g][(nh,ns)]
+  TS Dg[NG][kGPOut];    // this element's Gauss-point blocks
+  TS psi[NG][NL];       // pressure basis at the Gauss points
 };
+static_assert(sizeof(float) * kCRows % 16 == 0 && sizeof(float) * 28 % 16 == 0, "vector rows");
+static_assert(sizeof(float) * 81 * kCRows % 16 == 0, "G follows A on a 16-byte boundary");
+
+template <typename TS>
+__device__ __forceinline__ void load4(const TS* p, TS (&v)[4]) {
+  if constexpr (std::is_same<TS, float>::value) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  } else {
+    const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+}
 
 // Element matrices of `count` elements into Kel[e][89][89] (element number e = elems[item]).
 template <typename TS, bool EXACT>
@@ -1344,68 +1446,58 @@ mr_contract_kernel(const int32_t* __restrict__ elems, int32_t count, const Table
   extern __shared__ __align__(16) unsigned char craw[];
   ContractShared<TS>& S = *reinterpret_cast<ContractShared<TS>*>(craw);
   const int tid = threadIdx.x;
-  for (int t = tid; t < 81 * 27; t += blockDim.x) {
-    const int k = t / 27, ms = t % 27;
-    S.G[k][ms] = (TS)Tg->dphi[k / 3][k % 3][ms];
+  for (int t = tid; t < 81 * 28; t += blockDim.x) {
+    const int k = t / 28, ms = t % 28;
+    S.G[k][ms] = ms < 27 ? (TS)Tg->dphi[k / 3][k % 3][ms] : TS(0);
   }
   for (int t = tid; t < NG * NL; t += blockDim.x) S.psi[t / NL][t % NL] = (TS)Tg->psi[t / NL][t % NL];
+  const int rq = tid / kCTileCols, cq = tid % kCTileCols;  // product tile of this thread
+  const bool in_product = tid < kCTileRows * kCTileCols;
   for (int item = blockIdx.x; item < count; item += gridDim.x) {
     __syncthreads();
     const TS* src = gp + (size_t)item * NG * kGPOut;
     for (int t = tid; t < NG * kGPOut; t += blockDim.x) (&S.Dg[0][0])[t] = src[t];
     __syncthreads();
-    // u-p / p-u coefficients
-    for (int t = tid; t < 2 * NG * 81; t += blockDim.x) {
-      const int which = t / (NG * 81), r = t % (NG * 81), g = r / 81, c = r % 81, h = c / 27, s = c % 27;
-      const int off = which == 0 ? 81 : 90;
-      const TS v = S.G[g * 3 + 0][s] * S.Dg[g][off + 0 * 3 + h] + S.G[g * 3 + 1][s] * S.Dg[g][off + 1 * 3 + h] +
-                   S.G[g * 3 + 2][s] * S.Dg[g][off + 2 * 3 + h];
-      if (which == 0) S.HvG[g][c] = v; else S.PvG[g][c] = v;
-    }
-    // per displacement component mh: H_mh = D G, then K_mh^T = H_mh^T G^T with 3x3 thread tiles
-    const bool active = tid < 243;
-    const int rg = tid / 9, cg = tid % 9;
-    for (int mh = 0; mh < 3; ++mh) {
-      __syncthreads();
-      for (int t = tid; t < 81 * 81; t += blockDim.x) {
-        const int k = t / 81, c = t % 81;
-        const int g = k / 3, xi = k % 3, nh = c / 27, ns = c % 27;
-        const TS* D = &S.Dg[g][(mh * 3 + nh) * 9 + xi * 3];
-        S.H[k][c] = D[0] * S.G[g * 3 + 0][ns] + D[1] * S.G[g * 3 + 1][ns] + D[2] * S.G[g * 3 + 2][ns];
+    form_up_coefficients<TS, 28>(S.G, S.Dg, S.HvG, S.PvG);
+    for (int pass = 0; pass < 2; ++pass) {
+      // operand rows [pass * kCRows, pass * kCRows + kCRows); rows past 242 are zero
+      for (int t = tid; t < 81 * kCRows; t += blockDim.x) {
+        const int k = t / kCRows, rl = t % kCRows, row = pass * kCRows + rl;
+        TS v = TS(0);
+        if (row < 243) {
+          const int pair = row / 27, ms = row % 27, g = k / 3, zeta = k % 3;
+          const TS* D = &S.Dg[g][pair * 9 + zeta];
+          v = S.G[g * 3 + 0][ms] * D[0] + S.G[g * 3 + 1][ms] * D[3] + S.G[g * 3 + 2][ms] * D[6];
+        }
+        S.A[k][rl] = v;
       }
       __syncthreads();
-      if (active) {
-        TS acc[3][3];
+      if (in_product) {
+        TS acc[4][4];
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+        for (int a = 0; a < 4; ++a)
 #pragma unroll
-          for (int b = 0; b < 3; ++b) acc[a][b] = TS(0);
+          for (int b = 0; b < 4; ++b) acc[a][b] = TS(0);
 #pragma unroll 3
         for (int k = 0; k < 81; ++k) {
-          const TS h0 = S.H[k][rg * 3 + 0], h1 = S.H[k][rg * 3 + 1], h2 = S.H[k][rg * 3 + 2];
-          const TS g0 = S.G[k][cg * 3 + 0], g1 = S.G[k][cg * 3 + 1], g2 = S.G[k][cg * 3 + 2];
-          acc[0][0] += h0 * g0; acc[0][1] += h0 * g1; acc[0][2] += h0 * g2;
-          acc[1][0] += h1 * g0; acc[1][1] += h1 * g1; acc[1][2] += h1 * g2;
-          acc[2][0] += h2 * g0; acc[2][1] += h2 * g1; acc[2][2] += h2 * g2;
+          TS av[4], bv[4];
+          load4(&S.A[k][rq * 4], av);
+          load4(&S.G[k][cq * 4], bv);
+#pragma unroll
+          for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] += av[a] * bv[b];
         }
 #pragma unroll
-        for (int a = 0; a < 3; ++a)
+        for (int a = 0; a < 4; ++a)
 #pragma unroll
-          for (int b = 0; b < 3; ++b) S.Kuu[mh * 27 + cg * 3 + b][rg * 3 + a] = acc[a][b];
+          for (int b = 0; b < 4; ++b) S.C[pass * kCRows + rq * 4 + a][cq * 4 + b] = acc[a][b];
       }
+      __syncthreads();  // A is rewritten by the next pass
     }
-    __syncthreads();
-    TS(*Kuu)[81] = S.Kuu;
-    store_element(Kel + (size_t)__ldg(elems + item) * ND * ND, [&](int r, int c) -> TS {
-      if (r < 81 && c < 81) return (EXACT || r >= c) ? Kuu[r][c] : Kuu[c][r];  // Iron mirrors the lower u-u triangle
-      TS s = TS(0);
-      if (r < 81) {  // u rows, p columns
-        for (int g = 0; g < NG; ++g) s += S.HvG[g][r] * S.psi[g][c - 81];
-      } else if (c < 81) {  // p rows, u columns
-        for (int g = 0; g < NG; ++g) s += S.psi[g][r - 81] * S.PvG[g][c];
-      }
-      return s;
-    });
+    TS* Ke = Kel + (size_t)__ldg(elems + item) * ND * ND;
+    write_up_blocks<TS, TS>(Ke, S.HvG, S.PvG, S.psi);
+    write_uu_block<EXACT, TS, TS, 28>(Ke, S.C);
   }
 }
 
@@ -1422,7 +1514,7 @@ mr_contract_kernel(const int32_t* __restrict__ elems, int32_t count, const Table
 // hi*hi + lo*hi + hi*lo recover about FP32 accuracy; without it the contraction is plain TF32
 // (about 1e-3 relative).  u-p / p-u blocks, Iron's lower-triangle mirror and the element-matrix
 // output are as in mr_contract_kernel.
-constexpr int kTCThreads = 256;
+constexpr int kTCThreads = 512;                // 16 warps: the operand formation is latency bound
 constexpr int kTK = 88;                        // K = 27 Gauss points x 3, padded to 11 steps of 8
 constexpr int kTKC = kTK / 4;                  // core-matrix columns along K (4 TF32 = 16 bytes)
 constexpr int kTABytes = 16 * kTKC * 128;      // one M = 128 operand tile
@@ -1434,7 +1526,7 @@ constexpr uint32_t kTWaitPolls = 1u << 24;     // bounded mbarrier wait
 struct __align__(128) TCShared {
   unsigned char A[2][kTABytes];  // head, tail of the current M half
   unsigned char B[2][kTBBytes];  // G head, tail: B[ns][(g,zeta)]
-  float G[81][28];               // G[(g,xi)][ms]
+  float G[81][28];               // G[(g,xi)][ms]; column 27 zero
   float psi[NG][NL];
   float Dg[NG][kGPOut];
   float K[256][kTKRow];          // product rows (mh,nh,ms), columns ns
@@ -1454,13 +1546,14 @@ template <bool EXACT, bool SPLIT3>
 __global__ void __launch_bounds__(kTCThreads, 1)
 mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Tables* __restrict__ Tg,
                       const float* __restrict__ gp, float* __restrict__ Kel, unsigned* err) {
+  static_assert(kTCThreads == 16 * 32, "one warp per 8-row group of an M = 128 operand tile");
   extern __shared__ __align__(1024) unsigned char traw[];
   TCShared& S = *reinterpret_cast<TCShared*>(traw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // constant operands: G (FP32, for forming A) and B = G^T split into TF32 head / tail
-  for (int t = tid; t < 81 * 27; t += blockDim.x) {
-    const int k = t / 27, ms = t % 27;
-    S.G[k][ms] = (float)Tg->dphi[k / 3][k % 3][ms];
+  for (int t = tid; t < 81 * 28; t += blockDim.x) {
+    const int k = t / 28, ms = t % 28;
+    S.G[k][ms] = ms < 27 ? (float)Tg->dphi[k / 3][k % 3][ms] : 0.0f;
   }
   for (int t = tid; t < NG * NL; t += blockDim.x) S.psi[t / NL][t % NL] = (float)Tg->psi[t / NL][t % NL];
   for (int t = tid; t < 32 * kTK; t += blockDim.x) {
@@ -1484,35 +1577,37 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
   const uint32_t a_hi = tc::smem_u32(S.A[0]), a_lo = tc::smem_u32(S.A[1]);
   const uint32_t b_hi = tc::smem_u32(S.B[0]), b_lo = tc::smem_u32(S.B[1]);
   uint32_t parity = 0;
+  // operand formation: warp w writes the 8-row group w of the current M = 128 tile, lane l its
+  // row 8 w + l / 4 and the K columns 4 kc + l % 4 (each step one core matrix, 128 bytes)
+  const int r_in = lane >> 2, kq = lane & 3;
 
   for (int item = blockIdx.x; item < count; item += gridDim.x) {
     __syncthreads();
     const float* src = gp + (size_t)item * NG * kGPOut;
     for (int t = tid; t < NG * kGPOut; t += blockDim.x) (&S.Dg[0][0])[t] = src[t];
     __syncthreads();
-    for (int t = tid; t < 2 * NG * 81; t += blockDim.x) {
-      const int which = t / (NG * 81), r = t % (NG * 81), g = r / 81, c = r % 81, h = c / 27, s = c % 27;
-      const int off = which == 0 ? 81 : 90;
-      const float v = S.G[g * 3 + 0][s] * S.Dg[g][off + 0 * 3 + h] + S.G[g * 3 + 1][s] * S.Dg[g][off + 1 * 3 + h] +
-                      S.G[g * 3 + 2][s] * S.Dg[g][off + 2 * 3 + h];
-      if (which == 0) S.HvG[g][c] = v; else S.PvG[g][c] = v;
-    }
+    float* Ke = Kel + (size_t)__ldg(elems + item) * ND * ND;
     for (int half = 0; half < 2; ++half) {
-      // A rows [128 half, 128 half + 128): one core matrix (8 rows x 4 k) per warp step, so each
-      // warp writes 128 contiguous bytes
-      for (int cm = warp; cm < 16 * kTKC; cm += kTCThreads / 32) {
-        const int rg = cm / kTKC, kc = cm % kTKC;
-        const int row = half * 128 + rg * 8 + (lane >> 2), k = kc * 4 + (lane & 3);
+      const int row = half * 128 + warp * 8 + r_in;
+      const bool valid = row < 243;
+      const int pair = valid ? row / 27 : 0, ms = valid ? row % 27 : 0;
+      const float* Gm = &S.G[0][ms];
+      const float* Dp = &S.Dg[0][pair * 9];
+      unsigned char* a0 = S.A[0] + (warp * kTKC) * 128 + lane * 4;
+      unsigned char* a1 = S.A[1] + (warp * kTKC) * 128 + lane * 4;
+#pragma unroll 2
+      for (int kc = 0; kc < kTKC; ++kc) {
+        const int k = kc * 4 + kq;
         float v = 0.0f;
-        if (row < 243 && k < 81) {
-          const int pair = row / 27, ms = row % 27, g = k / 3, zeta = k % 3;
-          const float* D = &S.Dg[g][pair * 9 + zeta];
-          v = S.G[g * 3 + 0][ms] * D[0] + S.G[g * 3 + 1][ms] * D[3] + S.G[g * 3 + 2][ms] * D[6];
+        if (valid && k < 81) {
+          const int g = k / 3, zeta = k - 3 * g;
+          const float* D = Dp + g * kGPOut + zeta;
+          const float* Gg = Gm + (g * 3) * 28;
+          v = Gg[0] * D[0] + Gg[28] * D[3] + Gg[56] * D[6];
         }
         const float hi = tc::to_tf32(v);
-        const uint32_t o = (uint32_t)(cm * 128 + lane * 4);
-        *reinterpret_cast<float*>(S.A[0] + o) = hi;
-        if (SPLIT3) *reinterpret_cast<float*>(S.A[1] + o) = tc::to_tf32(v - hi);
+        *reinterpret_cast<float*>(a0 + kc * 128) = hi;
+        if (SPLIT3) *reinterpret_cast<float*>(a1 + kc * 128) = tc::to_tf32(v - hi);
       }
       tc::fence_proxy_async();
       __syncthreads();
@@ -1530,24 +1625,27 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
           }
         }
         tc::commit(&S.mbar);
+        // the A tile is rewritten by the next half: wait (bounded) for this half's products
+        if (!tc::mbar_wait(&S.mbar, parity, kTWaitPolls)) {
+          // the MMAs may still be writing tensor memory: wait once more for their commit before
+          // anything releases it; if that also ends without it, the tensor memory stays
+          // allocated (abort = 2) rather than being freed under the MMAs
+          gfe_raise(err, GFE_DEVERR_TIMEOUT);
+          const bool drained = tc::mbar_wait(&S.mbar, parity, kTWaitPolls);
+          S.abort = drained ? 1 : 2;
+        }
       }
-      // the A tile is rewritten by the next half: wait for this half's products
-      if (!tc::mbar_wait(&S.mbar, parity, kTWaitPolls)) {
-        // the MMAs of this half may still be writing tensor memory: wait once more (bounded) for
-        // their commit before anything releases it; if that wait also ends without the commit,
-        // the tensor memory stays allocated (abort = 2) rather than being freed under the MMAs
-        gfe_raise(err, GFE_DEVERR_TIMEOUT);
-        const bool drained = tc::mbar_wait(&S.mbar, parity, kTWaitPolls);
-        atomicMax(&S.abort, drained ? 1 : 2);
-      }
+      // work that needs neither A nor the product runs while the tensor cores multiply
+      if (half == 0) form_up_coefficients<float, 28>(S.G, S.Dg, S.HvG, S.PvG);
+      else write_up_blocks<float, float>(Ke, S.HvG, S.PvG, S.psi);
       parity ^= 1u;
-      tc::fence_after_sync();
       __syncthreads();
+      tc::fence_after_sync();
       if (S.abort) break;
     }
     if (S.abort) break;
-    // tensor memory -> staged product: warp w reads lanes 32 (w % 4) .. of half w / 4
-    {
+    // tensor memory -> staged product: warp w < 8 reads lanes 32 (w % 4) .. of half w / 4
+    if (warp < 8) {
       const int half = warp >> 2, q = warp & 3;
       float v[32];
       tc::tmem_ld_32x32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(half * 32), v);
@@ -1557,19 +1655,7 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
     }
     tc::fence_before_sync();
     __syncthreads();
-    store_element(Kel + (size_t)__ldg(elems + item) * ND * ND, [&](int r, int c) -> float {
-      if (r < 81 && c < 81) {
-        const int rr = (EXACT || r >= c) ? r : c, cc = (EXACT || r >= c) ? c : r;  // Iron mirrors the lower triangle
-        return S.K[(rr / 27 * 3 + cc / 27) * 27 + rr % 27][cc % 27];
-      }
-      float s = 0.0f;
-      if (r < 81) {
-        for (int g = 0; g < NG; ++g) s += S.HvG[g][r] * S.psi[g][c - 81];
-      } else if (c < 81) {
-        for (int g = 0; g < NG; ++g) s += S.psi[g][r - 81] * S.PvG[g][c];
-      }
-      return s;
-    });
+    write_uu_block<EXACT, float, float, kTKRow>(Ke, S.K);
   }
   tc::fence_before_sync();
   __syncthreads();
