@@ -282,7 +282,7 @@ def bench_laplace_bases(args, log, clock_sampler, cpu_fn=None):
 def bench_mr_newton(args, log, clock_sampler):
     """Uniaxial stretch of the Mooney-Rivlin box to lambda = 1.1 in 5 load steps (Iron's increment
     rule), roller conditions, Newton with the consistent tangent and MINRES; FP64 plain against
-    mixed precision (FP32 contraction + FP32 MINRES inside FP64 refinement, FP64 residual)."""
+    mixed precision (tensor-core contraction + FP32 MINRES inside FP64 refinement, FP64 residual)."""
     from .newton import NewtonSolver, uniaxial_exact_state, uniaxial_roller_conditions
 
     n = 32 if args.n == 128 else args.n

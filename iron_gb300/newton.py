@@ -17,9 +17,12 @@ replaces PETSc KSP: preconditioned MINRES for the consistent tangent (symmetric 
 restarted GMRES (Iron's default Krylov method) for the FD and analytic Jacobians, which are not
 symmetric; all are preconditioned by the diagonal of gfe_saddle_preconditioner.
 
-Precision 'mixed': FP32 basis-gradient contraction for the Jacobian and FP32 Krylov iterations
-(FP32 matrix copy and vectors) inside FP64 refinement residuals; the nonlinear residual, its norm, the line search and the
-convergence test stay in FP64, so the converged state is set by the FP64 residual alone.
+Precision 'mixed': the Jacobian's basis-gradient contraction on the tensor cores (tcgen05, TF32
+in three passes, about FP32 accuracy; `contraction` selects "fp32" for the CUDA-core FP32
+contraction or "tf32" for one pass) with FP32 kinematics, and FP32 Krylov iterations (FP32 matrix
+copy and vectors) inside FP64 refinement residuals; the nonlinear residual, its norm, the line
+search and the convergence test stay in FP64, so the converged state is set by the FP64 residual
+alone.
 """
 from __future__ import annotations
 
@@ -121,7 +124,8 @@ class NewtonSolver:
     """Newton's method with a backtracking (cubic) line search on R(dep) = 0 for a
     MooneyRivlinAssembly, with Dirichlet DOFs eliminated."""
 
-    def __init__(self, asm, c, *, jacobian: str = "consistent", precision: str = "fp64", fd_step: float = 1e-6,
+    def __init__(self, asm, c, *, jacobian: str = "consistent", precision: str = "fp64", contraction: str | None = None,
+                 fd_step: float = 1e-6,
                  absolute_tolerance: float = 1e-10, relative_tolerance: float = 1e-5,
                  solution_tolerance: float = 1e-5, maximum_iterations: int = 50, linesearch_alpha: float = 1e-4,
                  linear_relative_tolerance: float = 1e-5, linear_maximum_iterations: int = 50000,
@@ -136,6 +140,11 @@ class NewtonSolver:
             raise GfeError(-1, f"the {jacobian} Jacobian is not symmetric: use linear_solver='gmres'")
         if precision not in ("fp64", "mixed"):
             raise GfeError(-1, f"unknown precision {precision!r} (fp64 | mixed)")
+        if contraction is None:
+            contraction = "tf32x3" if precision == "mixed" else "fp64"
+        contraction = {"fp32": "mixed"}.get(contraction, contraction)
+        if contraction not in ("fp64", "mixed", "tf32x3", "tf32") or (precision == "fp64") != (contraction == "fp64"):
+            raise GfeError(-1, f"contraction {contraction!r} does not go with precision {precision!r}")
         if asm.row_ptr is None:
             asm.build_structure(stream)
         self.asm = asm
@@ -143,6 +152,7 @@ class NewtonSolver:
         self.jacobian = jacobian
         self.fd_step = float(fd_step)
         self.precision = precision
+        self.contraction = contraction
         self.atol = float(absolute_tolerance)
         self.rtol = float(relative_tolerance)
         self.stol = float(solution_tolerance)
@@ -178,11 +188,11 @@ class NewtonSolver:
     def _linear_solve(self, dep, fixed_u8, info: NewtonInfo):
         asm = self.asm
         if self.jacobian == "consistent":
-            vals = asm.tangent(dep, self.c, precision=self.precision, stream=self.stream)
+            vals = asm.tangent(dep, self.c, precision=self.contraction, stream=self.stream)
         elif self.jacobian == "fd":
             vals = asm.jacobian_fd(dep, self.c, step=self.fd_step, stream=self.stream)
         else:
-            vals = asm.jacobian(dep, self.c, precision=self.precision, stream=self.stream)
+            vals = asm.jacobian(dep, self.c, precision=self.contraction, stream=self.stream)
         info.jacobian_evaluations += 1
         saddle_preconditioner(asm.row_ptr, asm.col_idx, vals, 3 * asm.n_q2, fixed_u8, out=self._minv,
                               stream=self.stream)
