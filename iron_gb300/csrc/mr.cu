@@ -37,8 +37,9 @@ constexpr int NL = 8;    // linear (pressure) element nodes
 constexpr int NG = 27;   // Gauss points (3x3x3)
 constexpr int ND = 89;   // element DOFs
 
+// 16-byte multiple in size, so that a TMA bulk copy can stage the whole table
 template <typename S>
-struct TablesT {
+struct alignas(16) TablesT {
   S dphi[NG][3][NQ];  // d phi_ns / d xi_k at Gauss point g (quadratic basis)
   S w[NG];
   S psi[NG][NL];      // linear basis values at the Gauss points
@@ -1223,15 +1224,17 @@ __device__ void iron_point_tensors(const GPT<S>& q, S c1, S c2, S sub[6][9], S h
 }
 
 constexpr int kGPElems = 4;                // elements per CTA of mr_gp_kernel
+constexpr uint32_t kTableWaitPolls = 1u << 24;  // bounded wait for the TMA copy of the tables
 constexpr int kGPThreads = kGPElems * NG;  // 108
 constexpr int kGPOut = 81 + 9 + 9;         // D (9 blocks x 9), Hv, Pv per Gauss point
+constexpr int kGPItem = (NG * kGPOut + 3) / 4 * 4;  // per-element stride: a 16-byte multiple (TMA)
 
 template <typename KS>
 struct GPShared {
   KS x[kGPElems][81], z[kGPElems][81], p[kGPElems][8];
 };
 
-// One thread per (element, Gauss point).  out[item][g][kGPOut] in the contraction type TO:
+// One thread per (element, Gauss point).  out[item * kGPItem + g * kGPOut + j] in the contraction type TO:
 // D[(mh*3+nh)*9 + xi*3+zeta], Hv[81 + xi*3+mh], Pv[90 + xi*3+nh].  KS is the kinematics type:
 // double, or float on the FP32 paths (element data rounded once per node when staged, the volume
 // Jacobians det(Z), det(X) still evaluated in FP64 from the exactly widened gradients; for the
@@ -1243,12 +1246,17 @@ mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __
              const int32_t* __restrict__ elin, int32_t nq2, const double* __restrict__ xg,
              const double* __restrict__ dep, const double* __restrict__ cpar, const TablesT<KS>* __restrict__ Tg,
              TO* __restrict__ out, unsigned* err) {
-  extern __shared__ double smem_d[];
-  KS* smem = reinterpret_cast<KS*>(smem_d);
-  constexpr int kTabWords = (int)(sizeof(TablesT<KS>) / sizeof(KS));
-  TablesT<KS>& T = *reinterpret_cast<TablesT<KS>*>(smem);
-  GPShared<KS>& S = *reinterpret_cast<GPShared<KS>*>(smem + kTabWords);
-  for (int i = threadIdx.x; i < kTabWords; i += blockDim.x) smem[i] = reinterpret_cast<const KS*>(Tg)[i];
+  extern __shared__ __align__(16) double smem_d[];
+  unsigned char* sbase = reinterpret_cast<unsigned char*>(smem_d);
+  TablesT<KS>& T = *reinterpret_cast<TablesT<KS>*>(sbase);
+  GPShared<KS>& S = *reinterpret_cast<GPShared<KS>*>(sbase + sizeof(TablesT<KS>));
+  uint64_t* tbar = reinterpret_cast<uint64_t*>(sbase + sizeof(TablesT<KS>) + sizeof(GPShared<KS>));
+  // the basis tables arrive by one TMA bulk copy while the threads gather the element data
+  if (threadIdx.x == 0) {
+    tc::mbar_init(tbar, 1);
+    tc::mbar_arrive_expect_tx(tbar, (uint32_t)sizeof(TablesT<KS>));
+    tc::bulk_copy_g2s(&T, Tg, (uint32_t)sizeof(TablesT<KS>), tbar);
+  }
   const int le = threadIdx.x / NG, g = threadIdx.x % NG;
   const int item = blockIdx.x * kGPElems + le;
   // cooperative load of the CTA's elements
@@ -1270,8 +1278,14 @@ mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __
     S.p[l][i] = (KS)dep[(size_t)3 * nq2 + __ldg(elin + (size_t)e * NL + i)];
   }
   __syncthreads();
+  // every thread waits for the tables (so none exits while the copy is in flight); bounded
+  if (!tc::mbar_wait(tbar, 0, kTableWaitPolls)) {
+    gfe_raise(err, GFE_DEVERR_TIMEOUT);
+    tc::mbar_wait(tbar, 0, kTableWaitPolls);
+    return;
+  }
   if (item >= count) return;
-  TO* o = out + ((size_t)item * NG + g) * kGPOut;
+  TO* o = out + (size_t)item * kGPItem + (size_t)g * kGPOut;
   if constexpr (!EXACT) {
     const KS c1 = (KS)cpar[0], c2 = (KS)cpar[1];
     GPT<KS> q;
@@ -1455,7 +1469,7 @@ mr_contract_kernel(const int32_t* __restrict__ elems, int32_t count, const Table
   const bool in_product = tid < kCTileRows * kCTileCols;
   for (int item = blockIdx.x; item < count; item += gridDim.x) {
     __syncthreads();
-    const TS* src = gp + (size_t)item * NG * kGPOut;
+    const TS* src = gp + (size_t)item * kGPItem;
     for (int t = tid; t < NG * kGPOut; t += blockDim.x) (&S.Dg[0][0])[t] = src[t];
     __syncthreads();
     form_up_coefficients<TS, 28>(S.G, S.Dg, S.HvG, S.PvG);
@@ -1528,11 +1542,12 @@ struct __align__(128) TCShared {
   unsigned char B[2][kTBBytes];  // G head, tail: B[ns][(g,zeta)]
   float G[81][28];               // G[(g,xi)][ms]; column 27 zero
   float psi[NG][NL];
-  float Dg[NG][kGPOut];
+  alignas(16) float Dg[2][kGPItem];  // Gauss-point blocks of the current and the next element (TMA)
   float K[256][kTKRow];          // product rows (mh,nh,ms), columns ns
   float HvG[NG][81];
   float PvG[NG][81];
   uint64_t mbar;
+  uint64_t dbar[2];              // completion of the bulk copies into Dg[0], Dg[1]
   uint32_t tmem;
   int abort;
 };
@@ -1564,9 +1579,17 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
     *reinterpret_cast<float*>(S.B[1] + tc_offset(n, k)) = tc::to_tf32(v - hi);
   }
   if (warp == 0) tc::tmem_alloc(&S.tmem, 64);
+  constexpr uint32_t kDgBytes = kGPItem * sizeof(float);
   if (tid == 0) {
     tc::mbar_init(&S.mbar, 1);
+    tc::mbar_init(&S.dbar[0], 1);
+    tc::mbar_init(&S.dbar[1], 1);
     S.abort = 0;
+    // the first element's Gauss-point blocks: one TMA bulk copy
+    if ((int)blockIdx.x < count) {
+      tc::mbar_arrive_expect_tx(&S.dbar[0], kDgBytes);
+      tc::bulk_copy_g2s(S.Dg[0], gp + (size_t)blockIdx.x * kGPItem, kDgBytes, &S.dbar[0]);
+    }
   }
   tc::fence_proxy_async();
   tc::fence_before_sync();
@@ -1577,22 +1600,40 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
   const uint32_t a_hi = tc::smem_u32(S.A[0]), a_lo = tc::smem_u32(S.A[1]);
   const uint32_t b_hi = tc::smem_u32(S.B[0]), b_lo = tc::smem_u32(S.B[1]);
   uint32_t parity = 0;
+  uint32_t dpar[2] = {0u, 0u};
+  bool pending[2] = {(int)blockIdx.x < count, false};  // (thread 0) copies issued and not yet waited for
   // operand formation: warp w writes the 8-row group w of the current M = 128 tile, lane l its
   // row 8 w + l / 4 and the K columns 4 kc + l % 4 (each step one core matrix, 128 bytes)
   const int r_in = lane >> 2, kq = lane & 3;
 
-  for (int item = blockIdx.x; item < count; item += gridDim.x) {
+  int buf = 0;
+  for (int item = blockIdx.x; item < count; item += gridDim.x, buf ^= 1) {
+    __syncthreads();  // every thread is done with the previous element, whose buffer is Dg[buf ^ 1]
+    const int next = item + (int)gridDim.x;
+    if (tid == 0 && next < count) {
+      // prefetch the next element's blocks while this one is computed
+      tc::fence_proxy_async();
+      tc::mbar_arrive_expect_tx(&S.dbar[buf ^ 1], kDgBytes);
+      tc::bulk_copy_g2s(S.Dg[buf ^ 1], gp + (size_t)next * kGPItem, kDgBytes, &S.dbar[buf ^ 1]);
+      pending[buf ^ 1] = true;
+    }
+    if (!tc::mbar_wait(&S.dbar[buf], dpar[buf], kTWaitPolls)) {
+      gfe_raise(err, GFE_DEVERR_TIMEOUT);
+      tc::mbar_wait(&S.dbar[buf], dpar[buf], kTWaitPolls);
+      atomicMax(&S.abort, 1);
+    }
+    if (tid == 0) pending[buf] = false;
+    dpar[buf] ^= 1u;
     __syncthreads();
-    const float* src = gp + (size_t)item * NG * kGPOut;
-    for (int t = tid; t < NG * kGPOut; t += blockDim.x) (&S.Dg[0][0])[t] = src[t];
-    __syncthreads();
+    if (S.abort) break;
+    const float(*Dg)[kGPOut] = reinterpret_cast<const float(*)[kGPOut]>(S.Dg[buf]);
     float* Ke = Kel + (size_t)__ldg(elems + item) * ND * ND;
     for (int half = 0; half < 2; ++half) {
       const int row = half * 128 + warp * 8 + r_in;
       const bool valid = row < 243;
       const int pair = valid ? row / 27 : 0, ms = valid ? row % 27 : 0;
       const float* Gm = &S.G[0][ms];
-      const float* Dp = &S.Dg[0][pair * 9];
+      const float* Dp = &Dg[0][pair * 9];
       unsigned char* a0 = S.A[0] + (warp * kTKC) * 128 + lane * 4;
       unsigned char* a1 = S.A[1] + (warp * kTKC) * 128 + lane * 4;
 #pragma unroll 2
@@ -1636,7 +1677,7 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
         }
       }
       // work that needs neither A nor the product runs while the tensor cores multiply
-      if (half == 0) form_up_coefficients<float, 28>(S.G, S.Dg, S.HvG, S.PvG);
+      if (half == 0) form_up_coefficients<float, 28>(S.G, Dg, S.HvG, S.PvG);
       else write_up_blocks<float, float>(Ke, S.HvG, S.PvG, S.psi);
       parity ^= 1u;
       __syncthreads();
@@ -1657,6 +1698,10 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
     __syncthreads();
     write_uu_block<EXACT, float, float, kTKRow>(Ke, S.K);
   }
+  // no bulk copy may still be landing in this CTA's shared memory when it exits (bounded)
+  if (tid == 0)
+    for (int b = 0; b < 2; ++b)
+      if (pending[b] && !tc::mbar_wait(&S.dbar[b], dpar[b], kTWaitPolls)) gfe_raise(err, GFE_DEVERR_TIMEOUT);
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0 && S.abort < 2) tc::tmem_dealloc(tmem, 64);
@@ -1786,7 +1831,7 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
     TK = T;
   }
   if (n_elem == 0) return GFE_OK;
-  const size_t gsm_k = sizeof(TablesT<KF>) + sizeof(GPShared<KF>);
+  const size_t gsm_k = sizeof(TablesT<KF>) + sizeof(GPShared<KF>) + 16;  // + the tables' mbarrier
   const size_t csm = sizeof(ContractShared<TS>);
   const void* gk = mode == 0 ? (const void*)mr_gp_kernel<TS, false, KF> : (const void*)mr_gp_kernel<TS, true, KF>;
   const void* ck = mode == 0 ? (const void*)mr_contract_kernel<TS, false> : (const void*)mr_contract_kernel<TS, true>;
@@ -1809,7 +1854,7 @@ int jacobian_impl(int mode, int32_t n_elem, const int32_t* eq2, const int32_t* e
     return rc;
   }
   TS* gpbuf = nullptr;
-  if ((rc = gfe::scratch_alloc((void**)&gpbuf, sizeof(TS) * (size_t)chunk * NG * kGPOut + 16, s,
+  if ((rc = gfe::scratch_alloc((void**)&gpbuf, sizeof(TS) * (size_t)chunk * kGPItem + 16, s,
                                "Gauss-point tangent blocks"))) {
     if (own_kel) gfe::scratch_free(Kel, s);
     return rc;

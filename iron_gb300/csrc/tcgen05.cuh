@@ -1,6 +1,7 @@
 // tcgen05.cuh -- inline-PTX helpers for the 5th-generation tensor cores (sm_100a / sm_103a):
 // tensor-memory allocation, single-CTA MMA with shared-memory operand descriptors, commit to an
-// mbarrier, tensor-memory loads and the ordering fences between them.
+// mbarrier, tensor-memory loads and the ordering fences between them, and the untiled TMA bulk
+// copy from global to shared memory that completes on an mbarrier.
 //
 // Operands use the no-swizzle K-major canonical layout: the unit is a core matrix of 8 rows x 16
 // bytes stored contiguously (row i at byte 16 i).  A descriptor names the first core matrix of the
@@ -75,6 +76,23 @@ __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.
 __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// One thread: announce `bytes` of asynchronous copies into the current phase and arrive once.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+               : "memory");
+}
+
+// One thread: bulk copy (TMA, untiled) of `bytes` from global to this CTA's shared memory; the
+// mbarrier's transaction count is decremented when the bytes have landed.  Both addresses 16-byte
+// aligned, `bytes` a multiple of 16.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
 }
 
 // Wait until the phase of parity `parity` has completed; gives up after `max_tries` polls.
