@@ -62,6 +62,13 @@ int gfe_last_error(char* buf, int len);
  * leave nothing behind.  No counterpart in the reference. */
 int gfe_clear_stale_error(void);
 
+/* The library's working memory (Krylov vectors, element matrices, Gauss-point blocks) comes from
+ * the current device's default stream-ordered memory pool, whose release threshold the library
+ * raises to 4 GiB so that freed scratch stays mapped for the next call.  This call synchronises
+ * the device and returns all unused pool memory to the device (for a caller that needs it, e.g.
+ * after an out-of-memory failure).  No counterpart in the reference. */
+int gfe_release_scratch(void);
+
 /* Read and clear the device error word (bit set of GFE_DEVERR_* raised by kernels). */
 int gfe_device_errors(uint32_t* bits_host, void* stream);
 

@@ -49,6 +49,7 @@ vp, i32, i64, f64 = C.c_void_p, C.c_int32, C.c_int64, C.c_double
 SIGNATURES = {
     "gfe_version": (C.c_int, []),
     "gfe_clear_stale_error": (C.c_int, []),
+    "gfe_release_scratch": (C.c_int, []),
     "gfe_last_error": (C.c_int, [C.c_char_p, C.c_int]),
     "gfe_device_errors": (C.c_int, [C.POINTER(C.c_uint32), vp]),
     "gfe_set_thread_error_word": (C.c_int, [vp]),

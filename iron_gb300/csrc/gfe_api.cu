@@ -10,6 +10,29 @@ thread_local unsigned* t_err_word = nullptr;  // gfe_set_thread_error_word overr
 std::mutex g_mu;
 unsigned* g_err_word[64] = {nullptr};
 int g_sm_count[64] = {0};
+bool g_pool_ready[64] = {false};
+// Freed stream-ordered scratch the device's default memory pool keeps mapped for the next call
+// (the pool's release threshold; the default of 0 unmaps it at every synchronisation, so each
+// Jacobian or Krylov solve would map its gigabytes of scratch again).  A process setting: it ends
+// with the process.
+constexpr uint64_t kScratchCacheBytes = 4ull << 30;
+
+void prepare_pool() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (g_pool_ready[dev]) return;
+  g_pool_ready[dev] = true;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t thr = kScratchCacheBytes;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  cudaGetLastError();
+}
 }  // namespace
 
 namespace gfe {
@@ -47,6 +70,7 @@ void set_thread_error_word(unsigned* w) { t_err_word = w; }
 int scratch_alloc(void** p, size_t bytes, cudaStream_t s, const char* what) {
   *p = nullptr;
   if (bytes == 0) bytes = 16;
+  prepare_pool();
   cudaError_t e = cudaMallocAsync(p, bytes, s);
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -76,6 +100,16 @@ int sm_count() {
 extern "C" int gfe_version(void) { return 100; }
 
 extern "C" int gfe_clear_stale_error(void) { return (int)cudaGetLastError(); }
+
+extern "C" int gfe_release_scratch(void) {
+  int dev = 0;
+  GFE_CUDA_TRY(cudaGetDevice(&dev));
+  cudaMemPool_t pool;
+  GFE_CUDA_TRY(cudaDeviceGetDefaultMemPool(&pool, dev));
+  GFE_CUDA_TRY(cudaDeviceSynchronize());
+  GFE_CUDA_TRY(cudaMemPoolTrimTo(pool, 0));
+  return GFE_OK;
+}
 
 extern "C" int gfe_last_error(char* buf, int len) {
   int n = (int)t_last_error.size();

@@ -760,6 +760,8 @@ class ServingEngine:
             del dead
         torch.cuda.synchronize(self.dev)
         torch.cuda.empty_cache()
+        with torch.cuda.device(self.dev):
+            _lib.call("gfe_release_scratch")  # the library's cached stream-ordered scratch too
 
     def __del__(self):
         try:
