@@ -442,8 +442,9 @@ int gfe_csr_spmv(int32_t n_rows, const int32_t* row_ptr, const int32_t* col_idx,
  * PETSc KSP in Iron, src/solver_routines.F90:11775-11991).
  *  f          [n] right-hand side (may be NULL = zero)
  *  x          [n] in: Dirichlet values on fixed DOFs; out: solution
- *  values32   optional FP32 copy of values: when given and precision == GFE_MIXED, runs
- *             FP64-residual iterative refinement around FP32 inner CG solves
+ *  values32   optional FP32 copy of values: when given and precision == GFE_MIXED, runs FP32 CG
+ *             with reliable updates (the true residual formed in FP64 with values replaces the
+ *             FP32 one after each 1e3-fold reduction; the FP32 search direction is kept)
  *  rtol       relative residual target ||f - K x|| / ||f - K x0||
  *  iters_host out: total (inner) iterations;  rel_host out: final relative FP64 residual
  * Synchronises `stream`.  Allocates and frees its scratch on `stream`. */

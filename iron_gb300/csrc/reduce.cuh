@@ -12,12 +12,15 @@ namespace gfe_red {
 
 constexpr int kThreads = 256;
 
-// Sum of one double per thread of a kThreads-wide block; valid in thread 0.
-__device__ __forceinline__ double block_sum(double v) {
+// Sum of one value per thread of a kThreads-wide block, in double; valid in thread 0.  The warp
+// stage runs in the threads' own type (FP32 partials of the FP32 Krylov vectors stay off the FP64
+// pipe), the warp totals are added in FP64 in warp order.
+template <typename T>
+__device__ __forceinline__ double block_sum(T v) {
   __shared__ double sh[kThreads / 32];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)v;
   __syncthreads();
   double s = 0.0;
   if (threadIdx.x == 0)
@@ -40,20 +43,17 @@ __device__ __forceinline__ bool last_block(int* ticket) {
   return amlast;
 }
 
-// Sum red[0..n) in index order using the whole block; result valid in thread 0.
+// Sum red[0..n) in a fixed order using the whole block: each thread adds a contiguous run of
+// partials, then the runs are combined by the same fixed-shape tree as block_sum.  A serial sum of
+// the 256 runs by one thread would be 256 dependent FP64 adds: at one FP64 warp instruction every
+// 64 cycles per scheduler, about 8 us per reduction, several times per Krylov iteration.  Result
+// valid in thread 0.
 __device__ __forceinline__ double ordered_sum(const double* red, int n) {
-  __shared__ double sh[kThreads];
   const int per = (n + kThreads - 1) / kThreads;
   double s = 0.0;
   const int i0 = threadIdx.x * per;
   for (int i = i0; i < i0 + per && i < n; ++i) s += __ldcg(red + i);
-  sh[threadIdx.x] = s;
-  __syncthreads();
-  double t = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < kThreads; ++i) t += sh[i];
-  __syncthreads();
-  return t;
+  return block_sum(s);
 }
 
 }  // namespace gfe_red

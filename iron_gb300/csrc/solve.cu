@@ -12,10 +12,11 @@
 // Kernels return immediately once the device-side `done` flag is set, so the host can launch
 // iterations in chunks and synchronise only between chunks.
 //
-// Mixed precision (precision == GFE_MIXED with an FP32 copy of the matrix): iterative refinement.
-// The outer loop forms r = f - A x in FP64 with the FP64 matrix and tests ||r|| against the target;
-// the correction A d = r is solved by FP32 CG (FP32 matrix and vectors, FP64 dot products) to a
-// loose relative tolerance and added to x in FP64.
+// Mixed precision (precision == GFE_MIXED with an FP32 copy of the matrix): FP32 CG (FP32 matrix
+// and vectors, FP64 dot products) with reliable updates.  Each time its recurrence residual has
+// dropped 1e3-fold, the FP32 correction is added to x in FP64, the true residual f - A x is formed
+// in FP64 with the FP64 matrix and tested against the target, and it replaces the FP32 residual
+// while the FP32 CG keeps its search direction.
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -79,7 +80,7 @@ cg_spmv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, c
       dot += p[row] * s;
     }
   }
-  double b = block_sum((double)dot);
+  double b = block_sum(dot);
   if (threadIdx.x == 0) red[blockIdx.x] = b;
   if (last_block(&sc->ticket1)) {
     double pq = ordered_sum(red, gridDim.x);
@@ -109,8 +110,8 @@ cg_update(int n, TX* __restrict__ x, TV* __restrict__ r, TV* __restrict__ z, con
     rz += rv * zv;
     rr += rv * rv;
   }
-  double b1 = block_sum((double)rz);
-  double b2 = block_sum((double)rr);
+  double b1 = block_sum(rz);
+  double b2 = block_sum(rr);
   if (threadIdx.x == 0) { red[blockIdx.x] = b1; red2[blockIdx.x] = b2; }
   if (last_block(&sc->ticket2)) {
     double rzn = ordered_sum(red, gridDim.x);
@@ -169,17 +170,23 @@ __global__ void jacobi_inverse(int n, const int32_t* __restrict__ rp, const int3
   }
 }
 
-// Start an inner CG from residual r64 (FP64) into vectors of type TV: r = r64, z = p = dinv r, x = 0.
+// Start an inner CG from residual r64 (FP64) into vectors of type TV: r = r64, z = dinv r, x = 0
+// when zero_x.  keep_p false: a fresh start, p = z.  keep_p true: a reliable update after a CG that
+// stopped on convergence (so its last direction update was skipped): the true residual replaces
+// the recurrence residual r_k+1 and the search direction p_k is kept; beta = <r,z> / rho_k, where
+// rho_k = rho_k+1 / beta_k+1 from the stopped CG's scalars, for a following cg_direction, which
+// forms p = z + beta p.
 template <typename TV, typename TX>
 __global__ void __launch_bounds__(kThreads)
 cg_start(int n, const double* __restrict__ r64, const double* __restrict__ dinv, TV* __restrict__ r,
-         TV* __restrict__ z, TV* __restrict__ p, TX* __restrict__ xz, bool zero_x, double* red, double* red2,
-         Scalars* sc, double rtol2) {
+         TV* __restrict__ z, TV* __restrict__ p, TX* __restrict__ xz, bool zero_x, bool keep_p, double* red,
+         double* red2, Scalars* sc, double rtol2) {
   double rz = 0.0, rr = 0.0;
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     TV rv = (TV)r64[i];
     TV zv = (TV)(dinv[i] * (double)rv);
-    r[i] = rv; z[i] = zv; p[i] = zv;
+    r[i] = rv; z[i] = zv;
+    if (!keep_p) p[i] = zv;
     if (zero_x) xz[i] = (TX)0;
     rz += (double)rv * (double)zv;
     rr += (double)rv * (double)rv;
@@ -189,6 +196,7 @@ cg_start(int n, const double* __restrict__ r64, const double* __restrict__ dinv,
   if (last_block(&sc->ticket2)) {
     double rzn = ordered_sum(red, gridDim.x), rrn = ordered_sum(red2, gridDim.x);
     if (threadIdx.x == 0) {
+      sc->beta = keep_p && sc->rz != 0.0 ? sc->beta * (rzn / sc->rz) : 0.0;
       sc->rz = rzn; sc->rr = rrn; sc->rr0 = rrn; sc->tol2 = rtol2 * rrn;
       sc->done = rrn == 0.0 ? 2 : 0; sc->it = 0; sc->bad = 0; sc->ticket2 = 0; sc->ticket1 = 0;
     }
@@ -349,11 +357,13 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
   if (precision == GFE_FP64) {
     double* r = (double*)vr; double* z = (double*)vz; double* p = (double*)vp; double* q = (double*)vq;
     // The recurrence residual drifts from the true residual b - A x, so CG aims at half the target
-    // and restarts from the true residual (residual replacement) while the latter is above it.
+    // and, while the true residual is above it, replaces the recurrence residual by the true one
+    // and continues along the same search direction (a reliable update).
     double r2_start = b2;
     for (int round = 0; round < 4 && rc == GFE_OK; ++round) {
-      cg_start<double, double><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, x, false, red, red2, sc,
+      cg_start<double, double><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, x, false, round > 0, red, red2, sc,
                                                          0.25 * rtol * rtol * b2 / r2_start);
+      if (round > 0) cg_direction<double><<<grid, kThreads, 0, s>>>(n, p, z, sc);
       rc = run_cg<double, double, double>(s, n, row_ptr, col_idx, values, fixed, dinv, x, r, z, p, q, red, red2, sc,
                                           &sh, lpr, grid, max_iters - total_it, chunk);
       total_it += sh.it;
@@ -368,11 +378,15 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
     float* r = (float*)vr; float* z = (float*)vz; float* p = (float*)vp; float* q = (float*)vq; float* d = (float*)vd;
     float* dinv32 = (float*)vdinv;
     to_float<<<grid, kThreads, 0, s>>>(n, dinv, dinv32);
-    // each FP32 CG reduces the residual 1e5-fold before the FP64 residual is formed again: fewer
-    // restarts than 1e4 (925 instead of 1,207 iterations, 173 instead of 225 ms at 128^3 to 1e-12),
-    // while 1e6 runs past what the FP32 recursion tracks (1,079 iterations)
-    const double inner_rtol = 1e-5;
-    for (int outer = 0; outer < 64 && rc == GFE_OK; ++outer) {
+    // Reliable updates: the FP32 CG runs until its recurrence residual has dropped by inner_rtol
+    // since the last update; then its correction d is added to x in FP64, the true residual
+    // f - A x is formed with the FP64 matrix, replaces the FP32 residual, and the FP32 CG continues
+    // along its current search direction.  At 128^3 to 1e-12: 727 iterations (FP64 CG: 670);
+    // restarting the FP32 CG from the true residual instead discards its Krylov space (928
+    // iterations with the best restart tolerance, 1e-5).  Reductions of 1e-1 to 1e-3 per update
+    // all take 727-742 iterations; 1e-3 needs the fewest updates.
+    const double inner_rtol = 1e-3;
+    for (int outer = 0; outer < 200 && rc == GFE_OK; ++outer) {
       if (outer > 0) {
         cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
         norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, sc, red2 + grid - 1);
@@ -381,8 +395,9 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
         if (r2 <= rtol * rtol * b2) break;
         if (total_it >= max_iters) break;
       }
-      cg_start<float, float><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, d, true, red, red2, sc,
+      cg_start<float, float><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, d, true, outer > 0, red, red2, sc,
                                                        inner_rtol * inner_rtol);
+      if (outer > 0) cg_direction<float><<<grid, kThreads, 0, s>>>(n, p, z, sc);
       rc = run_cg<float, float, float>(s, n, row_ptr, col_idx, values32, fixed, dinv32, d, r, z, p, q, red, red2, sc,
                                        &sh, lpr, grid, max_iters - total_it, chunk);
       total_it += sh.it;
@@ -477,7 +492,7 @@ extern "C" int gfe_cg_begin(int32_t n, const int32_t* row_ptr, const int32_t* co
   jacobi_inverse<<<w.grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, fixed, w.dinv, err);
   set_dirichlet<<<w.grid, kThreads, 0, s>>>(n, x, fixed, true);
   cg_residual<double><<<w.grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, w.q);
-  cg_start<double, double><<<w.grid, kThreads, 0, s>>>(n, w.q, w.dinv, w.r, w.z, w.p, x, false, w.red, w.red2, w.sc,
+  cg_start<double, double><<<w.grid, kThreads, 0, s>>>(n, w.q, w.dinv, w.r, w.z, w.p, x, false, false, w.red, w.red2, w.sc,
                                                        rtol * rtol);
   GFE_LAUNCH_CHECK("gfe_cg_begin");
   return GFE_OK;
@@ -573,7 +588,7 @@ minres_spmv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ c
       }
     }
   }
-  const double b = block_sum((double)dot);
+  const double b = block_sum(dot);
   if (threadIdx.x == 0) red[blockIdx.x] = b;
   if (last_block(&sc->ticket1)) {
     const double d = ordered_sum(red, gridDim.x);
@@ -659,7 +674,7 @@ minres_spmv_nodal(int n, int n_node, const int32_t* __restrict__ rp, const int32
       }
     }
   }
-  const double b = block_sum((double)dot);
+  const double b = block_sum(dot);
   if (threadIdx.x == 0) red[blockIdx.x] = b;
   if (last_block(&sc->ticket1)) {
     const double d = ordered_sum(red, gridDim.x);
@@ -1525,8 +1540,9 @@ extern "C" int gfe_cg_solve_noalloc(int32_t n, const int32_t* row_ptr, const int
   int total_it = 0;
   r2 = b2;
   for (int round = 0; round < 4; ++round) {
-    cg_start<double, double><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, x, false, red, red2, sc,
+    cg_start<double, double><<<grid, kThreads, 0, s>>>(n, r64, dinv, r, z, p, x, false, round > 0, red, red2, sc,
                                                        0.25 * rtol * rtol * b2 / r2);
+    if (round > 0) cg_direction<double><<<grid, kThreads, 0, s>>>(n, p, z, sc);
     rc = run_cg<double, double, double>(s, n, row_ptr, col_idx, values, fixed, dinv, x, r, z, p, q, red, red2, sc,
                                         &sh, lpr, grid, max_iters - total_it, chunk);
     if (rc) return rc;
