@@ -93,6 +93,76 @@ cg_spmv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, c
   }
 }
 
+// q = A p as cg_spmv, with each lane's first E entries of its row loaded before any is used (the
+// per-row loop keeps about four loads in flight a lane, and each row waits on its bounds, then on
+// its entries, then on the gathers), R rows per lane group at a time, and the next rows' bounds
+// loaded ahead.  Same summation order as cg_spmv with the same LPR.
+template <typename TM, typename TV, int LPR, int E, int R, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB)
+cg_spmv_batched(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, const TM* __restrict__ val,
+                const TV* __restrict__ p, TV* __restrict__ q, const uint8_t* __restrict__ fixed, double* red,
+                Scalars* sc) {
+  if (sc->done) return;
+  constexpr int RPB = kThreads / LPR;  // rows per block for each of the R row slots
+  const int sub = threadIdx.x % LPR, grp = threadIdx.x / LPR;
+  const int stride = gridDim.x * RPB * R;
+  TV dot = TV(0);
+  int k0[R], k1[R];
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    const int row = blockIdx.x * RPB * R + j * RPB + grp;
+    k0[j] = row < n ? __ldg(rp + row) - 1 : 0;
+    k1[j] = row < n ? __ldg(rp + row + 1) - 1 : 0;
+  }
+  for (int base = blockIdx.x * RPB * R; base < n; base += stride) {
+    int nk0[R], nk1[R];
+    TM v[R][E];
+    int c[R][E];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int nrow = base + stride + j * RPB + grp;
+      nk0[j] = nrow < n ? __ldg(rp + nrow) - 1 : 0;
+      nk1[j] = nrow < n ? __ldg(rp + nrow + 1) - 1 : 0;
+#pragma unroll
+      for (int u = 0; u < E; ++u) {
+        const int k = k0[j] + sub + u * LPR;
+        v[j][u] = k < k1[j] ? ld_csr<LPR>(val + k) : TM(0);
+        c[j][u] = k < k1[j] ? ld_csr<LPR>(ci + k) : 0;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int row = base + j * RPB + grp;
+      TV s = TV(0);
+#pragma unroll
+      for (int u = 0; u < E; ++u)
+        if (c[j][u] > 0) s += (TV)v[j][u] * p[c[j][u] - 1];
+#pragma unroll 1
+      for (int k = k0[j] + sub + E * LPR; k < k1[j]; k += LPR) s += (TV)ld_csr<LPR>(val + k) * p[ld_csr<LPR>(ci + k) - 1];
+#pragma unroll
+      for (int o = LPR / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, LPR);
+      if (row < n && sub == 0) {
+        if (fixed && fixed[row]) s = TV(0);
+        q[row] = s;
+        dot += p[row] * s;
+      }
+      k0[j] = nk0[j];
+      k1[j] = nk1[j];
+    }
+  }
+  double b = block_sum(dot);
+  if (threadIdx.x == 0) red[blockIdx.x] = b;
+  if (last_block(&sc->ticket1)) {
+    double pq = ordered_sum(red, gridDim.x);
+    if (threadIdx.x == 0) {
+      sc->pq = pq;
+      sc->alpha = pq != 0.0 ? sc->rz / pq : 0.0;
+      if (!(pq > 0.0) || !isfinite(pq)) { sc->bad = 1; sc->done = 1; }
+      sc->ticket1 = 0;
+    }
+  }
+}
+
 // x += alpha p; r -= alpha q; z = dinv r; partial <r,z>, <r,r>; last block: beta, convergence.
 template <typename TX, typename TV>
 __global__ void __launch_bounds__(kThreads)
@@ -227,16 +297,39 @@ __global__ void norm2_kernel(int n, const double* __restrict__ v, double* red, S
   }
 }
 
-// lanes per row: FP64 rows use one thread each (the FP64 pipe is the bound); FP32 rows use few
-// lanes on short rows so several rows' loads are in flight per warp
+// SpMV form of the CG iterations.  Short rows (the trilinear hexahedron's 27-entry rows, tetrahedra)
+// take cg_spmv_batched: FP32 with 8 lanes a row and 4 entries a lane loaded at once (128^3 Laplace:
+// 105 us a product, 126 us for the per-row loop, 4-28 lanes a row and two rows a group measured
+// slower); FP64 with 2 lanes a row, 14 entries a lane and two rows a group (152 us, 216 us for one
+// thread a row with the per-row loop; the shuffle of the 2-lane sum is one FP64 add a row).
+// Longer FP32 rows keep the per-row loop with 16 or 32 lanes; longer FP64 rows one thread a row.
+constexpr int kSpmvShort32 = -1;
+constexpr int kSpmvShort64 = -2;
+
 int pick_lpr(double avg, bool fp64) {
-  if (fp64) return 1;
-  return avg >= 96 ? 32 : (avg >= 48 ? 16 : 8);
+  if (fp64) return avg <= 32 ? kSpmvShort64 : 1;
+  return avg < 48 ? kSpmvShort32 : (avg >= 96 ? 32 : 16);
 }
 
 template <typename TM, typename TV>
 void launch_spmv(int lpr, int grid, cudaStream_t s, int n, const int32_t* rp, const int32_t* ci, const TM* val,
                  const TV* p, TV* q, const uint8_t* fixed, double* red, Scalars* sc) {
+  // the batched kernels' register bounds guarantee MINB resident blocks an SM: their grids are
+  // whole waves
+  if constexpr (std::is_same<TM, float>::value && std::is_same<TV, float>::value) {
+    if (lpr == kSpmvShort32) {
+      const int g = std::min(grid, 8 * gfe::sm_count());
+      cg_spmv_batched<TM, TV, 8, 4, 1, 8><<<g, kThreads, 0, s>>>(n, rp, ci, val, p, q, fixed, red, sc);
+      return;
+    }
+  }
+  if constexpr (std::is_same<TM, double>::value && std::is_same<TV, double>::value) {
+    if (lpr == kSpmvShort64) {
+      const int g = std::min(grid, 4 * gfe::sm_count());
+      cg_spmv_batched<TM, TV, 2, 14, 2, 4><<<g, kThreads, 0, s>>>(n, rp, ci, val, p, q, fixed, red, sc);
+      return;
+    }
+  }
   if (lpr == 32) cg_spmv<TM, TV, 32><<<grid, kThreads, 0, s>>>(n, rp, ci, val, p, q, fixed, red, sc);
   else if (lpr == 16) cg_spmv<TM, TV, 16><<<grid, kThreads, 0, s>>>(n, rp, ci, val, p, q, fixed, red, sc);
   else if (lpr == 8) cg_spmv<TM, TV, 8><<<grid, kThreads, 0, s>>>(n, rp, ci, val, p, q, fixed, red, sc);
@@ -284,7 +377,7 @@ extern "C" int gfe_csr_spmv(int32_t n_rows, const int32_t* row_ptr, const int32_
   rc = gfe::scratch_alloc((void**)&red, sizeof(double) * grid, s, "spmv partials");
   if (rc) { gfe::scratch_free(sc, s); return rc; }
   cudaMemsetAsync(sc, 0, sizeof(Scalars), s);
-  launch_spmv<double, double>(1, grid, s, n_rows, row_ptr, col_idx, values, x, y, fixed, red, sc);
+  launch_spmv<double, double>(kSpmvShort64, grid, s, n_rows, row_ptr, col_idx, values, x, y, fixed, red, sc);
   gfe::scratch_free(red, s);
   gfe::scratch_free(sc, s);
   GFE_LAUNCH_CHECK("gfe_csr_spmv");
@@ -507,7 +600,7 @@ extern "C" int gfe_cg_steps(int32_t n, const int32_t* row_ptr, const int32_t* co
   if (int rc = cg_work_layout(n, workspace, &w)) return rc;
   cudaStream_t s = as_stream(stream);
   for (int i = 0; i < steps; ++i) {
-    launch_spmv<double, double>(1, w.grid, s, n, row_ptr, col_idx, values, w.p, w.q, fixed, w.red, w.sc);
+    launch_spmv<double, double>(kSpmvShort64, w.grid, s, n, row_ptr, col_idx, values, w.p, w.q, fixed, w.red, w.sc);
     cg_update<double, double><<<w.grid, kThreads, 0, s>>>(n, x, w.r, w.z, w.p, w.q, w.dinv, w.red, w.red2, w.sc);
     cg_direction<double><<<w.grid, kThreads, 0, s>>>(n, w.p, w.z, w.sc);
   }
@@ -549,6 +642,8 @@ struct MinresScalars {
   int done, pending, it, ticket1, ticket2, bad;
 };
 
+constexpr int kNodalBatch = 8;  // entries a lane loads at once in the MINRES products
+
 // (A): pending w / x update of the previous iteration, then q = A z / gamma (0 on fixed rows) and
 // delta = <q, z / gamma>.
 template <typename TM, typename TV, typename TX, int LPR>
@@ -577,8 +672,26 @@ minres_spmv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ c
       const bool valid = row < n;
       const int k0 = valid ? __ldg(rp + row) - 1 : 0, k1 = valid ? __ldg(rp + row + 1) - 1 : 0;
       TV acc = TV(0);
+      if constexpr (std::is_same<TV, double>::value) {
+        // FP64: bound by the FP64 pipe; the batched loads below cost it 3 % (32^3 Newton)
 #pragma unroll 4
-      for (int k = k0 + sub; k < k1; k += LPR) acc += (TV)ld_csr<LPR>(val + k) * z[ld_csr<LPR>(ci + k) - 1];
+        for (int k = k0 + sub; k < k1; k += LPR) acc += (TV)ld_csr<LPR>(val + k) * z[ld_csr<LPR>(ci + k) - 1];
+      } else {
+        // batches of kNodalBatch entries a lane, all loaded before the first gather
+        for (int t0 = k0 + sub; t0 < k1; t0 += kNodalBatch * LPR) {
+          TM v[kNodalBatch];
+          int c[kNodalBatch];
+#pragma unroll
+          for (int u = 0; u < kNodalBatch; ++u) {
+            const int k = t0 + u * LPR;
+            v[u] = k < k1 ? ld_csr<LPR>(val + k) : TM(0);
+            c[u] = k < k1 ? ld_csr<LPR>(ci + k) : 0;
+          }
+#pragma unroll
+          for (int u = 0; u < kNodalBatch; ++u)
+            if (c[u] > 0) acc += (TV)v[u] * z[c[u] - 1];
+        }
+      }
 #pragma unroll
       for (int o = LPR / 2; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o, LPR);
       if (valid && sub == 0) {
@@ -609,8 +722,10 @@ minres_spmv(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ c
 // takes one node: each column index and gathered z entry is loaded once for the NC rows, which
 // cuts the matrix traffic from 8 to 4 + 4 / NC bytes an entry in FP32.  Groups past n_node are the
 // remaining rows (the pressure rows of a u-p system), one each.
+constexpr int kNodalBlocks = 4;  // resident blocks an SM the register bound guarantees
+
 template <typename TM, typename TV, typename TX, int LPR, int NC>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kNodalBlocks)
 minres_spmv_nodal(int n, int n_node, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                   const TM* __restrict__ val, const TV* __restrict__ z, TV* __restrict__ q,
                   const uint8_t* __restrict__ fixed, const TV* __restrict__ zprev, TV* __restrict__ wold,
@@ -646,11 +761,26 @@ minres_spmv_nodal(int n, int n_node, const int32_t* __restrict__ rp, const int32
 #pragma unroll
       for (int j = 0; j < NC; ++j) acc[j] = TV(0);
       if (multi) {
-#pragma unroll 2
-        for (int t = sub; t < len; t += LPR) {
-          const TV zc = z[ld_csr<LPR>(ci + k0[0] + t) - 1];
+        // batches of kNodalBatch columns a lane: all their column indices and NC values are loaded
+        // before the first gather, so a lane keeps (1 + NC) kNodalBatch loads in flight
+        for (int t0 = sub; t0 < len; t0 += kNodalBatch * LPR) {
+          int c[kNodalBatch];
+          TM v[NC][kNodalBatch];
 #pragma unroll
-          for (int j = 0; j < NC; ++j) acc[j] += (TV)ld_csr<LPR>(val + k0[j] + t) * zc;
+          for (int u = 0; u < kNodalBatch; ++u) {
+            const int t = t0 + u * LPR;
+            c[u] = t < len ? ld_csr<LPR>(ci + k0[0] + t) : 0;
+#pragma unroll
+            for (int j = 0; j < NC; ++j) v[j][u] = t < len ? ld_csr<LPR>(val + k0[j] + t) : TM(0);
+          }
+#pragma unroll
+          for (int u = 0; u < kNodalBatch; ++u) {
+            if (c[u] > 0) {
+              const TV zc = z[c[u] - 1];
+#pragma unroll
+              for (int j = 0; j < NC; ++j) acc[j] += (TV)v[j][u] * zc;
+            }
+          }
         }
       } else {
 #pragma unroll 4
@@ -819,9 +949,9 @@ template <typename TM, typename TV, typename TX>
 void launch_minres_spmv(int lpr, int grid, cudaStream_t s, int n, const int32_t* rp, const int32_t* ci,
                         const TM* val, const TV* z, TV* q, const uint8_t* fixed, const TV* zprev, TV* wold,
                         const TV* wnew, TX* x, double* red, MinresScalars* sc, NodalRows nodal) {
-#define GFE_MINRES_NODAL(L, C)                                                                                \
-  minres_spmv_nodal<TM, TV, TX, L, C><<<grid, kThreads, 0, s>>>(n, nodal.n_node, rp, ci, val, z, q, fixed, zprev, \
-                                                                wold, wnew, x, red, sc)
+#define GFE_MINRES_NODAL(L, C)                                                                                 \
+  minres_spmv_nodal<TM, TV, TX, L, C><<<std::min(grid, kNodalBlocks * gfe::sm_count()), kThreads, 0, s>>>(         \
+      n, nodal.n_node, rp, ci, val, z, q, fixed, zprev, wold, wnew, x, red, sc)
   if constexpr (std::is_same<TV, float>::value) {
    if (nodal.n_node > 0) {
     if (nodal.nc == 3) {
