@@ -620,7 +620,7 @@ constexpr int kGatherWarps = 8;
 constexpr int kGatherStage = 32 * 27;  // entries of 32 rows at most
 
 template <typename T>
-__global__ void __launch_bounds__(kGatherWarps * 32)
+__global__ void __launch_bounds__(kGatherWarps * 32, 4)
 laplace_gather_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ Kel, const int32_t* __restrict__ rp,
                       double* __restrict__ values, float* __restrict__ values32, double* __restrict__ rhs,
                       int32_t l0, int32_t l1) {
@@ -639,45 +639,52 @@ laplace_gather_kernel(int32_t nx, int32_t ny, int32_t nz, const T* __restrict__ 
     const long long pos_end = (long long)__ldg(rp + (base + 32 < r_end ? base + 32 : r_end)) - 1;
     if (active) {
       const int ni = (int)(r % NX), nj = (int)((r / NX) % NY), k = (int)(r / NXY);
-      A acc[27];
-#pragma unroll
-      for (int t = 0; t < 27; ++t) acc[t] = from_double<A>(0.0);
-#pragma unroll
-      for (int c = 0; c < 2; ++c) {
-        const int ez = k - 1 + c;
-        if (ez < 0 || ez >= nz) continue;
-#pragma unroll
-        for (int b = 0; b < 2; ++b) {
-          const int ey2 = nj - 1 + b;
-          if (ey2 < 0 || ey2 >= ny) continue;
-#pragma unroll
-          for (int a = 0; a < 2; ++a) {
-            const int ex2 = ni - 1 + a;
-            if (ex2 < 0 || ex2 >= nx) continue;
-            const long long e = ex2 + ey2 * (long long)nx + ez * EXY;
-            const int li = (1 - a) + 2 * (1 - b) + 4 * (1 - c);
-#pragma unroll
-            for (int lj = 0; lj < 8; ++lj) {
-              const int di = a - 1 + (lj & 1), dj = b - 1 + ((lj >> 1) & 1), dk = c - 1 + (lj >> 2);
-              const int m = li < lj ? li : lj, n = li < lj ? lj : li;
-              const int t = (dk + 1) * 9 + (dj + 1) * 3 + (di + 1);
-              acc[t] = acc_add(acc[t], load_coord(Kel + tri(m, n) * E + e));
-            }
-          }
-        }
-      }
-      // the row, clipped to the mesh, in ascending column order, staged at its offset in the range
       int o = (int)((long long)__ldg(rp + r) - 1 - pos0);
+      // one column layer dk of the row at a time (9 accumulators live instead of 27): the element
+      // layer ez = k - 1 + c adds its local columns lj < 4 to layer dk = c - 1 and lj >= 4 to
+      // dk = c, so every entry is loaded once and each sum keeps the order c, b, a
 #pragma unroll
       for (int dk = -1; dk <= 1; ++dk) {
         if (k + dk < 0 || k + dk >= NZ) continue;
+        A acc[9];
+#pragma unroll
+        for (int t = 0; t < 9; ++t) acc[t] = from_double<A>(0.0);
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const int hi = dk - c + 1;  // which half of the element's local columns
+          if (hi < 0 || hi > 1) continue;
+          const int ez = k - 1 + c;
+          if (ez < 0 || ez >= nz) continue;
+#pragma unroll
+          for (int b = 0; b < 2; ++b) {
+            const int ey2 = nj - 1 + b;
+            if (ey2 < 0 || ey2 >= ny) continue;
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+              const int ex2 = ni - 1 + a;
+              if (ex2 < 0 || ex2 >= nx) continue;
+              const long long e = ex2 + ey2 * (long long)nx + ez * EXY;
+              const int li = (1 - a) + 2 * (1 - b) + 4 * (1 - c);
+#pragma unroll
+              for (int l4 = 0; l4 < 4; ++l4) {
+                const int lj = hi * 4 + l4;
+                const int di = a - 1 + (lj & 1), dj = b - 1 + ((lj >> 1) & 1);
+                const int m = li < lj ? li : lj, n = li < lj ? lj : li;
+                const int t = (dj + 1) * 3 + (di + 1);
+                acc[t] = acc_add(acc[t], load_coord(Kel + tri(m, n) * E + e));
+              }
+            }
+          }
+        }
+        // this layer of the row, clipped to the mesh, in ascending column order, staged at its
+        // offset in the range
 #pragma unroll
         for (int dj = -1; dj <= 1; ++dj) {
           if (nj + dj < 0 || nj + dj >= NY) continue;
 #pragma unroll
           for (int di = -1; di <= 1; ++di) {
             if (ni + di < 0 || ni + di >= NX) continue;
-            stage[o++] = acc[(dk + 1) * 9 + (dj + 1) * 3 + (di + 1)];
+            stage[o++] = acc[(dj + 1) * 3 + (di + 1)];
           }
         }
       }
