@@ -559,19 +559,31 @@ __global__ void mr_incidence_sort(int32_t n_nodes, const int32_t* __restrict__ c
   }
 }
 
+// The double with the value of f, formed with integer operations (GB300's FP64 pipe, which also
+// converts, issues a warp instruction every 64 cycles); subnormal floats take the conversion.
+__device__ __forceinline__ double widen_bits(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t ex = (u >> 23) & 0xffu, man = u & 0x7fffffu;
+  if (ex == 0u && man != 0u) return (double)f;
+  const uint64_t e64 = ex == 0u ? 0ull : (ex == 0xffu ? 0x7ffull : (uint64_t)(ex + 896u));
+  return __longlong_as_double((long long)(((uint64_t)(u >> 31) << 63) | (e64 << 52) | ((uint64_t)man << 29)));
+}
+
 // One warp per CSR row: values[row] = sum over the elements around the row's node of their element
 // rows, through the slot map (element number order).  Rows of displacement component mh take local
 // row mh * 27 + node index; pressure rows local row 81 + corner index.  The pressure-pressure block
 // is not assembled (zero in Iron's matrix).  Every entry of every row is written, so the values
-// need no zeroing first.
+// need no zeroing first.  FP32 element matrices are summed in FP32 (at most 8 terms an entry,
+// against the 5e-6 of their own contraction) and widened exactly with integer operations: the FP64
+// additions and conversions kept the FP64 pipe 77 % busy and bounded the kernel.
 template <typename TS>
 __global__ void __launch_bounds__(kRowWarps * 32)
 mr_row_gather_kernel(int32_t nq2, int32_t nlin, const int32_t* __restrict__ cnt, const int32_t* __restrict__ list,
                      const TS* __restrict__ Kel, const int32_t* __restrict__ slots, const int32_t* __restrict__ rp,
                      double* __restrict__ values, float* __restrict__ values32, unsigned* err) {
-  __shared__ double buf[kRowWarps][kMaxRowLen];
+  __shared__ TS buf[kRowWarps][kMaxRowLen];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  double* B = buf[w];
+  TS* B = buf[w];
   const long long n_rows = 3ll * nq2 + nlin;
   for (long long row = (long long)blockIdx.x * kRowWarps + w; row < n_rows; row += (long long)gridDim.x * kRowWarps) {
     int node, mh;
@@ -588,7 +600,7 @@ mr_row_gather_kernel(int32_t nq2, int32_t nlin, const int32_t* __restrict__ cnt,
       if (lane == 0) gfe_raise(err, GFE_DEVERR_SLOT);
       continue;
     }
-    for (int j = lane; j < len; j += 32) B[j] = 0.0;
+    for (int j = lane; j < len; j += 32) B[j] = TS(0);
     __syncwarp();
     const int m = min(__ldg(cnt + node), kMaxInc);
     const int32_t* L = list + (size_t)node * kMaxInc;
@@ -621,15 +633,16 @@ mr_row_gather_kernel(int32_t nq2, int32_t nlin, const int32_t* __restrict__ cnt,
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           const long long o = (long long)pos[u][j] - r0;
-          if (pos[u][j] >= 0 && o >= 0 && o < len) B[o] += (double)val[u][j];
+          if (pos[u][j] >= 0 && o >= 0 && o < len) B[o] += val[u][j];
           else if (pos[u][j] != -2) gfe_raise(err, GFE_DEVERR_SLOT);
         }
         __syncwarp();  // the next element may add to the same entries
       }
     }
     for (int j = lane; j < len; j += 32) {
-      const double v = B[j];
-      values[r0 + j] = v;
+      const TS v = B[j];
+      if constexpr (std::is_same<TS, float>::value) values[r0 + j] = widen_bits(v);
+      else values[r0 + j] = v;
       if (values32) values32[r0 + j] = (float)v;
     }
     __syncwarp();

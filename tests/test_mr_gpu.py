@@ -128,13 +128,16 @@ def test_tensor_core_assembly_matches_fp64(gfe_cuda, precision, tol):
         ref = getattr(A, fn)(dep, [C1, C2], precision="fp64").clone()
         got = getattr(A, fn)(dep, [C1, C2], precision=precision).cpu().numpy()
         assert np.abs(got - ref.cpu().numpy()).max() <= tol * ref.abs().max().item(), fn
-        # the row gather sums exactly the element matrices of this precision
+        # the row gather sums exactly the FP32 element matrices of this precision: in FP32, in
+        # ascending element order (np.add.at takes the entries element by element), widened to FP64
         K = getattr(A, dense)(dep, [C1, C2], precision=precision).cpu().numpy().reshape(A.n_elements, -1)
         keep = slots >= 0
         keep &= ~((np.arange(89 * 89) // 89 >= 81) & (np.arange(89 * 89) % 89 >= 81))[None, :]
-        v = np.zeros(A.nnz)
-        np.add.at(v, slots[keep], K[keep])
-        assert np.abs(got - v).max() <= 1e-14 * np.abs(v).max(), fn
+        K32 = K[keep].astype(np.float32)
+        assert np.array_equal(K32.astype(np.float64), K[keep]), fn
+        v = np.zeros(A.nnz, np.float32)
+        np.add.at(v, slots[keep], K32)
+        assert np.array_equal(got, v.astype(np.float64)), fn
 
 
 @pytest.mark.parametrize("ne", [(1, 1, 1), (2, 3, 1), (3, 2, 4), (5, 1, 2)])
