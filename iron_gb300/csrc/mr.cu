@@ -559,23 +559,14 @@ __global__ void mr_incidence_sort(int32_t n_nodes, const int32_t* __restrict__ c
   }
 }
 
-// The double with the value of f, formed with integer operations (GB300's FP64 pipe, which also
-// converts, issues a warp instruction every 64 cycles); subnormal floats take the conversion.
-__device__ __forceinline__ double widen_bits(float f) {
-  const uint32_t u = __float_as_uint(f);
-  const uint32_t ex = (u >> 23) & 0xffu, man = u & 0x7fffffu;
-  if (ex == 0u && man != 0u) return (double)f;
-  const uint64_t e64 = ex == 0u ? 0ull : (ex == 0xffu ? 0x7ffull : (uint64_t)(ex + 896u));
-  return __longlong_as_double((long long)(((uint64_t)(u >> 31) << 63) | (e64 << 52) | ((uint64_t)man << 29)));
-}
-
 // One warp per CSR row: values[row] = sum over the elements around the row's node of their element
 // rows, through the slot map (element number order).  Rows of displacement component mh take local
 // row mh * 27 + node index; pressure rows local row 81 + corner index.  The pressure-pressure block
 // is not assembled (zero in Iron's matrix).  Every entry of every row is written, so the values
 // need no zeroing first.  FP32 element matrices are summed in FP32 (at most 8 terms an entry,
-// against the 5e-6 of their own contraction) and widened exactly with integer operations: the FP64
-// additions and conversions kept the FP64 pipe 77 % busy and bounded the kernel.
+// against the 5e-6 of their own contraction) and widened exactly with integer operations
+// (f32_to_f64_exact): the FP64 additions and conversions kept the FP64 pipe 77 % busy and bounded
+// the kernel.
 template <typename TS>
 __global__ void __launch_bounds__(kRowWarps * 32)
 mr_row_gather_kernel(int32_t nq2, int32_t nlin, const int32_t* __restrict__ cnt, const int32_t* __restrict__ list,
@@ -641,7 +632,7 @@ mr_row_gather_kernel(int32_t nq2, int32_t nlin, const int32_t* __restrict__ cnt,
     }
     for (int j = lane; j < len; j += 32) {
       const TS v = B[j];
-      if constexpr (std::is_same<TS, float>::value) values[r0 + j] = widen_bits(v);
+      if constexpr (std::is_same<TS, float>::value) values[r0 + j] = f32_to_f64_exact(v);
       else values[r0 + j] = v;
       if (values32) values32[r0 + j] = (float)v;
     }
