@@ -843,13 +843,15 @@ minres_lanczos(int n, const TV* __restrict__ q, const TV* __restrict__ vcur, TV*
                const TV* __restrict__ minv, TV* __restrict__ znew, double* red, MinresScalars* sc) {
   if (sc->done) return;
   const TV a = (TV)(sc->delta / sc->gamma), b = (TV)(sc->gamma / sc->gamma_old);
-  double acc = 0.0;
+  // partials in the vector type (FP32 for the inner solves: no FP64 conversions per entry), warp
+  // totals and the grid sum in FP64
+  TV acc = TV(0);
   for (int i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
     const TV vn = q[i] - a * vcur[i] - b * vold[i];
     vold[i] = vn;
     const TV zn = minv[i] * vn;
     znew[i] = zn;
-    acc += (double)zn * (double)vn;
+    acc += zn * vn;
   }
   const double bs = block_sum(acc);
   if (threadIdx.x == 0) red[blockIdx.x] = bs;
