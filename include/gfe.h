@@ -458,10 +458,11 @@ int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* col_idx, cons
  * live in one static device array of the library sized for GFE_NOALLOC_MAX_ROWS rows (about
  * 24 MiB), held by every GPU that loads the library until the process exits; larger systems are
  * rejected with GFE_ERR_ARG.  The first call on a device looks up the array's device address
- * (set-up, once per device); make that first call before any stream capture.  All calls share
- * the one array and it keeps the last call's contents (each call clears what must start at zero):
- * calls that overlap on the GPU, from any stream or thread, race and must not be issued.
- * Synchronises `stream`.  Arguments and solution as gfe_cg_solve with precision GFE_FP64, with one
+ * (set-up, once per device).  All calls share the one array and it keeps the last call's contents
+ * (each call clears what must start at zero): calls that overlap on the GPU, from any stream or
+ * thread, race and must not be issued.  Synchronises `stream` (it reads scalars back between
+ * iterations), so it cannot be captured into a CUDA graph: gfe_cg_begin / gfe_cg_steps are the
+ * capturable form.  Arguments and solution as gfe_cg_solve with precision GFE_FP64, with one
  * difference in error reporting: a zero or non-finite diagonal entry on a free row, which
  * gfe_cg_solve raises as GFE_DEVERR_NONFINITE on the device error word, is returned here as
  * GFE_ERR_NUMERIC (this entry point uses no library error word). */
