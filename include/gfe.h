@@ -43,7 +43,8 @@ extern "C" {
 #define GFE_FP64 0  /* plain: element arithmetic and storage in FP64 */
 #define GFE_MIXED 1 /* FP32 element arithmetic, FP64 accumulation */
 #define GFE_MIXED_DF 2 /* float-float element arithmetic on the FP32 pipes (~48-bit), FP64 accumulation */
-#define GFE_TC_TF32X3 3 /* MR Jacobian: tensor-core (tcgen05) TF32 contraction, 3-pass split (~FP32 accuracy) */
+#define GFE_TC_TF32X3 3 /* MR Jacobian, hexahedral gfe_laplace_assemble_tp: tensor-core (tcgen05) TF32
+                           contraction, 3-pass split (~FP32 accuracy) */
 #define GFE_TC_TF32 4   /* MR Jacobian: tensor-core (tcgen05) TF32 contraction, one pass (~1e-3 relative) */
 
 /* ---- library -------------------------------------------------------------------------- */
@@ -334,8 +335,11 @@ int gfe_laplace_assemble_regular_host(int32_t nx, int32_t ny, int32_t nz, const 
  *             (src/Laplace_equations_routines.F90:555-579); NULL = unscaled
  *  colouring and CSR as for gfe_laplace_assemble
  *  values32 (optional) FP32 copy of the assembled values
- * precision GFE_FP64, GFE_MIXED (FP32 element arithmetic) or GFE_MIXED_DF (float-float).  The
- * matrix and rhs are zeroed first; each pair of element nodes is added through Iron's CSR search.
+ * precision GFE_FP64, GFE_MIXED (FP32 element arithmetic), GFE_MIXED_DF (float-float) or, for
+ * hexahedral bases, GFE_TC_TF32X3: the contraction K(m,n) = sum_g dphi_m^T M_g dphi_n as an
+ * M = 128 tcgen05 product (FP32 metrics, TF32 head / tail operands, FP32 accumulation in tensor
+ * memory; about FP32 accuracy).  The matrix and rhs are zeroed first; each pair of element nodes
+ * is added through Iron's CSR search.
  * Asynchronous; device-side failures are reported through gfe_device_errors(). */
 int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_gauss, int32_t n_elem, int32_t n_nodes,
                             const int32_t* elem_nodes, const double* coords, const double* scale, const double* kappa,

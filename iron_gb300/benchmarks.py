@@ -230,7 +230,8 @@ def bench_laplace_bases(args, log, clock_sampler, cpu_fn=None):
             in_bytes = E * (nns * 4 + 8) + ndof * (3 * 8 + 8) + (E * nns * 8 if scale is not None else 0)
             res = {}
             v64 = None
-            for prec in ("fp64", "mixed_df", "mixed"):
+            precs = ("fp64", "mixed_df", "mixed") + (() if kind.startswith("tet") else ("tf32x3",))
+            for prec in precs:
                 ms = _events_time(lambda: A.assemble(prec, check=False), args.steps, args.warmup, stream)
                 A.assemble(prec)
                 if prec == "fp64":
@@ -249,6 +250,9 @@ def bench_laplace_bases(args, log, clock_sampler, cpu_fn=None):
                     res[prec]["fp64_pipe_frac"] = flop / (ms * 1e-3) / 1e9 / fp64_peak
                 else:
                     res[prec]["speedup_vs_fp64"] = res["fp64"]["ms"] / ms
+                if prec == "tf32x3":
+                    # the contraction K = C B on the tensor cores: 2 nen (3 points) nen flops an element
+                    res[prec]["tensor_gflops"] = 2.0 * E * nns * 3 * pts * nns * 3 / (ms * 1e-3) / 1e9
             del v64
             cpu = None
             if cpu_fn is not None:

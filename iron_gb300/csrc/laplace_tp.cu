@@ -29,6 +29,7 @@
 
 #include "df.cuh"
 #include "gfe_internal.cuh"
+#include "tcgen05.cuh"
 
 namespace {
 
@@ -533,6 +534,224 @@ laplace_tet4_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Tensor-core (tcgen05, TF32 x 3) element matrices of tensor-product hexahedra
+// ---------------------------------------------------------------------------------------------
+// Per element K(m, n) = sum_{g,i} C[n][(g,i)] dphi_g(i, m), C[n][(g,i)] = sum_j M_g(i, j) dphi_g(j, n),
+// with M_g = GU Jacobian w kappa the symmetric Gauss-point metric of laplace_tp_kernel.  A tile stacks
+// EPT = 128 / R elements (R = 32 rows for up to 32 nodes, 64 for up to 64), so one M = 128 product
+// serves EPT elements: A = the stacked C, formed on the CUDA cores in FP32 and split into a TF32 head
+// and tail; B[m][(g,i)] = dphi_g(i, m), the basis table (constant, K-major); N = R.  K = 3 ng runs in
+// chunks of kTPKChunk columns through one A buffer and accumulates in tensor memory (three TF32
+// products a step, head x head + tail x head + head x tail: about FP32 accuracy).  The element pairs
+// m <= n take D[(e, n)][m] and are added at (m, n) and (n, m) through Iron's row search, colour by
+// colour, as in laplace_tp_kernel.
+constexpr int kTPTCThreads = 256;
+constexpr int kTPKChunk = 64;                   // K columns of A per chunk (8 steps of 8)
+constexpr int kTPKMax = 3 * kMaxNg;             // 192
+constexpr int kTPDRow = 65;                     // padded row of the staged product
+constexpr uint32_t kTPWaitPolls = 1u << 24;     // bounded mbarrier wait
+
+struct __align__(128) TPTCShared {
+  unsigned char B[2][kMaxNns * kTPKMax * 4];    // basis head, tail: [m][(g,i)], K-major core matrices
+  unsigned char A[2][128 * kTPKChunk * 4];      // C head, tail of the current K chunk; then the product
+  float sx[4][3][kMaxNns];
+  float sJ[4][kMaxNg][9];
+  float sM[4][kMaxNg][6];
+  double ssf[4][kMaxNns];
+  int32_t snode[4][kMaxNns];
+  float kap[4];
+  uint64_t mbar;
+  uint32_t tmem;
+  int abort;
+};
+static_assert(sizeof(float) * 128 * kTPDRow <= sizeof(TPTCShared::A), "the product is staged in the A buffer");
+
+template <int R>
+__global__ void __launch_bounds__(kTPTCThreads, 1)
+laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, const int32_t* __restrict__ en,
+                     const double* __restrict__ coords, const double* __restrict__ scale,
+                     const double* __restrict__ kappa, const float* __restrict__ dphi, const float* __restrict__ wg,
+                     const int32_t* __restrict__ pairs, TPConfig cfg, const int32_t* __restrict__ rp,
+                     const int32_t* __restrict__ ci, double* __restrict__ values, unsigned* err) {
+  static_assert(R == 32 || R == 64, "32 or 64 rows an element");
+  constexpr int EPT = 128 / R;
+  extern __shared__ __align__(1024) unsigned char tpraw[];
+  TPTCShared& S = *reinterpret_cast<TPTCShared*>(tpraw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nns = cfg.nns, ng = cfg.ng, kd = 3 * ng;
+  const int KP = (kd + 7) & ~7, KCB = KP / 4;  // K padded to whole MMA steps; B's core columns
+  // B head / tail: row m, column (g, i) -> core matrix (m / 8, k / 4)
+  for (int t = tid; t < R * KP; t += blockDim.x) {
+    const int m = t / KP, k = t % KP;
+    const float v = (m < nns && k < kd) ? dphi[(size_t)k * nns + m] : 0.0f;  // dphi[(g*3+i)*nns + m]
+    const uint32_t off = (uint32_t)((((m >> 3) * KCB + (k >> 2)) * 8 + (m & 7)) * 16 + (k & 3) * 4);
+    const float hi = tc::to_tf32(v);
+    *reinterpret_cast<float*>(S.B[0] + off) = hi;
+    *reinterpret_cast<float*>(S.B[1] + off) = tc::to_tf32(v - hi);
+  }
+  if (warp == 0) tc::tmem_alloc(&S.tmem, R);
+  if (tid == 0) {
+    tc::mbar_init(&S.mbar, 1);
+    S.abort = 0;
+  }
+  tc::fence_proxy_async();  // B is read by the tensor cores
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = S.tmem;
+  constexpr uint32_t idesc = tc::idesc_tf32(128, R);
+  const uint32_t a_hi = tc::smem_u32(S.A[0]), a_lo = tc::smem_u32(S.A[1]);
+  const uint32_t b_hi = tc::smem_u32(S.B[0]), b_lo = tc::smem_u32(S.B[1]);
+  constexpr uint32_t kLbo = 128, kSboA = (kTPKChunk / 4) * 128;
+  const uint32_t sbo_b = (uint32_t)KCB * 128;
+  float (*D)[kTPDRow] = reinterpret_cast<float (*)[kTPDRow]>(S.A[0]);
+  uint32_t parity = 0;
+  bool bad = false, nonfinite = false;
+
+  const int tiles = (cnt + EPT - 1) / EPT;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int item0 = tile * EPT;
+    const int slots = min(EPT, cnt - item0);
+    // element data of the tile's slots (geometry scaled as FIELD_INTERPOLATION_PARAMETERS_ELEMENT_GET)
+    for (int t = tid; t < slots * nns; t += blockDim.x) {
+      const int k = t / nns, n = t % nns;
+      const int e = ce[item0 + k];
+      const int node = en[(size_t)e * nns + n];
+      S.snode[k][n] = node;
+      const double sf = scale ? scale[(size_t)e * nns + n] : 1.0;
+      S.ssf[k][n] = sf;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) S.sx[k][c][n] = (float)(coords[(size_t)c * n_nodes + node] * sf);
+    }
+    if (tid < slots) {
+      const double kv = kappa ? kappa[ce[item0 + tid]] : 1.0;
+      if (!isfinite(kv)) nonfinite = true;
+      S.kap[tid] = (float)kv;
+    }
+    __syncthreads();
+    for (int q = tid; q < slots * ng * 9; q += blockDim.x) {
+      const int k = q / (ng * 9), r = q % (ng * 9), g = r / 9, c = (r % 9) / 3, a = r % 3;
+      const float* dg = dphi + ((size_t)g * 3 + a) * nns;
+      float sacc = 0.0f;
+      for (int n = 0; n < nns; ++n) sacc += S.sx[k][c][n] * dg[n];
+      S.sJ[k][g][r % 9] = sacc;
+    }
+    __syncthreads();
+    for (int q = tid; q < slots * ng; q += blockDim.x) {
+      const int k = q / ng, g = q % ng;
+      float J[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int a = 0; a < 3; ++a) J[c][a] = S.sJ[k][g][c * 3 + a];
+      const float G00 = J[0][0] * J[0][0] + J[1][0] * J[1][0] + J[2][0] * J[2][0];
+      const float G11 = J[0][1] * J[0][1] + J[1][1] * J[1][1] + J[2][1] * J[2][1];
+      const float G22 = J[0][2] * J[0][2] + J[1][2] * J[1][2] + J[2][2] * J[2][2];
+      const float G01 = J[0][0] * J[0][1] + J[1][0] * J[1][1] + J[2][0] * J[2][1];
+      const float G02 = J[0][0] * J[0][2] + J[1][0] * J[1][2] + J[2][0] * J[2][2];
+      const float G12 = J[0][1] * J[0][2] + J[1][1] * J[1][2] + J[2][1] * J[2][2];
+      const float A00 = G11 * G22 - G12 * G12, A11 = G00 * G22 - G02 * G02, A22 = G00 * G11 - G01 * G01;
+      const float A01 = G02 * G12 - G01 * G22, A02 = G01 * G12 - G02 * G11, A12 = G01 * G02 - G00 * G12;
+      const float det = G00 * A00 + G01 * A01 + G02 * A02;
+      if (!(det > 0.0f)) bad = true;
+      const float sc = S.kap[k] * wg[g] * rsqrtf(det);
+      float* M = S.sM[k][g];
+      M[0] = A00 * sc; M[1] = A11 * sc; M[2] = A22 * sc; M[3] = A01 * sc; M[4] = A02 * sc; M[5] = A12 * sc;
+    }
+    __syncthreads();
+    // the product, one K chunk at a time: warp w forms the 8-row groups w and w + 8 of A, lane l its
+    // row 8 rg + l / 4 and the K column 4 kc + l % 4 of each core matrix (one 128-byte store a step)
+    for (int c0 = 0; c0 < KP; c0 += kTPKChunk) {
+      const int kcn = min(kTPKChunk, KP - c0) / 4;  // core columns of this chunk (even)
+      for (int rg = warp; rg < 16; rg += kTPTCThreads / 32) {
+        const int row = rg * 8 + (lane >> 2), k = row / R, n = row % R;
+        const bool live = k < slots && n < nns;
+        for (int kc = 0; kc < kcn; ++kc) {
+          const int kk = c0 + kc * 4 + (lane & 3);
+          float v = 0.0f;
+          if (live && kk < kd) {
+            const int g = kk / 3, i = kk - 3 * g;
+            const float* M = S.sM[k][g];
+            // M(i, j) in the packed order 00 11 22 01 02 12
+            const float mi0 = i == 0 ? M[0] : (i == 1 ? M[3] : M[4]);
+            const float mi1 = i == 0 ? M[3] : (i == 1 ? M[1] : M[5]);
+            const float mi2 = i == 0 ? M[4] : (i == 1 ? M[5] : M[2]);
+            const float* dg = dphi + (size_t)g * 3 * nns + n;
+            v = mi0 * dg[0] + mi1 * dg[nns] + mi2 * dg[2 * nns];
+          }
+          const float hi = tc::to_tf32(v);
+          const int off = (rg * (kTPKChunk / 4) + kc) * 128 + lane * 4;
+          *reinterpret_cast<float*>(S.A[0] + off) = hi;
+          *reinterpret_cast<float*>(S.A[1] + off) = tc::to_tf32(v - hi);
+        }
+      }
+      tc::fence_proxy_async();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+#pragma unroll 1
+        for (int st = 0; st < kcn / 2; ++st) {
+          const uint32_t ao = (uint32_t)(st * 256), bo = (uint32_t)((c0 / 8 + st) * 256);
+          const uint64_t ah = tc::smem_desc(a_hi + ao, kLbo, kSboA), al = tc::smem_desc(a_lo + ao, kLbo, kSboA);
+          const uint64_t bh = tc::smem_desc(b_hi + bo, kLbo, sbo_b), bl = tc::smem_desc(b_lo + bo, kLbo, sbo_b);
+          tc::mma_tf32(tmem, ah, bh, idesc, (c0 > 0 || st > 0) ? 1u : 0u);
+          tc::mma_tf32(tmem, al, bh, idesc, 1u);
+          tc::mma_tf32(tmem, ah, bl, idesc, 1u);
+        }
+        tc::commit(&S.mbar);
+        // A is rewritten by the next chunk: wait (bounded) for this chunk's products
+        if (!tc::mbar_wait(&S.mbar, parity, kTPWaitPolls)) {
+          // the MMAs may still be writing tensor memory: wait once more for their commit before
+          // anything releases it; if that also ends without it, the tensor memory stays allocated
+          gfe_raise(err, GFE_DEVERR_TIMEOUT);
+          const bool drained = tc::mbar_wait(&S.mbar, parity, kTPWaitPolls);
+          S.abort = drained ? 1 : 2;
+        }
+      }
+      parity ^= 1u;
+      __syncthreads();
+      tc::fence_after_sync();
+      if (S.abort) break;
+    }
+    if (S.abort) break;
+    // tensor memory -> staged product: warp w < 4 reads lanes 32 w .. 32 w + 31
+    if (warp < 4) {
+#pragma unroll
+      for (int c0 = 0; c0 < R; c0 += 32) {
+        float v[32];
+        tc::tmem_ld_32x32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) D[warp * 32 + lane][c0 + j] = v[j];
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    for (int t = tid; t < slots * cfg.npairs; t += blockDim.x) {
+      const int k = t / cfg.npairs;
+      const int32_t mn = pairs[t - k * cfg.npairs];
+      const int m = mn & 0xffff, n = mn >> 16;
+      double v = (double)D[k * R + n][m];
+      if (scale) v = v * S.ssf[k][m] * S.ssf[k][n];  // K(ms, ns) * SF(ms) * SF(ns)
+      const int rm = S.snode[k][m], rn = S.snode[k][n];
+      const long long pmn = csr_find(rp, ci, rm, rn + 1);
+      if (pmn < 0) gfe_raise(err, GFE_DEVERR_SLOT);
+      else values[pmn] += v;
+      if (m != n) {
+        const long long pnm = csr_find(rp, ci, rn, rm + 1);
+        if (pnm < 0) gfe_raise(err, GFE_DEVERR_SLOT);
+        else values[pnm] += v;
+      }
+    }
+    __syncthreads();  // the staged product and the element data are rewritten by the next tile
+  }
+  if (bad) gfe_raise(err, GFE_DEVERR_JACOBIAN);
+  if (nonfinite) gfe_raise(err, GFE_DEVERR_NONFINITE);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0 && S.abort < 2) tc::tmem_dealloc(tmem, R);
+}
+
 __global__ void values_to_fp32(const double* __restrict__ v, float* __restrict__ v32, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     v32[i] = (float)v[i];
@@ -571,6 +790,41 @@ int launch_tp(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, cons
   return GFE_OK;
 }
 
+// Tensor-core element matrices (GFE_TC_TF32X3) of hexahedral bases with up to 64 nodes and 64 Gauss
+// points, colour by colour; one CTA an SM (about 186 KB of shared memory).
+int launch_tp_tc(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, const int32_t* en, const double* coords,
+                 const double* scale, const double* kappa, const int32_t* color_elems, const int32_t* color_ptr_host,
+                 int32_t n_colors, const int32_t* rp, const int32_t* ci, double* values, cudaStream_t s,
+                 int* launches) {
+  const TPTables<float>* t = nullptr;
+  if (int rc = tp_tables<float>(order, ngauss, &t)) return rc;
+  const int nns = t->cfg.nns;
+  if (nns > kMaxNns || t->cfg.ng > kMaxNg)
+    return gfe::set_error(GFE_ERR_ARG, "gfe_laplace_assemble_tp: the tensor-core path takes up to %d nodes and %d "
+                          "Gauss points an element", kMaxNns, kMaxNg);
+  const size_t smem = sizeof(TPTCShared);
+  const void* k32 = (const void*)laplace_tp_tc_kernel<32>;
+  const void* k64 = (const void*)laplace_tp_tc_kernel<64>;
+  GFE_CUDA_TRY(cudaFuncSetAttribute(nns <= 32 ? k32 : k64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  unsigned* err = gfe::device_error_word();
+  const int ept = nns <= 32 ? 4 : 2;
+  for (int c = 0; c < n_colors; ++c) {
+    const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
+    if (cnt <= 0) continue;
+    const int grid = std::min((cnt + ept - 1) / ept, gfe::sm_count());
+    if (nns <= 32)
+      laplace_tp_tc_kernel<32><<<grid, kTPTCThreads, smem, s>>>(color_elems + c0, cnt, n_nodes, en, coords, scale,
+                                                                kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci,
+                                                                values, err);
+    else
+      laplace_tp_tc_kernel<64><<<grid, kTPTCThreads, smem, s>>>(color_elems + c0, cnt, n_nodes, en, coords, scale,
+                                                                kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci,
+                                                                values, err);
+    ++*launches;
+  }
+  return GFE_OK;
+}
+
 }  // namespace
 
 extern "C" int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_gauss, int32_t n_elem, int32_t n_nodes,
@@ -597,8 +851,10 @@ extern "C" int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_ga
     return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
   if (color_ptr_host && n_colors > 0 && (color_ptr_host[0] != 0 || color_ptr_host[n_colors] != n_elem))
     return gfe::set_error(GFE_ERR_ARG, "%s: colour offsets must run from 0 to n_elem", fn);
-  if (precision != GFE_FP64 && precision != GFE_MIXED && precision != GFE_MIXED_DF)
+  if (precision != GFE_FP64 && precision != GFE_MIXED && precision != GFE_MIXED_DF && precision != GFE_TC_TF32X3)
     return gfe::set_error(GFE_ERR_ARG, "%s: unknown precision %d", fn, precision);
+  if (precision == GFE_TC_TF32X3 && simplex)
+    return gfe::set_error(GFE_ERR_ARG, "%s: the tensor-core path covers hexahedral bases", fn);
   cudaStream_t s = gfe::as_stream(stream);
   GFE_CUDA_TRY(cudaMemsetAsync(values, 0, sizeof(double) * (size_t)nnz, s));
   if (rhs) GFE_CUDA_TRY(cudaMemsetAsync(rhs, 0, sizeof(double) * (size_t)n_nodes, s));
@@ -610,6 +866,9 @@ extern "C" int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_ga
   else if (precision == GFE_MIXED)
     rc = launch_tp<float>(order, n_gauss, n_nodes, elem_nodes, coords, scale, kappa, color_elems, color_ptr_host,
                           n_colors, row_ptr, col_idx, values, s, &launches);
+  else if (precision == GFE_TC_TF32X3)
+    rc = launch_tp_tc(order, n_gauss, n_nodes, elem_nodes, coords, scale, kappa, color_elems, color_ptr_host,
+                      n_colors, row_ptr, col_idx, values, s, &launches);
   else
     rc = launch_tp<f2>(order, n_gauss, n_nodes, elem_nodes, coords, scale, kappa, color_elems, color_ptr_host,
                        n_colors, row_ptr, col_idx, values, s, &launches);

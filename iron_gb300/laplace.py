@@ -18,9 +18,12 @@ from . import _lib
 from ._lib import GFE_FP64, GFE_MIXED, GfeError
 
 GFE_MIXED_DF = 2
+GFE_TC_TF32X3 = 3
 # fp64: FP64 element arithmetic; mixed: FP32 element arithmetic (about 1e-6 relative), FP64
-# accumulation; mixed_df: float-float element arithmetic on the FP32 pipes (FP64-level accuracy)
-PRECISIONS = {"fp64": GFE_FP64, "mixed": GFE_MIXED, "mixed_df": GFE_MIXED_DF}
+# accumulation; mixed_df: float-float element arithmetic on the FP32 pipes (FP64-level accuracy);
+# tf32x3 (hexahedral bases of the basis-generic path): the element contraction on the tensor cores
+# (tcgen05, three TF32 products, about FP32 accuracy)
+PRECISIONS = {"fp64": GFE_FP64, "mixed": GFE_MIXED, "mixed_df": GFE_MIXED_DF, "tf32x3": GFE_TC_TF32X3}
 
 
 def csr_structure(elem_dofs: torch.Tensor, n_dofs: int, stream=None):

@@ -2,7 +2,7 @@
 and on linear, quadratic and cubic tetrahedra with Gauss_Simplex orders 1..5
 against the oracle's restatement of Iron's basis-generic element routine: triquadratic and
 tricubic elements, anisotropic Gauss rules, trilinear elements with a non-default rule, FP64 /
-float-float / FP32 element arithmetic; the patch test u = x on curved (jittered) quadratic and
+float-float / FP32 element arithmetic and the tensor-core (tcgen05 TF32x3) contraction; the patch test u = x on curved (jittered) quadratic and
 cubic meshes, through Iron's reduced solve."""
 import numpy as np
 import pytest
@@ -24,7 +24,7 @@ def _problem(ne, order, seed):
 
 @pytest.mark.parametrize("order,n_gauss,ne", [(2, 3, (2, 2, 2)), (3, 4, (2, 1, 2)), (2, (3, 2, 4), (2, 2, 1)),
                                               (1, 3, (3, 2, 2)), (3, 2, (1, 2, 1))])
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed_df", 1e-12), ("mixed", 2e-5)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed_df", 1e-12), ("mixed", 2e-5), ("tf32x3", 2e-5)])
 def test_matches_oracle(gfe_cuda, order, n_gauss, ne, precision, tol):
     m, kap = _problem(ne, order, 1)
     A = LaplaceAssembly.from_regular_mesh(m, kappa=kap, n_gauss=n_gauss)
@@ -69,10 +69,14 @@ def test_rejects_unsupported_bases(gfe_cuda):
     m = M.RegularMesh((1, 1, 1), order=2)
     with pytest.raises(Exception, match="Gauss"):
         LaplaceAssembly.from_regular_mesh(m, n_gauss=5).assemble("fp64")
+    # the tensor-core contraction covers hexahedral bases only
+    tm = M.TetMesh((1, 1, 1), order=2)
+    with pytest.raises(Exception, match="hexahedral"):
+        LaplaceAssembly.from_tet_mesh(tm).assemble("tf32x3")
 
 
 @pytest.mark.parametrize("scaling", ["unit", "arc_length"])
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed_df", 1e-12), ("mixed", 2e-5)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("mixed_df", 1e-12), ("mixed", 2e-5), ("tf32x3", 2e-5)])
 def test_cubic_hermite_matches_oracle(gfe_cuda, scaling, precision, tol):
     hm = M.HermiteMesh((2, 2, 2), extent=(1.0, 0.8, 1.2), scaling=scaling)
     hm.jitter_interior(5)
