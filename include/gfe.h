@@ -334,6 +334,9 @@ int gfe_laplace_assemble_regular_host(int32_t nx, int32_t ny, int32_t nz, const 
  *             interpolated scaled and the element matrix is scaled as K(m,n) SF(m) SF(n)
  *             (src/Laplace_equations_routines.F90:555-579); NULL = unscaled
  *  colouring and CSR as for gfe_laplace_assemble
+ *  slots      optional [n_elem][nns][nns] CSR positions of the element entries from
+ *             gfe_laplace_tp_slot_map (the same positions Iron's search finds, computed once per
+ *             mesh); NULL = Iron's search per entry pair during the assembly
  *  values32 (optional) FP32 copy of the assembled values
  * precision GFE_FP64, GFE_MIXED (FP32 element arithmetic), GFE_MIXED_DF (float-float) or, for
  * hexahedral bases, GFE_TC_TF32X3: the contraction K(m,n) = sum_g dphi_m^T M_g dphi_n as an
@@ -344,8 +347,18 @@ int gfe_laplace_assemble_regular_host(int32_t nx, int32_t ny, int32_t nz, const 
 int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_gauss, int32_t n_elem, int32_t n_nodes,
                             const int32_t* elem_nodes, const double* coords, const double* scale, const double* kappa,
                             const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
-                            const int32_t* row_ptr, const int32_t* col_idx, int64_t nnz, double* values,
-                            float* values32, double* rhs, int32_t precision, void* stream);
+                            const int32_t* row_ptr, const int32_t* col_idx, int64_t nnz, const int32_t* slots,
+                            double* values, float* values32, double* rhs, int32_t precision, void* stream);
+
+/* Element slot map of a basis-generic mesh: slots[e][m][n] = the 0-based CSR position of the entry
+ * (row elem_nodes[e][m], column elem_nodes[e][n]) found by Iron's row search (bisection to a
+ * width of 10, then a linear scan: MATRIX_VALUES_ADD_DP2, src/matrix_vector.F90:3202-3240), or
+ * -1 where the structure lacks it (the assembly then raises GFE_DEVERR_SLOT).  nns <= 64;
+ * positions must fit int32 (nnz <= 2^31 - 1).  The map depends on the structure only: compute it
+ * once per mesh and pass it to every gfe_laplace_assemble_tp call; for 27- to 64-node elements the
+ * per-entry search otherwise dominates the assembly.  Asynchronous on `stream`. */
+int gfe_laplace_tp_slot_map(int32_t n_elem, int32_t nns, const int32_t* elem_nodes, const int32_t* row_ptr,
+                            const int32_t* col_idx, int64_t nnz, int32_t* slots, void* stream);
 
 /* Number of CSR rows/entries that differ from the clipped 27-point stencil of the regular mesh
  * (0 = the structure is the one gfe_laplace_assemble_regular writes).  Synchronises `stream`. */

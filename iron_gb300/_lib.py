@@ -80,7 +80,8 @@ SIGNATURES = {
     "gfe_laplace_assemble_regular_host": (C.c_int, [i32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, i32, vp, i32,
                                                     vp]),
     "gfe_laplace_assemble_tp": (C.c_int, [vp, vp, i32, i32, vp, vp, vp, vp, vp, vp, i32, vp, vp, C.c_int64, vp, vp,
-                                          vp, i32, vp]),
+                                          vp, vp, i32, vp]),
+    "gfe_laplace_tp_slot_map": (C.c_int, [i32, i32, vp, vp, vp, C.c_int64, vp, vp]),
     "gfe_laplace_regular_check": (C.c_int, [i32, i32, i32, vp, vp, C.POINTER(C.c_int64), vp]),
     "gfe_mr_regular_structure": (C.c_int, [i32, i32, i32, vp, vp, C.c_int64, C.POINTER(C.c_int64), vp]),
     "gfe_csr_spmv": (C.c_int, [i32, vp, vp, vp, vp, vp, vp, vp]),

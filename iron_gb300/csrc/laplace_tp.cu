@@ -323,6 +323,62 @@ __device__ __forceinline__ long long csr_find(const int32_t* __restrict__ rp, co
   return -1;
 }
 
+// CSR position of element entry (m, n): from the element slot map slots[e][m][n] when given (Iron's
+// search above, run once per mesh by gfe_laplace_tp_slot_map), else by the search itself.  The
+// search is a chain of dependent loads per entry; for 27- to 64-node elements it dominated the
+// assembly.
+__device__ __forceinline__ long long entry_pos(const int32_t* __restrict__ slots, int e, int nns, int m, int n,
+                                               const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                                               int row, int col1) {
+  if (slots) return (long long)__ldg(slots + ((size_t)e * nns + m) * nns + n);
+  return csr_find(rp, ci, row, col1);
+}
+
+// Element pairs a thread scatters at a time.  Their positions, then their CSR values, are loaded
+// before any value is written (the entries of one colour's elements are distinct), so a thread
+// keeps several loads in flight instead of one dependent position -> value -> store chain a pair.
+constexpr int kTPScatter = 4;
+
+// Pairs t = t0, t0 + stride, ... (below total): at(t, v, pmn, pnm) gives the value and its two CSR
+// positions (pnm = -2 for a diagonal pair, -1 for an absent entry).
+template <typename PairAt>
+__device__ __forceinline__ void scatter_batch(int t0, int stride, int total, PairAt at, double* __restrict__ values,
+                                              unsigned* err) {
+  long long pos[kTPScatter][2];
+  double v[kTPScatter];
+#pragma unroll
+  for (int u = 0; u < kTPScatter; ++u) {
+    const int t = t0 + u * stride;
+    pos[u][0] = pos[u][1] = -2;  // nothing to add
+    v[u] = 0.0;
+    if (t < total) at(t, v[u], pos[u][0], pos[u][1]);
+  }
+  double old[kTPScatter][2];
+#pragma unroll
+  for (int u = 0; u < kTPScatter; ++u)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) old[u][h] = pos[u][h] >= 0 ? values[pos[u][h]] : 0.0;
+#pragma unroll
+  for (int u = 0; u < kTPScatter; ++u)
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (pos[u][h] >= 0) values[pos[u][h]] = old[u][h] + v[u];
+      else if (pos[u][h] == -1) gfe_raise(err, GFE_DEVERR_SLOT);
+    }
+}
+
+__global__ void tp_slot_kernel(int32_t n_elem, int32_t nns, const int32_t* __restrict__ en,
+                               const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                               int32_t* __restrict__ slots) {
+  const long long per = (long long)nns * nns, total = (long long)n_elem * per;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const long long e = t / per;
+    const int r = (int)(t - e * per), m = r / nns, n = r % nns;
+    slots[t] = (int32_t)csr_find(rp, ci, en[e * nns + m], en[e * nns + n] + 1);
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ T tp_rsqrt(T a) {
   return rsqrt(a);
@@ -351,8 +407,8 @@ laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, 
                   const double* __restrict__ coords, const double* __restrict__ scale,
                   const double* __restrict__ kappa, const T* __restrict__ dphi,
                   const T* __restrict__ wg, const int32_t* __restrict__ pairs, TPConfig cfg,
-                  const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, double* __restrict__ values,
-                  unsigned* err) {
+                  const int32_t* __restrict__ rp, const int32_t* __restrict__ ci, const int32_t* __restrict__ slots,
+                  double* __restrict__ values, unsigned* err) {
   static_assert(GROUP == kTPThreads || GROUP == 32, "an element takes a block or a warp");
   constexpr int EPB = kTPThreads / GROUP;
   __shared__ T sx_all[EPB][3][MAXN];
@@ -435,12 +491,15 @@ laplace_tp_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, 
       finish(acc);
       double v = to_double(acc);
       if (scale) v = v * ssf[m] * ssf[n];  // K(ms, ns) * SF(ms) * SF(ns)
+      // (staging the pair values and scattering them in batches, as the tensor-core kernel does,
+      // was slower here: its shared array costs resident blocks, and the Gauss loop of the other
+      // warps already hides the scatter's latency)
       const int rm = snode[m], rn = snode[n];
-      const long long pmn = csr_find(rp, ci, rm, rn + 1);
+      const long long pmn = entry_pos(slots, e, nns, m, n, rp, ci, rm, rn + 1);
       if (pmn < 0) gfe_raise(err, GFE_DEVERR_SLOT);
       else values[pmn] += v;
       if (m != n) {
-        const long long pnm = csr_find(rp, ci, rn, rm + 1);
+        const long long pnm = entry_pos(slots, e, nns, n, m, rp, ci, rn, rm + 1);
         if (pnm < 0) gfe_raise(err, GFE_DEVERR_SLOT);
         else values[pnm] += v;
       }
@@ -560,6 +619,7 @@ struct __align__(128) TPTCShared {
   float sM[4][kMaxNg][6];
   double ssf[4][kMaxNns];
   int32_t snode[4][kMaxNns];
+  int32_t elem[4];
   float kap[4];
   uint64_t mbar;
   uint32_t tmem;
@@ -573,7 +633,8 @@ laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_node
                      const double* __restrict__ coords, const double* __restrict__ scale,
                      const double* __restrict__ kappa, const float* __restrict__ dphi, const float* __restrict__ wg,
                      const int32_t* __restrict__ pairs, TPConfig cfg, const int32_t* __restrict__ rp,
-                     const int32_t* __restrict__ ci, double* __restrict__ values, unsigned* err) {
+                     const int32_t* __restrict__ ci, const int32_t* __restrict__ slots, double* __restrict__ values,
+                     unsigned* err) {
   static_assert(R == 32 || R == 64, "32 or 64 rows an element");
   constexpr int EPT = 128 / R;
   extern __shared__ __align__(1024) unsigned char tpraw[];
@@ -612,9 +673,9 @@ laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_node
   const int tiles = (cnt + EPT - 1) / EPT;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const int item0 = tile * EPT;
-    const int slots = min(EPT, cnt - item0);
+    const int live_slots = min(EPT, cnt - item0);
     // element data of the tile's slots (geometry scaled as FIELD_INTERPOLATION_PARAMETERS_ELEMENT_GET)
-    for (int t = tid; t < slots * nns; t += blockDim.x) {
+    for (int t = tid; t < live_slots * nns; t += blockDim.x) {
       const int k = t / nns, n = t % nns;
       const int e = ce[item0 + k];
       const int node = en[(size_t)e * nns + n];
@@ -624,13 +685,14 @@ laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_node
 #pragma unroll
       for (int c = 0; c < 3; ++c) S.sx[k][c][n] = (float)(coords[(size_t)c * n_nodes + node] * sf);
     }
-    if (tid < slots) {
+    if (tid < live_slots) {
+      S.elem[tid] = ce[item0 + tid];
       const double kv = kappa ? kappa[ce[item0 + tid]] : 1.0;
       if (!isfinite(kv)) nonfinite = true;
       S.kap[tid] = (float)kv;
     }
     __syncthreads();
-    for (int q = tid; q < slots * ng * 9; q += blockDim.x) {
+    for (int q = tid; q < live_slots * ng * 9; q += blockDim.x) {
       const int k = q / (ng * 9), r = q % (ng * 9), g = r / 9, c = (r % 9) / 3, a = r % 3;
       const float* dg = dphi + ((size_t)g * 3 + a) * nns;
       float sacc = 0.0f;
@@ -638,7 +700,7 @@ laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_node
       S.sJ[k][g][r % 9] = sacc;
     }
     __syncthreads();
-    for (int q = tid; q < slots * ng; q += blockDim.x) {
+    for (int q = tid; q < live_slots * ng; q += blockDim.x) {
       const int k = q / ng, g = q % ng;
       float J[3][3];
 #pragma unroll
@@ -666,7 +728,7 @@ laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_node
       const int kcn = min(kTPKChunk, KP - c0) / 4;  // core columns of this chunk (even)
       for (int rg = warp; rg < 16; rg += kTPTCThreads / 32) {
         const int row = rg * 8 + (lane >> 2), k = row / R, n = row % R;
-        const bool live = k < slots && n < nns;
+        const bool live = k < live_slots && n < nns;
         for (int kc = 0; kc < kcn; ++kc) {
           const int kk = c0 + kc * 4 + (lane & 3);
           float v = 0.0f;
@@ -727,22 +789,18 @@ laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_node
     }
     tc::fence_before_sync();
     __syncthreads();
-    for (int t = tid; t < slots * cfg.npairs; t += blockDim.x) {
-      const int k = t / cfg.npairs;
-      const int32_t mn = pairs[t - k * cfg.npairs];
-      const int m = mn & 0xffff, n = mn >> 16;
-      double v = (double)D[k * R + n][m];
-      if (scale) v = v * S.ssf[k][m] * S.ssf[k][n];  // K(ms, ns) * SF(ms) * SF(ns)
-      const int rm = S.snode[k][m], rn = S.snode[k][n];
-      const long long pmn = csr_find(rp, ci, rm, rn + 1);
-      if (pmn < 0) gfe_raise(err, GFE_DEVERR_SLOT);
-      else values[pmn] += v;
-      if (m != n) {
-        const long long pnm = csr_find(rp, ci, rn, rm + 1);
-        if (pnm < 0) gfe_raise(err, GFE_DEVERR_SLOT);
-        else values[pnm] += v;
-      }
-    }
+    const int total = live_slots * cfg.npairs;
+    for (int t0 = tid; t0 < total; t0 += kTPScatter * blockDim.x)
+      scatter_batch(t0, blockDim.x, total, [&](int t, double& v, long long& pmn, long long& pnm) {
+        const int k = t / cfg.npairs;
+        const int32_t mn = pairs[t - k * cfg.npairs];
+        const int m = mn & 0xffff, n = mn >> 16;
+        v = (double)D[k * R + n][m];
+        if (scale) v = v * S.ssf[k][m] * S.ssf[k][n];  // K(ms, ns) * SF(ms) * SF(ns)
+        const int rm = S.snode[k][m], rn = S.snode[k][n];
+        pmn = entry_pos(slots, S.elem[k], nns, m, n, rp, ci, rm, rn + 1);
+        if (m != n) pnm = entry_pos(slots, S.elem[k], nns, n, m, rp, ci, rn, rm + 1);
+      }, values, err);
     __syncthreads();  // the staged product and the element data are rewritten by the next tile
   }
   if (bad) gfe_raise(err, GFE_DEVERR_JACOBIAN);
@@ -760,7 +818,8 @@ __global__ void values_to_fp32(const double* __restrict__ v, float* __restrict__
 template <typename T>
 int launch_tp(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, const int32_t* en, const double* coords,
               const double* scale, const double* kappa, const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
-              const int32_t* rp, const int32_t* ci, double* values, cudaStream_t s, int* launches) {
+              const int32_t* rp, const int32_t* ci, const int32_t* slots, double* values, cudaStream_t s,
+              int* launches) {
   const TPTables<T>* t = nullptr;
   if (int rc = tp_tables<T>(order, ngauss, &t)) return rc;
   unsigned* err = gfe::device_error_word();
@@ -777,13 +836,13 @@ int launch_tp(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, cons
       constexpr int EPB = kTPThreads / 32;
       const int grid = std::min((cnt + EPB - 1) / EPB, 8 * gfe::sm_count());
       laplace_tp_kernel<T, 32, kSmallNns, kSmallNg><<<grid, kTPThreads, 0, s>>>(
-          color_elems + c0, cnt, n_nodes, en, coords, scale, kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci, values,
-          err);
+          color_elems + c0, cnt, n_nodes, en, coords, scale, kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci, slots,
+          values, err);
     } else {
       const int grid = std::min(cnt, 8 * gfe::sm_count());
       laplace_tp_kernel<T, kTPThreads, kMaxNns, kMaxNg><<<grid, kTPThreads, 0, s>>>(
-          color_elems + c0, cnt, n_nodes, en, coords, scale, kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci, values,
-          err);
+          color_elems + c0, cnt, n_nodes, en, coords, scale, kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci, slots,
+          values, err);
     }
     ++*launches;
   }
@@ -794,8 +853,8 @@ int launch_tp(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, cons
 // points, colour by colour; one CTA an SM (about 186 KB of shared memory).
 int launch_tp_tc(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, const int32_t* en, const double* coords,
                  const double* scale, const double* kappa, const int32_t* color_elems, const int32_t* color_ptr_host,
-                 int32_t n_colors, const int32_t* rp, const int32_t* ci, double* values, cudaStream_t s,
-                 int* launches) {
+                 int32_t n_colors, const int32_t* rp, const int32_t* ci, const int32_t* slots, double* values,
+                 cudaStream_t s, int* launches) {
   const TPTables<float>* t = nullptr;
   if (int rc = tp_tables<float>(order, ngauss, &t)) return rc;
   const int nns = t->cfg.nns;
@@ -815,11 +874,11 @@ int launch_tp_tc(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, c
     if (nns <= 32)
       laplace_tp_tc_kernel<32><<<grid, kTPTCThreads, smem, s>>>(color_elems + c0, cnt, n_nodes, en, coords, scale,
                                                                 kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci,
-                                                                values, err);
+                                                                slots, values, err);
     else
       laplace_tp_tc_kernel<64><<<grid, kTPTCThreads, smem, s>>>(color_elems + c0, cnt, n_nodes, en, coords, scale,
                                                                 kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci,
-                                                                values, err);
+                                                                slots, values, err);
     ++*launches;
   }
   return GFE_OK;
@@ -827,12 +886,27 @@ int launch_tp_tc(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, c
 
 }  // namespace
 
+extern "C" int gfe_laplace_tp_slot_map(int32_t n_elem, int32_t nns, const int32_t* elem_nodes, const int32_t* row_ptr,
+                                       const int32_t* col_idx, int64_t nnz, int32_t* slots, void* stream) {
+  const char* fn = "gfe_laplace_tp_slot_map";
+  if (n_elem < 0 || nns <= 0 || nns > kMaxNns || (n_elem > 0 && (!elem_nodes || !row_ptr || !col_idx || !slots)))
+    return gfe::set_error(GFE_ERR_ARG, "%s: invalid arguments", fn);
+  if (nnz < 0 || nnz > INT32_MAX)
+    return gfe::set_error(GFE_ERR_ARG, "%s: CSR positions must fit in int32 (nnz %lld)", fn, (long long)nnz);
+  if (n_elem == 0) return GFE_OK;
+  cudaStream_t s = gfe::as_stream(stream);
+  tp_slot_kernel<<<16 * gfe::sm_count(), 256, 0, s>>>(n_elem, nns, elem_nodes, row_ptr, col_idx, slots);
+  GFE_LAUNCH_CHECK(fn);
+  return GFE_OK;
+}
+
 extern "C" int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_gauss, int32_t n_elem, int32_t n_nodes,
                                        const int32_t* elem_nodes, const double* coords, const double* scale,
                                        const double* kappa,
                                        const int32_t* color_elems, const int32_t* color_ptr_host, int32_t n_colors,
-                                       const int32_t* row_ptr, const int32_t* col_idx, int64_t nnz, double* values,
-                                       float* values32, double* rhs, int32_t precision, void* stream) {
+                                       const int32_t* row_ptr, const int32_t* col_idx, int64_t nnz,
+                                       const int32_t* slots, double* values, float* values32, double* rhs,
+                                       int32_t precision, void* stream) {
   const char* fn = "gfe_laplace_assemble_tp";
   if (!order || !n_gauss) return gfe::set_error(GFE_ERR_ARG, "%s: order and n_gauss are required", fn);
   const bool simplex = order[0] == 7 || order[0] == 8 || order[0] == 9;
@@ -862,16 +936,16 @@ extern "C" int gfe_laplace_assemble_tp(const int32_t* order, const int32_t* n_ga
   int launches = 0, rc;
   if (precision == GFE_FP64)
     rc = launch_tp<double>(order, n_gauss, n_nodes, elem_nodes, coords, scale, kappa, color_elems, color_ptr_host,
-                           n_colors, row_ptr, col_idx, values, s, &launches);
+                           n_colors, row_ptr, col_idx, slots, values, s, &launches);
   else if (precision == GFE_MIXED)
     rc = launch_tp<float>(order, n_gauss, n_nodes, elem_nodes, coords, scale, kappa, color_elems, color_ptr_host,
-                          n_colors, row_ptr, col_idx, values, s, &launches);
+                          n_colors, row_ptr, col_idx, slots, values, s, &launches);
   else if (precision == GFE_TC_TF32X3)
     rc = launch_tp_tc(order, n_gauss, n_nodes, elem_nodes, coords, scale, kappa, color_elems, color_ptr_host,
-                      n_colors, row_ptr, col_idx, values, s, &launches);
+                      n_colors, row_ptr, col_idx, slots, values, s, &launches);
   else
     rc = launch_tp<f2>(order, n_gauss, n_nodes, elem_nodes, coords, scale, kappa, color_elems, color_ptr_host,
-                       n_colors, row_ptr, col_idx, values, s, &launches);
+                       n_colors, row_ptr, col_idx, slots, values, s, &launches);
   gfe::stage_end(GFE_STAGE_LAPLACE_ELEMENTS, prof, s, launches);
   if (rc) return rc;
   if (values32 && nnz > 0) values_to_fp32<<<4 * gfe::sm_count(), 256, 0, s>>>(values, values32, nnz);

@@ -64,10 +64,13 @@ class LaplaceAssembly:
     per DOF (positions and derivatives).
     Trilinear elements with 2x2x2 Gauss points use the sum-factorised kernels (and, on Iron's
     regular generated mesh, the row-owning one); every other basis uses gfe_laplace_assemble_tp.
+    slot_map: for the basis-generic path, compute the element slot map (the CSR position of every
+    element entry, gfe_laplace_tp_slot_map) once and pass it to every assembly instead of Iron's
+    per-entry row search; default for elements of 20 or more nodes (4 nns^2 bytes an element).
     """
 
     def __init__(self, elem_nodes, coords, kappa=None, colour_elems=None, colour_ptr=None, device=None,
-                 structure=None, order=1, n_gauss=None, scale=None):
+                 structure=None, order=1, n_gauss=None, scale=None, slot_map=None):
         dev = device if device is not None else _lib.require_cuda()
         _lib.load()
         self.device = torch.device(dev)
@@ -120,6 +123,9 @@ class LaplaceAssembly:
         self.rhs = torch.empty(self.n_nodes, dtype=torch.float64, device=self.device)
         self.regular = None  # (nx, ny, nz) when the mesh is Iron's trilinear regular generated mesh
         self.grid = None     # (nelem, order) of a regular generated mesh of any order
+        self.nns = nns
+        self._want_slots = (nns >= 20 if slot_map is None else bool(slot_map)) and self.nnz < 2 ** 31
+        self.tp_slots = None  # [E][nns][nns] CSR positions (basis-generic path), built on first use
 
     @classmethod
     def from_tet_mesh(cls, mesh, kappa=None, device=None, n_gauss=None):
@@ -135,10 +141,10 @@ class LaplaceAssembly:
                    order=4, n_gauss=n_gauss, scale=mesh.scale)
 
     @classmethod
-    def from_regular_mesh(cls, mesh, kappa=None, device=None, n_gauss=None):
+    def from_regular_mesh(cls, mesh, kappa=None, device=None, n_gauss=None, slot_map=None):
         order, ptr = mesh.colouring()
         obj = cls(mesh.elem_nodes, mesh.coords, kappa=kappa, colour_elems=order, colour_ptr=ptr, device=device,
-                  order=mesh.order, n_gauss=n_gauss)
+                  order=mesh.order, n_gauss=n_gauss, slot_map=slot_map)
         obj.grid = (tuple(mesh.nelem), mesh.order)
         if mesh.order == 1 and not obj.tensor_product:
             nx, ny, nz = mesh.nelem
@@ -163,13 +169,19 @@ class LaplaceAssembly:
         if self.tensor_product:
             if path == "regular":
                 raise GfeError(-1, "the regular-mesh kernel is trilinear with 2x2x2 Gauss points")
+            if self._want_slots and self.tp_slots is None and self.n_elements > 0:
+                self.tp_slots = torch.empty((self.n_elements, self.nns, self.nns), dtype=torch.int32,
+                                            device=self.device)
+                _lib.call("gfe_laplace_tp_slot_map", self.n_elements, self.nns, _lib.ptr(self.elem_nodes),
+                          _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx), self.nnz, _lib.ptr(self.tp_slots),
+                          _lib.stream_handle(stream))
             cp = self.colour_ptr
             _lib.call("gfe_laplace_assemble_tp", (C.c_int32 * 3)(*self.order), (C.c_int32 * 3)(*self.n_gauss),
                       self.n_elements, self.n_nodes, _lib.ptr(self.elem_nodes), _lib.ptr(self.coords),
                       _lib.ptr(self.scale), _lib.ptr(self.kappa), _lib.ptr(self.colour_elems),
                       cp.ctypes.data_as(C.c_void_p), len(cp) - 1,
-                      _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx), self.nnz, _lib.ptr(self.values), _lib.ptr(v32),
-                      _lib.ptr(self.rhs), prec, _lib.stream_handle(stream))
+                      _lib.ptr(self.row_ptr), _lib.ptr(self.col_idx), self.nnz, _lib.ptr(self.tp_slots),
+                      _lib.ptr(self.values), _lib.ptr(v32), _lib.ptr(self.rhs), prec, _lib.stream_handle(stream))
             if check:
                 _lib.raise_device_errors("gfe_laplace_assemble_tp", stream)
             return self.values

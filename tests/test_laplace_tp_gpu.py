@@ -41,6 +41,21 @@ def test_matches_oracle(gfe_cuda, order, n_gauss, ne, precision, tol):
         assert np.array_equal(A.values32.cpu().numpy(), vals.astype(np.float32))
 
 
+@pytest.mark.parametrize("order,n_gauss", [(2, 3), (3, 4), (3, 2)])
+@pytest.mark.parametrize("precision", ["fp64", "mixed_df", "tf32x3"])
+def test_slot_map_equals_search(gfe_cuda, order, n_gauss, precision):
+    """The element slot map holds the positions Iron's row search finds: assembling through it gives
+    bit-identical values to searching every entry during the assembly."""
+    m, kap = _problem((2, 3, 2), order, 3)
+    A = LaplaceAssembly.from_regular_mesh(m, kappa=kap, n_gauss=n_gauss, slot_map=True)
+    B = LaplaceAssembly.from_regular_mesh(m, kappa=kap, n_gauss=n_gauss, slot_map=False)
+    va = A.assemble(precision).clone()
+    vb = B.assemble(precision)
+    assert A.tp_slots is not None and B.tp_slots is None
+    assert int((A.tp_slots < 0).sum()) == 0
+    assert torch.equal(va, vb)
+
+
 @pytest.mark.parametrize("order", [2, 3])
 def test_patch_test_through_reduced_solve(gfe_cuda, order):
     """u = x is reproduced on interior-jittered (curved) quadratic elements, where 3-point Gauss
