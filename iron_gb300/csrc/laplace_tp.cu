@@ -605,7 +605,7 @@ laplace_tet4_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes
 // products a step, head x head + tail x head + head x tail: about FP32 accuracy).  The element pairs
 // m <= n take D[(e, n)][m] and are added at (m, n) and (n, m) through Iron's row search, colour by
 // colour, as in laplace_tp_kernel.
-constexpr int kTPTCThreads = 256;
+constexpr int kTPTCThreads = 512;                // 16 warps: every phase is load-latency bound
 constexpr int kTPKChunk = 64;                   // K columns of A per chunk (8 steps of 8)
 constexpr int kTPKMax = 3 * kMaxNg;             // 192
 constexpr int kTPDRow = 65;                     // padded row of the staged product
