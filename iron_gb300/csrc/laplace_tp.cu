@@ -601,34 +601,48 @@ laplace_tet4_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes
 // EPT = 128 / R elements (R = 32 rows for up to 32 nodes, 64 for up to 64), so one M = 128 product
 // serves EPT elements: A = the stacked C, formed on the CUDA cores in FP32 and split into a TF32 head
 // and tail; B[m][(g,i)] = dphi_g(i, m), the basis table (constant, K-major); N = R.  K = 3 ng runs in
-// chunks of kTPKChunk columns through one A buffer and accumulates in tensor memory (three TF32
-// products a step, head x head + tail x head + head x tail: about FP32 accuracy).  The element pairs
-// m <= n take D[(e, n)][m] and are added at (m, n) and (n, m) through Iron's row search, colour by
-// colour, as in laplace_tp_kernel.
-constexpr int kTPTCThreads = 512;                // 16 warps: every phase is load-latency bound
-constexpr int kTPKChunk = 64;                   // K columns of A per chunk (8 steps of 8)
+// chunks through one A buffer and accumulates in tensor memory (three TF32 products a step,
+// head x head + tail x head + head x tail: about FP32 accuracy).  The element pairs m <= n take
+// D[(e, n)][m] and are added at (m, n) and (n, m) through the slot map or Iron's row search, colour
+// by colour, as in laplace_tp_kernel.
 constexpr int kTPKMax = 3 * kMaxNg;             // 192
-constexpr int kTPDRow = 65;                     // padded row of the staged product
 constexpr uint32_t kTPWaitPolls = 1u << 24;     // bounded mbarrier wait
 
+// Shape of the kernel for R rows an element: elements of up to 64 nodes take one CTA of 512
+// threads an SM (16 warps: every phase is bound by load latency) and 64-column K chunks; elements
+// of up to 32 nodes take two CTAs of 256 threads an SM with 32-column chunks (about 100 KB of
+// shared memory each), so one CTA's barriers and MMA waits overlap the other's work.
+template <int R>
+struct TPTCShape {
+  static constexpr int kThreads = R == 64 ? 512 : 256;
+  static constexpr int kBlocksPerSM = R == 64 ? 1 : 2;
+  static constexpr int kKChunk = R == 64 ? 64 : 32;  // K columns of A per chunk
+  static constexpr int kEPT = 128 / R;               // elements a tile
+  static constexpr int kDRow = R + 1;                // padded row of the staged product
+};
+
+template <int R>
 struct __align__(128) TPTCShared {
-  unsigned char B[2][kMaxNns * kTPKMax * 4];    // basis head, tail: [m][(g,i)], K-major core matrices
-  unsigned char A[2][128 * kTPKChunk * 4];      // C head, tail of the current K chunk; then the product
-  float sx[4][3][kMaxNns];
-  float sJ[4][kMaxNg][9];
-  float sM[4][kMaxNg][6];
-  double ssf[4][kMaxNns];
-  int32_t snode[4][kMaxNns];
-  int32_t elem[4];
-  float kap[4];
+  using Sh = TPTCShape<R>;
+  unsigned char B[2][R * kTPKMax * 4];          // basis head, tail: [m][(g,i)], K-major core matrices
+  unsigned char A[2][128 * Sh::kKChunk * 4];    // C head, tail of the current K chunk; then the product
+  float sx[Sh::kEPT][3][R];
+  float sJ[Sh::kEPT][kMaxNg][9];
+  float sM[Sh::kEPT][kMaxNg][6];
+  double ssf[Sh::kEPT][R];
+  int32_t snode[Sh::kEPT][R];
+  int32_t elem[Sh::kEPT];
+  float kap[Sh::kEPT];
   uint64_t mbar;
   uint32_t tmem;
   int abort;
 };
-static_assert(sizeof(float) * 128 * kTPDRow <= sizeof(TPTCShared::A), "the product is staged in the A buffer");
+static_assert(sizeof(float) * 128 * TPTCShape<64>::kDRow <= sizeof(TPTCShared<64>::A), "product staged in A");
+static_assert(sizeof(float) * 128 * TPTCShape<32>::kDRow <= sizeof(TPTCShared<32>::A), "product staged in A");
+static_assert(2 * (sizeof(TPTCShared<32>) + 1024) <= 228 * 1024, "two CTAs an SM for up to 32 nodes");
 
 template <int R>
-__global__ void __launch_bounds__(kTPTCThreads, 1)
+__global__ void __launch_bounds__(TPTCShape<R>::kThreads, TPTCShape<R>::kBlocksPerSM)
 laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_nodes, const int32_t* __restrict__ en,
                      const double* __restrict__ coords, const double* __restrict__ scale,
                      const double* __restrict__ kappa, const float* __restrict__ dphi, const float* __restrict__ wg,
@@ -636,9 +650,10 @@ laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_node
                      const int32_t* __restrict__ ci, const int32_t* __restrict__ slots, double* __restrict__ values,
                      unsigned* err) {
   static_assert(R == 32 || R == 64, "32 or 64 rows an element");
-  constexpr int EPT = 128 / R;
+  using Sh = TPTCShape<R>;
+  constexpr int EPT = Sh::kEPT, KCH = Sh::kKChunk;
   extern __shared__ __align__(1024) unsigned char tpraw[];
-  TPTCShared& S = *reinterpret_cast<TPTCShared*>(tpraw);
+  TPTCShared<R>& S = *reinterpret_cast<TPTCShared<R>*>(tpraw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nns = cfg.nns, ng = cfg.ng, kd = 3 * ng;
   const int KP = (kd + 7) & ~7, KCB = KP / 4;  // K padded to whole MMA steps; B's core columns
@@ -664,9 +679,9 @@ laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_node
   constexpr uint32_t idesc = tc::idesc_tf32(128, R);
   const uint32_t a_hi = tc::smem_u32(S.A[0]), a_lo = tc::smem_u32(S.A[1]);
   const uint32_t b_hi = tc::smem_u32(S.B[0]), b_lo = tc::smem_u32(S.B[1]);
-  constexpr uint32_t kLbo = 128, kSboA = (kTPKChunk / 4) * 128;
+  constexpr uint32_t kLbo = 128, kSboA = (KCH / 4) * 128;
   const uint32_t sbo_b = (uint32_t)KCB * 128;
-  float (*D)[kTPDRow] = reinterpret_cast<float (*)[kTPDRow]>(S.A[0]);
+  float (*D)[Sh::kDRow] = reinterpret_cast<float (*)[Sh::kDRow]>(S.A[0]);
   uint32_t parity = 0;
   bool bad = false, nonfinite = false;
 
@@ -724,9 +739,9 @@ laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_node
     __syncthreads();
     // the product, one K chunk at a time: warp w forms the 8-row groups w and w + 8 of A, lane l its
     // row 8 rg + l / 4 and the K column 4 kc + l % 4 of each core matrix (one 128-byte store a step)
-    for (int c0 = 0; c0 < KP; c0 += kTPKChunk) {
-      const int kcn = min(kTPKChunk, KP - c0) / 4;  // core columns of this chunk (even)
-      for (int rg = warp; rg < 16; rg += kTPTCThreads / 32) {
+    for (int c0 = 0; c0 < KP; c0 += KCH) {
+      const int kcn = min(KCH, KP - c0) / 4;  // core columns of this chunk (even)
+      for (int rg = warp; rg < 16; rg += Sh::kThreads / 32) {
         const int row = rg * 8 + (lane >> 2), k = row / R, n = row % R;
         const bool live = k < live_slots && n < nns;
         for (int kc = 0; kc < kcn; ++kc) {
@@ -743,7 +758,7 @@ laplace_tp_tc_kernel(const int32_t* __restrict__ ce, int32_t cnt, int32_t n_node
             v = mi0 * dg[0] + mi1 * dg[nns] + mi2 * dg[2 * nns];
           }
           const float hi = tc::to_tf32(v);
-          const int off = (rg * (kTPKChunk / 4) + kc) * 128 + lane * 4;
+          const int off = (rg * (KCH / 4) + kc) * 128 + lane * 4;
           *reinterpret_cast<float*>(S.A[0] + off) = hi;
           *reinterpret_cast<float*>(S.A[1] + off) = tc::to_tf32(v - hi);
         }
@@ -861,24 +876,25 @@ int launch_tp_tc(const int32_t* order, const int32_t* ngauss, int32_t n_nodes, c
   if (nns > kMaxNns || t->cfg.ng > kMaxNg)
     return gfe::set_error(GFE_ERR_ARG, "gfe_laplace_assemble_tp: the tensor-core path takes up to %d nodes and %d "
                           "Gauss points an element", kMaxNns, kMaxNg);
-  const size_t smem = sizeof(TPTCShared);
   const void* k32 = (const void*)laplace_tp_tc_kernel<32>;
   const void* k64 = (const void*)laplace_tp_tc_kernel<64>;
+  const size_t smem = nns <= 32 ? sizeof(TPTCShared<32>) : sizeof(TPTCShared<64>);
   GFE_CUDA_TRY(cudaFuncSetAttribute(nns <= 32 ? k32 : k64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   unsigned* err = gfe::device_error_word();
-  const int ept = nns <= 32 ? 4 : 2;
+  const int ept = nns <= 32 ? TPTCShape<32>::kEPT : TPTCShape<64>::kEPT;
+  const int per_sm = nns <= 32 ? TPTCShape<32>::kBlocksPerSM : TPTCShape<64>::kBlocksPerSM;
   for (int c = 0; c < n_colors; ++c) {
     const int c0 = color_ptr_host[c], cnt = color_ptr_host[c + 1] - c0;
     if (cnt <= 0) continue;
-    const int grid = std::min((cnt + ept - 1) / ept, gfe::sm_count());
+    const int grid = std::min((cnt + ept - 1) / ept, per_sm * gfe::sm_count());
     if (nns <= 32)
-      laplace_tp_tc_kernel<32><<<grid, kTPTCThreads, smem, s>>>(color_elems + c0, cnt, n_nodes, en, coords, scale,
-                                                                kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci,
-                                                                slots, values, err);
+      laplace_tp_tc_kernel<32><<<grid, TPTCShape<32>::kThreads, smem, s>>>(
+          color_elems + c0, cnt, n_nodes, en, coords, scale, kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci, slots,
+          values, err);
     else
-      laplace_tp_tc_kernel<64><<<grid, kTPTCThreads, smem, s>>>(color_elems + c0, cnt, n_nodes, en, coords, scale,
-                                                                kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci,
-                                                                slots, values, err);
+      laplace_tp_tc_kernel<64><<<grid, TPTCShape<64>::kThreads, smem, s>>>(
+          color_elems + c0, cnt, n_nodes, en, coords, scale, kappa, t->dphi, t->w, t->pairs, t->cfg, rp, ci, slots,
+          values, err);
     ++*launches;
   }
   return GFE_OK;
