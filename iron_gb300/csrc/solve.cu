@@ -25,6 +25,7 @@
 
 #include "gfe_internal.cuh"
 #include "reduce.cuh"
+#include "scan.cuh"
 
 namespace {
 
@@ -297,6 +298,139 @@ __global__ void norm2_kernel(int n, const double* __restrict__ v, double* red, S
   }
 }
 
+// Sliced-ELL copy of a CSR matrix with short rows, for the CG products: slices of 32 consecutive
+// rows, each stored column-major and padded to its longest row (column 0 marks padding), so entry
+// k of row r sits at sptr[r / 32] + 32 k + r % 32.  A lane per row then reads one contiguous
+// 128-byte line per warp and entry, and no row waits on its bounds; the per-row CSR forms wait on
+// the row bounds, then on the entries, then on the gathers.  Built inside each solve call from the
+// caller's CSR (the values change with every assembly).
+constexpr int kSell = 32;
+
+template <typename TM>
+struct SellMatrix {
+  const long long* sptr;  // [n_slices] first entry of each slice
+  const int32_t* slen;    // [n_slices] entries of each slice (32 x its longest row)
+  const int32_t* col;     // 1-based column, 0 = padding
+  const TM* val;
+};
+
+__global__ void sell_slice_len(int n, const int32_t* __restrict__ rp, int32_t* __restrict__ slen) {
+  const int n_pad = (n + kSell - 1) / kSell * kSell;
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n_pad; row += gridDim.x * blockDim.x) {
+    const int len = row < n ? __ldg(rp + row + 1) - __ldg(rp + row) : 0;
+    const int mx = __reduce_max_sync(0xffffffffu, len);
+    if ((row & (kSell - 1)) == 0) slen[row / kSell] = mx * kSell;
+  }
+}
+
+template <typename TM>
+__global__ void sell_fill(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                          const TM* __restrict__ val, const long long* __restrict__ sptr,
+                          const int32_t* __restrict__ slen, int32_t* __restrict__ col, TM* __restrict__ sval) {
+  const int n_pad = (n + kSell - 1) / kSell * kSell;
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n_pad; row += gridDim.x * blockDim.x) {
+    const int sl = row / kSell, lane = row & (kSell - 1);
+    const long long base = sptr[sl] + lane;
+    const int L = slen[sl] / kSell;
+    const int k0 = row < n ? __ldg(rp + row) - 1 : 0, len = row < n ? __ldg(rp + row + 1) - 1 - k0 : 0;
+    for (int k = 0; k < L; ++k) {
+      const bool in = k < len;
+      col[base + (long long)k * kSell] = in ? __ldg(ci + k0 + k) : 0;
+      sval[base + (long long)k * kSell] = in ? __ldg(val + k0 + k) : TM(0);
+    }
+  }
+}
+
+// q = A p on free rows (0 on fixed rows) from the sliced-ELL copy, partial <p, q> and alpha as
+// cg_spmv; each row's entries in column order, kSellUnroll loads in flight a lane.
+constexpr int kSellUnroll = 8;
+
+template <typename TM, typename TV>
+__global__ void __launch_bounds__(kThreads)
+cg_spmv_sell(int n, SellMatrix<TM> A, const TV* __restrict__ p, TV* __restrict__ q,
+             const uint8_t* __restrict__ fixed, double* red, Scalars* sc) {
+  if (sc->done) return;
+  const int n_pad = (n + kSell - 1) / kSell * kSell;
+  TV dot = TV(0);
+  // the loop bound is warp-uniform (whole slices)
+  for (int row = blockIdx.x * kThreads + threadIdx.x; row < n_pad; row += gridDim.x * kThreads) {
+    const int sl = row / kSell, lane = row & (kSell - 1);
+    const long long base = __ldg(A.sptr + sl) + lane;
+    const int L = __ldg(A.slen + sl) / kSell;
+    TV acc = TV(0);
+    for (int k0 = 0; k0 < L; k0 += kSellUnroll) {
+      TM v[kSellUnroll];
+      int c[kSellUnroll];
+#pragma unroll
+      for (int u = 0; u < kSellUnroll; ++u) {
+        const bool in = k0 + u < L;
+        const long long at = base + (long long)(k0 + u) * kSell;
+        v[u] = in ? __ldcs(A.val + at) : TM(0);
+        c[u] = in ? __ldcs(A.col + at) : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < kSellUnroll; ++u)
+        if (c[u] > 0) acc += (TV)v[u] * p[c[u] - 1];
+    }
+    if (row < n) {
+      if (fixed && fixed[row]) acc = TV(0);
+      q[row] = acc;
+      dot += p[row] * acc;
+    }
+  }
+  double b = block_sum(dot);
+  if (threadIdx.x == 0) red[blockIdx.x] = b;
+  if (last_block(&sc->ticket1)) {
+    double pq = ordered_sum(red, gridDim.x);
+    if (threadIdx.x == 0) {
+      sc->pq = pq;
+      sc->alpha = pq != 0.0 ? sc->rz / pq : 0.0;
+      if (!(pq > 0.0) || !isfinite(pq)) { sc->bad = 1; sc->done = 1; }
+      sc->ticket1 = 0;
+    }
+  }
+}
+
+// Builds the sliced-ELL copy of (rp, ci, val) in two scratch allocations bufs[0], bufs[1] (the
+// caller frees both with scratch_free).  Synchronises the stream once (the copy's size).
+template <typename TM>
+int build_sell(int n, const int32_t* rp, const int32_t* ci, const TM* val, cudaStream_t s, void* bufs[2],
+               SellMatrix<TM>* out) {
+  using namespace gfe;
+  bufs[0] = bufs[1] = nullptr;
+  const long long n_slices = (n + kSell - 1) / kSell;
+  char* head = nullptr;
+  const size_t head_bytes = ((sizeof(long long) * (n_slices + 1) + 255) & ~size_t(255)) +
+                            ((sizeof(int32_t) * n_slices + 255) & ~size_t(255));
+  int rc = scratch_alloc((void**)&head, head_bytes, s, "sliced-ELL offsets");
+  if (rc) return rc;
+  long long* sptr = (long long*)head;
+  int32_t* slen = (int32_t*)(head + ((sizeof(long long) * (n_slices + 1) + 255) & ~size_t(255)));
+  const int grid = 8 * sm_count();
+  sell_slice_len<<<grid, kThreads, 0, s>>>(n, rp, slen);
+  if ((rc = exclusive_scan(slen, n_slices, sptr, sptr + n_slices, s))) { scratch_free(head, s); return rc; }
+  long long total = 0;
+  cudaError_t e = cudaMemcpyAsync(&total, sptr + n_slices, sizeof(long long), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) { scratch_free(head, s); return set_error(GFE_ERR_CUDA, "sliced-ELL size: %s", cudaGetErrorString(e)); }
+  char* body = nullptr;
+  const size_t col_bytes = ((sizeof(int32_t) * (size_t)total + 255) & ~size_t(255));
+  if ((rc = scratch_alloc((void**)&body, col_bytes + sizeof(TM) * (size_t)total + 256, s, "sliced-ELL copy"))) {
+    scratch_free(head, s);
+    return rc;
+  }
+  int32_t* col = (int32_t*)body;
+  TM* sval = (TM*)(body + col_bytes);
+  sell_fill<TM><<<grid, kThreads, 0, s>>>(n, rp, ci, val, sptr, slen, col, sval);
+  out->sptr = sptr;
+  out->slen = slen;
+  out->col = col;
+  out->val = sval;
+  bufs[0] = head;
+  bufs[1] = body;
+  return GFE_OK;
+}
+
 // SpMV form of the CG iterations.  Short rows (the trilinear hexahedron's 27-entry rows, tetrahedra)
 // take cg_spmv_batched: FP32 with 8 lanes a row and 4 entries a lane loaded at once (128^3 Laplace:
 // 105 us a product, 126 us for the per-row loop, 4-28 lanes a row and two rows a group measured
@@ -340,13 +474,14 @@ void launch_spmv(int lpr, int grid, cudaStream_t s, int n, const int32_t* rp, co
 template <typename TM, typename TV, typename TX>
 int run_cg(cudaStream_t s, int n, const int32_t* rp, const int32_t* ci, const TM* val, const uint8_t* fixed,
            const TV* dinv, TX* x, TV* r, TV* z, TV* p, TV* q, double* red, double* red2, Scalars* sc,
-           Scalars* sc_host, int lpr, int grid, int max_iters, int chunk) {
+           Scalars* sc_host, int lpr, int grid, int max_iters, int chunk, const SellMatrix<TM>* sell = nullptr) {
   int launched = 0;
   while (launched < max_iters) {
     int k = chunk < max_iters - launched ? chunk : max_iters - launched;
     for (int i = 0; i < k; ++i) {
       void* prof = gfe::stage_begin(GFE_STAGE_SPMV, s);
-      launch_spmv<TM, TV>(lpr, grid, s, n, rp, ci, val, p, q, fixed, red, sc);
+      if (sell) cg_spmv_sell<TM, TV><<<grid, kThreads, 0, s>>>(n, *sell, p, q, fixed, red, sc);
+      else launch_spmv<TM, TV>(lpr, grid, s, n, rp, ci, val, p, q, fixed, red, sc);
       gfe::stage_end(GFE_STAGE_SPMV, prof, s, 1);
       cg_update<TX, TV><<<grid, kThreads, 0, s>>>(n, x, r, z, p, q, dinv, red, red2, sc);
       cg_direction<TV><<<grid, kThreads, 0, s>>>(n, p, z, sc);
@@ -403,6 +538,11 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
   const int lpr = pick_lpr((double)(nnz1 - 1) / n, precision == GFE_FP64);
   const int grid = 8 * sm_count();
   const int chunk = 50;
+  // short rows: the FP32 iterations of the mixed solve run on a sliced-ELL copy of values32 (128^3
+  // Laplace: 104 -> 91 us a product, 103 -> 93 ms a solve); the FP64 product, bound by FP64 work
+  // as much as by its loads, gained nothing from it and keeps the batched CSR form
+  const bool use_sell = precision == GFE_MIXED && (double)(nnz1 - 1) / n <= 32.0 && n >= 4 * kSell;
+  void* sell_bufs[2] = {nullptr, nullptr};
 
   // scratch: dinv, r64, then vector set (FP64 or FP32) and an FP32 copy of dinv
   const size_t vbytes = precision == GFE_FP64 ? sizeof(double) : sizeof(float);
@@ -479,6 +619,8 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
     // iterations with the best restart tolerance, 1e-5).  Reductions of 1e-1 to 1e-3 per update
     // all take 727-742 iterations; 1e-3 needs the fewest updates.
     const double inner_rtol = 1e-3;
+    SellMatrix<float> sell{};
+    if (use_sell) rc = build_sell<float>(n, row_ptr, col_idx, values32, s, sell_bufs, &sell);
     for (int outer = 0; outer < 200 && rc == GFE_OK; ++outer) {
       if (outer > 0) {
         cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
@@ -492,7 +634,7 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
                                                        inner_rtol * inner_rtol);
       if (outer > 0) cg_direction<float><<<grid, kThreads, 0, s>>>(n, p, z, sc);
       rc = run_cg<float, float, float>(s, n, row_ptr, col_idx, values32, fixed, dinv32, d, r, z, p, q, red, red2, sc,
-                                       &sh, lpr, grid, max_iters - total_it, chunk);
+                                       &sh, lpr, grid, max_iters - total_it, chunk, use_sell ? &sell : nullptr);
       total_it += sh.it;
       if (sh.bad) break;
       add_correction<<<grid, kThreads, 0, s>>>(n, x, d, fixed);
@@ -504,6 +646,8 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
   cudaMemcpyAsync(&r2, red2 + grid - 1, sizeof(double), cudaMemcpyDeviceToHost, s);
   cudaError_t e = cudaStreamSynchronize(s);
   scratch_free(base, s);
+  scratch_free(sell_bufs[0], s);
+  scratch_free(sell_bufs[1], s);
   if (rc) return rc;
   if (e != cudaSuccess) return set_error(GFE_ERR_CUDA, "%s: %s", fn, cudaGetErrorString(e));
   const double rel = std::sqrt(r2 / b2);
