@@ -228,6 +228,56 @@ cg_residual(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ c
   }
 }
 
+// cg_residual for short rows (up to about 32 entries): 2 lanes a row, 14 entries a lane loaded
+// before the first gather, the next row's bounds loaded ahead (the loads of cg_spmv_batched).  The warp-per-row form spends 5 levels of FP64 shuffle additions on every row,
+// more FP64 work than the row's own products.
+__global__ void __launch_bounds__(kThreads, 4)
+cg_residual_short(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
+                  const double* __restrict__ val, const double* __restrict__ f, const uint8_t* __restrict__ fixed,
+                  const double* __restrict__ x, double* __restrict__ r) {
+  constexpr int LPR = 2, E = 14, R = 1, RPB = kThreads / LPR;
+  const int sub = threadIdx.x % LPR, grp = threadIdx.x / LPR;
+  const int stride = gridDim.x * RPB * R;
+  int k0[R], k1[R];
+#pragma unroll
+  for (int j = 0; j < R; ++j) {
+    const int row = blockIdx.x * RPB * R + j * RPB + grp;
+    k0[j] = row < n ? __ldg(rp + row) - 1 : 0;
+    k1[j] = row < n ? __ldg(rp + row + 1) - 1 : 0;
+  }
+  for (int base = blockIdx.x * RPB * R; base < n; base += stride) {
+    int nk0[R], nk1[R];
+    double v[R][E];
+    int c[R][E];
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int nrow = base + stride + j * RPB + grp;
+      nk0[j] = nrow < n ? __ldg(rp + nrow) - 1 : 0;
+      nk1[j] = nrow < n ? __ldg(rp + nrow + 1) - 1 : 0;
+#pragma unroll
+      for (int u = 0; u < E; ++u) {
+        const int k = k0[j] + sub + u * LPR;
+        v[j][u] = k < k1[j] ? __ldg(val + k) : 0.0;
+        c[j][u] = k < k1[j] ? __ldg(ci + k) : 0;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < R; ++j) {
+      const int row = base + j * RPB + grp;
+      double acc = 0.0;
+#pragma unroll
+      for (int u = 0; u < E; ++u)
+        if (c[j][u] > 0) acc += v[j][u] * x[c[j][u] - 1];
+#pragma unroll 1
+      for (int k = k0[j] + sub + E * LPR; k < k1[j]; k += LPR) acc += __ldg(val + k) * x[__ldg(ci + k) - 1];
+      acc += __shfl_down_sync(0xffffffffu, acc, 1, LPR);
+      if (row < n && sub == 0) r[row] = (fixed && fixed[row]) ? 0.0 : (f ? f[row] : 0.0) - acc;
+      k0[j] = nk0[j];
+      k1[j] = nk1[j];
+    }
+  }
+}
+
 __global__ void jacobi_inverse(int n, const int32_t* __restrict__ rp, const int32_t* __restrict__ ci,
                                const double* __restrict__ val, const uint8_t* __restrict__ fixed,
                                double* __restrict__ dinv, unsigned* err) {
@@ -470,6 +520,15 @@ void launch_spmv(int lpr, int grid, cudaStream_t s, int n, const int32_t* rp, co
   else cg_spmv<TM, TV, 1><<<grid, kThreads, 0, s>>>(n, rp, ci, val, p, q, fixed, red, sc);
 }
 
+// r = f - A x (FP64) on free rows: the batched 2-lane form for short rows, a warp a row otherwise.
+void residual64(bool short_rows, int grid, cudaStream_t s, int n, const int32_t* rp, const int32_t* ci,
+                const double* val, const double* f, const uint8_t* fixed, const double* x, double* r) {
+  if (short_rows)
+    cg_residual_short<<<std::min(grid, 4 * gfe::sm_count()), kThreads, 0, s>>>(n, rp, ci, val, f, fixed, x, r);
+  else
+    cg_residual<double><<<grid, kThreads, 0, s>>>(n, rp, ci, val, f, fixed, x, r);
+}
+
 // Runs CG iterations (chunked, device-side convergence flag) on pre-started vectors.
 template <typename TM, typename TV, typename TX>
 int run_cg(cudaStream_t s, int n, const int32_t* rp, const int32_t* ci, const TM* val, const uint8_t* fixed,
@@ -538,6 +597,7 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
   const int lpr = pick_lpr((double)(nnz1 - 1) / n, precision == GFE_FP64);
   const int grid = 8 * sm_count();
   const int chunk = 50;
+  const bool short_rows = (double)(nnz1 - 1) / n <= 32.0;
   // short rows: the FP32 iterations of the mixed solve run on a sliced-ELL copy of values32 (128^3
   // Laplace: 104 -> 91 us a product, 103 -> 93 ms a solve); the FP64 product, bound by FP64 work
   // as much as by its loads, gained nothing from it and keeps the batched CSR form
@@ -577,7 +637,7 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
   jacobi_inverse<<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, fixed, dinv, err);
   // initial residual with x0 = Dirichlet values, zero elsewhere
   set_dirichlet<<<grid, kThreads, 0, s>>>(n, x, fixed, true);
-  cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
+  residual64(short_rows, grid, s, n, row_ptr, col_idx, values, f, fixed, x, r64);
   norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, sc, red2 + grid - 1);
   GFE_CUDA_TRY(cudaMemcpyAsync(&b2, red2 + grid - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
   GFE_CUDA_TRY(cudaStreamSynchronize(s));
@@ -601,7 +661,7 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
                                           &sh, lpr, grid, max_iters - total_it, chunk);
       total_it += sh.it;
       if (rc || sh.bad || total_it >= max_iters) break;
-      cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
+      residual64(short_rows, grid, s, n, row_ptr, col_idx, values, f, fixed, x, r64);
       norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, sc, red2 + grid - 1);
       GFE_CUDA_TRY(cudaMemcpyAsync(&r2_start, red2 + grid - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
       GFE_CUDA_TRY(cudaStreamSynchronize(s));
@@ -623,7 +683,7 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
     if (use_sell) rc = build_sell<float>(n, row_ptr, col_idx, values32, s, sell_bufs, &sell);
     for (int outer = 0; outer < 200 && rc == GFE_OK; ++outer) {
       if (outer > 0) {
-        cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
+        residual64(short_rows, grid, s, n, row_ptr, col_idx, values, f, fixed, x, r64);
         norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, sc, red2 + grid - 1);
         GFE_CUDA_TRY(cudaMemcpyAsync(&r2, red2 + grid - 1, sizeof(double), cudaMemcpyDeviceToHost, s));
         GFE_CUDA_TRY(cudaStreamSynchronize(s));
@@ -641,7 +701,7 @@ extern "C" int gfe_cg_solve(int32_t n, const int32_t* row_ptr, const int32_t* co
     }
   }
   // final FP64 residual
-  cg_residual<double><<<grid, kThreads, 0, s>>>(n, row_ptr, col_idx, values, f, fixed, x, r64);
+  residual64(short_rows, grid, s, n, row_ptr, col_idx, values, f, fixed, x, r64);
   norm2_kernel<<<grid, kThreads, 0, s>>>(n, r64, red, sc, red2 + grid - 1);
   cudaMemcpyAsync(&r2, red2 + grid - 1, sizeof(double), cudaMemcpyDeviceToHost, s);
   cudaError_t e = cudaStreamSynchronize(s);
