@@ -747,16 +747,21 @@ __device__ __forceinline__ DualF point_jz(const DualF (&Z)[3][3], const DualF (&
   return {(float)j.v, (float)j.d};
 }
 
-// P = w Jz Z^-1 sigma(Z, p) of the residual; also returns Jz.  R: type of the constants.
+// P = w Jz Z^-1 sigma(Z, p) of the residual; also returns Jz.  R: type of the constants.  jz_given:
+// J_z (with its derivative) when the caller has formed it already.
 template <typename T, typename R = double>
 __device__ __forceinline__ void point_P(const T (&Z)[3][3], const R A[3][3], R Jx, R w, T p, R c1, R c2, T P[3][3],
-                                        T& Jz) {
-  T G[3][3];
+                                        T& Jz, const T* jz_given = nullptr) {
+  if (jz_given) {
+    Jz = *jz_given;
+  } else {
+    T G[3][3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) G[i][j] = Z[0][i] * Z[0][j] + Z[1][i] * Z[1][j] + Z[2][i] * Z[2][j];
-  Jz = point_jz(Z, G);
+      for (int j = 0; j < 3; ++j) G[i][j] = Z[0][i] * Z[0][j] + Z[1][i] * Z[1][j] + Z[2][i] * Z[2][j];
+    Jz = point_jz(Z, G);
+  }
   T Zi[3][3];
   tinv3(Z, Zi);
   const T J = Jz / Jx;
@@ -839,9 +844,41 @@ __device__ __forceinline__ void gauss_inputs(const TablesT<S>& T, int g, const S
   o.w = T.w[g];
 }
 
+// J_z = |det Z| and its derivatives for the FP32 dual path, once per Gauss point: the value and the
+// signed cofactors (d|det Z| / dZ_ij) in FP64 on the exactly widened entries, rounded to FP32.
+// jz[0] = J_z, jz[1 + 3 i + j] = dJ_z/dZ_ij.  The seeds are unit directions, so each seed's
+// derivative is one cofactor: forming |det Z| in FP64 dual arithmetic per seed cost about 460 FP64
+// operations a Gauss point on GB300's narrow FP64 pipe, this about 30.
+__device__ __forceinline__ void jz_seeds(const float (&Zf)[3][3], float jz[10]) {
+  double Z[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Z[i][j] = f32_to_f64_exact(Zf[i][j]);
+  double cof[3][3];
+  cof[0][0] = Z[1][1] * Z[2][2] - Z[1][2] * Z[2][1];
+  cof[0][1] = Z[1][2] * Z[2][0] - Z[1][0] * Z[2][2];
+  cof[0][2] = Z[1][0] * Z[2][1] - Z[1][1] * Z[2][0];
+  cof[1][0] = Z[0][2] * Z[2][1] - Z[0][1] * Z[2][2];
+  cof[1][1] = Z[0][0] * Z[2][2] - Z[0][2] * Z[2][0];
+  cof[1][2] = Z[0][1] * Z[2][0] - Z[0][0] * Z[2][1];
+  cof[2][0] = Z[0][1] * Z[1][2] - Z[0][2] * Z[1][1];
+  cof[2][1] = Z[0][2] * Z[1][0] - Z[0][0] * Z[1][2];
+  cof[2][2] = Z[0][0] * Z[1][1] - Z[0][1] * Z[1][0];
+  const double det = tdet3(Z);
+  const double sg = det < 0.0 ? -1.0 : 1.0;
+  jz[0] = (float)(sg * det);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) jz[1 + 3 * i + j] = (float)(sg * cof[i][j]);
+}
+
 // dP/d(seed) for seed 0..8 = Z[seed/3][seed%3], seed 9 = p.  out[9] = dP[xi][mh] row-major.
+// jz: J_z and its seed derivatives from jz_seeds (FP32 path), or NULL.
 template <typename S>
-__device__ __forceinline__ void point_dP(const GPInT<S>& in, int seed, S c1, S c2, S out[9], S* Jz_v) {
+__device__ __forceinline__ void point_dP(const GPInT<S>& in, int seed, S c1, S c2, S out[9], S* Jz_v,
+                                         const float* jz = nullptr) {
   using D = typename DualOf<S>::type;
   D Z[3][3];
 #pragma unroll
@@ -850,7 +887,16 @@ __device__ __forceinline__ void point_dP(const GPInT<S>& in, int seed, S c1, S c
     for (int j = 0; j < 3; ++j) Z[i][j] = {in.Z[i][j], (i * 3 + j == seed) ? S(1) : S(0)};
   const D p = {in.p, seed == 9 ? S(1) : S(0)};
   D P[3][3], Jz;
-  point_P<D, S>(Z, in.A, in.Jx, in.w, p, c1, c2, P, Jz);
+  if constexpr (std::is_same<S, float>::value) {
+    if (jz) {
+      const D jg = {jz[0], seed < 9 ? jz[1 + seed] : 0.0f};
+      point_P<D, S>(Z, in.A, in.Jx, in.w, p, c1, c2, P, Jz, &jg);
+    } else {
+      point_P<D, S>(Z, in.A, in.Jx, in.w, p, c1, c2, P, Jz);
+    }
+  } else {
+    point_P<D, S>(Z, in.A, in.Jx, in.w, p, c1, c2, P, Jz);
+  }
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -1333,9 +1379,11 @@ mr_gp_kernel(const int32_t* __restrict__ elems, int32_t count, const int32_t* __
     const KS c1 = (KS)cpar[0], c2 = (KS)cpar[1];
     GPInT<KS> in;
     gauss_inputs(T, g, S.z[le], S.x[le], S.p[le], in);
+    float jz[10];
+    if constexpr (std::is_same<KS, float>::value) jz_seeds(in.Z, jz);
     for (int seed = 0; seed < 10; ++seed) {
       KS d[9], Jz;
-      point_dP(in, seed, c1, c2, d, &Jz);
+      point_dP(in, seed, c1, c2, d, &Jz, std::is_same<KS, float>::value ? jz : nullptr);
       if (seed < 9) {
         const int nh = seed / 3, z = seed % 3;
 #pragma unroll
