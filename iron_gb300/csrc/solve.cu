@@ -7,7 +7,9 @@
 // direction are zero, which is algebraically the eliminated system.
 //
 // All scalars of the iteration live on the device; one iteration is three kernels (SpMV + <p,q>,
-// update + <r,z>, direction update).  Reductions are deterministic: each block writes a partial
+// update + <r,z>, direction update).  The product takes the form that suits the rows: short rows
+// (the trilinear hexahedron's 27) a batched-load CSR form in FP64 and a sliced-ELL copy in FP32,
+// long rows (the Q2/Q1 tangent's ~390) several lanes a row.  Reductions are deterministic: each block writes a partial
 // sum and the last block to finish (detected by an atomic ticket) adds the partials in index order.
 // Kernels return immediately once the device-side `done` flag is set, so the host can launch
 // iterations in chunks and synchronise only between chunks.
