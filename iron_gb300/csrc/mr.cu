@@ -1580,7 +1580,8 @@ mr_contract_kernel(const int32_t* __restrict__ elems, int32_t count, const Table
 // hi*hi + lo*hi + hi*lo recover about FP32 accuracy; without it the contraction is plain TF32
 // (about 1e-3 relative).  u-p / p-u blocks, Iron's lower-triangle mirror and the element-matrix
 // output are as in mr_contract_kernel.
-constexpr int kTCThreads = 512;                // 16 warps: the operand formation is latency bound
+constexpr int kTCThreads = 1024;               // 32 warps: every phase is latency bound
+constexpr int kTCGroupWarps = kTCThreads / 32 / 16;  // warps sharing one 8-row group of the operand
 constexpr int kTK = 88;                        // K = 27 Gauss points x 3, padded to 11 steps of 8
 constexpr int kTKC = kTK / 4;                  // core-matrix columns along K (4 TF32 = 16 bytes)
 constexpr int kTABytes = 16 * kTKC * 128;      // one M = 128 operand tile
@@ -1613,7 +1614,7 @@ template <bool EXACT, bool SPLIT3>
 __global__ void __launch_bounds__(kTCThreads, 1)
 mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Tables* __restrict__ Tg,
                       const float* __restrict__ gp, float* __restrict__ Kel, unsigned* err) {
-  static_assert(kTCThreads == 16 * 32, "one warp per 8-row group of an M = 128 operand tile");
+  static_assert(kTCThreads % (16 * 32) == 0, "whole warps per 8-row group of an M = 128 operand tile");
   extern __shared__ __align__(1024) unsigned char traw[];
   TCShared& S = *reinterpret_cast<TCShared*>(traw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -1680,16 +1681,18 @@ mr_contract_tc_kernel(const int32_t* __restrict__ elems, int32_t count, const Ta
     if (S.abort) break;
     const float(*Dg)[kGPOut] = reinterpret_cast<const float(*)[kGPOut]>(S.Dg[buf]);
     float* Ke = Kel + (size_t)__ldg(elems + item) * ND * ND;
+    // warp w forms the core columns kc = w / 16, w / 16 + kTCGroupWarps, ... of the 8-row group w % 16
+    const int rg = warp & 15, kc0 = warp >> 4;
     for (int half = 0; half < 2; ++half) {
-      const int row = half * 128 + warp * 8 + r_in;
+      const int row = half * 128 + rg * 8 + r_in;
       const bool valid = row < 243;
       const int pair = valid ? row / 27 : 0, ms = valid ? row % 27 : 0;
       const float* Gm = &S.G[0][ms];
       const float* Dp = &Dg[0][pair * 9];
-      unsigned char* a0 = S.A[0] + (warp * kTKC) * 128 + lane * 4;
-      unsigned char* a1 = S.A[1] + (warp * kTKC) * 128 + lane * 4;
+      unsigned char* a0 = S.A[0] + (rg * kTKC) * 128 + lane * 4;
+      unsigned char* a1 = S.A[1] + (rg * kTKC) * 128 + lane * 4;
 #pragma unroll 2
-      for (int kc = 0; kc < kTKC; ++kc) {
+      for (int kc = kc0; kc < kTKC; kc += kTCGroupWarps) {
         const int k = kc * 4 + kq;
         float v = 0.0f;
         if (valid && k < 81) {
