@@ -19,6 +19,9 @@ Sources:
   tests/FiniteElasticity/output_cantilever/{linear_3x2x2,cubic_2x1x1}/Cantilever.part0.{exnode,exelem}
       Iron's exported results of the Cantilever finite-elasticity test (FieldExport.c formats):
       copied verbatim into exfile/ to pin the exnode/exelem reader and writer by round trip.
+  tests/FiniteElasticity/output_shear/SimpleShear.part0.{exnode,exelem}
+      Iron's exported results of the SimpleShear test (triquadratic Lagrange elements of 27 nodes
+      with one scale-factor set): copied verbatim into exfile/ as a third round-trip case.
 """
 from __future__ import annotations
 
@@ -90,6 +93,11 @@ def main():
             dst = OUT / "exfile" / f"cantilever_{case}.{ext}"
             shutil.copyfile(src, dst)
             print("copied", src.relative_to(REF), "->", dst.name)
+    for ext in ("exnode", "exelem"):
+        src = REF / "tests/FiniteElasticity/output_shear" / f"SimpleShear.part0.{ext}"
+        dst = OUT / "exfile" / f"simple_shear.{ext}"
+        shutil.copyfile(src, dst)
+        print("copied", src.relative_to(REF), "->", dst.name)
 
 
 if __name__ == "__main__":

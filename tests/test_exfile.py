@@ -1,7 +1,8 @@
-"""exnode / exelem reader and writer (iron_gb300/exfile.py).  Iron's own Cantilever outputs (linear
-Lagrange with grid-based element fields; cubic Hermite with derivatives and two scale-factor
-sets; tests/golden/exfile, copied by tests/golden/make_golden.py) read and written again are
-byte-identical, which pins the writer to Iron's FieldExport.c formats.  This package's Laplace and
+"""exnode / exelem reader and writer (iron_gb300/exfile.py).  Iron's own Cantilever and SimpleShear
+outputs (linear Lagrange with grid-based element fields; cubic Hermite with derivatives and two
+scale-factor sets; triquadratic Lagrange with one scale-factor set; tests/golden/exfile, copied by
+tests/golden/make_golden.py) read and written again are byte-identical, which pins the writer to
+Iron's FieldExport.c formats; the SimpleShear mesh pins the triquadratic generated-mesh numbering.  This package's Laplace and
 Mooney-Rivlin exports round-trip exactly.  CPU only."""
 from pathlib import Path
 
@@ -12,7 +13,7 @@ from iron_gb300 import exfile as X
 from iron_gb300 import mesh as M
 
 GOLD = Path(__file__).resolve().parent / "golden" / "exfile"
-CASES = ["cantilever_linear_3x2x2", "cantilever_cubic_2x1x1"]
+CASES = ["cantilever_linear_3x2x2", "cantilever_cubic_2x1x1", "simple_shear"]
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -42,6 +43,24 @@ def test_linear_cantilever_content():
     assert es.elements[0].nodes == [1, 2, 5, 6, 13, 14, 17, 18]
     # the pressure component of the dependent field is grid based (element constant)
     assert es.header.fields[2].components[3].grid == "#xi1=1, #xi2=1, #xi3=1"
+
+
+def test_triquadratic_mesh_matches_irons_generated_mesh():
+    """Iron's SimpleShear output (a 2x2x2 triquadratic generated mesh of the unit cube) has the
+    element node lists and node positions of mesh.RegularMesh(order=2), the mesh the Q2/Q1
+    Mooney-Rivlin path builds its element DOF lists from."""
+    elems = X.read_exelem(GOLD / "simple_shear.exelem")
+    es = elems.sections[0]
+    assert es.header.n_nodes == 27 and len(es.elements) == 8
+    assert es.header.scale_sets == [("q.Lagrange*q.Lagrange*q.Lagrange", 27)]
+    m = M.RegularMesh((2, 2, 2), order=2)
+    assert np.array_equal(np.array([e.nodes for e in es.elements]) - 1, m.elem_nodes)
+    nodes = X.read_exnode(GOLD / "simple_shear.exnode")
+    assert [f.name for f in nodes.sections[0].fields] == ["Geometry", "Fibre", "Dependent", "del U/del n",
+                                                          "Material"]
+    xyz = [X.node_values(nodes, "Geometry", c) for c in range(3)]
+    coords = np.array([[xyz[c][k] for k in sorted(xyz[c])] for c in range(3)])
+    assert np.array_equal(coords, m.coords)
 
 
 def test_cubic_hermite_derivatives_and_scale_factors():
