@@ -63,6 +63,33 @@ def test_triquadratic_mesh_matches_irons_generated_mesh():
     assert np.array_equal(coords, m.coords)
 
 
+def test_trilinear_mesh_matches_irons_generated_mesh():
+    """The linear Cantilever output (a 3x2x2 trilinear generated mesh of a 60 x 40 x 40 beam) has
+    the element node lists and node positions of mesh.RegularMesh(order=1), the mesh of the
+    regular-mesh Laplace kernels."""
+    es = X.read_exelem(GOLD / "cantilever_linear_3x2x2.exelem").sections[0]
+    m = M.RegularMesh((3, 2, 2), order=1, extent=(60.0, 40.0, 40.0))
+    assert np.array_equal(np.array([e.nodes for e in es.elements]) - 1, m.elem_nodes)
+    nodes = X.read_exnode(GOLD / "cantilever_linear_3x2x2.exnode")
+    xyz = [X.node_values(nodes, "Geometry", c) for c in range(3)]
+    assert np.array_equal(np.array([[xyz[c][k] for k in sorted(xyz[c])] for c in range(3)]), m.coords)
+
+
+def test_cubic_hermite_mesh_matches_irons_generated_mesh():
+    """The cubic Cantilever output (a 2x1x1 tricubic Hermite generated mesh of a 60 x 40 x 40
+    beam, arc-length scaling) has the geometric parameters (value and 7 derivatives a node and
+    component), element node lists and Hermite scale factors of mesh.HermiteMesh(scaling=
+    "arc_length"), whose element parameter lists run node by node, 8 derivatives each."""
+    hm = M.HermiteMesh((2, 1, 1), extent=(60.0, 40.0, 40.0), scaling="arc_length")
+    sec = X.read_exnode(GOLD / "cantilever_cubic_2x1x1.exnode").sections[0]
+    geo = np.array([[sec.nodes[i][1][c] for i in range(len(sec.nodes))] for c in range(3)])
+    assert np.array_equal(geo.reshape(3, -1), hm.params)
+    els = X.read_exelem(GOLD / "cantilever_cubic_2x1x1.exelem").sections[0].elements
+    nodes = np.array([e.nodes for e in els]) - 1
+    assert np.array_equal(hm.elem_params.reshape(len(els), 8, 8), nodes[:, :, None] * 8 + np.arange(8))
+    assert np.array_equal(np.array([e.scale_factors[0] for e in els]), hm.scale)
+
+
 def test_cubic_hermite_derivatives_and_scale_factors():
     nodes = X.read_exnode(GOLD / "cantilever_cubic_2x1x1.exnode")
     comp = nodes.sections[0].fields[0].components[0]
